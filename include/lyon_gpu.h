@@ -1,0 +1,226 @@
+/*
+ * lyon_gpu.h — C ABI of the GB300 tessellation library (liblyon_gb300.so).
+ *
+ * The library implements lyon's tessellation hot path on the GPU:
+ *   - curve flattening   (lyon_geom quadratic/cubic `for_each_flattened`),
+ *   - StrokeTessellator  (fixed line width: miter, miter-clip, bevel and round joins,
+ *                         butt, square and round caps),
+ *   - FillTessellator    (even-odd and non-zero fill rules, holes, self-intersections).
+ *
+ * Every entry point below replaces one call a lyon user makes; each declaration cites the
+ * reference interface (file:line inside the lyon repository) whose behaviour it reproduces.
+ * Signatures use plain pointers and sizes only.
+ *
+ * Path layout ("lyon_path_batch") is lyon's own `Path` storage (crates/path/src/path.rs:75-79):
+ * one verb byte per event and the endpoint/control points in order; `Close` stores the first
+ * point of the sub-path again (crates/path/src/path.rs:534-542). A batch concatenates paths and
+ * adds offset arrays.
+ *
+ * Vertex output is the `Positions` layout (crates/tessellation/src/geometry_builder.rs:403-415):
+ * two f32 per vertex. Index output is u16 or u32, with lyon's `BuffersBuilder` semantics
+ * (crates/tessellation/src/geometry_builder.rs:338-350): an index is the vertex's position in the
+ * destination vertex buffer plus the builder's vertex offset.
+ */
+#ifndef LYON_GPU_H
+#define LYON_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Path verbs: same order as lyon's `Verb` (crates/path/src/path.rs:29-36). ------------- */
+enum {
+    LYON_VERB_LINE_TO = 0,
+    LYON_VERB_QUADRATIC_TO = 1,
+    LYON_VERB_CUBIC_TO = 2,
+    LYON_VERB_BEGIN = 3,
+    LYON_VERB_CLOSE = 4,
+    LYON_VERB_END = 5
+};
+
+/* ---- Options (crates/path/src/lib.rs:170-281, crates/tessellation/src/lib.rs:315-537). ---- */
+enum { LYON_CAP_BUTT = 0, LYON_CAP_SQUARE = 1, LYON_CAP_ROUND = 2 };
+enum { LYON_JOIN_MITER = 0, LYON_JOIN_MITER_CLIP = 1, LYON_JOIN_ROUND = 2, LYON_JOIN_BEVEL = 3 };
+enum { LYON_FILL_EVEN_ODD = 0, LYON_FILL_NON_ZERO = 1 };
+enum { LYON_ORIENTATION_VERTICAL = 0, LYON_ORIENTATION_HORIZONTAL = 1 };
+
+/* Mirrors `StrokeOptions` (crates/tessellation/src/lib.rs:315-433) for the fixed-width path.
+ * Defaults (StrokeOptions::DEFAULT): butt caps, miter join, width 1, miter limit 4, tol 0.1. */
+typedef struct lyon_stroke_options {
+    int32_t start_cap;
+    int32_t end_cap;
+    int32_t line_join;
+    float line_width;
+    float miter_limit;
+    float tolerance;
+} lyon_stroke_options;
+
+/* Mirrors `FillOptions` (crates/tessellation/src/lib.rs:445-537).
+ * Defaults: tolerance 0.1, even-odd, vertical sweep, intersections handled. */
+typedef struct lyon_fill_options {
+    float tolerance;
+    int32_t fill_rule;
+    int32_t sweep_orientation;
+    int32_t handle_intersections;
+} lyon_fill_options;
+
+/* ---- Status codes: mirror `TessellationError` (crates/tessellation/src/error.rs:1-142). --- */
+enum {
+    LYON_OK = 0,
+    /* TessellationError::UnsupportedParamater(PositionIsNaN) */
+    LYON_ERR_POSITION_IS_NAN = 1,
+    /* TessellationError::UnsupportedParamater(ToleranceIsNaN) */
+    LYON_ERR_TOLERANCE_IS_NAN = 2,
+    /* TessellationError::GeometryBuilder(TooManyVertices) */
+    LYON_ERR_TOO_MANY_VERTICES = 3,
+    /* TessellationError::GeometryBuilder(InvalidVertex) */
+    LYON_ERR_INVALID_VERTEX = 4,
+    /* TessellationError::Internal(..): the fill sweep gave up (its retry also failed). */
+    LYON_ERR_INTERNAL = 5,
+    /* Library-level errors (no lyon counterpart). */
+    LYON_ERR_INVALID_ARGUMENT = 100,
+    LYON_ERR_CUDA = 101,
+    LYON_ERR_OUT_OF_MEMORY = 102,
+    LYON_ERR_CAPACITY = 103,      /* a caller-provided buffer or a fixed device arena is too small */
+    LYON_ERR_UNSUPPORTED = 104    /* an option this build does not implement */
+};
+
+/* Index output modes for batched calls. */
+enum {
+    /* Each path is appended to one shared VertexBuffers, as if `tessellate_path` were called
+     * on every path in order with the same BuffersBuilder: indices are absolute positions in the
+     * concatenated vertex buffer (plus `vertex_offset`). A path whose last index would exceed the
+     * index type's maximum fails with TOO_MANY_VERTICES and is rolled back (abort_geometry), and
+     * later paths continue from the rolled-back length. */
+    LYON_INDEX_GLOBAL = 0,
+    /* Each path has its own VertexBuffers: indices start at 0 (plus `vertex_offset`) per path. */
+    LYON_INDEX_PER_PATH = 1
+};
+
+/* A batch of paths in lyon's `Path` layout. All pointers are either all host or all device,
+ * as each entry point states. */
+typedef struct lyon_path_batch {
+    const uint8_t* verbs;          /* LYON_VERB_* per event, all paths concatenated */
+    const float* points;           /* x, y pairs, all paths concatenated */
+    const uint32_t* verb_offsets;  /* num_paths + 1 entries, into verbs */
+    const uint32_t* point_offsets; /* num_paths + 1 entries, into points (in points, not floats) */
+    uint32_t num_paths;
+} lyon_path_batch;
+
+/* Per-path output record written by batched calls (device memory). */
+typedef struct lyon_path_range {
+    uint32_t first_vertex;   /* offset of the path's first vertex in the vertex buffer */
+    uint32_t num_vertices;
+    uint32_t first_index;    /* offset of the path's first index in the index buffer */
+    uint32_t num_indices;
+} lyon_path_range;
+
+typedef struct lyon_gpu_context lyon_gpu_context;
+
+/* Creates a context on the given CUDA device: a stream, device scratch arenas that grow on
+ * demand, and pinned host staging buffers for the single-path entry points. Returns NULL on
+ * failure. The equivalent of constructing a `StrokeTessellator`/`FillTessellator`
+ * (crates/tessellation/src/stroke.rs:108-118, crates/tessellation/src/fill.rs:523-575),
+ * which own their scratch allocations and are reused across calls. */
+lyon_gpu_context* lyon_gpu_create(int device);
+void lyon_gpu_destroy(lyon_gpu_context* ctx);
+/* The CUDA stream (cudaStream_t) the context launches on. */
+void* lyon_gpu_stream(lyon_gpu_context* ctx);
+/* Last error message recorded on the context (never NULL). */
+const char* lyon_gpu_last_error(lyon_gpu_context* ctx);
+
+/* ----------------------------------------------------------------------------------------- */
+/* Single-path drop-ins (host memory in, host memory out, synchronous).                       */
+/* ----------------------------------------------------------------------------------------- */
+
+/* Result of a single-path call: views into the context's pinned staging buffers, valid until
+ * the next call on the same context. Indices are u16 or u32 as requested, already offset by
+ * `index_base`. On failure num_vertices == num_indices == 0 (abort_geometry). */
+typedef struct lyon_gpu_result {
+    const float* vertices;
+    uint32_t num_vertices;
+    const void* indices;
+    uint32_t num_indices;
+    int32_t status;
+} lyon_gpu_result;
+
+/* StrokeTessellator::tessellate_path(path, options, &mut BuffersBuilder)
+ * (crates/tessellation/src/stroke.rs:164-177), fixed line width, `Positions` vertices.
+ * `index_base` is the id of the first vertex the builder would hand out
+ * (vertices.len() + vertex_offset, crates/tessellation/src/geometry_builder.rs:338-350);
+ * `index_bits` is 16 or 32 and selects u16/u32 indices and MaxIndex
+ * (crates/tessellation/src/geometry_builder.rs:562-603). Returns the status code. */
+int lyon_gpu_stroke_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                         const float* points, uint32_t num_points,
+                         const lyon_stroke_options* options, int index_bits, uint32_t index_base,
+                         lyon_gpu_result* result);
+
+/* FillTessellator::tessellate_path(path, options, &mut BuffersBuilder)
+ * (crates/tessellation/src/fill.rs:628-641), `Positions` vertices. Same conventions as above. */
+int lyon_gpu_fill_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                       const float* points, uint32_t num_points, const lyon_fill_options* options,
+                       int index_bits, uint32_t index_base, lyon_gpu_result* result);
+
+/* ----------------------------------------------------------------------------------------- */
+/* Batched, device-resident entry points (the `tessellate_paths` hot path).                   */
+/* All pointers are device pointers; work is queued on the context's stream and the call      */
+/* returns after the last kernel is queued, unless stated otherwise.                          */
+/* ----------------------------------------------------------------------------------------- */
+
+/* Output of a batched call: device buffers owned by the context (grown on demand, reused by
+ * the next batched call of the same kind), plus host-visible totals. */
+typedef struct lyon_gpu_batch_output {
+    float* vertices;            /* device, 2 * total_vertices floats */
+    void* indices;              /* device, total_indices u16/u32 */
+    lyon_path_range* ranges;    /* device, one per path */
+    int32_t* status;            /* device, one status per path */
+    uint64_t total_vertices;
+    uint64_t total_indices;
+    uint32_t num_failed_paths;  /* paths whose status is not LYON_OK */
+} lyon_gpu_batch_output;
+
+/* Batched `StrokeTessellator::tessellate_path` over every path of `batch`
+ * (crates/tessellation/src/stroke.rs:164-177 applied path by path; no lyon counterpart for the
+ * batching itself). `options` points to `num_options` records in device memory: 1 record shared
+ * by all paths, or one per path. `index_mode` is LYON_INDEX_GLOBAL or LYON_INDEX_PER_PATH.
+ * Runs the count kernel, the look-back scan and the emit kernel; synchronises once to read the
+ * totals (needed to size the output). */
+int lyon_gpu_stroke_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                          const lyon_stroke_options* options, uint32_t num_options,
+                          int index_bits, int index_mode, uint32_t vertex_offset,
+                          lyon_gpu_batch_output* out);
+
+/* Batched `FillTessellator::tessellate_path` (crates/tessellation/src/fill.rs:628-641 applied
+ * path by path). Same conventions as lyon_gpu_stroke_paths. */
+int lyon_gpu_fill_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                        const lyon_fill_options* options, uint32_t num_options, int index_bits,
+                        int index_mode, uint32_t vertex_offset, lyon_gpu_batch_output* out);
+
+/* Per-segment flattened point counts, as computed by `flattened_segments_wang` and the
+ * `to_u32` truncation of `for_each_flattened` (crates/geom/src/quadratic_bezier.rs:337-359,
+ * 943-974; crates/geom/src/cubic_bezier.rs:563-583, 1369-1403). One u32 per verb: lines give 1,
+ * quadratics and cubics their flattened segment count, Begin/Close/End give 0. Device pointers. */
+int lyon_gpu_flatten_counts(lyon_gpu_context* ctx, const lyon_path_batch* batch, float tolerance,
+                            uint32_t* counts);
+
+/* `path.iter().flattened(tolerance)` (crates/path/src/iterator.rs:125-215) for every path:
+ * writes the flattened polyline points (the `to` point of every Line event, in event order) and
+ * per-verb offsets into `out_points`. `out_offsets` has total_verbs + 1 entries (exclusive scan
+ * of the per-verb counts). The output buffers are owned by the context (device pointers). */
+int lyon_gpu_flatten_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch, float tolerance,
+                           float** out_points, uint32_t** out_offsets, uint64_t* total_points);
+
+/* Synchronise the context's stream. Returns LYON_OK or LYON_ERR_CUDA. */
+int lyon_gpu_synchronize(lyon_gpu_context* ctx);
+
+/* Library version and build information (static string). */
+const char* lyon_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LYON_GPU_H */

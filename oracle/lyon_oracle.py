@@ -1,0 +1,196 @@
+"""ctypes binding of the oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle is a CPU restatement of lyon's flattening, stroke and fill tessellators
+(oracle/lyon_oracle.cpp). Only tests, `__graft_entry__.smoke()` and the CPU-baseline leg of
+`bench.py` use it, as the checker; the product never imports this module.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblyon_oracle.so")
+
+_lib = None
+_lock = threading.Lock()
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with its Makefile (g++ only, a few seconds)."""
+    if force or not os.path.exists(LIB_PATH) or (
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "lyon_oracle.cpp"))):
+        subprocess.check_call(["make", "-s", "-C", HERE], stdout=subprocess.DEVNULL)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB_PATH)
+            c_p = ctypes.c_void_p
+            L.lyon_oracle_out_new.restype = c_p
+            L.lyon_oracle_out_new.argtypes = [ctypes.c_int, ctypes.c_uint64]
+            L.lyon_oracle_out_free.argtypes = [c_p]
+            L.lyon_oracle_out_clear.argtypes = [c_p]
+            for n in ("num_vertices", "num_indices"):
+                f = getattr(L, "lyon_oracle_out_" + n)
+                f.restype = ctypes.c_uint64
+                f.argtypes = [c_p]
+            L.lyon_oracle_out_vertices.restype = ctypes.POINTER(ctypes.c_float)
+            L.lyon_oracle_out_vertices.argtypes = [c_p]
+            L.lyon_oracle_out_indices32.restype = ctypes.POINTER(ctypes.c_uint32)
+            L.lyon_oracle_out_indices32.argtypes = [c_p]
+            L.lyon_oracle_out_near_ties.restype = ctypes.c_uint32
+            L.lyon_oracle_out_near_ties.argtypes = [c_p]
+            for n in ("stroke", "fill"):
+                f = getattr(L, f"lyon_oracle_{n}_path")
+                f.restype = ctypes.c_int
+                f.argtypes = [c_p, c_p, ctypes.c_uint32, c_p, ctypes.c_uint32, c_p]
+            L.lyon_oracle_flatten_path.restype = ctypes.c_uint64
+            L.lyon_oracle_flatten_path.argtypes = [c_p, ctypes.c_uint32, c_p, ctypes.c_uint32,
+                                                   ctypes.c_float, c_p, c_p, ctypes.c_uint64]
+            L.lyon_oracle_wang.restype = ctypes.c_float
+            L.lyon_oracle_wang.argtypes = [c_p, ctypes.c_int, ctypes.c_float]
+            L.lyon_oracle_batch.restype = ctypes.c_int
+            L.lyon_oracle_batch.argtypes = [ctypes.c_int, c_p, c_p, ctypes.c_uint32, ctypes.c_int,
+                                            ctypes.c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
+            _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
+
+
+class Result:
+    """Output of one oracle call: positions, indices (u32 VertexId values), status."""
+
+    def __init__(self, status, vertices, indices, near_ties, index_bits):
+        self.status = status
+        self.vertices = vertices
+        self.indices = indices if index_bits == 32 else indices.astype(np.uint16)
+        self.indices32 = indices
+        self.near_ties = near_ties
+
+    @property
+    def num_triangles(self):
+        return len(self.indices) // 3
+
+
+class Output:
+    """A VertexBuffers + BuffersBuilder pair on the oracle side (append semantics)."""
+
+    def __init__(self, index_bits: int = 32, vertex_offset: int = 0):
+        self.L = lib()
+        self.h = self.L.lyon_oracle_out_new(index_bits, vertex_offset)
+        self.index_bits = index_bits
+
+    def __del__(self):
+        try:
+            self.L.lyon_oracle_out_free(self.h)
+        except Exception:
+            pass
+
+    def clear(self):
+        self.L.lyon_oracle_out_clear(self.h)
+
+    def snapshot(self, status) -> Result:
+        nv = self.L.lyon_oracle_out_num_vertices(self.h)
+        ni = self.L.lyon_oracle_out_num_indices(self.h)
+        v = np.ctypeslib.as_array(self.L.lyon_oracle_out_vertices(self.h), shape=(nv * 2,)).copy() \
+            if nv else np.zeros(0, np.float32)
+        i = np.ctypeslib.as_array(self.L.lyon_oracle_out_indices32(self.h), shape=(ni,)).copy() \
+            if ni else np.zeros(0, np.uint32)
+        return Result(status, v.reshape(-1, 2), i, self.L.lyon_oracle_out_near_ties(self.h),
+                      self.index_bits)
+
+    def stroke(self, path, options):
+        o = options.to_c()
+        v = np.ascontiguousarray(path.verbs, dtype=np.uint8)
+        p = np.ascontiguousarray(path.points, dtype=np.float32)
+        return self.L.lyon_oracle_stroke_path(self.h, _ptr(v), len(v), _ptr(p), len(p),
+                                              ctypes.byref(o))
+
+    def fill(self, path, options):
+        o = options.to_c()
+        v = np.ascontiguousarray(path.verbs, dtype=np.uint8)
+        p = np.ascontiguousarray(path.points, dtype=np.float32)
+        return self.L.lyon_oracle_fill_path(self.h, _ptr(v), len(v), _ptr(p), len(p),
+                                            ctypes.byref(o))
+
+
+def stroke(path, options, index_bits: int = 32, vertex_offset: int = 0) -> Result:
+    out = Output(index_bits, vertex_offset)
+    st = out.stroke(path, options)
+    return out.snapshot(st)
+
+
+def fill(path, options, index_bits: int = 32, vertex_offset: int = 0) -> Result:
+    out = Output(index_bits, vertex_offset)
+    st = out.fill(path, options)
+    return out.snapshot(st)
+
+
+def flatten(path, tolerance: float):
+    """path.iter().flattened(tol): (per-verb counts, points)."""
+    L = lib()
+    v = np.ascontiguousarray(path.verbs, dtype=np.uint8)
+    p = np.ascontiguousarray(path.points, dtype=np.float32)
+    counts = np.zeros(max(len(v), 1), dtype=np.uint32)
+    n = L.lyon_oracle_flatten_path(_ptr(v), len(v), _ptr(p), len(p), tolerance, _ptr(counts),
+                                   None, 0)
+    pts = np.zeros((max(n, 1), 2), dtype=np.float32)
+    L.lyon_oracle_flatten_path(_ptr(v), len(v), _ptr(p), len(p), tolerance, _ptr(counts),
+                               _ptr(pts), n)
+    return counts[:len(v)], pts[:n]
+
+
+def wang(points, tolerance: float) -> float:
+    a = np.ascontiguousarray(np.asarray(points, dtype=np.float32).reshape(-1))
+    return float(lib().lyon_oracle_wang(_ptr(a), len(a) // 2, tolerance))
+
+
+class _CBatch(ctypes.Structure):
+    _fields_ = [("verbs", ctypes.c_void_p), ("points", ctypes.c_void_p),
+                ("verb_offsets", ctypes.c_void_p), ("point_offsets", ctypes.c_void_p),
+                ("num_paths", ctypes.c_uint32)]
+
+
+def batch(kind: str, pb, options_records: np.ndarray, index_bits: int = 32,
+          num_threads: int = 1, want_output: bool = True):
+    """Tessellates every path of a PathBatch with the oracle (per-path buffers).
+
+    Returns dict with per-path vertex/index counts, statuses, near-tie counts and, when
+    `want_output`, the concatenated outputs with per-path offsets."""
+    L = lib()
+    n = pb.num_paths
+    cb = _CBatch(_ptr(pb.verbs), _ptr(pb.points), _ptr(pb.verb_offsets),
+                 _ptr(pb.point_offsets), n)
+    opts = np.ascontiguousarray(options_records)
+    vc = np.zeros(n, np.uint32)
+    ic = np.zeros(n, np.uint32)
+    st = np.zeros(n, np.int32)
+    nt = np.zeros(n, np.uint32)
+    k = 0 if kind == "stroke" else 1
+    L.lyon_oracle_batch(k, ctypes.byref(cb), _ptr(opts), len(opts), index_bits, num_threads,
+                        _ptr(vc), _ptr(ic), _ptr(st), _ptr(nt), None, None, None, None)
+    res = {"vtx_counts": vc, "idx_counts": ic, "status": st, "near_ties": nt}
+    if want_output:
+        vo = np.zeros(n + 1, np.uint64)
+        io = np.zeros(n + 1, np.uint64)
+        vo[1:] = np.cumsum(vc, dtype=np.uint64)
+        io[1:] = np.cumsum(ic, dtype=np.uint64)
+        verts = np.zeros((int(vo[-1]), 2), np.float32)
+        idx = np.zeros(int(io[-1]), np.uint32)
+        L.lyon_oracle_batch(k, ctypes.byref(cb), _ptr(opts), len(opts), index_bits, num_threads,
+                            None, None, None, None, _ptr(verts), _ptr(idx), _ptr(vo), _ptr(io))
+        res.update(vertices=verts, indices=idx, vtx_offsets=vo, idx_offsets=io)
+    return res

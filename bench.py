@@ -1,0 +1,379 @@
+"""Benchmark: output vertices/s of batched stroke tessellation on one GB300 (per GPU replica).
+
+Workload (default): 1,000,000 stroke paths, log-normal segment counts (median 12, sigma 1,
+clamped to 1..4096), a third each of lines, quadratics and cubics, f32 points uniform in
+[0, 1024]^2, half of the paths closed, round joins and caps, tolerance 0.05, per-path widths
+uniform in [0.5, 8], u32 indices in one global index space; seeded synthetic data.
+
+One step = one `lyon_gpu_stroke_paths` call (count kernel, index-range check, look-back scan,
+emit kernel) over the whole batch. `value` times K steps with inputs resident in HBM; `e2e`
+times the C ABI call with host buffers (`lyon_gpu_stroke_paths_host`: inputs copied in, every
+output byte copied back to host memory). The roofline is taken for the emit kernel from CUDA
+events the library records around it on its stream. The CPU baseline is the oracle (the C++
+restatement of lyon's stroker) on a bounded sample with all host threads.
+
+Usage: python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--paths P]
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "output vertices/s"
+UNIT = "vertices/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--paths", type=int, default=1_000_000)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=100_000)
+    ap.add_argument("--profile", action="store_true",
+                    help="only run the warm-up and timed device steps (for profilers)")
+    return ap.parse_args()
+
+
+def workload_config(n_paths: int) -> dict:
+    return {
+        "workload": f"batched_stroke_{n_paths}_paths",
+        "paths": n_paths,
+        "segments": "lognormal(median 12, sigma 1.0), clamp 1..4096; 1/3 line, quad, cubic",
+        "coordinates": "f32 uniform [0,1024]^2, 50% closed",
+        "join": "round", "caps": "round", "tolerance": 0.05, "line_width": "U[0.5, 8] per path",
+        "index_bits": 32, "index_mode": "global",
+        "l2": "no flush: inputs (~0.5 GB) and outputs (~52 GB) exceed the 129 MB L2",
+        "seed": 2,
+    }
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:  # noqa: BLE001
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:  # noqa: BLE001
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001
+        return 6800.0, "fallback"
+
+
+def profiled_traffic_per_vertex():
+    """DRAM bytes per output vertex of the emit kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "stroke_emit_batched_stroke.md")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_output_vertex:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(batch, opts, sample_paths: int):
+    """The oracle on a bounded sample, all host threads."""
+    from oracle import lyon_oracle as orc
+    n = min(sample_paths, batch.num_paths)
+    sub = batch.subset(range(n))
+    sub_opts = opts[:n] if len(opts) > 1 else opts
+    threads = os.cpu_count() or 1
+    orc.batch("stroke", sub.subset(range(min(n, 2000))),
+              sub_opts[:min(n, 2000)] if len(sub_opts) > 1 else sub_opts, 32, threads, False)
+    t0 = time.perf_counter()
+    r = orc.batch("stroke", sub, sub_opts, 32, threads, want_output=False)
+    dt = time.perf_counter() - t0
+    verts = int(r["vtx_counts"].sum())
+    return {"value": verts / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {n} paths of the workload, {verts} output vertices, "
+                      f"{dt:.2f} s wall on {threads} threads"}
+
+
+def run_reference(args):
+    """The reference arm: lyon's algorithm on the host cores (the oracle port: lyon itself is
+    Rust and has no toolchain on this machine), each step a bounded sample of the workload."""
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    from lyon_gb300 import workloads
+    from oracle import lyon_oracle as orc
+    sample = min(args.paths, 100_000)
+    batch, opts = workloads.batched_stroke(args.paths, seed=2)
+    sub = batch.subset(range(sample))
+    sub_opts = opts[:sample]
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        orc.batch("stroke", sub.subset(range(min(sample, 5000))), sub_opts[:min(sample, 5000)],
+                  32, threads, want_output=False)
+    verts = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = orc.batch("stroke", sub, sub_opts, 32, threads, want_output=False)
+        verts += int(r["vtx_counts"].sum())
+    dt = time.perf_counter() - t0
+    value = verts / dt
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": workload_config(args.paths),
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"first {sample} paths of the workload per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    from lyon_gb300 import _native, workloads
+    from lyon_gb300 import tessellation as T
+
+    rank, world, local = dist_info()
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    batch, opts = workloads.batched_stroke(args.paths, seed=2)
+    ctx = T.Context(dev)
+    lib = ctx.lib
+    db = T.DeviceBatch.upload(batch, dev)
+    od = T.upload_options(opts, dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", dev))
+    lib.lyon_gpu_set_timing(ctx.h, 1)
+
+    def step():
+        return T.tessellate_paths("stroke", db, od, len(opts), 32, T.INDEX_GLOBAL, 0, ctx)
+
+    for _ in range(args.warmup):
+        res = step()
+    ctx.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    emit_ms = []
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clocks:
+        start.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = step()
+            ms4 = (ctypes.c_float * 4)()
+            lib.lyon_gpu_last_timings(ctx.h, ms4)
+            emit_ms.append(ms4[2])
+        end.record(stream)
+        end.synchronize()
+        wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    elapsed_ms = start.elapsed_time(end)
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    verts_per_step = res.total_vertices
+    idx_per_step = res.total_indices
+    ms_per_step = elapsed_ms / args.steps
+    value = verts_per_step * world / (ms_per_step / 1e3)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_ms_per_step": ms_per_step, "vertices": verts_per_step}))
+        return 0
+
+    # Roofline of the emit kernel: algorithmic bytes / its event-timed duration.
+    n = batch.num_paths
+    in_bytes = batch.input_bytes(options_bytes_per_path=24)
+    out_bytes = verts_per_step * 8 + idx_per_step * 4 + 16 * n
+    emit_s = statistics.median(emit_ms) / 1e3
+    achieved = (in_bytes + out_bytes) / emit_s / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    tpv = profiled_traffic_per_vertex()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": (tpv * verts_per_step) if tpv is not None else None,
+                "kernel": "stroke_kernel<true> (emit)",
+                "algorithmic_bytes": in_bytes + out_bytes,
+                "emit_ms": emit_s * 1e3}
+
+    # End to end through the C ABI with host buffers.
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(lib, ctx, batch, opts, verts_per_step, idx_per_step, args, T, _native)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": workload_config(args.paths),
+        "roofline": roofline, "clocks": clocks.summary(),
+        "gpu_launches": 4 * args.steps,
+        "wall_ms_per_step": wall / args.steps * 1e3,
+        "output_vertices_per_step": verts_per_step, "output_indices_per_step": idx_per_step,
+    }
+    if e2e is not None:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(batch, opts, args.cpu_sample)
+    if rank == 0:
+        line["plain_per_path"] = plain_per_path(ctx, batch, opts, T)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+def plain_per_path(ctx, batch, opts, T, count: int = 300):
+    """The plain per-path GPU launch: lyon_gpu_stroke_path per path (host in, host out)."""
+    from lyon_gb300.options import StrokeOptions
+    st = T.StrokeTessellator(ctx)
+    verts = 0
+    buf = T.VertexBuffers(32)
+    t0 = time.perf_counter()
+    for p in range(count):
+        o = opts[p]
+        so = StrokeOptions(int(o["start_cap"]), int(o["end_cap"]), int(o["line_join"]),
+                           float(o["line_width"]), float(o["miter_limit"]), float(o["tolerance"]))
+        buf.clear()
+        st.tessellate_path(batch.path(p), so, T.BuffersBuilder(buf))
+        verts += len(buf.vertices)
+    dt = time.perf_counter() - t0
+    return {"value": verts / dt, "unit": UNIT, "paths": count, "us_per_path": dt / count * 1e6}
+
+
+def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
+    """Times lyon_gpu_stroke_paths_host: host inputs, host outputs (every byte)."""
+    import torch
+    try:
+        hv = torch.empty(int(tv) * 2, dtype=torch.float32, pin_memory=True)
+        hi = torch.empty(int(ti), dtype=torch.int32, pin_memory=True)
+        vptr, iptr = hv.data_ptr(), hi.data_ptr()
+        host_kind = "pinned"
+    except Exception:  # noqa: BLE001
+        hvn = np.empty(int(tv) * 2, np.float32)
+        hin = np.empty(int(ti), np.uint32)
+        vptr, iptr = hvn.ctypes.data, hin.ctypes.data
+        host_kind = "pageable"
+    verbs = np.ascontiguousarray(batch.verbs)
+    pts = np.ascontiguousarray(batch.points)
+    vo = np.ascontiguousarray(batch.verb_offsets)
+    po = np.ascontiguousarray(batch.point_offsets)
+    hb = _native.CPathBatch(verbs.ctypes.data, pts.ctypes.data, vo.ctypes.data, po.ctypes.data,
+                            batch.num_paths)
+    oh = np.ascontiguousarray(opts)
+    status = np.zeros(batch.num_paths, np.int32)
+    tvo = ctypes.c_uint64()
+    tio = ctypes.c_uint64()
+
+    def call():
+        r = lib.lyon_gpu_stroke_paths_host(ctx.h, ctypes.byref(hb), oh.ctypes.data, len(oh), 32,
+                                           T.INDEX_GLOBAL, 0, vptr, tv, iptr, ti,
+                                           status.ctypes.data, ctypes.byref(tvo),
+                                           ctypes.byref(tio))
+        if r != 0:
+            raise RuntimeError(f"lyon_gpu_stroke_paths_host: {r} {ctx.last_error()}")
+
+    lib.lyon_gpu_set_timing(ctx.h, 0)
+    call()
+    steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        call()
+    dt = (time.perf_counter() - t0) / steps
+    h2d = batch.input_bytes(options_bytes_per_path=24)
+    d2h = int(tv) * 8 + int(ti) * 4 + batch.num_paths * 4
+    return {"value": int(tvo.value) / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3, "steps": steps,
+            "host_buffers": host_kind}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -110,14 +110,6 @@ typedef struct lyon_path_batch {
     uint32_t num_paths;
 } lyon_path_batch;
 
-/* Per-path output record written by batched calls (device memory). */
-typedef struct lyon_path_range {
-    uint32_t first_vertex;   /* offset of the path's first vertex in the vertex buffer */
-    uint32_t num_vertices;
-    uint32_t first_index;    /* offset of the path's first index in the index buffer */
-    uint32_t num_indices;
-} lyon_path_range;
-
 typedef struct lyon_gpu_context lyon_gpu_context;
 
 /* Creates a context on the given CUDA device: a stream, device scratch arenas that grow on
@@ -175,7 +167,9 @@ int lyon_gpu_fill_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num
 typedef struct lyon_gpu_batch_output {
     float* vertices;            /* device, 2 * total_vertices floats */
     void* indices;              /* device, total_indices u16/u32 */
-    lyon_path_range* ranges;    /* device, one per path */
+    uint64_t* vertex_offsets;   /* device, num_paths + 1: first vertex of each path (exclusive
+                                   scan of the per-path vertex counts; the last entry is the total) */
+    uint64_t* index_offsets;    /* device, num_paths + 1: same for indices */
     int32_t* status;            /* device, one status per path */
     uint64_t total_vertices;
     uint64_t total_indices;
@@ -212,6 +206,36 @@ int lyon_gpu_flatten_counts(lyon_gpu_context* ctx, const lyon_path_batch* batch,
  * of the per-verb counts). The output buffers are owned by the context (device pointers). */
 int lyon_gpu_flatten_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch, float tolerance,
                            float** out_points, uint32_t** out_offsets, uint64_t* total_points);
+
+/* Batched stroke with HOST buffers (the end-to-end form of lyon_gpu_stroke_paths): the batch
+ * and options live in host memory, outputs are written to host memory. The call processes the
+ * paths in chunks, overlapping each chunk's host->device copy, kernels and device->host copy with
+ * its neighbours', and returns when every output byte is on the host. `vertices`/`indices` must
+ * hold `vertex_capacity` vertices and `index_capacity` indices; if they are too small the call
+ * returns LYON_ERR_CAPACITY after setting *total_vertices / *total_indices to the sizes needed.
+ * `status` (host, num_paths entries) receives the per-path status and may be NULL.
+ * Index semantics are those of lyon_gpu_stroke_paths. No lyon counterpart (batching). */
+int lyon_gpu_stroke_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                               const lyon_stroke_options* options, uint32_t num_options,
+                               int index_bits, int index_mode, uint32_t vertex_offset,
+                               float* vertices, uint64_t vertex_capacity, void* indices,
+                               uint64_t index_capacity, int32_t* status,
+                               uint64_t* total_vertices, uint64_t* total_indices);
+
+/* Batched fill with host buffers; same conventions as lyon_gpu_stroke_paths_host. */
+int lyon_gpu_fill_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                             const lyon_fill_options* options, uint32_t num_options,
+                             int index_bits, int index_mode, uint32_t vertex_offset,
+                             float* vertices, uint64_t vertex_capacity, void* indices,
+                             uint64_t index_capacity, int32_t* status, uint64_t* total_vertices,
+                             uint64_t* total_indices);
+
+/* Kernel timing: when enabled, batched calls record CUDA events around their count, scan and
+ * emit phases on the context's stream; lyon_gpu_last_timings returns the durations (ms) of the
+ * last batched call: [0] count kernel, [1] scan (+ index-range check), [2] emit kernel,
+ * [3] whole call. */
+void lyon_gpu_set_timing(lyon_gpu_context* ctx, int enabled);
+int lyon_gpu_last_timings(lyon_gpu_context* ctx, float* ms4);
 
 /* Synchronise the context's stream. Returns LYON_OK or LYON_ERR_CUDA. */
 int lyon_gpu_synchronize(lyon_gpu_context* ctx);

@@ -1,0 +1,110 @@
+"""ctypes binding of liblyon_gb300.so (C ABI in include/lyon_gpu.h).
+
+The library is the only compute path: when it is missing or no CUDA device is present, loading
+raises instead of falling back to anything else.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lib = None
+_lock = threading.Lock()
+
+c_p = ctypes.c_void_p
+u32 = ctypes.c_uint32
+u64 = ctypes.c_uint64
+i32 = ctypes.c_int32
+
+
+class CPathBatch(ctypes.Structure):
+    _fields_ = [("verbs", c_p), ("points", c_p), ("verb_offsets", c_p),
+                ("point_offsets", c_p), ("num_paths", u32)]
+
+
+class CResult(ctypes.Structure):
+    _fields_ = [("vertices", c_p), ("num_vertices", u32), ("indices", c_p),
+                ("num_indices", u32), ("status", i32)]
+
+
+class CBatchOutput(ctypes.Structure):
+    _fields_ = [("vertices", c_p), ("indices", c_p), ("vertex_offsets", c_p),
+                ("index_offsets", c_p), ("status", c_p),
+                ("total_vertices", u64), ("total_indices", u64), ("num_failed_paths", u32)]
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Loads the CUDA library, building it first when nvcc is available and it is stale."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = os.environ.get("LYON_GB300_LIB") or _build.LIB_PATH
+        if path == _build.LIB_PATH and build_if_missing and not _build.up_to_date():
+            try:
+                _build.build()
+            except Exception as e:  # noqa: BLE001
+                if not os.path.exists(path):
+                    raise NativeLibraryMissing(f"cannot build {path}: {e}") from e
+        if not os.path.exists(path):
+            raise NativeLibraryMissing(f"{path} is missing; run lyon_gb300.build.build()")
+        L = ctypes.CDLL(path)
+        L.lyon_gpu_version.restype = ctypes.c_char_p
+        L.lyon_gpu_create.restype = c_p
+        L.lyon_gpu_create.argtypes = [ctypes.c_int]
+        L.lyon_gpu_destroy.argtypes = [c_p]
+        L.lyon_gpu_stream.restype = c_p
+        L.lyon_gpu_stream.argtypes = [c_p]
+        L.lyon_gpu_last_error.restype = ctypes.c_char_p
+        L.lyon_gpu_last_error.argtypes = [c_p]
+        L.lyon_gpu_synchronize.restype = ctypes.c_int
+        L.lyon_gpu_synchronize.argtypes = [c_p]
+        for name in ("lyon_gpu_stroke_path", "lyon_gpu_fill_path"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [c_p, c_p, u32, c_p, u32, c_p, ctypes.c_int, u32,
+                          ctypes.POINTER(CResult)]
+        for name in ("lyon_gpu_stroke_paths", "lyon_gpu_fill_paths"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, ctypes.c_int, ctypes.c_int,
+                          u32, ctypes.POINTER(CBatchOutput)]
+        for name in ("lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, ctypes.c_int, ctypes.c_int,
+                          u32, c_p, u64, c_p, u64, c_p, ctypes.POINTER(u64), ctypes.POINTER(u64)]
+        L.lyon_gpu_set_timing.argtypes = [c_p, ctypes.c_int]
+        L.lyon_gpu_last_timings.restype = ctypes.c_int
+        L.lyon_gpu_last_timings.argtypes = [c_p, ctypes.POINTER(ctypes.c_float)]
+        L.lyon_gpu_flatten_counts.restype = ctypes.c_int
+        L.lyon_gpu_flatten_counts.argtypes = [c_p, ctypes.POINTER(CPathBatch), ctypes.c_float,
+                                              c_p]
+        L.lyon_gpu_flatten_paths.restype = ctypes.c_int
+        L.lyon_gpu_flatten_paths.argtypes = [c_p, ctypes.POINTER(CPathBatch), ctypes.c_float,
+                                             ctypes.POINTER(c_p), ctypes.POINTER(c_p),
+                                             ctypes.POINTER(u64)]
+        _lib = L
+        return L
+
+
+# Symbols that include/lyon_gpu.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "lyon_gpu_create", "lyon_gpu_destroy", "lyon_gpu_stream", "lyon_gpu_last_error",
+    "lyon_gpu_stroke_path", "lyon_gpu_fill_path", "lyon_gpu_stroke_paths", "lyon_gpu_fill_paths",
+    "lyon_gpu_flatten_counts", "lyon_gpu_flatten_paths", "lyon_gpu_synchronize",
+    "lyon_gpu_version", "lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host",
+    "lyon_gpu_set_timing", "lyon_gpu_last_timings",
+]

@@ -1,0 +1,763 @@
+// api.cu — the C ABI of liblyon_gb300.so (declarations and reference citations in
+// include/lyon_gpu.h): contexts, device arenas, the batched pipelines (device and host buffers)
+// and the single-path drop-ins.
+//
+// Every batched call is count -> index-range policy -> look-back scan -> (one host read of the
+// totals) -> emit. The host-buffer form runs that pipeline per chunk of paths and overlaps each
+// chunk's device->host copy (second stream) with the next chunk's kernels.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "kernels_flatten.h"
+#include "fill.h"
+
+namespace {
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t cap = 0;
+};
+
+struct HostBuf {
+    void* ptr = nullptr;
+    size_t cap = 0;
+};
+
+enum Kind { KIND_STROKE = 0, KIND_FILL = 1 };
+
+}  // namespace
+
+struct lyon_gpu_context {
+    int device = 0;
+    int num_sms = 1;
+    int stroke_bps = 1;
+    cudaStream_t stream = nullptr;       // kernels
+    cudaStream_t copy_stream = nullptr;  // device->host copies of the host-buffer calls
+    std::string last_error;
+    // per-path work arrays
+    DevBuf vtx_counts, idx_counts, status, vtx_offsets, idx_offsets, scan_state;
+    DevBuf small;  // [0] work counter, [1] scan counter, [2] error flag, [3] failed paths
+    // outputs of device-buffer batched calls
+    DevBuf out_vertices, out_indices;
+    // host-buffer calls: inputs and double-buffered outputs
+    DevBuf h_in_verbs, h_in_points, h_in_voff, h_in_poff, h_in_opts;
+    DevBuf slot_v[2], slot_i[2];
+    cudaEvent_t slot_done[2] = {nullptr, nullptr};
+    cudaEvent_t emitted = nullptr;
+    // fill scratch / staging
+    lg::FillBuffers fill;
+    // flatten outputs
+    DevBuf flat_counts, flat_offsets, flat_points;
+    // single-path staging
+    DevBuf in_verbs, in_points, in_offsets, in_options;
+    HostBuf h_verbs, h_points, h_out_v, h_out_i, h_small, h_offs;
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float last_ms[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+const char* kVersion = "lyon_gb300 0.1 (sm_103a)";
+
+bool set_err(lyon_gpu_context* ctx, const char* what, cudaError_t e) {
+    if (e == cudaSuccess) return true;
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    ctx->last_error = buf;
+    return false;
+}
+
+bool ensure(lyon_gpu_context* ctx, DevBuf& b, size_t bytes) {
+    if (bytes <= b.cap && b.ptr) return true;
+    if (b.ptr) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaFree(b.ptr);
+        b.ptr = nullptr;
+        b.cap = 0;
+    }
+    size_t cap = bytes < 256 ? 256 : bytes + bytes / 8;
+    cudaError_t e = cudaMalloc(&b.ptr, cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_err(ctx, "cudaMalloc", e);
+        return false;
+    }
+    b.cap = cap;
+    return true;
+}
+
+bool ensure_host(lyon_gpu_context* ctx, HostBuf& b, size_t bytes) {
+    if (bytes <= b.cap && b.ptr) return true;
+    if (b.ptr) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFreeHost(b.ptr);
+        b.ptr = nullptr;
+        b.cap = 0;
+    }
+    size_t cap = bytes < 4096 ? 4096 : bytes + bytes / 4;
+    cudaError_t e = cudaMallocHost(&b.ptr, cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_err(ctx, "cudaMallocHost", e);
+        return false;
+    }
+    b.cap = cap;
+    return true;
+}
+
+template <class T>
+T* as(DevBuf& b) {
+    return reinterpret_cast<T*>(b.ptr);
+}
+
+uint64_t max_index_for(int bits) { return bits == 16 ? 65535ull : 0xFFFFFFFEull; }
+
+uint32_t* small_words(lyon_gpu_context* ctx) { return as<uint32_t>(ctx->small); }
+
+void free_buf(DevBuf& b) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.cap = 0;
+}
+void free_host(HostBuf& b) {
+    if (b.ptr) cudaFreeHost(b.ptr);
+    b.ptr = nullptr;
+    b.cap = 0;
+}
+
+void mark(lyon_gpu_context* ctx, int i) {
+    if (ctx->timing) cudaEventRecord(ctx->ev[i], ctx->stream);
+}
+
+// Sequential index assignment for LYON_INDEX_GLOBAL when the batch overflows the index type:
+// BuffersBuilder semantics (geometry_builder.rs:338-350, 478-481) applied path by path, on the
+// host. Only taken when the parallel totals exceed the index range.
+bool global_overflow_fixup(lyon_gpu_context* ctx, uint32_t n, uint64_t vertex_offset,
+                           uint64_t max_index) {
+    std::vector<uint32_t> vc(n), ic(n);
+    std::vector<int32_t> st(n);
+    cudaStream_t s = ctx->stream;
+    if (!set_err(ctx, "D2H counts",
+                 cudaMemcpyAsync(vc.data(), ctx->vtx_counts.ptr, n * 4ull,
+                                 cudaMemcpyDeviceToHost, s)))
+        return false;
+    cudaMemcpyAsync(ic.data(), ctx->idx_counts.ptr, n * 4ull, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(st.data(), ctx->status.ptr, n * 4ull, cudaMemcpyDeviceToHost, s);
+    if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return false;
+    uint64_t len = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (st[i] != LYON_OK) continue;
+        if (vc[i] > 0 && vertex_offset + len + vc[i] - 1 > max_index) {
+            st[i] = LYON_ERR_TOO_MANY_VERTICES;
+            vc[i] = 0;
+            ic[i] = 0;
+            continue;
+        }
+        len += vc[i];
+    }
+    cudaMemcpyAsync(ctx->vtx_counts.ptr, vc.data(), n * 4ull, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ctx->idx_counts.ptr, ic.data(), n * 4ull, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ctx->status.ptr, st.data(), n * 4ull, cudaMemcpyHostToDevice, s);
+    return set_err(ctx, "sync", cudaStreamSynchronize(s));
+}
+
+bool alloc_path_arrays(lyon_gpu_context* ctx, uint32_t n) {
+    return ensure(ctx, ctx->vtx_counts, (size_t)n * 4 + 4) &&
+           ensure(ctx, ctx->idx_counts, (size_t)n * 4 + 4) &&
+           ensure(ctx, ctx->status, (size_t)n * 4 + 4) &&
+           ensure(ctx, ctx->vtx_offsets, ((size_t)n + 1) * 8) &&
+           ensure(ctx, ctx->idx_offsets, ((size_t)n + 1) * 8) &&
+           ensure(ctx, ctx->scan_state, 2 * lg::scan_tile_count(n) * 8 + 16);
+}
+
+// Index-range policy + scan + totals. On return the offsets are valid and *tv / *ti hold the
+// totals (one host synchronisation).
+bool finish_counts(lyon_gpu_context* ctx, uint32_t n, int index_bits, int index_mode,
+                   uint64_t vertex_offset, uint64_t* tv, uint64_t* ti, uint32_t* failed) {
+    cudaStream_t s = ctx->stream;
+    uint32_t* sw = small_words(ctx);
+    uint64_t maxi = max_index_for(index_bits);
+    cudaMemsetAsync(sw + 2, 0, 8, s);
+    // Per-path mode applies the index range per path; the global mode only counts failures.
+    if (!set_err(ctx, "per-path limit",
+                 lg::launch_per_path_limit(
+                     as<uint32_t>(ctx->vtx_counts), as<uint32_t>(ctx->idx_counts),
+                     as<int32_t>(ctx->status), n, vertex_offset,
+                     index_mode == LYON_INDEX_PER_PATH ? maxi : ~0ull, sw + 3, s)))
+        return false;
+    for (int pass = 0; pass < 2; ++pass) {
+        if (!set_err(ctx, "scan",
+                     lg::launch_scan_pairs(as<uint32_t>(ctx->vtx_counts),
+                                           as<uint32_t>(ctx->idx_counts),
+                                           as<uint64_t>(ctx->vtx_offsets),
+                                           as<uint64_t>(ctx->idx_offsets), n,
+                                           as<unsigned long long>(ctx->scan_state), sw + 1,
+                                           reinterpret_cast<int*>(sw + 2), s)))
+            return false;
+        if (!ensure_host(ctx, ctx->h_small, 64)) return false;
+        uint64_t* hs = reinterpret_cast<uint64_t*>(ctx->h_small.ptr);
+        cudaMemcpyAsync(hs, as<uint64_t>(ctx->vtx_offsets) + n, 8, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hs + 1, as<uint64_t>(ctx->idx_offsets) + n, 8, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hs + 2, sw + 2, 8, cudaMemcpyDeviceToHost, s);
+        if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return false;
+        *tv = hs[0];
+        *ti = hs[1];
+        uint32_t* hw = reinterpret_cast<uint32_t*>(hs + 2);
+        if (hw[0] != 0) {
+            ctx->last_error = "scan look-back wait exceeded its bound";
+            return false;
+        }
+        *failed = hw[1];
+        if (index_mode == LYON_INDEX_GLOBAL && *tv > 0 && vertex_offset + *tv - 1 > maxi &&
+            pass == 0) {
+            if (!global_overflow_fixup(ctx, n, vertex_offset, maxi)) return false;
+            cudaMemsetAsync(sw + 2, 0, 8, s);
+            if (!set_err(ctx, "count failures",
+                         lg::launch_per_path_limit(as<uint32_t>(ctx->vtx_counts),
+                                                   as<uint32_t>(ctx->idx_counts),
+                                                   as<int32_t>(ctx->status), n, vertex_offset,
+                                                   ~0ull, sw + 3, s)))
+                return false;
+            continue;
+        }
+        break;
+    }
+    return true;
+}
+
+bool valid_args(lyon_gpu_context* ctx, const lyon_path_batch* batch, const void* options,
+                uint32_t num_options, int index_bits, int index_mode) {
+    if (!ctx || !batch || !options || num_options == 0 || (index_bits != 16 && index_bits != 32) ||
+        (index_mode != LYON_INDEX_GLOBAL && index_mode != LYON_INDEX_PER_PATH) ||
+        (num_options != 1 && num_options != batch->num_paths)) {
+        if (ctx) ctx->last_error = "invalid argument";
+        return false;
+    }
+    return true;
+}
+
+lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                           const lyon_stroke_options* options, uint32_t num_options,
+                           int index_bits, int index_mode, uint64_t vertex_offset) {
+    lg::StrokeArgs a;
+    memset(&a, 0, sizeof a);
+    a.verbs = batch->verbs;
+    a.points = batch->points;
+    a.verb_offsets = batch->verb_offsets;
+    a.point_offsets = batch->point_offsets;
+    a.num_paths = batch->num_paths;
+    a.options = options;
+    a.num_options = num_options;
+    a.order = nullptr;
+    a.work_counter = small_words(ctx);
+    a.vtx_counts = as<uint32_t>(ctx->vtx_counts);
+    a.idx_counts = as<uint32_t>(ctx->idx_counts);
+    a.status = as<int32_t>(ctx->status);
+    a.index_bits = index_bits;
+    a.index_mode = index_mode;
+    a.vertex_offset = (uint32_t)vertex_offset;
+    a.vtx_offsets = as<uint64_t>(ctx->vtx_offsets);
+    a.idx_offsets = as<uint64_t>(ctx->idx_offsets);
+    return a;
+}
+
+int stroke_grid(lyon_gpu_context* ctx, uint32_t n) {
+    const int max_grid = ctx->num_sms * ctx->stroke_bps;
+    const int needed = (int)((n + 3) / 4);
+    return needed < max_grid ? (needed > 0 ? needed : 1) : max_grid;
+}
+
+// Count pass + scan for one device-resident batch.
+int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
+                   const void* options, uint32_t num_options, int index_bits, int index_mode,
+                   uint64_t vertex_offset, uint64_t* tv, uint64_t* ti, uint32_t* failed) {
+    const uint32_t n = batch->num_paths;
+    if (!alloc_path_arrays(ctx, n)) return LYON_ERR_OUT_OF_MEMORY;
+    cudaStream_t s = ctx->stream;
+    mark(ctx, 0);
+    if (kind == KIND_STROKE) {
+        lg::StrokeArgs a = stroke_args(ctx, batch, (const lyon_stroke_options*)options,
+                                       num_options, index_bits, index_mode, vertex_offset);
+        if (n > 0) {
+            cudaMemsetAsync(small_words(ctx), 0, 4, s);
+            if (!set_err(ctx, "stroke count", lg::launch_stroke(a, false, stroke_grid(ctx, n), s)))
+                return LYON_ERR_CUDA;
+        }
+    } else {
+        int r = lg::fill_count(ctx->fill, batch, (const lyon_fill_options*)options, num_options,
+                               ctx->num_sms, as<uint32_t>(ctx->vtx_counts),
+                               as<uint32_t>(ctx->idx_counts), as<int32_t>(ctx->status),
+                               small_words(ctx), s, &ctx->last_error);
+        if (r != LYON_OK) return r;
+    }
+    mark(ctx, 1);
+    if (!finish_counts(ctx, n, index_bits, index_mode, vertex_offset, tv, ti, failed))
+        return LYON_ERR_CUDA;
+    mark(ctx, 2);
+    return LYON_OK;
+}
+
+// Emit pass into caller-chosen device buffers (after pipeline_count on the same batch).
+int pipeline_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
+                  const void* options, uint32_t num_options, int index_bits, int index_mode,
+                  uint64_t vertex_offset, float* vout, void* iout, uint64_t tv) {
+    const uint32_t n = batch->num_paths;
+    cudaStream_t s = ctx->stream;
+    if (kind == KIND_STROKE) {
+        lg::StrokeArgs a = stroke_args(ctx, batch, (const lyon_stroke_options*)options,
+                                       num_options, index_bits, index_mode, vertex_offset);
+        a.vertices = vout;
+        a.indices = iout;
+        if (n > 0 && tv > 0) {
+            cudaMemsetAsync(small_words(ctx), 0, 4, s);
+            if (!set_err(ctx, "stroke emit", lg::launch_stroke(a, true, stroke_grid(ctx, n), s)))
+                return LYON_ERR_CUDA;
+        }
+    } else {
+        if (!set_err(ctx, "fill emit",
+                     lg::fill_emit(ctx->fill, n, as<uint32_t>(ctx->vtx_counts),
+                                   as<uint32_t>(ctx->idx_counts), as<int32_t>(ctx->status),
+                                   as<uint64_t>(ctx->vtx_offsets),
+                                   as<uint64_t>(ctx->idx_offsets), vout, iout, index_bits,
+                                   index_mode, (uint32_t)vertex_offset, s)))
+            return LYON_ERR_CUDA;
+    }
+    mark(ctx, 3);
+    if (ctx->timing) {
+        cudaEventSynchronize(ctx->ev[3]);
+        cudaEventElapsedTime(&ctx->last_ms[0], ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&ctx->last_ms[1], ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&ctx->last_ms[2], ctx->ev[2], ctx->ev[3]);
+        cudaEventElapsedTime(&ctx->last_ms[3], ctx->ev[0], ctx->ev[3]);
+    }
+    return LYON_OK;
+}
+
+int batched_device(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
+                   const void* options, uint32_t num_options, int index_bits, int index_mode,
+                   uint32_t vertex_offset, lyon_gpu_batch_output* out) {
+    if (!out || !valid_args(ctx, batch, options, num_options, index_bits, index_mode))
+        return LYON_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    memset(out, 0, sizeof(*out));
+    uint64_t tv = 0, ti = 0;
+    uint32_t failed = 0;
+    int r = pipeline_count(ctx, kind, batch, options, num_options, index_bits, index_mode,
+                           vertex_offset, &tv, &ti, &failed);
+    if (r != LYON_OK) return r;
+    if (!ensure(ctx, ctx->out_vertices, tv * 8 + 16) ||
+        !ensure(ctx, ctx->out_indices, ti * (index_bits / 8) + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    r = pipeline_emit(ctx, kind, batch, options, num_options, index_bits, index_mode,
+                      vertex_offset, as<float>(ctx->out_vertices), ctx->out_indices.ptr, tv);
+    if (r != LYON_OK) return r;
+    out->vertices = as<float>(ctx->out_vertices);
+    out->indices = ctx->out_indices.ptr;
+    out->vertex_offsets = as<uint64_t>(ctx->vtx_offsets);
+    out->index_offsets = as<uint64_t>(ctx->idx_offsets);
+    out->status = as<int32_t>(ctx->status);
+    out->total_vertices = tv;
+    out->total_indices = ti;
+    out->num_failed_paths = failed;
+    return LYON_OK;
+}
+
+// Host-buffer batched call: chunks of paths; inputs copied in, outputs copied out with the
+// copy of chunk c overlapping the kernels of chunk c + 1.
+int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, const void* hopts,
+                 size_t opt_size, uint32_t num_options, int index_bits, int index_mode,
+                 uint32_t vertex_offset, float* hv, uint64_t vcap, void* hi, uint64_t icap,
+                 int32_t* hstatus, uint64_t* total_v, uint64_t* total_i) {
+    if (!valid_args(ctx, hb, hopts, num_options, index_bits, index_mode))
+        return LYON_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    const uint32_t n = hb->num_paths;
+    const size_t isz = index_bits / 8;
+    // Chunks of at most CH paths and ~64 MB of points.
+    const uint32_t CH = 1u << 17;
+    uint64_t run_v = 0, run_i = 0;
+    bool capacity_ok = true;
+    int slot = 0;
+    uint32_t c0 = 0;
+    while (c0 < n || (n == 0 && c0 == 0)) {
+        uint32_t c1 = c0 + CH < n ? c0 + CH : n;
+        while (c1 > c0 + 1 &&
+               (uint64_t)(hb->point_offsets[c1] - hb->point_offsets[c0]) * 8 > (64ull << 20))
+            c1 = c0 + (c1 - c0) / 2;
+        const uint32_t cn = c1 - c0;
+        const uint32_t vb = hb->verb_offsets[c0], ve = hb->verb_offsets[c1];
+        const uint32_t pb = hb->point_offsets[c0], pe = hb->point_offsets[c1];
+        cudaStream_t s = ctx->stream;
+        // Inputs (offsets rebased on the host).
+        if (!ensure(ctx, ctx->h_in_verbs, (size_t)(ve - vb) + 16) ||
+            !ensure(ctx, ctx->h_in_points, (size_t)(pe - pb) * 8 + 16) ||
+            !ensure(ctx, ctx->h_in_voff, ((size_t)cn + 1) * 4) ||
+            !ensure(ctx, ctx->h_in_poff, ((size_t)cn + 1) * 4) ||
+            !ensure(ctx, ctx->h_in_opts, (num_options > 1 ? (size_t)cn : 1) * opt_size) ||
+            !ensure_host(ctx, ctx->h_offs, ((size_t)cn + 1) * 8))
+            return LYON_ERR_OUT_OF_MEMORY;
+        // The host staging of offsets is reused per chunk: wait for its previous copy.
+        cudaStreamSynchronize(s);
+        uint32_t* ho = reinterpret_cast<uint32_t*>(ctx->h_offs.ptr);
+        for (uint32_t i = 0; i <= cn; ++i) {
+            ho[i] = hb->verb_offsets[c0 + i] - vb;
+            ho[cn + 1 + i] = hb->point_offsets[c0 + i] - pb;
+        }
+        cudaMemcpyAsync(ctx->h_in_voff.ptr, ho, ((size_t)cn + 1) * 4, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(ctx->h_in_poff.ptr, ho + cn + 1, ((size_t)cn + 1) * 4,
+                        cudaMemcpyHostToDevice, s);
+        if (ve > vb)
+            cudaMemcpyAsync(ctx->h_in_verbs.ptr, hb->verbs + vb, ve - vb, cudaMemcpyHostToDevice, s);
+        if (pe > pb)
+            cudaMemcpyAsync(ctx->h_in_points.ptr, hb->points + 2 * (size_t)pb, (size_t)(pe - pb) * 8,
+                            cudaMemcpyHostToDevice, s);
+        const unsigned char* op = reinterpret_cast<const unsigned char*>(hopts);
+        size_t ob = (num_options > 1 ? (size_t)cn : 1) * opt_size;
+        cudaMemcpyAsync(ctx->h_in_opts.ptr, op + (num_options > 1 ? (size_t)c0 * opt_size : 0), ob,
+                        cudaMemcpyHostToDevice, s);
+        lyon_path_batch db;
+        db.verbs = as<uint8_t>(ctx->h_in_verbs);
+        db.points = as<float>(ctx->h_in_points);
+        db.verb_offsets = as<uint32_t>(ctx->h_in_voff);
+        db.point_offsets = as<uint32_t>(ctx->h_in_poff);
+        db.num_paths = cn;
+        uint64_t tv = 0, ti = 0;
+        uint32_t failed = 0;
+        uint64_t voff = index_mode == LYON_INDEX_GLOBAL ? vertex_offset + run_v : vertex_offset;
+        int r = pipeline_count(ctx, kind, &db, ctx->h_in_opts.ptr, num_options > 1 ? cn : 1,
+                               index_bits, index_mode, voff, &tv, &ti, &failed);
+        if (r != LYON_OK) return r;
+        if (run_v + tv > vcap || run_i + ti > icap || !hv || (ti && !hi)) capacity_ok = false;
+        if (capacity_ok && cn > 0) {
+            // Wait until this slot's previous device->host copy is done, then emit into it.
+            cudaEventSynchronize(ctx->slot_done[slot]);
+            if (!ensure(ctx, ctx->slot_v[slot], tv * 8 + 16) ||
+                !ensure(ctx, ctx->slot_i[slot], ti * isz + 16))
+                return LYON_ERR_OUT_OF_MEMORY;
+            r = pipeline_emit(ctx, kind, &db, ctx->h_in_opts.ptr, num_options > 1 ? cn : 1,
+                              index_bits, index_mode, voff, as<float>(ctx->slot_v[slot]),
+                              ctx->slot_i[slot].ptr, tv);
+            if (r != LYON_OK) return r;
+            if (hstatus)
+                cudaMemcpyAsync(hstatus + c0, ctx->status.ptr, (size_t)cn * 4,
+                                cudaMemcpyDeviceToHost, s);
+            cudaEventRecord(ctx->emitted, s);
+            cudaStreamWaitEvent(ctx->copy_stream, ctx->emitted, 0);
+            if (tv)
+                cudaMemcpyAsync(hv + 2 * run_v, ctx->slot_v[slot].ptr, tv * 8,
+                                cudaMemcpyDeviceToHost, ctx->copy_stream);
+            if (ti)
+                cudaMemcpyAsync(reinterpret_cast<unsigned char*>(hi) + run_i * isz,
+                                ctx->slot_i[slot].ptr, ti * isz, cudaMemcpyDeviceToHost,
+                                ctx->copy_stream);
+            cudaEventRecord(ctx->slot_done[slot], ctx->copy_stream);
+            slot ^= 1;
+        }
+        run_v += tv;
+        run_i += ti;
+        if (n == 0) break;
+        c0 = c1;
+    }
+    if (!set_err(ctx, "sync", cudaStreamSynchronize(ctx->copy_stream)) ||
+        !set_err(ctx, "sync", cudaStreamSynchronize(ctx->stream)))
+        return LYON_ERR_CUDA;
+    if (total_v) *total_v = run_v;
+    if (total_i) *total_i = run_i;
+    if (!capacity_ok) {
+        ctx->last_error = "output buffers too small";
+        return LYON_ERR_CAPACITY;
+    }
+    return LYON_OK;
+}
+
+// Copies a host path into the context's device input arena (one-path batch).
+bool stage_single_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                       const float* points, uint32_t num_points, const void* options,
+                       size_t options_size, lyon_path_batch* batch) {
+    cudaStream_t s = ctx->stream;
+    size_t vb = num_verbs, pb = (size_t)num_points * 8;
+    if (!ensure(ctx, ctx->in_verbs, vb + 16) || !ensure(ctx, ctx->in_points, pb + 16) ||
+        !ensure(ctx, ctx->in_offsets, 64) || !ensure(ctx, ctx->in_options, 64) ||
+        !ensure_host(ctx, ctx->h_verbs, vb + 128 + options_size) ||
+        !ensure_host(ctx, ctx->h_points, pb + 16))
+        return false;
+    cudaStreamSynchronize(s);
+    unsigned char* hv = reinterpret_cast<unsigned char*>(ctx->h_verbs.ptr);
+    uint32_t* hoff = reinterpret_cast<uint32_t*>(hv);
+    hoff[0] = 0;
+    hoff[1] = num_verbs;
+    hoff[2] = 0;
+    hoff[3] = num_points;
+    memcpy(hv + 16, options, options_size);
+    if (num_verbs) memcpy(hv + 64, verbs, vb);
+    if (num_points) memcpy(ctx->h_points.ptr, points, pb);
+    cudaMemcpyAsync(ctx->in_offsets.ptr, hv, 16, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ctx->in_options.ptr, hv + 16, options_size, cudaMemcpyHostToDevice, s);
+    if (num_verbs) cudaMemcpyAsync(ctx->in_verbs.ptr, hv + 64, vb, cudaMemcpyHostToDevice, s);
+    if (num_points)
+        cudaMemcpyAsync(ctx->in_points.ptr, ctx->h_points.ptr, pb, cudaMemcpyHostToDevice, s);
+    batch->verbs = as<uint8_t>(ctx->in_verbs);
+    batch->points = as<float>(ctx->in_points);
+    batch->verb_offsets = as<uint32_t>(ctx->in_offsets);
+    batch->point_offsets = as<uint32_t>(ctx->in_offsets) + 2;
+    batch->num_paths = 1;
+    return true;
+}
+
+int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t num_verbs,
+                const float* points, uint32_t num_points, const void* options, size_t opt_size,
+                int index_bits, uint32_t index_base, lyon_gpu_result* result) {
+    if (!ctx || !options || !result || (index_bits != 16 && index_bits != 32) ||
+        (num_verbs && !verbs) || (num_points && !points)) {
+        if (ctx) ctx->last_error = "invalid argument";
+        return LYON_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(ctx->device);
+    memset(result, 0, sizeof(*result));
+    lyon_path_batch b;
+    if (!stage_single_path(ctx, verbs, num_verbs, points, num_points, options, opt_size, &b))
+        return LYON_ERR_OUT_OF_MEMORY;
+    lyon_gpu_batch_output bo;
+    int r = batched_device(ctx, kind, &b, ctx->in_options.ptr, 1, index_bits,
+                           LYON_INDEX_PER_PATH, index_base, &bo);
+    if (r != LYON_OK) return r;
+    cudaStream_t s = ctx->stream;
+    if (!ensure_host(ctx, ctx->h_small, 64)) return LYON_ERR_OUT_OF_MEMORY;
+    size_t vb = bo.total_vertices * 8, ib = bo.total_indices * (index_bits / 8);
+    if (!ensure_host(ctx, ctx->h_out_v, vb + 16) || !ensure_host(ctx, ctx->h_out_i, ib + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    cudaMemcpyAsync(ctx->h_small.ptr, bo.status, 4, cudaMemcpyDeviceToHost, s);
+    if (vb) cudaMemcpyAsync(ctx->h_out_v.ptr, bo.vertices, vb, cudaMemcpyDeviceToHost, s);
+    if (ib) cudaMemcpyAsync(ctx->h_out_i.ptr, bo.indices, ib, cudaMemcpyDeviceToHost, s);
+    if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return LYON_ERR_CUDA;
+    int32_t st = *reinterpret_cast<int32_t*>(ctx->h_small.ptr);
+    result->status = st;
+    result->vertices = reinterpret_cast<const float*>(ctx->h_out_v.ptr);
+    result->indices = ctx->h_out_i.ptr;
+    if (st != LYON_OK) return st;
+    result->num_vertices = (uint32_t)bo.total_vertices;
+    result->num_indices = (uint32_t)bo.total_indices;
+    return LYON_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lyon_gpu_version(void) { return kVersion; }
+
+lyon_gpu_context* lyon_gpu_create(int device) {
+    lyon_gpu_context* ctx = new lyon_gpu_context();
+    ctx->device = device;
+    cudaDeviceProp prop;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return nullptr;
+    }
+    ctx->num_sms = prop.multiProcessorCount;
+    ctx->stroke_bps = lg::stroke_blocks_per_sm();
+    for (int i = 0; i < 4; ++i) cudaEventCreate(&ctx->ev[i]);
+    cudaEventCreateWithFlags(&ctx->slot_done[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ctx->slot_done[1], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ctx->emitted, cudaEventDisableTiming);
+    if (!ensure(ctx, ctx->small, 64)) {
+        lyon_gpu_destroy(ctx);
+        return nullptr;
+    }
+    cudaMemsetAsync(ctx->small.ptr, 0, 64, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    return ctx;
+}
+
+void lyon_gpu_destroy(lyon_gpu_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    DevBuf* bufs[] = {&ctx->vtx_counts, &ctx->idx_counts,  &ctx->status,      &ctx->vtx_offsets,
+                      &ctx->idx_offsets, &ctx->scan_state, &ctx->small,       &ctx->out_vertices,
+                      &ctx->out_indices, &ctx->h_in_verbs, &ctx->h_in_points, &ctx->h_in_voff,
+                      &ctx->h_in_poff,  &ctx->h_in_opts,   &ctx->slot_v[0],   &ctx->slot_v[1],
+                      &ctx->slot_i[0],  &ctx->slot_i[1],   &ctx->flat_counts, &ctx->flat_offsets,
+                      &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
+                      &ctx->in_options};
+    for (DevBuf* b : bufs) free_buf(*b);
+    lg::fill_free(ctx->fill);
+    HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v, &ctx->h_out_i, &ctx->h_small,
+                     &ctx->h_offs};
+    for (HostBuf* b : hb) free_host(*b);
+    for (int i = 0; i < 4; ++i)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    for (int i = 0; i < 2; ++i)
+        if (ctx->slot_done[i]) cudaEventDestroy(ctx->slot_done[i]);
+    if (ctx->emitted) cudaEventDestroy(ctx->emitted);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+void* lyon_gpu_stream(lyon_gpu_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+const char* lyon_gpu_last_error(lyon_gpu_context* ctx) {
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int lyon_gpu_synchronize(lyon_gpu_context* ctx) {
+    if (!ctx) return LYON_ERR_INVALID_ARGUMENT;
+    return set_err(ctx, "cudaStreamSynchronize", cudaStreamSynchronize(ctx->stream))
+               ? LYON_OK
+               : LYON_ERR_CUDA;
+}
+
+void lyon_gpu_set_timing(lyon_gpu_context* ctx, int enabled) {
+    if (ctx) ctx->timing = enabled != 0;
+}
+
+int lyon_gpu_last_timings(lyon_gpu_context* ctx, float* ms4) {
+    if (!ctx || !ms4) return LYON_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 4; ++i) ms4[i] = ctx->last_ms[i];
+    return LYON_OK;
+}
+
+int lyon_gpu_stroke_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                          const lyon_stroke_options* options, uint32_t num_options,
+                          int index_bits, int index_mode, uint32_t vertex_offset,
+                          lyon_gpu_batch_output* out) {
+    return batched_device(ctx, KIND_STROKE, batch, options, num_options, index_bits, index_mode,
+                          vertex_offset, out);
+}
+
+int lyon_gpu_fill_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                        const lyon_fill_options* options, uint32_t num_options, int index_bits,
+                        int index_mode, uint32_t vertex_offset, lyon_gpu_batch_output* out) {
+    return batched_device(ctx, KIND_FILL, batch, options, num_options, index_bits, index_mode,
+                          vertex_offset, out);
+}
+
+int lyon_gpu_stroke_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                               const lyon_stroke_options* options, uint32_t num_options,
+                               int index_bits, int index_mode, uint32_t vertex_offset,
+                               float* vertices, uint64_t vertex_capacity, void* indices,
+                               uint64_t index_capacity, int32_t* status,
+                               uint64_t* total_vertices, uint64_t* total_indices) {
+    return batched_host(ctx, KIND_STROKE, batch, options, sizeof(lyon_stroke_options),
+                        num_options, index_bits, index_mode, vertex_offset, vertices,
+                        vertex_capacity, indices, index_capacity, status, total_vertices,
+                        total_indices);
+}
+
+int lyon_gpu_fill_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                             const lyon_fill_options* options, uint32_t num_options,
+                             int index_bits, int index_mode, uint32_t vertex_offset,
+                             float* vertices, uint64_t vertex_capacity, void* indices,
+                             uint64_t index_capacity, int32_t* status, uint64_t* total_vertices,
+                             uint64_t* total_indices) {
+    return batched_host(ctx, KIND_FILL, batch, options, sizeof(lyon_fill_options), num_options,
+                        index_bits, index_mode, vertex_offset, vertices, vertex_capacity,
+                        indices, index_capacity, status, total_vertices, total_indices);
+}
+
+int lyon_gpu_stroke_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                         const float* points, uint32_t num_points,
+                         const lyon_stroke_options* options, int index_bits, uint32_t index_base,
+                         lyon_gpu_result* result) {
+    return single_path(ctx, KIND_STROKE, verbs, num_verbs, points, num_points, options,
+                       sizeof(lyon_stroke_options), index_bits, index_base, result);
+}
+
+int lyon_gpu_fill_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                       const float* points, uint32_t num_points, const lyon_fill_options* options,
+                       int index_bits, uint32_t index_base, lyon_gpu_result* result) {
+    return single_path(ctx, KIND_FILL, verbs, num_verbs, points, num_points, options,
+                       sizeof(lyon_fill_options), index_bits, index_base, result);
+}
+
+int lyon_gpu_flatten_counts(lyon_gpu_context* ctx, const lyon_path_batch* batch, float tolerance,
+                            uint32_t* counts) {
+    if (!ctx || !batch || !counts) return LYON_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (batch->num_paths == 0) return LYON_OK;
+    lg::FlattenArgs a;
+    memset(&a, 0, sizeof a);
+    a.verbs = batch->verbs;
+    a.points = batch->points;
+    a.verb_offsets = batch->verb_offsets;
+    a.point_offsets = batch->point_offsets;
+    a.num_paths = batch->num_paths;
+    a.tolerance = tolerance;
+    a.counts = counts;
+    return set_err(ctx, "flatten counts",
+                   lg::launch_flatten(a, false, ctx->num_sms * 8, ctx->stream))
+               ? LYON_OK
+               : LYON_ERR_CUDA;
+}
+
+int lyon_gpu_flatten_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch, float tolerance,
+                           float** out_points, uint32_t** out_offsets, uint64_t* total_points) {
+    if (!ctx || !batch || !out_points || !out_offsets || !total_points)
+        return LYON_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    uint32_t nv = 0;
+    if (!ensure_host(ctx, ctx->h_small, 64)) return LYON_ERR_OUT_OF_MEMORY;
+    if (batch->num_paths > 0) {
+        if (!set_err(ctx, "D2H verb count",
+                     cudaMemcpyAsync(ctx->h_small.ptr, batch->verb_offsets + batch->num_paths, 4,
+                                     cudaMemcpyDeviceToHost, s)) ||
+            !set_err(ctx, "sync", cudaStreamSynchronize(s)))
+            return LYON_ERR_CUDA;
+        nv = *reinterpret_cast<uint32_t*>(ctx->h_small.ptr);
+    }
+    if (!ensure(ctx, ctx->flat_counts, (size_t)nv * 4 + 16) ||
+        !ensure(ctx, ctx->flat_offsets, ((size_t)nv + 1) * 8 * 2 + 16) ||
+        !ensure(ctx, ctx->scan_state, 2 * lg::scan_tile_count(nv) * 8 + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    int r = lyon_gpu_flatten_counts(ctx, batch, tolerance, as<uint32_t>(ctx->flat_counts));
+    if (r != LYON_OK) return r;
+    uint64_t* offs = as<uint64_t>(ctx->flat_offsets);
+    uint64_t* offs2 = offs + nv + 1;
+    uint32_t* sw = small_words(ctx);
+    cudaMemsetAsync(sw + 2, 0, 4, s);
+    if (!set_err(ctx, "scan",
+                 lg::launch_scan_pairs(as<uint32_t>(ctx->flat_counts),
+                                       as<uint32_t>(ctx->flat_counts), offs, offs2, nv,
+                                       as<unsigned long long>(ctx->scan_state), sw + 1,
+                                       reinterpret_cast<int*>(sw + 2), s)))
+        return LYON_ERR_CUDA;
+    cudaMemcpyAsync(ctx->h_small.ptr, offs + nv, 8, cudaMemcpyDeviceToHost, s);
+    if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return LYON_ERR_CUDA;
+    uint64_t total = *reinterpret_cast<uint64_t*>(ctx->h_small.ptr);
+    if (!ensure(ctx, ctx->flat_points, total * 8 + 16)) return LYON_ERR_OUT_OF_MEMORY;
+    lg::FlattenArgs a;
+    memset(&a, 0, sizeof a);
+    a.verbs = batch->verbs;
+    a.points = batch->points;
+    a.verb_offsets = batch->verb_offsets;
+    a.point_offsets = batch->point_offsets;
+    a.num_paths = batch->num_paths;
+    a.tolerance = tolerance;
+    a.offsets = offs;
+    a.out_points = as<float>(ctx->flat_points);
+    if (batch->num_paths > 0 &&
+        !set_err(ctx, "flatten points", lg::launch_flatten(a, true, ctx->num_sms * 8, s)))
+        return LYON_ERR_CUDA;
+    *out_points = as<float>(ctx->flat_points);
+    *out_offsets = reinterpret_cast<uint32_t*>(offs2);
+    if (!set_err(ctx, "narrow offsets",
+                 lg::launch_narrow_u64(offs, reinterpret_cast<uint32_t*>(offs2), nv + 1, s)))
+        return LYON_ERR_CUDA;
+    *total_points = total;
+    return LYON_OK;
+}
+
+}  // extern "C"

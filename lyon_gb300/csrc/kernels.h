@@ -1,0 +1,77 @@
+// kernels.h — launch interfaces between the C ABI layer (api.cu) and the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/lyon_gpu.h"
+
+namespace lg {
+
+struct StrokeArgs {
+    const uint8_t* verbs;
+    const float* points;
+    const uint32_t* verb_offsets;
+    const uint32_t* point_offsets;
+    uint32_t num_paths;
+    const lyon_stroke_options* options;
+    uint32_t num_options;
+    const uint32_t* order;     // optional processing order (null: path index order)
+    uint32_t* work_counter;    // zeroed before each launch
+    // count pass outputs / emit pass inputs
+    uint32_t* vtx_counts;
+    uint32_t* idx_counts;
+    int32_t* status;
+    const uint64_t* vtx_offsets;
+    const uint64_t* idx_offsets;
+    float* vertices;
+    void* indices;
+    int index_bits;
+    int index_mode;
+    uint32_t vertex_offset;
+};
+
+struct FillArgs {
+    const uint8_t* verbs;
+    const float* points;
+    const uint32_t* verb_offsets;
+    const uint32_t* point_offsets;
+    uint32_t num_paths;
+    const lyon_fill_options* options;
+    uint32_t num_options;
+    const uint32_t* order;
+    uint32_t* work_counter;
+    // per-path scratch arena (events, edges, spans, output staging)
+    unsigned char* scratch;
+    uint64_t scratch_per_thread;
+    uint32_t num_slots;
+    // outputs of the sweep pass (staged vertices/indices per path) and counts
+    float* stage_vertices;
+    uint32_t* stage_indices;
+    const uint64_t* stage_vtx_offsets;
+    const uint64_t* stage_idx_offsets;
+    uint32_t* vtx_counts;
+    uint32_t* idx_counts;
+    int32_t* status;
+};
+
+int stroke_blocks_per_sm();
+cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);
+
+// Exclusive scan of two u32 arrays into two u64 arrays (decoupled look-back), plus totals at
+// out_a[n] / out_b[n]. `tile_state` holds 2 * num_tiles(n) u64 and `counter` one u32; both are
+// reset by the call. `error` receives 1 if a look-back wait exceeded its bound.
+__host__ __device__ size_t scan_tile_count(uint32_t n);
+cudaError_t launch_scan_pairs(const uint32_t* a, const uint32_t* b, uint64_t* out_a,
+                              uint64_t* out_b, uint32_t n, unsigned long long* tile_state,
+                              uint32_t* counter, int* error, cudaStream_t stream);
+
+// Per-path index-range check for LYON_INDEX_PER_PATH (geometry_builder.rs:338-350): a path whose
+// last vertex id exceeds max_index fails with TOO_MANY_VERTICES and produces nothing.
+cudaError_t launch_per_path_limit(uint32_t* vtx_counts, uint32_t* idx_counts, int32_t* status,
+                                  uint32_t n, uint64_t vertex_offset, uint64_t max_index,
+                                  uint32_t* failed, cudaStream_t stream);
+
+cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cudaStream_t s);
+
+}  // namespace lg

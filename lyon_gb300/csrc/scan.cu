@@ -1,0 +1,192 @@
+// scan.cu — single-pass exclusive scan with decoupled look-back.
+//
+// Turns per-path vertex and index counts (u32) into u64 output offsets. Each block takes the
+// next tile from an atomic counter (so every tile it looks back at is already running), scans it
+// in shared memory, publishes its aggregate, walks back over the predecessors' published states
+// until it meets an inclusive prefix, and publishes its own inclusive prefix. States pack a 2-bit
+// flag with a 62-bit value in one u64 so that a single load sees a consistent pair. Waits are
+// bounded: past the bound the kernel records an error and returns without hanging the GPU.
+#include "kernels.h"
+
+namespace lg {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr unsigned long long FLAG_AGG = 1ull << 62;
+constexpr unsigned long long FLAG_INC = 2ull << 62;
+constexpr unsigned long long VALUE_MASK = (1ull << 62) - 1;
+constexpr uint32_t SPIN_LIMIT = 1u << 24;
+
+__host__ __device__ size_t scan_tile_count(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+
+__device__ __forceinline__ unsigned long long block_excl_scan(unsigned long long v,
+                                                              unsigned long long* total) {
+    __shared__ unsigned long long warp_sums[SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long n = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += n;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        unsigned long long s = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long n = __shfl_up_sync(0xFFFFFFFFu, s, o);
+            if (lane >= o) s += n;
+        }
+        if (lane < SCAN_THREADS / 32) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    unsigned long long before = w > 0 ? warp_sums[w - 1] : 0ull;
+    *total = warp_sums[SCAN_THREADS / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+// Looks back from `tile` and returns the exclusive prefix of one channel.
+__device__ __forceinline__ unsigned long long look_back(unsigned long long* state, uint32_t tile,
+                                                        int* error) {
+    unsigned long long prefix = 0;
+    int64_t j = (int64_t)tile - 1;
+    while (j >= 0) {
+        unsigned long long s;
+        uint32_t spins = 0;
+        do {
+            s = atomicAdd(&state[j], 0ull);
+            if ((s >> 62) != 0) break;
+            if (++spins > SPIN_LIMIT) {
+                atomicExch(error, 1);
+                return prefix;
+            }
+            __nanosleep(64);
+        } while (true);
+        prefix += s & VALUE_MASK;
+        if ((s >> 62) == 2) break;
+        --j;
+    }
+    return prefix;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    scan_pairs_kernel(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
+                      uint64_t* __restrict__ out_a, uint64_t* __restrict__ out_b, uint32_t n,
+                      unsigned long long* state, uint32_t* counter, int* error) {
+    __shared__ uint32_t tile_s;
+    __shared__ unsigned long long prefix_s[2];
+    const uint32_t num_tiles = (uint32_t)scan_tile_count(n);
+    if (threadIdx.x == 0) tile_s = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t tile = tile_s;
+    if (tile >= num_tiles) return;
+    const uint64_t base = (uint64_t)tile * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t va[SCAN_ITEMS], vb[SCAN_ITEMS];
+    unsigned long long sa = 0, sb = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        uint64_t idx = base + i;
+        va[i] = idx < n ? a[idx] : 0u;
+        vb[i] = idx < n ? b[idx] : 0u;
+        sa += va[i];
+        sb += vb[i];
+    }
+    unsigned long long ta, tb;
+    unsigned long long ea = block_excl_scan(sa, &ta);
+    unsigned long long eb = block_excl_scan(sb, &tb);
+    unsigned long long* state_a = state;
+    unsigned long long* state_b = state + num_tiles;
+    if (threadIdx.x == 0) {
+        if (tile == 0) {
+            atomicExch(&state_a[0], FLAG_INC | ta);
+            atomicExch(&state_b[0], FLAG_INC | tb);
+            prefix_s[0] = 0;
+            prefix_s[1] = 0;
+        } else {
+            atomicExch(&state_a[tile], FLAG_AGG | ta);
+            atomicExch(&state_b[tile], FLAG_AGG | tb);
+            unsigned long long pa = look_back(state_a, tile, error);
+            unsigned long long pb = look_back(state_b, tile, error);
+            __threadfence();
+            atomicExch(&state_a[tile], FLAG_INC | ((pa + ta) & VALUE_MASK));
+            atomicExch(&state_b[tile], FLAG_INC | ((pb + tb) & VALUE_MASK));
+            prefix_s[0] = pa;
+            prefix_s[1] = pb;
+        }
+    }
+    __syncthreads();
+    unsigned long long ra = prefix_s[0] + ea, rb = prefix_s[1] + eb;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        uint64_t idx = base + i;
+        if (idx < n) {
+            out_a[idx] = ra;
+            out_b[idx] = rb;
+        }
+        ra += va[i];
+        rb += vb[i];
+    }
+    if (tile == num_tiles - 1 && threadIdx.x == 0) {
+        out_a[n] = prefix_s[0] + ta;
+        out_b[n] = prefix_s[1] + tb;
+    }
+}
+
+__global__ void per_path_limit_kernel(uint32_t* vtx, uint32_t* idx, int32_t* status, uint32_t n,
+                                      uint64_t vertex_offset, uint64_t max_index,
+                                      uint32_t* failed) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t v = vtx[i];
+    if (status[i] == LYON_OK && v > 0 && vertex_offset + v - 1 > max_index) {
+        status[i] = LYON_ERR_TOO_MANY_VERTICES;
+        vtx[i] = 0;
+        idx[i] = 0;
+    }
+    if (status[i] != LYON_OK) atomicAdd(failed, 1u);
+}
+
+cudaError_t launch_scan_pairs(const uint32_t* a, const uint32_t* b, uint64_t* out_a,
+                              uint64_t* out_b, uint32_t n, unsigned long long* tile_state,
+                              uint32_t* counter, int* error, cudaStream_t stream) {
+    size_t tiles = scan_tile_count(n);
+    if (tiles == 0) {
+        cudaMemsetAsync(out_a, 0, sizeof(uint64_t), stream);
+        cudaMemsetAsync(out_b, 0, sizeof(uint64_t), stream);
+        return cudaGetLastError();
+    }
+    cudaMemsetAsync(tile_state, 0, 2 * tiles * sizeof(unsigned long long), stream);
+    cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
+    scan_pairs_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, stream>>>(a, b, out_a, out_b, n,
+                                                                   tile_state, counter, error);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_per_path_limit(uint32_t* vtx_counts, uint32_t* idx_counts, int32_t* status,
+                                  uint32_t n, uint64_t vertex_offset, uint64_t max_index,
+                                  uint32_t* failed, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    per_path_limit_kernel<<<(n + 255) / 256, 256, 0, stream>>>(vtx_counts, idx_counts, status, n,
+                                                              vertex_offset, max_index, failed);
+    return cudaGetLastError();
+}
+
+}  // namespace lg
+
+namespace lg {
+
+__global__ void narrow_u64_kernel(const uint64_t* in, uint32_t* out, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (uint32_t)in[i];
+}
+
+cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    narrow_u64_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+}  // namespace lg

@@ -1,0 +1,764 @@
+// stroke_core.cuh — lyon's fixed-width stroke logic for the GPU (crates/tessellation/src/stroke.rs).
+//
+// The per-join work of `fixed_width_step_impl` (stroke.rs:1521-1632) is split in three parts so
+// that a warp can process 32 joins at once: geometry (side points, folds, single vertices),
+// counts (vertices and indices, from which the warp scans output offsets), and emission through a
+// Sink that writes vertices/indices at the scanned offsets. The sub-path tail (caps, closing,
+// empty caps) runs sequentially on one lane with the same primitives.
+#pragma once
+
+#include "geom.cuh"
+
+namespace lg {
+
+constexpr uint32_t INVALID_ID = 0xFFFFFFFFu;
+constexpr int SP = 0;  // SIDE_POSITIVE
+constexpr int SN = 1;  // SIDE_NEGATIVE
+// lyon recurses 2^depth - 1 times per arc (stroke.rs:2001-2004,2487-2490). A depth above this
+// bound means more than a million vertices per arc (or, for a zero step, no end at all): the
+// path then fails with LYON_ERR_UNSUPPORTED, identically in the oracle.
+constexpr uint32_t MAX_ARC_DEPTH = 20;
+
+struct SidePts {  // stroke.rs:300-307
+    V2 prev, next, single;
+    uint32_t prev_vertex, next_vertex;
+    bool has_single;
+};
+
+struct DEP {  // EndpointData, stroke.rs:309-342 (advancement is not tracked: no output uses it)
+    V2 pos;
+    float hw;
+    int join;
+    bool is_flat;
+    bool fold[2];
+    SidePts s[2];
+};
+
+__device__ __forceinline__ void dep_init(DEP& d, V2 pos, float hw, int join, bool flat) {
+    d.pos = pos;
+    d.hw = hw;
+    d.join = join;
+    d.is_flat = flat;
+    d.fold[0] = d.fold[1] = false;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        d.s[i].prev = V2{__int_as_float(0x7fc00000), __int_as_float(0x7fc00000)};
+        d.s[i].next = d.s[i].prev;
+        d.s[i].single = V2{0.0f, 0.0f};
+        d.s[i].prev_vertex = INVALID_ID;
+        d.s[i].next_vertex = INVALID_ID;
+        d.s[i].has_single = false;
+    }
+}
+
+// Output sink: vertices get consecutive ids starting at `id_base`; when `vout`/`iout` are null
+// only the counters move (count pass). `vcap`/`icap` bound the writes to what the count pass
+// measured for this sink's range, so a disagreement between the passes can never write outside
+// the caller's buffers (it is reported through `overflow`).
+struct Sink {
+    uint32_t id_base;
+    uint32_t nv, ni;
+    float2* vout;
+    void* iout;
+    int index_bits;
+    uint32_t vcap = 0xFFFFFFFFu, icap = 0xFFFFFFFFu;
+    bool overflow = false;
+
+    __device__ __forceinline__ uint32_t vertex(V2 p) {
+        uint32_t id = id_base + nv;
+        if (vout) {
+            if (nv < vcap) vout[nv] = make_float2(p.x, p.y);
+            else overflow = true;
+        }
+        ++nv;
+        return id;
+    }
+    __device__ __forceinline__ void tri(uint32_t a, uint32_t b, uint32_t c) {
+        if (iout && ni + 3 > icap) {
+            overflow = true;
+        } else if (iout) {
+            if (index_bits == 16) {
+                uint16_t* o = reinterpret_cast<uint16_t*>(iout) + ni;
+                o[0] = (uint16_t)a;
+                o[1] = (uint16_t)b;
+                o[2] = (uint16_t)c;
+            } else {
+                uint32_t* o = reinterpret_cast<uint32_t*>(iout) + ni;
+                o[0] = a;
+                o[1] = b;
+                o[2] = c;
+            }
+        }
+        ni += 3;
+    }
+};
+
+struct StrokeParams {
+    float hw;          // line_width * 0.5
+    float miter_limit;
+    float tolerance;
+    float merge_threshold;  // square_merge_threshold, stroke.rs:603-605
+    int line_join;
+    int start_cap, end_cap;
+};
+
+__device__ __forceinline__ StrokeParams make_params(const lyon_stroke_options& o) {
+    StrokeParams p;
+    p.hw = o.line_width * 0.5f;
+    p.miter_limit = o.miter_limit;
+    p.tolerance = o.tolerance;
+    p.merge_threshold = fmaxf(
+        fminf(o.tolerance * o.tolerance * 0.5f, o.line_width * o.line_width * 0.05f), 1e-8f);
+    p.line_join = o.line_join;
+    p.start_cap = o.start_cap;
+    p.end_cap = o.end_cap;
+    return p;
+}
+
+__device__ __forceinline__ bool too_close(V2 a, V2 b, float thr) {  // stroke.rs:1318-1320
+    return sqlen(a - b) < thr;
+}
+
+// math_utils.rs:16-40
+__device__ __forceinline__ V2 compute_normal(V2 v1, V2 v2_) {
+    const float epsilon = 1e-4f;
+    V2 n1 = V2{-v1.y, v1.x};
+    V2 v12 = v1 + v2_;
+    if (sqlen(v12) < epsilon) return V2{0.0f, 0.0f};
+    V2 tan = normalize(v12);
+    V2 n = V2{-tan.y, tan.x};
+    float inv_len = dot(n, n1);
+    if (fabsf(inv_len) < epsilon) return n1;
+    return n / inv_len;
+}
+
+// geom line.rs:562-578 with S = f64.
+__device__ __forceinline__ bool line_intersection_f64(V2 p0, V2 v0, V2 p1, V2 v1, V2* out) {
+    double p0x = p0.x, p0y = p0.y, v0x = v0.x, v0y = v0.y;
+    double p1x = p1.x, p1y = p1.y, v1x = v1.x, v1y = v1.y;
+    double det = v0x * v1y - v0y * v1x;
+    if (fabs(det) <= 1e-8) return false;
+    double inv_det = 1.0 / det;
+    double s2x = p0x + v0x, s2y = p0y + v0y;
+    double o2x = p1x + v1x, o2y = p1y + v1y;
+    double a = p0x * s2y - p0y * s2x;
+    double b = p1x * o2y - p1y * o2x;
+    out->x = (float)((b * v0x - a * v1x) * inv_det);
+    out->y = (float)((b * v0y - a * v1y) * inv_det);
+    return true;
+}
+
+__device__ __forceinline__ bool miter_limit_exceeded(V2 n, float ml) {  // stroke.rs:2320-2322
+    return sqlen(n) > ml * ml * 4.0f;
+}
+
+// stroke.rs:2279-2315
+__device__ __forceinline__ void get_clip_intersections(V2 prev_n, V2 next_n, V2 normal,
+                                                       float clip_distance, V2* i1, V2* i2) {
+    V2 clip_pt = normalize(normal) * clip_distance;
+    V2 clip_vec = perp(normal);
+    if (!line_intersection_f64(clip_pt, clip_vec, prev_n, perp(prev_n), i1)) *i1 = normal;
+    if (!line_intersection_f64(clip_pt, clip_vec, next_n, perp(next_n), i2)) *i2 = normal;
+}
+
+// Correctly rounded f32 transcendentals (f64 evaluation, one rounding).
+__device__ __forceinline__ float cr_atan2(float y, float x) { return (float)atan2((double)y, (double)x); }
+__device__ __forceinline__ float cr_acos(float x) { return (float)acos((double)x); }
+__device__ __forceinline__ float cr_cos(float x) { return (float)cos((double)x); }
+__device__ __forceinline__ float cr_sin(float x) { return (float)sin((double)x); }
+
+// An arc's subdivision count is ceil(|diff| / step) with diff from two atan2 values and step from
+// acos (stroke.rs:1986-2004, 2482-2490, 2749-2753). f32 libms differ by an ulp between
+// platforms, which can move the quotient across an integer; within this margin of an integer the
+// angles, step and quotient are re-evaluated correctly rounded, identically in the oracle.
+__device__ __forceinline__ bool arc_near_tie(float x, float step) {
+    float margin = 1e-3f + 4e-6f / step;
+    return fabsf(x - rintf(x)) < margin;
+}
+
+// round(log2(ceil(x))) as u32 (stroke.rs:2003-2004).
+__device__ __forceinline__ uint32_t depth_of(float x, int* status) {
+    float num_segments = ceilf(x);
+    uint32_t d = sat_u32(roundf(log2f(num_segments)));
+    if (d > MAX_ARC_DEPTH) {
+        *status = LYON_ERR_UNSUPPORTED;
+        return 0;
+    }
+    return d;
+}
+
+// ---- join geometry ----------------------------------------------------------------------------
+
+struct JoinGeo {
+    bool fast;
+    bool skip;
+    V2 normal;  // fast path normal
+};
+
+// stroke.rs:1643-1733
+__device__ __forceinline__ void compute_join_side_positions_fw(V2 prev_pos, DEP& join, V2 next_pos,
+                                                               float miter_limit) {
+    V2 prev_tangent = join.pos - prev_pos;
+    V2 next_tangent = next_pos - join.pos;
+    float prev_length = vlength(prev_tangent);
+    float next_length = vlength(next_tangent);
+    prev_tangent = prev_tangent / prev_length;
+    next_tangent = next_tangent / next_length;
+    float hw = join.hw;
+    V2 normal = compute_normal(prev_tangent, next_tangent);
+    int front_side;
+    V2 front_normal;
+    if (cross(prev_tangent, next_tangent) >= 0.0f) {
+        front_side = SN;
+        front_normal = -normal;
+    } else {
+        front_side = SP;
+        front_normal = normal;
+    }
+    int back_side = 1 - front_side;
+    V2 extruded_normal = front_normal * hw;
+    bool unclipped_miter = (join.join == LYON_JOIN_MITER || join.join == LYON_JOIN_MITER_CLIP) &&
+                           !miter_limit_exceeded(front_normal, miter_limit);
+    bool fold = false;
+    bool angle_is_sharp = dot(next_tangent, prev_tangent) < 0.0f;
+    if (!unclipped_miter && angle_is_sharp) {
+        float d_next = dot(extruded_normal, -next_tangent) - next_length;
+        float d_prev = dot(extruded_normal, prev_tangent) - prev_length;
+        if (fminf(d_next, d_prev) > 0.0f || sqlen(normal) < 1e-5f) {
+            join.fold[front_side] = true;
+            fold = true;
+        }
+    }
+    V2 n0 = V2{-prev_tangent.y, prev_tangent.x} * hw;
+    V2 n1 = V2{-next_tangent.y, next_tangent.x} * hw;
+    join.s[SP].prev = join.pos + n0;
+    join.s[SP].next = join.pos + n1;
+    join.s[SN].prev = join.pos - n0;
+    join.s[SN].next = join.pos - n1;
+    if (!fold) {
+        V2 mp = join.pos + normal * hw;
+        V2 mn = join.pos - normal * hw;
+        join.s[back_side].has_single = true;
+        join.s[back_side].single = back_side == SP ? mp : mn;
+        if (unclipped_miter) {
+            join.s[front_side].has_single = true;
+            join.s[front_side].single = front_side == SP ? mp : mn;
+        } else if (join.join == LYON_JOIN_MITER_CLIP) {
+            V2 a = join.s[front_side].prev - join.pos;
+            V2 b = join.s[front_side].next - join.pos;
+            V2 pn, nn;
+            get_clip_intersections(a, b, front_normal, miter_limit * hw, &pn, &nn);
+            join.s[front_side].prev = join.pos + pn;
+            join.s[front_side].next = join.pos + nn;
+        }
+    }
+}
+
+// Geometry of the join at `join` (stroke.rs:1559-1608 up to the vertex emission). The fast path
+// (stroke.rs:1743-1806) needs the previous join's side points for its skip test; callers that
+// process joins in parallel pass them after exchanging them (see flattened_skip).
+__device__ __forceinline__ JoinGeo join_geometry(V2 prev_pos, DEP& join, V2 next_pos,
+                                                 float miter_limit) {
+    JoinGeo g;
+    g.fast = false;
+    g.skip = false;
+    g.normal = V2{0.0f, 0.0f};
+    if (join.is_flat) {
+        V2 v0 = join.pos - prev_pos;
+        V2 v1 = next_pos - join.pos;
+        g.fast = dot(v0, v1) > 0.0f;
+    }
+    if (g.fast) {
+        join.join = LYON_JOIN_MITER;
+        V2 prev_edge = join.pos - prev_pos;
+        float prev_length = vlength(prev_edge);
+        V2 prev_tangent = prev_edge / prev_length;
+        V2 next_edge = next_pos - join.pos;
+        float next_length = vlength(next_edge);
+        V2 next_tangent = next_edge / next_length;
+        V2 normal = compute_normal(prev_tangent, next_tangent);
+        V2 p0 = join.pos + normal * join.hw;
+        V2 p1 = join.pos - normal * join.hw;
+        join.s[SP].prev = p0;
+        join.s[SP].next = p0;
+        join.s[SP].single = p0;
+        join.s[SP].has_single = true;
+        join.s[SN].prev = p1;
+        join.s[SN].next = p1;
+        join.s[SN].single = p1;
+        join.s[SN].has_single = true;
+        g.normal = normal;
+    } else {
+        compute_join_side_positions_fw(prev_pos, join, next_pos, miter_limit);
+    }
+    return g;
+}
+
+// The skip test of flattened_step (stroke.rs:1785-1789), given the previous join's side points.
+__device__ __forceinline__ bool flattened_skip(V2 prev_pos, V2 prev_pos_next, V2 prev_neg_next,
+                                               const DEP& join) {
+    V2 prev_edge = join.pos - prev_pos;
+    V2 v0 = join.s[SP].single - prev_pos_next;
+    V2 v1 = join.s[SN].single - prev_neg_next;
+    return dot(prev_edge, v0) < 0.0f && dot(prev_edge, v1) < 0.0f;
+}
+
+__device__ __forceinline__ void side_needs_join(const DEP& j, bool out[2]) {  // stroke.rs:1914-1917
+    out[SP] = !j.s[SP].has_single && !j.fold[SN];
+    out[SN] = !j.s[SN].has_single && !j.fold[SP];
+}
+
+// Number of interior join triangles (stroke.rs:1919-1950).
+__device__ __forceinline__ uint32_t join_interior_tris(const DEP& j) {
+    if (j.fold[SP] || j.fold[SN]) return 0;
+    bool nj[2];
+    side_needs_join(j, nj);
+    if (nj[SP] && nj[SN]) return 2;
+    if (nj[SP] != nj[SN]) return 1;
+    return 0;
+}
+
+// Round join arc of one side (stroke.rs:1968-2021): angles and subdivision depth.
+struct ArcPlan {
+    float a0, a1;
+    uint32_t depth;
+    bool cr;
+};
+
+__device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side, float tol,
+                                                int* status) {
+    V2 center = join.pos;
+    float radius = join.hw;
+    V2 sn = join.s[side].prev - center;
+    V2 en = join.s[side].next - center;
+    float angle_sign = side == SN ? 1.0f : -1.0f;
+    bool cr = false;
+    float start_angle, diff, step;
+    for (;;) {
+        start_angle = cr ? cr_atan2(sn.y, sn.x) : angle_from_x_axis(sn);
+        float end_a = cr ? cr_atan2(en.y, en.x) : angle_from_x_axis(en);
+        diff = angle_to(start_angle, end_a);
+        if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * LG_PI_F - fabsf(diff));
+        float t = fminf(tol, radius);
+        float arg = (radius - t) / radius;
+        step = 2.0f * (cr ? cr_acos(arg) : acosf(arg));
+        if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
+        cr = true;
+    }
+    float end_angle = start_angle + diff;
+    ArcPlan p;
+    if (side == SN) {
+        p.a0 = end_angle;
+        p.a1 = start_angle;
+    } else {
+        p.a0 = start_angle;
+        p.a1 = end_angle;
+    }
+    p.cr = cr;
+    p.depth = depth_of(fabsf(diff) / step, status);
+    return p;
+}
+
+__device__ __forceinline__ uint32_t arc_vertex_count(uint32_t depth) {
+    return depth == 0 ? 0u : ((1u << depth) - 1u);
+}
+
+// stroke.rs:2612-2653 (pre-order recursion, made iterative with an explicit stack).
+__device__ __noinline__ void tessellate_arc(V2 center, float radius, float a0, float a1, uint32_t va,
+                                            uint32_t vb, uint32_t depth, bool cr, Sink& sink) {
+    if (depth == 0) return;
+    struct Frame {
+        float a0, a1;
+        uint32_t va, vb, n;
+    };
+    Frame st[MAX_ARC_DEPTH + 2];
+    int sp = 0;
+    st[sp++] = Frame{a0, a1, va, vb, depth};
+    while (sp > 0) {
+        Frame f = st[--sp];
+        if (f.n == 0) continue;
+        float mid = (f.a0 + f.a1) * 0.5f;
+        V2 normal = cr ? V2{cr_cos(mid), cr_sin(mid)} : V2{cosf(mid), sinf(mid)};
+        uint32_t vid = sink.vertex(center + normal * radius);
+        sink.tri(f.va, vid, f.vb);
+        st[sp++] = Frame{mid, f.a1, vid, f.vb, f.n - 1};
+        st[sp++] = Frame{f.a0, mid, f.va, vid, f.n - 1};
+    }
+}
+
+// ---- emission ---------------------------------------------------------------------------------
+
+// stroke.rs:2024-2055
+__device__ __forceinline__ void add_join_base_vertices(DEP& j, int side, Sink& sink) {
+    if (j.s[side].has_single) {
+        V2 normal = (j.s[side].single - j.pos) / j.hw;
+        uint32_t v = sink.vertex(j.pos + normal * j.hw);
+        j.s[side].prev_vertex = v;
+        j.s[side].next_vertex = v;
+    } else {
+        V2 n0 = (j.s[side].prev - j.pos) / j.hw;
+        uint32_t pv = sink.vertex(j.pos + n0 * j.hw);
+        V2 n1 = (j.s[side].next - j.pos) / j.hw;
+        uint32_t nv = sink.vertex(j.pos + n1 * j.hw);
+        j.s[side].prev_vertex = pv;
+        j.s[side].next_vertex = nv;
+    }
+}
+
+// Base vertices of a join: fast path +,- (stroke.rs:1791-1797) or regular -,+ (:1595-1608).
+__device__ __forceinline__ void emit_join_base(DEP& j, const JoinGeo& g, Sink& sink) {
+    if (g.fast) {
+        if (g.skip) return;
+        uint32_t pv = sink.vertex(j.pos + g.normal * j.hw);
+        uint32_t nv = sink.vertex(j.pos + (-g.normal) * j.hw);
+        j.s[SP].prev_vertex = pv;
+        j.s[SP].next_vertex = pv;
+        j.s[SN].prev_vertex = nv;
+        j.s[SN].next_vertex = nv;
+    } else {
+        add_join_base_vertices(j, SN, sink);
+        add_join_base_vertices(j, SP, sink);
+    }
+}
+
+__device__ __forceinline__ uint32_t join_base_vertex_count(const DEP& j, const JoinGeo& g) {
+    if (g.fast) return g.skip ? 0u : 2u;
+    return (j.s[SN].has_single ? 1u : 2u) + (j.s[SP].has_single ? 1u : 2u);
+}
+
+// Ids an edge (p0 -> p1) uses, after the fold substitutions of stroke.rs:1874-1889.
+struct EdgeIds {
+    uint32_t p0_neg, p0_pos;
+};
+__device__ __forceinline__ void edge_ids_from(const DEP& p0, uint32_t* neg, uint32_t* pos) {
+    *neg = p0.fold[SP] ? p0.s[SP].prev_vertex : p0.s[SN].next_vertex;
+    *pos = p0.fold[SN] ? p0.s[SN].prev_vertex : p0.s[SP].next_vertex;
+}
+__device__ __forceinline__ void edge_ids_to(const DEP& p1, uint32_t* neg, uint32_t* pos) {
+    *neg = p1.fold[SP] ? p1.s[SP].next_vertex : p1.s[SN].prev_vertex;
+    *pos = p1.fold[SN] ? p1.s[SN].next_vertex : p1.s[SP].prev_vertex;
+}
+
+// stroke.rs:1869-1904 on already-resolved ids. Returns the number of triangles.
+__device__ __forceinline__ uint32_t edge_triangles(uint32_t p0_neg, uint32_t p0_pos,
+                                                   uint32_t p1_neg, uint32_t p1_pos, Sink* sink) {
+    if (p0_neg == p1_pos) return 0;
+    uint32_t n = 0;
+    if (p0_neg != p0_pos && p0_pos != p1_pos) {
+        if (sink) sink->tri(p0_neg, p0_pos, p1_pos);
+        ++n;
+    }
+    if (p0_neg != p1_neg && p1_pos != p1_neg) {
+        if (sink) sink->tri(p0_neg, p1_pos, p1_neg);
+        ++n;
+    }
+    return n;
+}
+
+__device__ __forceinline__ void add_edge_triangles(const DEP& p0, const DEP& p1, Sink& sink) {
+    uint32_t a, b, c, d;
+    edge_ids_from(p0, &a, &b);
+    edge_ids_to(p1, &c, &d);
+    edge_triangles(a, b, c, d, &sink);
+}
+
+// stroke.rs:1907-1965 (interior triangles then round arcs).
+__device__ __forceinline__ void tessellate_join(const DEP& j, const StrokeParams& P, Sink& sink,
+                                                int* status) {
+    bool nj[2];
+    side_needs_join(j, nj);
+    if (!j.fold[SP] && !j.fold[SN]) {
+        const SidePts& sp = j.s[SP];
+        const SidePts& sn = j.s[SN];
+        if (nj[SP] && nj[SN]) {
+            sink.tri(sp.prev_vertex, sp.next_vertex, sn.next_vertex);
+            sink.tri(sp.prev_vertex, sn.next_vertex, sn.prev_vertex);
+        } else if (!nj[SP] && nj[SN]) {
+            sink.tri(sn.prev_vertex, sp.prev_vertex, sn.next_vertex);
+        } else if (nj[SP] && !nj[SN]) {
+            sink.tri(sn.prev_vertex, sp.prev_vertex, sp.next_vertex);
+        }
+    }
+    if (j.join == LYON_JOIN_ROUND) {
+        for (int side = 0; side < 2; ++side) {
+            if (!nj[side]) continue;
+            ArcPlan a = round_join_plan(j, side, P.tolerance, status);
+            uint32_t va = side == SN ? j.s[side].next_vertex : j.s[side].prev_vertex;
+            uint32_t vb = side == SN ? j.s[side].prev_vertex : j.s[side].next_vertex;
+            tessellate_arc(j.pos, j.hw, a.a0, a.a1, va, vb, a.depth, a.cr, sink);
+        }
+    }
+}
+
+// Vertex and triangle counts of tessellate_join's arcs (0 unless the join is round).
+__device__ __forceinline__ uint32_t join_arc_vertices(const DEP& j, const StrokeParams& P,
+                                                      int* status) {
+    if (j.join != LYON_JOIN_ROUND) return 0;
+    bool nj[2];
+    side_needs_join(j, nj);
+    uint32_t n = 0;
+    for (int side = 0; side < 2; ++side) {
+        if (!nj[side]) continue;
+        ArcPlan a = round_join_plan(j, side, P.tolerance, status);
+        n += arc_vertex_count(a.depth);
+    }
+    return n;
+}
+
+// stroke.rs:2459-2524
+__device__ __noinline__ void tessellate_round_cap(V2 center, float radius, V2 start_normal,
+                                                  uint32_t start_vertex, uint32_t end_vertex,
+                                                  V2 edge_normal, bool is_start,
+                                                  const StrokeParams& P, Sink& sink,
+                                                  int* status) {
+    if (radius < P.tolerance) return;
+    bool cr = false;
+    float start_angle, diff, step;
+    for (;;) {
+        start_angle = cr ? cr_atan2(start_normal.y, start_normal.x)
+                         : angle_from_x_axis(start_normal);
+        float edge_a = cr ? cr_atan2(edge_normal.y, edge_normal.x) : angle_from_x_axis(edge_normal);
+        diff = angle_to(start_angle, edge_a);
+        float t = fminf(P.tolerance, radius);
+        float arg = (radius - t) / radius;
+        step = 2.0f * (cr ? cr_acos(arg) : acosf(arg));
+        if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
+        cr = true;
+    }
+    float mid_angle = start_angle + diff;
+    float end_angle = mid_angle + diff;
+    uint32_t depth = depth_of(fabsf(diff) / step, status);
+    uint32_t mid_vertex = sink.vertex(center + normalize(edge_normal) * radius);
+    sink.tri(start_vertex, mid_vertex, end_vertex);
+    tessellate_arc(center, radius, start_angle, mid_angle, start_vertex, mid_vertex, depth, cr,
+                   sink);
+    tessellate_arc(center, radius, mid_angle, end_angle, mid_vertex, end_vertex, depth, cr, sink);
+}
+
+// stroke.rs:2526-2560
+__device__ __forceinline__ void tessellate_empty_square_cap(V2 pos, float hw, Sink& sink) {
+    uint32_t a = sink.vertex(pos + V2{1.0f, 1.0f} * hw);
+    uint32_t b = sink.vertex(pos + V2{1.0f, -1.0f} * hw);
+    uint32_t c = sink.vertex(pos + V2{-1.0f, -1.0f} * hw);
+    uint32_t d = sink.vertex(pos + V2{-1.0f, 1.0f} * hw);
+    sink.tri(a, b, c);
+    sink.tri(a, c, d);
+}
+
+// stroke.rs:2562-2609
+__device__ __forceinline__ void tessellate_empty_round_cap(V2 center, float hw,
+                                                           const StrokeParams& P, Sink& sink,
+                                                           int* status) {
+    uint32_t left_id = sink.vertex(center + V2{-1.0f, 0.0f} * hw);
+    uint32_t right_id = sink.vertex(center + V2{1.0f, 0.0f} * hw);
+    tessellate_round_cap(center, hw, V2{-1.0f, 0.0f}, left_id, right_id, V2{0.0f, 1.0f}, true, P,
+                         sink, status);
+    tessellate_round_cap(center, hw, V2{1.0f, 0.0f}, right_id, left_id, V2{0.0f, -1.0f}, false,
+                         P, sink, status);
+}
+
+// stroke.rs:2130-2206
+__device__ __forceinline__ void tessellate_last_edge(const DEP& p0, DEP& p1, bool is_first_edge,
+                                                     const StrokeParams& P, Sink& sink,
+                                                     int* status) {
+    V2 v = p1.pos - p0.pos;
+    for (int side = 0; side < 2; ++side) {
+        V2 side_position = p1.s[side].prev;
+        if (P.end_cap == LYON_CAP_SQUARE || P.end_cap == LYON_CAP_BUTT) {
+            float clip = P.end_cap == LYON_CAP_SQUARE ? p1.hw : 0.0f;
+            V2 normal = normalize(p1.pos - p0.pos);
+            V2 clip_pt = p1.pos + normal * clip;
+            V2 r;
+            if (line_intersection_f64(clip_pt, perp(normal), side_position,
+                                      side_position - p0.s[side].next, &r)) {
+                p1.s[side].prev = r;
+            }
+        }
+        V2 normal = (p1.s[side].prev - p1.pos) / p1.hw;
+        p1.s[side].prev_vertex = sink.vertex(p1.pos + normal * p1.hw);
+    }
+    if (!is_first_edge) add_edge_triangles(p0, p1, sink);
+    if (P.end_cap == LYON_CAP_ROUND) {
+        tessellate_round_cap(p1.pos, p1.hw, p1.s[SP].prev - p1.pos, p1.s[SP].prev_vertex,
+                             p1.s[SN].prev_vertex, v, false, P, sink, status);
+    }
+}
+
+// stroke.rs:2208-2276
+__device__ __forceinline__ void tessellate_first_edge(DEP& first, const DEP& second,
+                                                      const StrokeParams& P, Sink& sink,
+                                                      int* status) {
+    for (int side = 0; side < 2; ++side) {
+        V2 side_position = first.s[side].next;
+        if (P.start_cap == LYON_CAP_SQUARE || P.start_cap == LYON_CAP_BUTT) {
+            float clip = P.start_cap == LYON_CAP_SQUARE ? first.hw : 0.0f;
+            V2 normal = normalize(first.pos - second.pos);
+            V2 clip_pt = first.pos + normal * clip;
+            V2 r;
+            if (line_intersection_f64(clip_pt, perp(normal), side_position,
+                                      side_position - second.s[side].prev, &r)) {
+                side_position = r;
+            } else {
+                side_position = first.s[side].next;
+            }
+        }
+        V2 normal = (side_position - first.pos) / first.hw;
+        first.s[side].next_vertex = sink.vertex(first.pos + normal * first.hw);
+    }
+    add_edge_triangles(first, second, sink);
+    if (P.start_cap == LYON_CAP_ROUND) {
+        tessellate_round_cap(first.pos, first.hw, first.s[SN].next - first.pos,
+                             first.s[SN].next_vertex, first.s[SP].next_vertex,
+                             first.pos - second.pos, true, P, sink, status);
+    }
+}
+
+// Sets the side "next" points of the first point of a sub-path from its first edge
+// (stroke.rs:1538-1556).
+__device__ __forceinline__ void first_point_sides(DEP& first, V2 next_pos, float next_hw) {
+    V2 edge = next_pos - first.pos;
+    float len = vlength(edge);
+    V2 tan = edge / len;
+    V2 n = V2{-tan.y, tan.x} * next_hw;
+    first.s[SP].next = first.pos + n;
+    first.s[SN].next = first.pos - n;
+}
+
+// ---- parallel join processing: summaries exchanged between neighbouring joins -------------
+
+// Which ids an edge uses at one of its ends (after fold substitutions): flags for the
+// structural edge-triangle count (ids of different joins never coincide unless both invalid).
+enum : uint32_t { EF_NEG_INV = 1u, EF_POS_INV = 2u, EF_SELF_EQ = 4u };
+
+__device__ __forceinline__ uint32_t id_flags(uint32_t neg, uint32_t pos) {
+    return (neg == INVALID_ID ? EF_NEG_INV : 0u) | (pos == INVALID_ID ? EF_POS_INV : 0u) |
+           (neg == pos ? EF_SELF_EQ : 0u);
+}
+
+// Number of triangles add_edge_triangles (stroke.rs:1869-1904) emits for an edge whose ends have
+// the given id structures.
+__device__ __forceinline__ uint32_t edge_count_flags(uint32_t from_f, uint32_t to_f) {
+    bool p0_neg_inv = from_f & EF_NEG_INV, p0_pos_inv = from_f & EF_POS_INV;
+    bool p0_self_eq = from_f & EF_SELF_EQ;
+    bool p1_neg_inv = to_f & EF_NEG_INV, p1_pos_inv = to_f & EF_POS_INV;
+    bool p1_self_eq = to_f & EF_SELF_EQ;
+    if (p0_neg_inv && p1_pos_inv) return 0;
+    uint32_t n = 0;
+    if (!p0_self_eq && !(p0_pos_inv && p1_pos_inv)) ++n;
+    if (!(p0_neg_inv && p1_neg_inv) && !p1_self_eq) ++n;
+    return n;
+}
+
+// Result of the general (non flattening-step) join geometry.
+struct SlowJoin {
+    V2 pn, nn;           // side "next" points (for the following join's skip test)
+    uint32_t from_f, to_f;
+    uint32_t from_neg_rel, from_pos_rel;  // ids relative to the join's first vertex (or INVALID)
+    uint32_t vcount;     // base + arc vertices
+    uint32_t jtris;      // interior + arc triangles
+    bool sym;            // side next points symmetric about the join point
+};
+
+// stroke.rs:1586-1608 for a join that is not a flattening step: side positions, folds and the
+// vertex layout. The join (without ids) is stored to *dep for the emission phase.
+__device__ __noinline__ void slow_join_geometry(DEP* dep, V2 prev, V2 cur, bool flat, V2 nxt,
+                                                const StrokeParams& P, SlowJoin* r,
+                                                int* status) {
+    DEP J;
+    dep_init(J, cur, P.hw, P.line_join, flat);
+    compute_join_side_positions_fw(prev, J, nxt, P.miter_limit);
+    *dep = J;
+    Sink probe{0u, 0, 0, nullptr, nullptr, 32};
+    add_join_base_vertices(J, SN, probe);
+    add_join_base_vertices(J, SP, probe);
+    uint32_t a, b;
+    edge_ids_from(J, &a, &b);
+    r->from_neg_rel = a;
+    r->from_pos_rel = b;
+    r->from_f = id_flags(a, b);
+    edge_ids_to(J, &a, &b);
+    r->to_f = id_flags(a, b);
+    uint32_t varc = join_arc_vertices(J, P, status);
+    r->vcount = probe.nv + varc;
+    r->jtris = join_interior_tris(J) + varc;
+    r->pn = J.s[SP].next;
+    r->nn = J.s[SN].next;
+    // Only a clipped miter moves one side's points off the symmetric offsets.
+    r->sym = J.join != LYON_JOIN_MITER_CLIP;
+}
+
+// Emission of a general join: base vertices (- then +), the edge triangles from the previous
+// join, then tessellate_join. *out receives the join with its ids (for the tail).
+__device__ __noinline__ void slow_join_emit(const DEP* dep, DEP* out, Sink& s, bool has_edge,
+                                            uint32_t pfn, uint32_t pfp, bool emit_tris,
+                                            const StrokeParams& P, int* status) {
+    DEP J = *dep;
+    add_join_base_vertices(J, SN, s);
+    add_join_base_vertices(J, SP, s);
+    if (emit_tris) {
+        if (has_edge) {
+            uint32_t c, d;
+            edge_ids_to(J, &c, &d);
+            edge_triangles(pfn, pfp, c, d, &s);
+        }
+        tessellate_join(J, P, s, status);
+    }
+    *out = J;
+}
+
+// The join of a flattening step (stroke.rs:1743-1806) as a DEP, for the tail.
+__device__ __forceinline__ void fast_join_dep(DEP& d, V2 cur, float hw, V2 pn, V2 nn,
+                                              uint32_t pos_id, uint32_t neg_id) {
+    dep_init(d, cur, hw, LYON_JOIN_MITER, true);
+    d.s[SP].prev = d.s[SP].next = d.s[SP].single = pn;
+    d.s[SP].has_single = true;
+    d.s[SN].prev = d.s[SN].next = d.s[SN].single = nn;
+    d.s[SN].has_single = true;
+    d.s[SP].prev_vertex = d.s[SP].next_vertex = pos_id;
+    d.s[SN].prev_vertex = d.s[SN].next_vertex = neg_id;
+}
+
+// A three-point buffer and the sequential fixed_width_step_impl (stroke.rs:1521-1632), used by
+// the sub-path tail on one lane.
+struct SeqBuffer {
+    DEP pts[3];
+    uint32_t start, count;  // count saturates at 3 entries stored; `n` is the logical count
+    uint32_t n;
+    __device__ __forceinline__ DEP& last() { return pts[(start + (count - 1)) % 3]; }
+    __device__ __forceinline__ DEP& second_last() { return pts[(start + count - 2) % 3]; }
+    __device__ __forceinline__ void push(const DEP& p) {
+        if (count < 3) {
+            pts[count] = p;
+            ++count;
+        } else {
+            pts[start] = p;
+            start = (start + 1) % 3;
+        }
+        ++n;
+    }
+};
+
+__device__ __noinline__ bool seq_step(SeqBuffer& pb, DEP next, const StrokeParams& P, Sink& sink,
+                                      bool* may_need_empty_cap, int* status) {
+    uint32_t count = pb.n;
+    if (count > 0) {
+        if (too_close(pb.last().pos, next.pos, P.merge_threshold)) {
+            if (count == 1) *may_need_empty_cap = true;
+            return false;
+        }
+        if (count == 1) first_point_sides(pb.last(), next.pos, next.hw);
+    }
+    if (count > 1) {
+        DEP& prev = pb.second_last();
+        DEP& join = pb.last();
+        JoinGeo g = join_geometry(prev.pos, join, next.pos, P.miter_limit);
+        if (g.fast) g.skip = flattened_skip(prev.pos, prev.s[SP].next, prev.s[SN].next, join);
+        emit_join_base(join, g, sink);
+        if (count > 2) add_edge_triangles(prev, join, sink);
+        tessellate_join(join, P, sink, status);
+    }
+    pb.push(next);
+    return true;
+}
+
+}  // namespace lg

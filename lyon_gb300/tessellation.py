@@ -1,0 +1,300 @@
+"""Host-side mirror of lyon's tessellation API over the CUDA library.
+
+Mirrors (names, argument meaning, error behaviour):
+  StrokeTessellator.tessellate_path(path, options, builder)  crates/tessellation/src/stroke.rs:164-177
+  FillTessellator.tessellate_path(path, options, builder)    crates/tessellation/src/fill.rs:628-641
+  VertexBuffers / BuffersBuilder (append, vertex offset, abort on error)
+                                           crates/tessellation/src/geometry_builder.rs:262-351,451-508
+  TessellationError / GeometryBuilderError / InternalError   crates/tessellation/src/error.rs:1-142
+plus the batched `tessellate_paths` the reference has no counterpart for.
+
+Every call goes to liblyon_gb300.so (lyon_gb300/_native.py); there is no CPU path.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+from .options import (FILL_OPTIONS_DTYPE, STROKE_OPTIONS_DTYPE, FillOptions, StrokeOptions)
+from .path import Path, PathBatch
+
+LYON_OK = 0
+LYON_ERR_POSITION_IS_NAN = 1
+LYON_ERR_TOLERANCE_IS_NAN = 2
+LYON_ERR_TOO_MANY_VERTICES = 3
+LYON_ERR_INVALID_VERTEX = 4
+LYON_ERR_INTERNAL = 5
+LYON_ERR_INVALID_ARGUMENT = 100
+LYON_ERR_CUDA = 101
+LYON_ERR_OUT_OF_MEMORY = 102
+LYON_ERR_CAPACITY = 103
+LYON_ERR_UNSUPPORTED = 104
+
+INDEX_GLOBAL = 0
+INDEX_PER_PATH = 1
+
+_ERROR_NAMES = {
+    LYON_ERR_POSITION_IS_NAN: "UnsupportedParamater(PositionIsNaN)",
+    LYON_ERR_TOLERANCE_IS_NAN: "UnsupportedParamater(ToleranceIsNaN)",
+    LYON_ERR_TOO_MANY_VERTICES: "GeometryBuilder(TooManyVertices)",
+    LYON_ERR_INVALID_VERTEX: "GeometryBuilder(InvalidVertex)",
+    LYON_ERR_INTERNAL: "Internal",
+    LYON_ERR_INVALID_ARGUMENT: "InvalidArgument",
+    LYON_ERR_CUDA: "Cuda",
+    LYON_ERR_OUT_OF_MEMORY: "OutOfMemory",
+    LYON_ERR_CAPACITY: "Capacity",
+    LYON_ERR_UNSUPPORTED: "Unsupported",
+}
+
+
+class TessellationError(Exception):
+    """lyon's TessellationError; `code` is the C ABI status."""
+
+    def __init__(self, code: int, detail: str = ""):
+        self.code = code
+        name = _ERROR_NAMES.get(code, f"status {code}")
+        super().__init__(f"{name}{': ' + detail if detail else ''}")
+
+
+class VertexBuffers:
+    """`VertexBuffers<Point, u16|u32>`: positions (N x 2 f32) and indices."""
+
+    def __init__(self, index_bits: int = 16):
+        assert index_bits in (16, 32)
+        self.index_bits = index_bits
+        self.vertices = np.zeros((0, 2), dtype=np.float32)
+        self.indices = np.zeros(0, dtype=np.uint16 if index_bits == 16 else np.uint32)
+
+    def clear(self):
+        self.vertices = self.vertices[:0]
+        self.indices = self.indices[:0]
+
+
+class BuffersBuilder:
+    """`BuffersBuilder::new(&mut buffers, Positions)` with an optional vertex offset."""
+
+    def __init__(self, buffers: VertexBuffers, vertex_offset: int = 0):
+        self.buffers = buffers
+        self.vertex_offset = vertex_offset
+
+    def with_vertex_offset(self, offset: int) -> "BuffersBuilder":
+        self.vertex_offset = offset
+        return self
+
+    def next_index(self) -> int:
+        return len(self.buffers.vertices) + self.vertex_offset
+
+    def append(self, vertices: np.ndarray, indices: np.ndarray) -> None:
+        b = self.buffers
+        b.vertices = np.concatenate([b.vertices, vertices.reshape(-1, 2)])
+        b.indices = np.concatenate([b.indices, indices.astype(b.indices.dtype)])
+
+
+def simple_builder(buffers: VertexBuffers) -> BuffersBuilder:
+    return BuffersBuilder(buffers)
+
+
+class Context:
+    """A `lyon_gpu_context` (device, stream, arenas)."""
+
+    _default: Optional["Context"] = None
+    _lock = threading.Lock()
+
+    def __init__(self, device: int = 0):
+        self.lib = _native.load()
+        self.device = device
+        self.h = self.lib.lyon_gpu_create(device)
+        if not self.h:
+            raise RuntimeError(f"lyon_gpu_create({device}) failed (no CUDA device?)")
+
+    @classmethod
+    def default(cls) -> "Context":
+        with cls._lock:
+            if cls._default is None:
+                cls._default = Context(0)
+            return cls._default
+
+    def close(self):
+        if self.h:
+            self.lib.lyon_gpu_destroy(self.h)
+            self.h = None
+
+    def last_error(self) -> str:
+        return self.lib.lyon_gpu_last_error(self.h).decode()
+
+    def synchronize(self):
+        r = self.lib.lyon_gpu_synchronize(self.h)
+        if r != LYON_OK:
+            raise TessellationError(r, self.last_error())
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.lyon_gpu_stream(self.h) or 0)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
+
+
+def _single(kind: str, ctx: Context, path: Path, options, builder: BuffersBuilder) -> None:
+    bits = builder.buffers.index_bits
+    verbs = np.ascontiguousarray(path.verbs, dtype=np.uint8)
+    pts = np.ascontiguousarray(path.points, dtype=np.float32)
+    opt = options.to_c()
+    res = _native.CResult()
+    fn = ctx.lib.lyon_gpu_stroke_path if kind == "stroke" else ctx.lib.lyon_gpu_fill_path
+    r = fn(ctx.h, _ptr(verbs), len(verbs), _ptr(pts), len(pts), ctypes.byref(opt), bits,
+           builder.next_index(), ctypes.byref(res))
+    if r != LYON_OK:
+        raise TessellationError(r, ctx.last_error() if r >= 100 else "")
+    nv, ni = res.num_vertices, res.num_indices
+    v = np.ctypeslib.as_array(ctypes.cast(res.vertices, ctypes.POINTER(ctypes.c_float)),
+                              shape=(nv * 2,)).copy() if nv else np.zeros(0, np.float32)
+    ctype = ctypes.c_uint16 if bits == 16 else ctypes.c_uint32
+    i = np.ctypeslib.as_array(ctypes.cast(res.indices, ctypes.POINTER(ctype)),
+                              shape=(ni,)).copy() if ni else np.zeros(0, builder.buffers.indices.dtype)
+    builder.append(v.reshape(-1, 2), i)
+
+
+class StrokeTessellator:
+    """lyon's StrokeTessellator (fixed line width, `Positions` vertices)."""
+
+    def __init__(self, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context.default()
+
+    def tessellate_path(self, path: Path, options: StrokeOptions, builder: BuffersBuilder) -> None:
+        _single("stroke", self.ctx, path, options, builder)
+
+    tessellate = tessellate_path
+
+
+class FillTessellator:
+    """lyon's FillTessellator (`Positions` vertices)."""
+
+    def __init__(self, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context.default()
+
+    def tessellate_path(self, path: Path, options: FillOptions, builder: BuffersBuilder) -> None:
+        _single("fill", self.ctx, path, options, builder)
+
+    tessellate = tessellate_path
+
+
+# ---------------------------------------------------------------------------------------------
+# Batched API over device memory.
+# ---------------------------------------------------------------------------------------------
+
+class _CudaArray:
+    """A view of library-owned device memory for torch.as_tensor (__cuda_array_interface__)."""
+
+    def __init__(self, ptr: int, shape, typestr: str):
+        self.__cuda_array_interface__ = {"data": (int(ptr), False), "shape": tuple(shape),
+                                         "typestr": typestr, "version": 3, "strides": None}
+
+
+@dataclass
+class DeviceBatch:
+    """A PathBatch uploaded to the GPU (torch tensors keep the memory alive)."""
+
+    verbs: object
+    points: object
+    verb_offsets: object
+    point_offsets: object
+    num_paths: int
+
+    @staticmethod
+    def upload(batch: PathBatch, device: int = 0) -> "DeviceBatch":
+        import torch
+        dev = torch.device("cuda", device)
+
+        def up(a):
+            t = torch.from_numpy(np.ascontiguousarray(a))
+            return t.to(dev, non_blocking=False) if t.numel() else torch.zeros(1, dtype=t.dtype,
+                                                                               device=dev)
+        d = DeviceBatch(up(batch.verbs), up(batch.points.reshape(-1)), up(batch.verb_offsets),
+                        up(batch.point_offsets), batch.num_paths)
+        torch.cuda.synchronize(dev)
+        return d
+
+    def c(self) -> _native.CPathBatch:
+        return _native.CPathBatch(self.verbs.data_ptr(), self.points.data_ptr(),
+                                  self.verb_offsets.data_ptr(), self.point_offsets.data_ptr(),
+                                  self.num_paths)
+
+
+def upload_options(records: np.ndarray, device: int = 0):
+    import torch
+    raw = np.ascontiguousarray(records).view(np.uint8)
+    t = torch.from_numpy(raw.copy()).to(torch.device("cuda", device))
+    torch.cuda.synchronize()
+    return t
+
+
+@dataclass
+class BatchResult:
+    status: int
+    total_vertices: int
+    total_indices: int
+    num_failed_paths: int
+    vertices_ptr: int
+    indices_ptr: int
+    status_ptr: int
+    index_bits: int
+    num_paths: int
+    vertex_offsets_ptr: int = 0
+    index_offsets_ptr: int = 0
+
+    def offsets(self):
+        """(vertex_offsets, index_offsets) as int64 torch tensors of num_paths + 1 entries."""
+        import torch
+        v = torch.as_tensor(_CudaArray(self.vertex_offsets_ptr, (self.num_paths + 1,), "<i8"),
+                            device="cuda")
+        i = torch.as_tensor(_CudaArray(self.index_offsets_ptr, (self.num_paths + 1,), "<i8"),
+                            device="cuda")
+        return v, i
+
+    def vertices(self):
+        import torch
+        return torch.as_tensor(_CudaArray(self.vertices_ptr, (self.total_vertices, 2), "<f4"),
+                               device="cuda")
+
+    def indices(self):
+        import torch
+        ts = "<u2" if self.index_bits == 16 else "<u4"
+        arr = _CudaArray(self.indices_ptr, (self.total_indices,), ts)
+        if self.index_bits == 32:
+            # torch has no uint32 view support everywhere: read as int32 with the same bits.
+            arr.__cuda_array_interface__["typestr"] = "<i4"
+        else:
+            arr.__cuda_array_interface__["typestr"] = "<i2"
+        return torch.as_tensor(arr, device="cuda")
+
+    def statuses(self):
+        import torch
+        return torch.as_tensor(_CudaArray(self.status_ptr, (self.num_paths,), "<i4"),
+                               device="cuda")
+
+
+def tessellate_paths(kind: str, dbatch: DeviceBatch, options_dev, num_options: int,
+                     index_bits: int = 32, index_mode: int = INDEX_GLOBAL,
+                     vertex_offset: int = 0, ctx: Optional[Context] = None) -> BatchResult:
+    """Batched stroke or fill of every path of a DeviceBatch (results stay on the device,
+    owned by the context until its next batched call)."""
+    ctx = ctx or Context.default()
+    out = _native.CBatchOutput()
+    cb = dbatch.c()
+    fn = ctx.lib.lyon_gpu_stroke_paths if kind == "stroke" else ctx.lib.lyon_gpu_fill_paths
+    r = fn(ctx.h, ctypes.byref(cb), options_dev.data_ptr(), num_options, index_bits, index_mode,
+           vertex_offset, ctypes.byref(out))
+    if r != LYON_OK:
+        raise TessellationError(r, ctx.last_error())
+    return BatchResult(r, int(out.total_vertices), int(out.total_indices),
+                       int(out.num_failed_paths), int(out.vertices or 0), int(out.indices or 0),
+                       int(out.status or 0), index_bits, dbatch.num_paths,
+                       int(out.vertex_offsets or 0), int(out.index_offsets or 0))

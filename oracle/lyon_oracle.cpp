@@ -479,24 +479,33 @@ static void get_clip_intersections(P previous_normal, P next_normal, P normal, f
     }
 }
 
-// stroke.rs:2749-2753
-static float circle_flattening_step(float radius, float tolerance) {
-    tolerance = fminf(tolerance, radius);
-    return 2.0f * acosf((radius - tolerance) / radius);
-}
-
 // Arc subdivision depth (stroke.rs:2001-2004, 2487-2490). lyon recurses 2^depth - 1 times; a
 // depth above this bound would mean more than a million vertices per arc (or, for a zero step,
 // no end at all), so both the oracle and the GPU report LYON_ERR_UNSUPPORTED instead.
 static const uint32_t MAX_ARC_DEPTH = 20;
 
-static uint32_t arc_depth(float diff, float step) {
-    float num_segments = ceilf(fabsf(diff) / step);
-    note_tie((double)fabsf(diff) / (double)step);
+// Arc step (stroke.rs:2749-2753, circle_flattening_step) is evaluated inline below:
+// 2 * acos((radius - min(tol, radius)) / radius).
+static uint32_t depth_of(float x) {
+    float num_segments = ceilf(x);
     uint32_t d = sat_u32(roundf(log2f(num_segments)));
     if (d > MAX_ARC_DEPTH) throw TessError{LYON_ERR_UNSUPPORTED, 0};
     return d;
 }
+
+// The arc's subdivision count is ceil(|diff| / step), where diff comes from two atan2 values and
+// step from acos. Platform f32 libms differ by an ulp, which can move the quotient across an
+// integer. When the quotient lies within `arc_tie_margin` of an integer, the angles, the step and
+// the quotient are re-evaluated with correctly rounded f32 functions (f64 evaluation, one
+// rounding), so every platform — and the GPU — takes the same decision.
+static inline bool arc_near_tie(float x, float step) {
+    float margin = 1e-3f + 4e-6f / step;
+    return fabsf(x - rintf(x)) < margin;
+}
+static inline float cr_atan2(float y, float x) { return (float)atan2((double)y, (double)x); }
+static inline float cr_acos(float x) { return (float)acos((double)x); }
+static inline float cr_cos(float x) { return (float)cos((double)x); }
+static inline float cr_sin(float x) { return (float)sin((double)x); }
 
 struct Stroker {
     lyon_stroke_options options;
@@ -550,15 +559,16 @@ struct Stroker {
         if (p0_neg != p1_neg && p1_pos != p1_neg) out->add_triangle(p0_neg, p1_pos, p1_neg);
     }
 
-    // stroke.rs:2612-2653
-    void tessellate_arc(float a0, float a1, uint32_t va, uint32_t vb, uint32_t n) {
+    // stroke.rs:2612-2653. `cr` selects correctly rounded cos/sin (arcs decided on a near tie).
+    void tessellate_arc(float a0, float a1, uint32_t va, uint32_t vb, uint32_t n, bool cr) {
         if (n == 0) return;
         float mid_angle = (a0 + a1) * 0.5f;
-        vertex.normal = P{cosf(mid_angle), sinf(mid_angle)};
+        vertex.normal = cr ? P{cr_cos(mid_angle), cr_sin(mid_angle)}
+                           : P{cosf(mid_angle), sinf(mid_angle)};
         uint32_t vid = add_stroke_vertex();
         out->add_triangle(va, vid, vb);
-        tessellate_arc(a0, mid_angle, va, vid, n - 1);
-        tessellate_arc(mid_angle, a1, vid, vb, n - 1);
+        tessellate_arc(a0, mid_angle, va, vid, n - 1, cr);
+        tessellate_arc(mid_angle, a1, vid, vb, n - 1, cr);
     }
 
     // stroke.rs:1968-2021
@@ -570,18 +580,27 @@ struct Stroker {
         uint32_t start_vertex = join.side[side].prev_vertex;
         uint32_t end_vertex = join.side[side].next_vertex;
         float angle_sign = side == SIDE_NEGATIVE ? 1.0f : -1.0f;
-        float start_angle = angle_from_x_axis(start_normal);
-        float diff = angle_to(start_angle, angle_from_x_axis(end_normal));
-        if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * PI_F - fabsf(diff));
+        bool cr = false;
+        float start_angle, diff, step;
+        for (;;) {
+            start_angle = cr ? cr_atan2(start_normal.y, start_normal.x)
+                             : angle_from_x_axis(start_normal);
+            float end_a = cr ? cr_atan2(end_normal.y, end_normal.x) : angle_from_x_axis(end_normal);
+            diff = angle_to(start_angle, end_a);
+            if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * PI_F - fabsf(diff));
+            float tol = fminf(options.tolerance, radius);
+            step = 2.0f * (cr ? cr_acos((radius - tol) / radius) : acosf((radius - tol) / radius));
+            if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
+            cr = true;
+        }
         float end_angle = start_angle + diff;
         if (side == SIDE_NEGATIVE) {
             std::swap(start_angle, end_angle);
             std::swap(start_vertex, end_vertex);
         }
-        float step = circle_flattening_step(radius, options.tolerance);
-        uint32_t num_subdivisions = arc_depth(diff, step);
+        uint32_t num_subdivisions = depth_of(fabsf(diff) / step);
         vertex.side = side;
-        tessellate_arc(start_angle, end_angle, start_vertex, end_vertex, num_subdivisions);
+        tessellate_arc(start_angle, end_angle, start_vertex, end_vertex, num_subdivisions, cr);
     }
 
     // stroke.rs:1907-1965
@@ -823,8 +842,11 @@ struct Stroker {
         } else {
             long_axis = baseline;
         }
-        float angle = -angle_from_x_axis(long_axis);
-        float s = sinf(angle), c = cosf(angle);
+        // atan2/sin/cos evaluated in f64 and rounded once: the correctly rounded f32 values
+        // (lyon's libm/euclid results agree with them to within an ulp). The GPU does the same,
+        // so the split point, which feeds later integer decisions, is bit-identical.
+        float angle = -(float)atan2((double)long_axis.y, (double)long_axis.x);
+        float s = (float)sin((double)angle), c = (float)cos((double)angle);
         Quad rotated;
         rotated.from = P{0.0f, 0.0f};
         rotated.ctrl = P{v.x * c - v.y * s, v.x * s + v.y * c};
@@ -870,21 +892,31 @@ struct Stroker {
         if (radius < options.tolerance) return;
         int first_side = (is_start ^ (cross(edge_normal, start_normal) >= 0.0f)) ? SIDE_POSITIVE
                                                                                 : SIDE_NEGATIVE;
-        float start_angle = angle_from_x_axis(start_normal);
-        float diff = angle_to(start_angle, angle_from_x_axis(edge_normal));
+        bool cr = false;
+        float start_angle, diff, step;
+        for (;;) {
+            start_angle = cr ? cr_atan2(start_normal.y, start_normal.x)
+                             : angle_from_x_axis(start_normal);
+            float edge_a = cr ? cr_atan2(edge_normal.y, edge_normal.x)
+                              : angle_from_x_axis(edge_normal);
+            diff = angle_to(start_angle, edge_a);
+            float tol = fminf(options.tolerance, radius);
+            step = 2.0f * (cr ? cr_acos((radius - tol) / radius) : acosf((radius - tol) / radius));
+            if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
+            cr = true;
+        }
         float mid_angle = start_angle + diff;
         float end_angle = mid_angle + diff;
-        float step = circle_flattening_step(radius, options.tolerance);
-        uint32_t num_subdivisions = arc_depth(diff, step);
+        uint32_t num_subdivisions = depth_of(fabsf(diff) / step);
         vertex.position_on_path = center;
         vertex.half_width = radius;
         vertex.side = first_side;
         vertex.normal = normalize(edge_normal);
         uint32_t mid_vertex = add_stroke_vertex();
         out->add_triangle(start_vertex, mid_vertex, end_vertex);
-        tessellate_arc(start_angle, mid_angle, start_vertex, mid_vertex, num_subdivisions);
+        tessellate_arc(start_angle, mid_angle, start_vertex, mid_vertex, num_subdivisions, cr);
         vertex.side = 1 - first_side;
-        tessellate_arc(mid_angle, end_angle, mid_vertex, end_vertex, num_subdivisions);
+        tessellate_arc(mid_angle, end_angle, mid_vertex, end_vertex, num_subdivisions, cr);
     }
 
     // stroke.rs:2526-2560

@@ -1,0 +1,174 @@
+"""GPU parity: the CUDA stroke path against the oracle on seeded inputs and lyon's fixtures.
+
+The bar (the benchmark spec): per-path vertex and index counts and the index topology match exactly,
+except where the oracle flags a count decided by a value within 1e-6 of an integer (counted and
+reported); vertex positions match within 1e-5 relative (`RTOL`).
+"""
+
+import numpy as np
+import pytest
+
+from lyon_gb300 import workloads
+from lyon_gb300 import tessellation as T
+from lyon_gb300.options import LineCap, LineJoin, StrokeOptions, stroke_options_array
+from lyon_gb300.path import PathBatch
+from oracle import lyon_oracle as orc
+
+from lyon_cases import case_path, load, rust_logo, stroke_options_from_case
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import gpu_helpers
+    return gpu_helpers
+
+
+def _report(s):
+    print(f"paths={s['paths']} mismatches={len(s['mismatches'])} "
+          f"near_tie_mismatches={s['near_tie_mismatches']} exact={s['exact_vertex_paths']}")
+
+
+def test_plain_stroke_workload(gpu):
+    # 1,000 paths x 16 segments, miter (4) / butt, width 4, tol 0.1, u16 per path.
+    batch, opts = workloads.plain_stroke(1000, seed=1)
+    s = gpu.compare_per_path("stroke", batch, opts, index_bits=16)
+    _report(s)
+    assert not s["mismatches"], s["mismatches"][:10]
+
+
+def test_batched_stroke_workload_subset(gpu):
+    # The batched workload's generator (round joins/caps, tol 0.05, widths 0.5-8, u32).
+    batch, opts = workloads.batched_stroke(20000, seed=2)
+    s = gpu.compare_per_path("stroke", batch, opts, index_bits=32)
+    _report(s)
+    assert not s["mismatches"], s["mismatches"][:10]
+    assert s["near_tie_mismatches"] <= max(2, batch.num_paths // 1000)
+
+
+@pytest.mark.parametrize("join", [LineJoin.Miter, LineJoin.MiterClip, LineJoin.Round,
+                                  LineJoin.Bevel])
+@pytest.mark.parametrize("cap", [LineCap.Butt, LineCap.Square, LineCap.Round])
+def test_joins_and_caps(gpu, join, cap):
+    batch, _ = workloads.plain_stroke(300, seed=7)
+    rng = np.random.default_rng(join * 3 + cap)
+    recs = []
+    for i in range(batch.num_paths):
+        o = StrokeOptions(line_join=join, line_width=float(rng.uniform(0.5, 40.0)),
+                          miter_limit=float(rng.uniform(1.0, 6.0)),
+                          tolerance=float(rng.choice([0.01, 0.1, 1.0]))).with_line_cap(cap)
+        recs.append(o.to_record()[0])
+    opts = stroke_options_array(recs)
+    s = gpu.compare_per_path("stroke", batch, opts, index_bits=32)
+    _report(s)
+    assert not s["mismatches"], s["mismatches"][:10]
+
+
+def test_lyon_stroke_fixtures(gpu):
+    # Every stroke fixture of lyon's tests, through the single-path drop-in, equals the oracle.
+    for case in load("lyon_stroke_cases.json"):
+        path = case_path(case)
+        opts = stroke_options_from_case(case["options"])
+        ref = orc.stroke(path, opts, index_bits=16)
+        buf = T.VertexBuffers(16)
+        T.StrokeTessellator(gpu.ctx()).tessellate_path(path, opts, T.BuffersBuilder(buf))
+        assert np.array_equal(buf.indices, ref.indices), case["src"]
+        assert np.allclose(buf.vertices, ref.vertices, rtol=RTOL, atol=RTOL), case["src"]
+        if case["expect_triangles"] is not None:
+            assert len(buf.indices) // 3 == case["expect_triangles"]
+
+
+def test_logo_all_options(gpu):
+    logo = rust_logo()
+    paths = [logo] * 12
+    recs = []
+    for join in (LineJoin.Miter, LineJoin.MiterClip, LineJoin.Round, LineJoin.Bevel):
+        for cap in (LineCap.Butt, LineCap.Square, LineCap.Round):
+            recs.append(StrokeOptions(line_join=join, tolerance=0.05).with_line_cap(cap)
+                        .to_record()[0])
+    batch = PathBatch.from_paths(paths)
+    s = gpu.compare_per_path("stroke", batch, stroke_options_array(recs), index_bits=32)
+    _report(s)
+    assert not s["mismatches"]
+
+
+def test_too_many_vertices_single_path(gpu):
+    # stroke.rs test_too_many_vertices: a builder with 0/10/100 ids left fails and appends
+    # nothing.
+    for free in (0, 10, 100):
+        buf = T.VertexBuffers(16)
+        b = T.BuffersBuilder(buf, vertex_offset=65536 - free)
+        with pytest.raises(T.TessellationError) as e:
+            T.StrokeTessellator(gpu.ctx()).tessellate_path(rust_logo(),
+                                                           StrokeOptions(tolerance=0.05), b)
+        assert e.value.code == T.LYON_ERR_TOO_MANY_VERTICES
+        assert len(buf.vertices) == 0 and len(buf.indices) == 0
+
+
+def test_global_index_mode_matches_sequential_appends(gpu):
+    # LYON_INDEX_GLOBAL: the batch equals tessellate_path called path by path on one
+    # VertexBuffers (u32), including absolute indices.
+    batch, opts = workloads.plain_stroke(200, seed=5)
+    g = gpu.gpu_batch("stroke", batch, opts, index_bits=32, index_mode=T.INDEX_GLOBAL)
+    out = orc.Output(32)
+    for p in range(batch.num_paths):
+        from lyon_gb300.options import StrokeOptions as SO
+        o = SO(*[opts[0][k].item() for k in opts.dtype.names])
+        assert out.stroke(batch.path(p), o) == 0
+    ref = out.snapshot(0)
+    assert np.array_equal(g["indices"], ref.indices32)
+    assert np.allclose(g["vertices"], ref.vertices, rtol=RTOL, atol=RTOL)
+
+
+def test_global_u16_overflow_rolls_back_per_path(gpu):
+    # 1,000 plain-stroke paths (~1.4M vertices) into one u16 buffer: paths that would overflow
+    # fail with TooManyVertices and are rolled back; later smaller paths may still fit.
+    batch, opts = workloads.plain_stroke(300, seed=9)
+    g = gpu.gpu_batch("stroke", batch, opts, index_bits=16, index_mode=T.INDEX_GLOBAL)
+    out = orc.Output(16)
+    from lyon_gb300.options import StrokeOptions as SO
+    o = SO(*[opts[0][k].item() for k in opts.dtype.names])
+    statuses = [out.stroke(batch.path(p), o) for p in range(batch.num_paths)]
+    ref = out.snapshot(0)
+    assert list(g["status"]) == statuses
+    assert np.array_equal(g["indices"], ref.indices)
+    assert np.allclose(g["vertices"], ref.vertices, rtol=RTOL, atol=RTOL)
+
+
+def test_flatten_counts_and_points(gpu):
+    import torch
+    batch, _ = workloads.batched_stroke(3000, seed=21)
+    c = gpu.ctx()
+    db = T.DeviceBatch.upload(batch, 0)
+    for tol in (0.01, 0.1, 1.0):
+        counts = torch.zeros(len(batch.verbs), dtype=torch.int32, device="cuda")
+        r = c.lib.lyon_gpu_flatten_counts(c.h, db.c(), tol, counts.data_ptr())
+        assert r == 0
+        import ctypes
+        pp = ctypes.c_void_p()
+        po = ctypes.c_void_p()
+        tot = ctypes.c_uint64()
+        r = c.lib.lyon_gpu_flatten_paths(c.h, db.c(), tol, ctypes.byref(pp), ctypes.byref(po),
+                                         ctypes.byref(tot))
+        assert r == 0
+        c.synchronize()
+        gc = counts.cpu().numpy().view(np.uint32)
+        gp = torch.as_tensor(T._CudaArray(pp.value, (tot.value, 2), "<f4"),
+                             device="cuda").cpu().numpy()
+        oc = []
+        op = []
+        for p in range(batch.num_paths):
+            cc, pts = orc.flatten(batch.path(p), tol)
+            oc.append(cc)
+            op.append(pts)
+        oc = np.concatenate(oc)
+        op = np.concatenate(op)
+        assert np.array_equal(gc, oc)
+        assert gp.shape == op.shape
+        assert np.array_equal(gp, op)

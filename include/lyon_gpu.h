@@ -187,6 +187,41 @@ int lyon_gpu_stroke_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                           int index_bits, int index_mode, uint32_t vertex_offset,
                           lyon_gpu_batch_output* out);
 
+/* Largest batch lyon_gpu_stroke_paths_noalloc accepts (its fixed scratch holds this many paths). */
+#define LYON_NOALLOC_MAX_PATHS 262144u
+
+/* lyon_gpu_stroke_paths for callers that cannot allocate device memory: a plugin handed device
+ * buffers by a host application that owns every GPU allocation, or code running under a memory
+ * pool or budget that forbids cudaMalloc. This entry point has no counterpart in the reference
+ * (lyon allocates its own buffers); it is an addition of this library.
+ *
+ * It allocates nothing: no cudaMalloc, cudaFree or allocating library call, and no context.
+ * The batch and options are device memory; the caller also passes every output in device
+ * memory: `vertices` (2 floats per vertex, `vertex_capacity` vertices), `indices`
+ * (`index_capacity` u16/u32), `vertex_offsets` and `index_offsets` (num_paths + 1 u64 each) and
+ * `status` (num_paths i32). The pipeline's scratch is a fixed array of about 2 MiB inside the
+ * library, held by every GPU that loads it until the process exits; batches of more than
+ * LYON_NOALLOC_MAX_PATHS paths are rejected with LYON_ERR_CAPACITY and a message. When the
+ * outputs are too small the call returns LYON_ERR_CAPACITY with *total_vertices /
+ * *total_indices set to the sizes needed and writes no vertices or indices.
+ *
+ * Runs on the calling thread's current device, on `stream` (a cudaStream_t; NULL is the default
+ * stream). The first call on a device resolves the scratch array's address for that device;
+ * make that first call before capturing any stream into a CUDA graph. Every call on a device
+ * shares the one scratch array and it keeps the previous call's contents: calls whose GPU work
+ * overlaps (other streams, other threads) race and give wrong results. The call synchronises
+ * `stream` once to read the totals; the emit kernel is still running when it returns.
+ * `error_text` (optional, `error_text_len` bytes) receives a message on failure. */
+int lyon_gpu_stroke_paths_noalloc(const lyon_path_batch* batch,
+                                  const lyon_stroke_options* options, uint32_t num_options,
+                                  int index_bits, int index_mode, uint32_t vertex_offset,
+                                  float* vertices, uint64_t vertex_capacity, void* indices,
+                                  uint64_t index_capacity, uint64_t* vertex_offsets,
+                                  uint64_t* index_offsets, int32_t* status,
+                                  uint64_t* total_vertices, uint64_t* total_indices,
+                                  uint32_t* num_failed_paths, void* stream, char* error_text,
+                                  size_t error_text_len);
+
 /* Batched `FillTessellator::tessellate_path` (crates/tessellation/src/fill.rs:628-641 applied
  * path by path). Same conventions as lyon_gpu_stroke_paths. */
 int lyon_gpu_fill_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,

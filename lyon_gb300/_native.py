@@ -96,6 +96,12 @@ def load(build_if_missing: bool = True):
         L.lyon_gpu_flatten_paths.argtypes = [c_p, ctypes.POINTER(CPathBatch), ctypes.c_float,
                                              ctypes.POINTER(c_p), ctypes.POINTER(c_p),
                                              ctypes.POINTER(u64)]
+        f = L.lyon_gpu_stroke_paths_noalloc
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.POINTER(CPathBatch), c_p, u32, ctypes.c_int, ctypes.c_int, u32,
+                      c_p, u64, c_p, u64, c_p, c_p, c_p, ctypes.POINTER(u64),
+                      ctypes.POINTER(u64), ctypes.POINTER(u32), c_p, ctypes.c_char_p,
+                      ctypes.c_size_t]
         _lib = L
         return L
 
@@ -106,5 +112,5 @@ EXPORTED = [
     "lyon_gpu_stroke_path", "lyon_gpu_fill_path", "lyon_gpu_stroke_paths", "lyon_gpu_fill_paths",
     "lyon_gpu_flatten_counts", "lyon_gpu_flatten_paths", "lyon_gpu_synchronize",
     "lyon_gpu_version", "lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host",
-    "lyon_gpu_set_timing", "lyon_gpu_last_timings",
+    "lyon_gpu_set_timing", "lyon_gpu_last_timings", "lyon_gpu_stroke_paths_noalloc",
 ]

@@ -1,47 +1,44 @@
 // stroke.cu — batched fixed-width stroke tessellation (count and emit kernels).
 //
 // One warp strokes one path at a time; warps of a persistent grid take paths from an atomic
-// work counter. For each sub-path the warp
-//   1. loads up to 32 verbs (a window ending at the sub-path's End/Close), derives each curve's
-//      flattening parameters (lyon's `flattened_segments_wang`, and the sharp-turn split of
-//      quadratics from stroke.rs:2755-2779), and scans the per-verb step counts;
-//   2. generates the flattened points in chunks of CH = 32 * RUN: lane i owns RUN consecutive
-//      points, evaluates lyon's accumulated parameter t in closed form for its first point
-//      (accumulate_t) and then sequentially (t += step, exactly as lyon), and writes the points
-//      into a per-warp ring in shared memory;
-//   3. applies the merge filter of stroke.rs:1530-1536: every lane checks its points against
-//      their predecessors; only when one is within the threshold does lane 0 replay the chain
-//      and compact the chunk;
-//   4. processes the joins in chunks of CH (lane i owns RUN consecutive joins): a counting pass
-//      (flattening-step joins need no arithmetic beyond a bound that proves lyon's skip test
-//      cannot fire), a warp scan for the output offsets, then the emission pass, which stages
-//      the chunk's vertices and indices in shared memory and copies them out coalesced;
-//   5. runs the sub-path tail (caps, closing, empty caps) on lane 0.
-// The count kernel runs steps 1-5 without writing; a look-back scan turns its per-path counts
-// into offsets; the emit kernel repeats the walk and writes at those offsets.
+// work counter. lyon's stroker (stroke.rs:1521-1632) is a sequential state machine over the
+// flattened points of a sub-path, but every step only looks at its two predecessors, so the
+// warp runs 32 consecutive steps at once, one per lane:
+//   1. a window of up to 32 verbs (ending at the sub-path's End/Close) is decoded, one verb per
+//      lane: lyon's segment counts (`flattened_segments_wang`, quadratic_bezier.rs:943-974,
+//      cubic_bezier.rs:1369-1403) and the sharp-turn split of quadratics (stroke.rs:2755-2779);
+//      a warp scan of the per-verb step counts gives every step its verb;
+//   2. the window's steps are processed 32 at a time, lane = step: the flattened point (lyon's
+//      accumulated parameter t is reproduced bit for bit in closed form by accumulate_t, from
+//      the previous chunk's last value), then the merge filter (stroke.rs:1530-1536): a ballot
+//      finds points within the threshold of their predecessor and only then is the chain
+//      replayed and the kept points compacted across lanes;
+//   3. lane L then performs the join at the previous kept point, whose neighbours come from
+//      lanes L-1 and L-2 (or the carry from the previous chunk): flattening-step joins
+//      (stroke.rs:1743-1806) are straight-line register arithmetic; other joins, the first
+//      point's sides and the first join's record go through out-of-line functions;
+//   4. a warp scan of the per-join vertex/index counts places every join's output; each lane
+//      writes its own vertices and indices;
+//   5. lane 0 runs the sub-path tail (caps, closing, empty caps).
+// The count kernel performs steps 1-5 without writing (it proves, by a bound, that the skip test
+// of flattened_step cannot fire instead of evaluating it, see below); a look-back scan turns its
+// per-path counts into offsets; the emit kernel repeats the walk and writes at those offsets.
 #include "stroke_core.cuh"
 #include "kernels.h"
 
 namespace lg {
 
 #ifndef LG_STROKE_WARPS
-#define LG_STROKE_WARPS 4
+#define LG_STROKE_WARPS 8
 #endif
 #ifndef LG_STROKE_MIN_BLOCKS
 #define LG_STROKE_MIN_BLOCKS 1
 #endif
-#ifndef LG_RUN
-#define LG_RUN 4
-#endif
 constexpr int STROKE_WARPS = LG_STROKE_WARPS;
-constexpr uint32_t RUN = LG_RUN;          // points (and joins) per lane
-constexpr uint32_t CH = 32 * RUN;         // points per chunk
-constexpr uint32_t RING = 4 * CH;         // kept-point ring (power of two)
-constexpr uint32_t RMASK = RING - 1;
-constexpr uint32_t STAGE_V = 2 * CH + 64;  // staged vertices per join chunk
-constexpr uint32_t STAGE_I = 6 * CH + 192; // staged indices per join chunk
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr uint32_t MAX_VERB_STEPS = 1u << 26;
+constexpr uint32_t NO_VERB = 0xFFFFFFFFu;
+constexpr uint32_t EF_ALLINV = EF_NEG_INV | EF_POS_INV | EF_SELF_EQ;
 
 struct VerbSlot {
     Poly pA, pB;
@@ -54,13 +51,9 @@ struct VerbSlot {
 
 struct WarpSmem {
     VerbSlot verbs[32];
-    float2 kp[RING];
-    uint8_t kflat[RING];
-    float2 sv[STAGE_V];
-    uint32_t si[STAGE_I];
-    DEP carry;   // last join processed (J_{next_join - 1}), with ids
-    DEP first0;  // first kept point of the sub-path, with its side points
-    DEP first1;  // J_1 after its processing (lyon's firsts[1])
+    DEP first0;  // first kept point of the sub-path, with its side points (lyon's firsts[0])
+    DEP first1;  // the first join after its processing, with ids (lyon's firsts[1])
+    DEP last;    // the last join, with ids (for the tail)
 };
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
@@ -70,6 +63,13 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
         if (lane >= o) v += n;
     }
     return v;
+}
+
+__device__ __forceinline__ V2 shfl_v2(V2 v, int src) {
+    return V2{__shfl_sync(FULL, v.x, src), __shfl_sync(FULL, v.y, src)};
+}
+__device__ __forceinline__ V2 shfl_up_v2(V2 v, int d) {
+    return V2{__shfl_up_sync(FULL, v.x, d), __shfl_up_sync(FULL, v.y, d)};
 }
 
 struct PathOut {
@@ -84,31 +84,30 @@ __device__ __forceinline__ uint32_t cap_left(uint32_t total, uint32_t used) {
     return used < total ? total - used : 0u;
 }
 
-// Warp-uniform summary of the last processed join (lyon's point buffer entry before the next
-// join), used by lane 0 of the next chunk.
-struct JCarry {
-    V2 pn, nn;            // side next points
-    uint32_t from_f;      // id structure of the edge leaving the join
-    uint32_t fneg, fpos;  // ids the next edge starts from
-    bool sym;             // side next points symmetric about the join point
-};
-
-__device__ __forceinline__ JCarry carry_from_dep(const DEP& d, bool sym) {
-    JCarry c;
-    c.pn = d.s[SP].next;
-    c.nn = d.s[SN].next;
-    edge_ids_from(d, &c.fneg, &c.fpos);
-    c.from_f = id_flags(c.fneg, c.fpos);
-    c.sym = sym;
-    return c;
-}
-
 // t state carried across step chunks: the chunk's last step.
 struct TCarry {
-    uint32_t verb;  // absolute verb index, or ~0 when the last step was not inside a curve
+    uint32_t verb;  // absolute verb index, or NO_VERB when the last step was not inside a curve
     uint32_t unit;
     uint32_t k;
     float t;
+};
+
+// Warp-uniform state of the sub-path being stroked (every lane holds the same values).
+struct SubState {
+    uint32_t n;      // kept points so far
+    V2 c1, c2, c3;   // the last three kept points: P[n-1], P[n-2], P[n-3]
+    bool f1, f2;     // flattening-step flags of c1 and c2
+    V2 jtan;         // tangent of the edge c2 -> c1
+    // The last processed join (at P[n-2]); when n == 2, the first point (its sides only).
+    V2 jpn, jnn;        // its side "next" points
+    bool jside_valid;   // jpn/jnn are known (the count pass computes them only when needed)
+    uint32_t jfneg, jfpos;  // ids the next edge starts from
+    uint32_t jfrom_f;       // their id structure (EF_* flags)
+    bool jsym;              // side next points symmetric about the join point
+    bool jfast, jskip;
+    uint32_t jbase;         // id of the join's first vertex
+    bool mnec;              // lyon's may_need_empty_cap
+    TCarry tc;
 };
 
 __device__ __forceinline__ uint32_t points_of_verb(int kind) {
@@ -189,41 +188,16 @@ __device__ __noinline__ uint32_t setup_verb(VerbSlot& out, int kind, uint32_t po
     return steps;
 }
 
-// The merge filter replayed on lane 0 over a chunk whose points start at kept index n0
-// (stroke.rs:1530-1536): points within the threshold of the last kept point are dropped and the
-// kept ones compacted in place. Returns the new kept count.
-__device__ __noinline__ uint32_t merge_compact(WarpSmem& sm, uint32_t n0, uint32_t nsteps,
-                                               V2 lastk, float thr, bool* mnec) {
-    V2 L = lastk;
-    uint32_t cnt = n0;
-    for (uint32_t i = 0; i < nsteps; ++i) {
-        float2 q = sm.kp[(n0 + i) & RMASK];
-        V2 pi = V2{q.x, q.y};
-        uint8_t fl = sm.kflat[(n0 + i) & RMASK];
-        if (cnt > 0 && too_close(L, pi, thr)) {
-            if (cnt == 1) *mnec = true;
-            continue;
-        }
-        sm.kp[cnt & RMASK] = q;
-        sm.kflat[cnt & RMASK] = fl;
-        L = pi;
-        ++cnt;
-    }
-    return cnt;
-}
-
-// A join's DEP with ids (fast joins: the flattened_step layout; general joins: recomputed), for
-// the carry and lyon's firsts[1].
+// A join as lyon's EndpointData after its processing, with vertex ids starting at base_id (the
+// fast layout of flattened_step, or the general layout), for firsts[1] and the tail.
 __device__ __noinline__ void join_dep_with_ids(DEP* out, V2 prev, V2 cur, V2 nxt, bool flat,
                                                bool fast, bool skip, uint32_t base_id,
                                                const StrokeParams& P, int* status) {
     if (fast) {
         V2 pe = cur - prev;
-        float pl = vlength(pe);
-        V2 pt = pe / pl;
+        V2 pt = pe / vlength(pe);
         V2 ne = nxt - cur;
-        float nl = vlength(ne);
-        V2 nt = ne / nl;
+        V2 nt = ne / vlength(ne);
         V2 nrm = compute_normal(pt, nt);
         fast_join_dep(*out, cur, P.hw, cur + nrm * P.hw, cur - nrm * P.hw,
                       skip ? INVALID_ID : base_id, skip ? INVALID_ID : base_id + 1);
@@ -238,300 +212,42 @@ __device__ __noinline__ void join_dep_with_ids(DEP* out, V2 prev, V2 cur, V2 nxt
     }
 }
 
-// Side "next" points of the join at kept index k (exact path of the skip test).
-__device__ __noinline__ void join_side_next(const WarpSmem& sm, uint32_t k, const StrokeParams& P,
-                                            V2* pn, V2* nn) {
-    float2 a = sm.kp[(k - 1) & RMASK], b = sm.kp[k & RMASK], c = sm.kp[(k + 1) & RMASK];
-    V2 prev = V2{a.x, a.y}, cur = V2{b.x, b.y}, nxt = V2{c.x, c.y};
-    bool flat = sm.kflat[k & RMASK] != 0;
-    if (flat && dot(cur - prev, nxt - cur) > 0.0f) {
-        V2 pe = cur - prev;
-        V2 pt = pe / vlength(pe);
-        V2 ne = nxt - cur;
-        V2 nt = ne / vlength(ne);
-        V2 nrm = compute_normal(pt, nt);
-        *pn = cur + nrm * P.hw;
-        *nn = cur - nrm * P.hw;
-    } else {
-        DEP d;
-        SlowJoin sj;
-        int st = LYON_OK;
-        slow_join_geometry(&d, prev, cur, flat, nxt, P, &sj, &st);
-        *pn = sj.pn;
-        *nn = sj.nn;
-    }
+// Side "next" points of the join at `cur` (neighbours `prev`, `nxt`) when it was a flattening
+// step: what the emit pass computed for it (stroke.rs:1760-1776).
+__device__ __noinline__ void fast_join_sides(V2 prev, V2 cur, V2 nxt, float hw, V2* pn, V2* nn) {
+    V2 pe = cur - prev;
+    V2 pt = pe / vlength(pe);
+    V2 ne = nxt - cur;
+    V2 nt = ne / vlength(ne);
+    V2 nrm = compute_normal(pt, nt);
+    *pn = cur + nrm * hw;
+    *nn = cur - nrm * hw;
 }
 
-// Whether the join at kept index k has symmetric side points (all but clipped miters).
-__device__ __forceinline__ bool join_is_sym(const WarpSmem& sm, uint32_t k, const StrokeParams& P) {
-    if (P.line_join != LYON_JOIN_MITER_CLIP) return true;
-    float2 a = sm.kp[(k - 1) & RMASK], b = sm.kp[k & RMASK], c = sm.kp[(k + 1) & RMASK];
-    bool flat = sm.kflat[k & RMASK] != 0;
-    return flat && ((b.x - a.x) * (c.x - b.x) + (b.y - a.y) * (c.y - b.y)) > 0.0f;
-}
-
-// Processes `count` (1..CH) joins starting at kept index `nj` (lane i owns RUN consecutive
-// joins). Updates the carry, first1 and the output cursors.
-template <bool EMIT>
-__device__ __noinline__ void process_joins(WarpSmem& sm, int lane, uint32_t nj, uint32_t count,
-                                           const StrokeParams& P, const PathOut& po,
-                                           uint32_t& vcur, uint32_t& icur, int& status,
-                                           JCarry& jc) {
-    const uint32_t k0 = nj + (uint32_t)lane * RUN;
-    const uint32_t kend = min(k0 + RUN, nj + count);
-    int st = LYON_OK;
-
-    // ---- pass 1: counts ----
-    // Flattening-step joins (stroke.rs:1743-1806) take 2 vertices and their edge 2 triangles,
-    // unless flattened_step's skip test fires; with side points symmetric about the previous
-    // point that needs the previous edge to be shorter than a few ulps of the coordinates (the
-    // bound below follows from the roundings of p0, p1 and the side points), so the test is only
-    // evaluated exactly when the bound fails somewhere in the chunk.
-    uint32_t V = 0, I = 0;
-    uint32_t first_to_f = 0, pf = 0;
-    uint32_t last_voff = 0, last_fneg_rel = INVALID_ID, last_fpos_rel = INVALID_ID;
-    bool last_fast = true, last_skip = false;
-    bool k1_fast = true, k1_skip = false;
-    bool exact = false;
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        V = 0;
-        I = 0;
-        bool need = false;
-        V2 ppn = V2{0.0f, 0.0f}, pnn = V2{0.0f, 0.0f};
-        bool psym = true;
-        if (k0 < kend) {
-            if (k0 == nj) {
-                ppn = jc.pn;
-                pnn = jc.nn;
-                psym = jc.sym;
-            } else {
-                psym = join_is_sym(sm, k0 - 1, P);
-                if (exact) join_side_next(sm, k0 - 1, P, &ppn, &pnn);
-            }
-        }
-        for (uint32_t k = k0; k < kend; ++k) {
-            float2 a = sm.kp[(k - 1) & RMASK], b = sm.kp[k & RMASK], c = sm.kp[(k + 1) & RMASK];
-            V2 prev = V2{a.x, a.y}, cur = V2{b.x, b.y}, nxt = V2{c.x, c.y};
-            bool flat = sm.kflat[k & RMASK] != 0;
-            V2 pe = cur - prev;
-            bool fast = flat && dot(pe, nxt - cur) > 0.0f;
-            uint32_t vc, jt, to_f, from_f, fneg_rel, fpos_rel;
-            bool skip = false, sym = true;
-            if (fast) {
-                if (exact) {
-                    V2 pt = pe / vlength(pe);
-                    V2 ne = nxt - cur;
-                    V2 nt = ne / vlength(ne);
-                    V2 nrm = compute_normal(pt, nt);
-                    V2 pn = cur + nrm * P.hw, nn = cur - nrm * P.hw;
-                    skip = dot(pe, pn - ppn) < 0.0f && dot(pe, nn - pnn) < 0.0f;
-                    ppn = pn;
-                    pnn = nn;
-                } else {
-                    float m = fmaxf(fmaxf(fabsf(cur.x), fabsf(cur.y)),
-                                    fmaxf(fabsf(prev.x), fabsf(prev.y))) + 3.0f * P.hw;
-                    float bnd = m * 7.62939453125e-06f;  // 2^-17
-                    if (!(psym && sqlen(pe) > bnd * bnd)) need = true;
-                }
-                vc = skip ? 0u : 2u;
-                jt = 0;
-                to_f = from_f = skip ? (EF_NEG_INV | EF_POS_INV | EF_SELF_EQ) : 0u;
-                fneg_rel = skip ? INVALID_ID : 1u;
-                fpos_rel = skip ? INVALID_ID : 0u;
-            } else {
-                DEP d;
-                SlowJoin sj;
-                slow_join_geometry(&d, prev, cur, flat, nxt, P, &sj, &st);
-                vc = sj.vcount;
-                jt = sj.jtris;
-                to_f = sj.to_f;
-                from_f = sj.from_f;
-                fneg_rel = sj.from_neg_rel;
-                fpos_rel = sj.from_pos_rel;
-                sym = sj.sym;
-                ppn = sj.pn;
-                pnn = sj.nn;
-            }
-            uint32_t e = 0;
-            if (k == k0) {
-                first_to_f = to_f;
-            } else if (k >= 2) {
-                e = edge_count_flags(pf, to_f);
-            }
-            last_voff = V;
-            last_fneg_rel = fneg_rel;
-            last_fpos_rel = fpos_rel;
-            last_fast = fast;
-            last_skip = skip;
-            if (k == 1) {
-                k1_fast = fast;
-                k1_skip = skip;
-            }
-            V += vc;
-            I += 3u * (jt + e);
-            pf = from_f;
-            psym = fast ? true : sym;
-        }
-        if (exact || !__any_sync(FULL, need)) break;
-        exact = true;
+// The first kept point of a sub-path as lyon's EndpointData, with the side points its first
+// edge gives it (stroke.rs:1538-1556) when there is one.
+__device__ __noinline__ void write_first0(DEP* out, V2 pos, bool has_sides, V2 pn, V2 nn,
+                                          const StrokeParams& P) {
+    DEP f;
+    dep_init(f, pos, P.hw, P.line_join, false);
+    if (has_sides) {
+        f.s[SP].next = pn;
+        f.s[SN].next = nn;
     }
-    // Edge triangles of each run's first join need the previous run's last join.
-    uint32_t pff = __shfl_up_sync(FULL, pf, 1);
-    if (lane == 0) pff = jc.from_f;
-    if (k0 < kend && k0 >= 2) I += 3u * edge_count_flags(pff, first_to_f);
-    const uint32_t vincl = warp_incl_scan(V, lane);
-    const uint32_t iincl = warp_incl_scan(I, lane);
-    const uint32_t vtot = __shfl_sync(FULL, vincl, 31);
-    const uint32_t itot = __shfl_sync(FULL, iincl, 31);
-    const uint32_t vrel = vincl - V;
-    const uint32_t irel = iincl - I;
-    const uint32_t base_id = po.id_base + vcur + vrel;
-    // Ids the next run's first edge starts from.
-    uint32_t fneg = INVALID_ID, fpos = INVALID_ID;
-    if (k0 < kend) {
-        fneg = last_fneg_rel == INVALID_ID ? INVALID_ID : base_id + last_voff + last_fneg_rel;
-        fpos = last_fpos_rel == INVALID_ID ? INVALID_ID : base_id + last_voff + last_fpos_rel;
-    }
-    uint32_t pfn = __shfl_up_sync(FULL, fneg, 1);
-    uint32_t pfp = __shfl_up_sync(FULL, fpos, 1);
-    if (lane == 0) {
-        pfn = jc.fneg;
-        pfp = jc.fpos;
-    }
-
-    // ---- pass 2: emission ----
-    if (EMIT) {
-        const bool staged = vtot <= STAGE_V && itot <= STAGE_I;
-        float2* vdst = staged ? sm.sv : po.vout + vcur;
-        uint32_t* i32dst = staged ? sm.si : (po.bits == 32 ? (uint32_t*)po.iout + icur : nullptr);
-        uint16_t* i16dst = (!staged && po.bits == 16) ? (uint16_t*)po.iout + icur : nullptr;
-        const uint32_t vlim = staged ? STAGE_V : cap_left(po.vmax, vcur);
-        const uint32_t ilim = staged ? STAGE_I : cap_left(po.imax, icur);
-        uint32_t vo = vrel, io = irel;
-        uint32_t pneg = pfn, ppos = pfp;
-        V2 ppn = jc.pn, pnn = jc.nn;
-        if (k0 < kend && k0 != nj && exact) join_side_next(sm, k0 - 1, P, &ppn, &pnn);
-        for (uint32_t k = k0; k < kend; ++k) {
-            float2 a = sm.kp[(k - 1) & RMASK], b = sm.kp[k & RMASK], c = sm.kp[(k + 1) & RMASK];
-            V2 prev = V2{a.x, a.y}, cur = V2{b.x, b.y}, nxt = V2{c.x, c.y};
-            bool flat = sm.kflat[k & RMASK] != 0;
-            V2 pe = cur - prev;
-            bool fast = flat && dot(pe, nxt - cur) > 0.0f;
-            const uint32_t my_id = po.id_base + vcur + vo;
-            if (fast) {
-                V2 pt = pe / vlength(pe);
-                V2 ne = nxt - cur;
-                V2 nt = ne / vlength(ne);
-                V2 nrm = compute_normal(pt, nt);
-                V2 pn = cur + nrm * P.hw, nn = cur - nrm * P.hw;
-                bool skip = exact && dot(pe, pn - ppn) < 0.0f && dot(pe, nn - pnn) < 0.0f;
-                ppn = pn;
-                pnn = nn;
-                uint32_t pos_id = INVALID_ID, neg_id = INVALID_ID;
-                if (!skip) {
-                    if (vo + 2 <= vlim) {
-                        vdst[vo] = make_float2(pn.x, pn.y);
-                        vdst[vo + 1] = make_float2(nn.x, nn.y);
-                    } else {
-                        st = LYON_ERR_INTERNAL;
-                    }
-                    pos_id = my_id;
-                    neg_id = my_id + 1;
-                    vo += 2;
-                }
-                if (k >= 2) {
-                    Sink s{my_id, 0, 0, nullptr, nullptr, 32};
-                    if (i32dst) s.iout = i32dst + io;
-                    if (i16dst) {
-                        s.iout = i16dst + io;
-                        s.index_bits = 16;
-                    }
-                    s.icap = cap_left(ilim, io);
-                    edge_triangles(pneg, ppos, neg_id, pos_id, &s);
-                    if (s.overflow) st = LYON_ERR_INTERNAL;
-                    io += s.ni;
-                }
-                pneg = neg_id;
-                ppos = pos_id;
-            } else {
-                DEP d;
-                SlowJoin sj;
-                slow_join_geometry(&d, prev, cur, flat, nxt, P, &sj, &st);
-                ppn = sj.pn;
-                pnn = sj.nn;
-                Sink s;
-                s.id_base = my_id;
-                s.nv = 0;
-                s.ni = 0;
-                s.vout = vdst + vo;
-                s.index_bits = i16dst ? 16 : 32;
-                s.iout = i16dst ? (void*)(i16dst + io) : (void*)(i32dst + io);
-                s.vcap = cap_left(vlim, vo);
-                s.icap = cap_left(ilim, io);
-                s.overflow = false;
-                slow_join_emit(&d, &d, s, k >= 2, pneg, ppos, true, P, &st);
-                if (s.overflow) st = LYON_ERR_INTERNAL;
-                edge_ids_from(d, &pneg, &ppos);
-                vo += s.nv;
-                io += s.ni;
-            }
-        }
-        __syncwarp();
-        if (staged) {
-            // Coalesced copy-out of the chunk's vertices and indices.
-            const float* sf = reinterpret_cast<const float*>(sm.sv);
-            float* df = reinterpret_cast<float*>(po.vout + vcur);
-            for (uint32_t w = lane; w < 2 * vtot; w += 32) df[w] = sf[w];
-            if (po.bits == 16) {
-                uint16_t* di = (uint16_t*)po.iout + icur;
-                for (uint32_t w = lane; w < itot; w += 32) di[w] = (uint16_t)sm.si[w];
-            } else {
-                uint32_t* di = (uint32_t*)po.iout + icur;
-                for (uint32_t w = lane; w < itot; w += 32) di[w] = sm.si[w];
-            }
-        }
-    }
-
-    // ---- carry, firsts[1] ----
-    const uint32_t last_k = nj + count - 1;
-    if (k0 <= last_k && last_k < kend) {
-        float2 a = sm.kp[(last_k - 1) & RMASK], b = sm.kp[last_k & RMASK],
-               c = sm.kp[(last_k + 1) & RMASK];
-        join_dep_with_ids(&sm.carry, V2{a.x, a.y}, V2{b.x, b.y}, V2{c.x, c.y},
-                          sm.kflat[last_k & RMASK] != 0, last_fast, last_skip,
-                          base_id + last_voff, P, &st);
-    }
-    if (k0 <= 1 && 1 < kend) {
-        // J_1 is the first join of lane 0's run in the first chunk of the sub-path.
-        float2 a = sm.kp[0], b = sm.kp[1], c = sm.kp[2];
-        join_dep_with_ids(&sm.first1, V2{a.x, a.y}, V2{b.x, b.y}, V2{c.x, c.y},
-                          sm.kflat[1] != 0, k1_fast, k1_skip, base_id, P, &st);
-    }
-    __syncwarp();
-    const uint32_t owner = (last_k - nj) / RUN;
-    bool lsym = __shfl_sync(FULL, last_fast ? true : (P.line_join != LYON_JOIN_MITER_CLIP),
-                            (int)owner);
-    jc = carry_from_dep(sm.carry, lsym);
-    if (__any_sync(FULL, st != LYON_OK)) {
-        int e = __reduce_max_sync(FULL, st);
-        if (status == LYON_OK) status = e;
-    }
-    vcur += vtot;
-    icur += itot;
-    __syncwarp();
+    *out = f;
 }
 
 // The tail of a sub-path on lane 0: stroke.rs:1179-1279 (end, close) and 1322-1378
-// (end_with_caps).
+// (end_with_caps). `lastp`/`lastflat` are the last kept point P[n-1]; sm.last holds the join at
+// P[n-2] when n >= 3.
 __device__ __noinline__ void subpath_tail(WarpSmem& sm, uint32_t n, bool close,
-                                          bool may_need_empty_cap, const StrokeParams& P,
-                                          Sink& s, int* status) {
+                                          bool may_need_empty_cap, V2 lastp, bool lastflat,
+                                          const StrokeParams& P, Sink& s, int* status) {
     may_need_empty_cap |= close && n == 1;
     if (close && n > 2) {
         SeqBuffer pb;
-        pb.pts[0] = sm.carry;
-        float2 ql = sm.kp[(n - 1) & RMASK];
-        dep_init(pb.pts[1], V2{ql.x, ql.y}, P.hw, P.line_join, sm.kflat[(n - 1) & RMASK] != 0);
+        pb.pts[0] = sm.last;
+        dep_init(pb.pts[1], lastp, P.hw, P.line_join, lastflat);
         pb.start = 0;
         pb.count = 2;
         pb.n = n;
@@ -561,10 +277,9 @@ __device__ __noinline__ void subpath_tail(WarpSmem& sm, uint32_t n, bool close,
         return;
     }
     if (n >= 2) {
-        DEP p0 = (n == 2) ? sm.first0 : sm.carry;
+        DEP p0 = (n == 2) ? sm.first0 : sm.last;
         DEP p1;
-        float2 ql = sm.kp[(n - 1) & RMASK];
-        dep_init(p1, V2{ql.x, ql.y}, P.hw, P.line_join, sm.kflat[(n - 1) & RMASK] != 0);
+        dep_init(p1, lastp, P.hw, P.line_join, lastflat);
         V2 tan = normalize(p1.pos - p0.pos);
         V2 nn = V2{-tan.y, tan.x} * p1.hw;
         p1.s[SP].prev = p1.pos + nn;
@@ -578,93 +293,313 @@ __device__ __noinline__ void subpath_tail(WarpSmem& sm, uint32_t n, bool close,
     }
 }
 
-// Generates the window steps [cb, min(cb + CH, S_w)) into the ring at kept indices n0...
-// (lane i owns RUN consecutive steps) and updates the t carry.
-__device__ __forceinline__ void gen_steps(WarpSmem& sm, int lane, uint32_t vi, uint32_t nv,
-                                          uint32_t sincl, uint32_t S_w, uint32_t cb, uint32_t n0,
-                                          TCarry& tc) {
-    const uint32_t g0 = cb + (uint32_t)lane * RUN;
-    const uint32_t gend = min(g0 + RUN, S_w);
-    // Owner verb of g0: first lane whose inclusive step count exceeds it.
-    const uint32_t gq = min(g0, S_w - 1);
-    uint32_t lo = 0, hi = nv - 1;
-#pragma unroll
-    for (int it = 0; it < 5; ++it) {
-        uint32_t mid = (lo + hi) >> 1;
-        uint32_t vmid = __shfl_sync(FULL, sincl, mid);
-        if (vmid > gq) hi = mid; else lo = mid + 1;
-        if (lo > hi) lo = hi;
-    }
-    uint32_t j = lo;
-    const TCarry c0 = tc;
-    uint32_t my_verb = 0xFFFFFFFFu, my_unit = 0, my_k = 0;
+// Steps [cb, cb + 32) of the current verb window (lane = step): flattened points, merge filter,
+// joins, output. See the file comment.
+template <bool EMIT>
+__device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, const uint32_t vi,
+                                              const uint32_t nv, const uint32_t sincl,
+                                              const uint32_t S_w, const uint32_t cb,
+                                              const StrokeParams& P, const PathOut& po,
+                                              SubState& S, uint32_t& vcur, uint32_t& icur,
+                                              int& status) {
+    const uint32_t nsteps = min(32u, S_w - cb);
+    const bool active = (uint32_t)lane < nsteps;
+
+    // ---- 1. the flattened point of step cb + lane ----
+    V2 q;
+    bool flat = false;
+    uint32_t my_verb = NO_VERB, my_unit = 0, my_k = 0;
     float my_t = 0.0f;
-    if (g0 < gend) {
-        uint32_t r = g0 - sm.verbs[j].excl;
-        int kind = sm.verbs[j].kind;
-        uint32_t vsteps = sm.verbs[j].steps;
-        int tunit = -1;
-        uint32_t tk = 0;
-        float t = 0.0f;
-        for (uint32_t g = g0; g < gend; ++g) {
-            while (r >= vsteps) {
-                ++j;
-                r = 0;
-                kind = sm.verbs[j].kind;
-                vsteps = sm.verbs[j].steps;
-                tunit = -1;
-            }
-            const VerbSlot& sl = sm.verbs[j];
-            V2 pos;
-            bool flat = false;
-            my_verb = 0xFFFFFFFFu;
-            if (kind == LYON_VERB_BEGIN || kind == LYON_VERB_LINE_TO) {
-                pos = sl.toA;
-            } else {
-                const uint32_t mA = sl.mA;
-                const bool unitA = r < mA;
-                const uint32_t kk = unitA ? r + 1 : r - mA + 1;
-                const uint32_t m = unitA ? mA : sl.mB;
-                const int u = unitA ? 0 : 1;
-                if (kk < m) {
-                    const float s = unitA ? sl.sA : sl.sB;
-                    if (tunit == u && tk + 1 == kk) {
-                        t = t + s;
-                    } else {
-                        uint32_t bk = 0;
-                        float bt = 0.0f;
-                        if (c0.verb == vi + j && c0.unit == (uint32_t)u && c0.k <= kk) {
-                            bk = c0.k;
-                            bt = c0.t;
-                        }
-                        t = accumulate_t(s, bk, bt, kk);
-                    }
-                    tunit = u;
-                    tk = kk;
-                    pos = poly_sample(unitA ? sl.pA : sl.pB, t);
-                    flat = t != 1.0f;
-                    my_verb = vi + j;
-                    my_unit = (uint32_t)u;
-                    my_k = kk;
-                    my_t = t;
-                } else {
-                    pos = unitA ? sl.toA : sl.toB;
-                    tunit = -1;
+    {
+        const uint32_t gq = min(cb + (uint32_t)lane, S_w - 1);
+        // Owner verb: the first whose inclusive step count exceeds gq.
+        uint32_t lo = 0, hi = nv - 1;
+#pragma unroll
+        for (int it = 0; it < 5; ++it) {
+            const uint32_t mid = (lo + hi) >> 1;
+            const uint32_t vmid = __shfl_sync(FULL, sincl, mid);
+            if (vmid > gq) hi = mid; else lo = mid + 1;
+            if (lo > hi) lo = hi;
+        }
+        const VerbSlot& sl = sm.verbs[lo];
+        const uint32_t r = gq - sl.excl;
+        const int kind = sl.kind;
+        if (kind == LYON_VERB_BEGIN || kind == LYON_VERB_LINE_TO) {
+            q = sl.toA;
+        } else {
+            const uint32_t mA = sl.mA;
+            const bool unitA = r < mA;
+            const uint32_t kk = unitA ? r + 1 : r - mA + 1;
+            const uint32_t m = unitA ? mA : sl.mB;
+            if (kk < m) {
+                const float s = unitA ? sl.sA : sl.sB;
+                const uint32_t u = unitA ? 0u : 1u;
+                uint32_t bk = 0;
+                float bt = 0.0f;
+                if (S.tc.verb == vi + lo && S.tc.unit == u && S.tc.k <= kk) {
+                    bk = S.tc.k;
+                    bt = S.tc.t;
                 }
+                const float t = accumulate_t(s, bk, bt, kk);
+                const Poly* pp = unitA ? &sl.pA : &sl.pB;
+                q = poly_sample(*pp, t);
+                flat = t != 1.0f;
+                my_verb = vi + lo;
+                my_unit = u;
+                my_k = kk;
+                my_t = t;
+            } else {
+                q = unitA ? sl.toA : sl.toB;
             }
-            const uint32_t idx = (n0 + (g - cb)) & RMASK;
-            sm.kp[idx] = make_float2(pos.x, pos.y);
-            sm.kflat[idx] = flat ? 1 : 0;
-            ++r;
         }
     }
-    // t carry: the state after the chunk's last step.
-    const uint32_t last_g = min(cb + CH, S_w) - 1;
-    const int owner = (int)((last_g - cb) / RUN);
-    tc.verb = __shfl_sync(FULL, my_verb, owner);
-    tc.unit = __shfl_sync(FULL, my_unit, owner);
-    tc.k = __shfl_sync(FULL, my_k, owner);
-    tc.t = __shfl_sync(FULL, my_t, owner);
+    {
+        const int ow = (int)nsteps - 1;
+        S.tc.verb = __shfl_sync(FULL, my_verb, ow);
+        S.tc.unit = __shfl_sync(FULL, my_unit, ow);
+        S.tc.k = __shfl_sync(FULL, my_k, ow);
+        S.tc.t = __shfl_sync(FULL, my_t, ow);
+    }
+
+    // ---- 2. merge filter (stroke.rs:1530-1536) ----
+    const uint32_t n0 = S.n;
+    uint32_t keep = __ballot_sync(FULL, active);
+    {
+        V2 qp = shfl_up_v2(q, 1);
+        if (lane == 0) qp = S.c1;
+        const bool close =
+            active && (lane > 0 || n0 > 0) && too_close(qp, q, P.merge_threshold);
+        if (__any_sync(FULL, close)) {
+            // Replay the chain in order (every lane computes the same mask), then compact.
+            uint32_t km = 0, cnt = n0;
+            V2 L = S.c1;
+            bool mn = S.mnec;
+            for (uint32_t i = 0; i < nsteps; ++i) {
+                const V2 qi = shfl_v2(q, (int)i);
+                if (cnt > 0 && too_close(L, qi, P.merge_threshold)) {
+                    if (cnt == 1) mn = true;
+                } else {
+                    km |= 1u << i;
+                    L = qi;
+                    ++cnt;
+                }
+            }
+            keep = km;
+            S.mnec = mn;
+            const uint32_t nkk = __popc(km);
+            const int src = (uint32_t)lane < nkk ? (int)__fns(km, 0, lane + 1) : 0;
+            q = shfl_v2(q, src);
+            flat = __shfl_sync(FULL, (int)flat, src) != 0;
+        }
+    }
+    const uint32_t nk = __popc(keep);
+    if (nk == 0) return;
+    const bool live = (uint32_t)lane < nk;
+
+    // ---- 3. joins: lane L performs the join at kept point n0 + L - 1 ----
+    const int k = (int)n0 + lane - 1;
+    V2 cur = shfl_up_v2(q, 1);
+    V2 prv = shfl_up_v2(q, 2);
+    bool fcur = __shfl_up_sync(FULL, (int)flat, 1) != 0;
+    if (lane == 0) {
+        cur = S.c1;
+        prv = S.c2;
+        fcur = S.f1;
+    } else if (lane == 1) {
+        prv = S.c1;
+    }
+    const V2 ne = q - cur;
+    const V2 nt = ne / vlength(ne);
+    V2 pt = shfl_up_v2(nt, 1);
+    if (lane == 0) pt = S.jtan;
+    const V2 pe = cur - prv;
+    const bool isjoin = live && k >= 1;
+    const bool fast = isjoin && fcur && dot(pe, ne) > 0.0f;
+    const bool slow = isjoin && !fast;
+
+    uint32_t vcnt = 0, jt = 0, to_f = 0, from_f = EF_ALLINV;
+    uint32_t fneg_rel = INVALID_ID, fpos_rel = INVALID_ID;
+    bool sym = true, skip = false, have_sides = false;
+    V2 pn = V2{0.0f, 0.0f}, nn = V2{0.0f, 0.0f};
+    int st = LYON_OK;
+    DEP d;
+    if (fast) {
+        vcnt = 2;
+        from_f = 0;
+        fneg_rel = 1;
+        fpos_rel = 0;
+    }
+    if (live && k == 0) {
+        // The first point: side points from its first edge (stroke.rs:1538-1556).
+        const V2 n = V2{-nt.y, nt.x} * P.hw;
+        pn = cur + n;
+        nn = cur - n;
+        have_sides = true;
+    }
+    if (slow) {
+        SlowJoin sj;
+        slow_join_geometry(&d, prv, cur, fcur, q, P, &sj, &st);
+        vcnt = sj.vcount;
+        jt = sj.jtris;
+        to_f = sj.to_f;
+        from_f = sj.from_f;
+        fneg_rel = sj.from_neg_rel;
+        fpos_rel = sj.from_pos_rel;
+        sym = sj.sym;
+        pn = sj.pn;
+        nn = sj.nn;
+        have_sides = true;
+    }
+    // flattened_step's skip test (stroke.rs:1778-1782). The emit pass evaluates it. The count pass
+    // first tries a bound: with the previous join's side points symmetric about the previous
+    // point, the test needs the previous edge to be shorter than a few ulps of the coordinates
+    // involved (2^-17 times their magnitude plus 3 half widths covers the roundings of both
+    // joins' side points), so when every fast lane's edge is longer the test cannot fire;
+    // otherwise the count pass evaluates it exactly as well.
+    bool exact = EMIT;
+    if (!EMIT) {
+        bool psym = __shfl_up_sync(FULL, (int)sym, 1) != 0;
+        if (lane == 0) psym = S.jsym;
+        bool ok = true;
+        if (fast) {
+            const float m = fmaxf(fmaxf(fabsf(cur.x), fabsf(cur.y)),
+                                  fmaxf(fabsf(prv.x), fabsf(prv.y))) + 3.0f * P.hw;
+            const float bnd = m * 7.62939453125e-06f;  // 2^-17
+            ok = psym && sqlen(pe) > bnd * bnd;
+        }
+        exact = __any_sync(FULL, !ok);
+    }
+    if (exact) {
+        if (fast) {
+            const V2 nrm = compute_normal(pt, nt);
+            pn = cur + nrm * P.hw;
+            nn = cur - nrm * P.hw;
+            have_sides = true;
+        }
+        V2 ppn = shfl_up_v2(pn, 1), pnn = shfl_up_v2(nn, 1);
+        if (lane == 0) {
+            if (!S.jside_valid) fast_join_sides(S.c3, S.c2, S.c1, P.hw, &S.jpn, &S.jnn);
+            ppn = S.jpn;
+            pnn = S.jnn;
+        }
+        skip = fast && dot(pe, pn - ppn) < 0.0f && dot(pe, nn - pnn) < 0.0f;
+        if (skip) {
+            vcnt = 0;
+            from_f = to_f = EF_ALLINV;
+            fneg_rel = fpos_rel = INVALID_ID;
+        }
+    }
+
+    // ---- 4. counts, offsets, output ----
+    uint32_t pf = __shfl_up_sync(FULL, from_f, 1);
+    if (lane == 0) pf = S.jfrom_f;
+    const uint32_t e = (isjoin && k >= 2) ? edge_count_flags(pf, to_f) : 0u;
+    const uint32_t icnt = 3u * (jt + e);
+    const uint32_t vincl = warp_incl_scan(vcnt, lane);
+    const uint32_t iincl = warp_incl_scan(icnt, lane);
+    const uint32_t vtot = __shfl_sync(FULL, vincl, 31);
+    const uint32_t itot = __shfl_sync(FULL, iincl, 31);
+    const uint32_t vrel = vincl - vcnt;
+    const uint32_t irel = iincl - icnt;
+    const uint32_t base = po.id_base + vcur + vrel;
+    const uint32_t fneg = fneg_rel == INVALID_ID ? INVALID_ID : base + fneg_rel;
+    const uint32_t fpos = fpos_rel == INVALID_ID ? INVALID_ID : base + fpos_rel;
+
+    if (EMIT) {
+        uint32_t pfn = __shfl_up_sync(FULL, fneg, 1);
+        uint32_t pfp = __shfl_up_sync(FULL, fpos, 1);
+        if (lane == 0) {
+            pfn = S.jfneg;
+            pfp = S.jfpos;
+        }
+        const uint32_t vo = vcur + vrel;
+        const uint32_t io = icur + irel;
+        if (fast) {
+            if (!skip) {
+                if (vo + 2 <= po.vmax) {
+                    float2* dst = po.vout + vo;
+                    if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+                        *reinterpret_cast<float4*>(dst) = make_float4(pn.x, pn.y, nn.x, nn.y);
+                    } else {
+                        dst[0] = make_float2(pn.x, pn.y);
+                        dst[1] = make_float2(nn.x, nn.y);
+                    }
+                } else {
+                    st = LYON_ERR_INTERNAL;
+                }
+            }
+            if (k >= 2) {
+                Sink s;
+                s.id_base = base;
+                s.nv = 0;
+                s.ni = 0;
+                s.vout = nullptr;
+                s.index_bits = po.bits;
+                s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + io)
+                                       : (void*)((uint32_t*)po.iout + io);
+                s.icap = cap_left(po.imax, io);
+                s.overflow = false;
+                edge_triangles(pfn, pfp, skip ? INVALID_ID : base + 1, skip ? INVALID_ID : base,
+                               &s);
+                if (s.overflow) st = LYON_ERR_INTERNAL;
+            }
+        }
+        if (slow) {
+            Sink s;
+            s.id_base = base;
+            s.nv = 0;
+            s.ni = 0;
+            s.vout = po.vout + vo;
+            s.index_bits = po.bits;
+            s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + io)
+                                   : (void*)((uint32_t*)po.iout + io);
+            s.vcap = cap_left(po.vmax, vo);
+            s.icap = cap_left(po.imax, io);
+            s.overflow = false;
+            slow_join_emit(&d, &d, s, k >= 2, pfn, pfp, true, P, &st);
+            if (s.overflow) st = LYON_ERR_INTERNAL;
+        }
+    }
+
+    // ---- lyon's firsts (stroke.rs:1624-1627) ----
+    if (live && k == 0) write_first0(&sm.first0, cur, true, pn, nn, P);
+    if (live && k == -1 && nk == 1) write_first0(&sm.first0, q, false, pn, nn, P);
+    if (live && k == 1) join_dep_with_ids(&sm.first1, prv, cur, q, fcur, fast, skip, base, P, &st);
+
+    // ---- carry to the next chunk ----
+    {
+        const int last = (int)nk - 1;
+        const V2 q3 = shfl_v2(q, last >= 2 ? last - 2 : 0);
+        const V2 q2 = shfl_v2(q, last >= 1 ? last - 1 : 0);
+        const bool fl2 = __shfl_sync(FULL, (int)flat, last >= 1 ? last - 1 : 0) != 0;
+        const V2 q1 = shfl_v2(q, last);
+        const bool fl1 = __shfl_sync(FULL, (int)flat, last) != 0;
+        const V2 oc1 = S.c1, oc2 = S.c2;
+        const bool of1 = S.f1;
+        S.c3 = nk >= 3 ? q3 : (nk == 2 ? oc1 : oc2);
+        S.c2 = nk >= 2 ? q2 : oc1;
+        S.f2 = nk >= 2 ? fl2 : of1;
+        S.c1 = q1;
+        S.f1 = fl1;
+        S.jtan = shfl_v2(nt, last);
+        S.jpn = shfl_v2(pn, last);
+        S.jnn = shfl_v2(nn, last);
+        S.jside_valid = __shfl_sync(FULL, (int)have_sides, last) != 0;
+        S.jfneg = __shfl_sync(FULL, fneg, last);
+        S.jfpos = __shfl_sync(FULL, fpos, last);
+        S.jfrom_f = __shfl_sync(FULL, from_f, last);
+        S.jsym = __shfl_sync(FULL, (int)sym, last) != 0;
+        S.jfast = __shfl_sync(FULL, (int)fast, last) != 0;
+        S.jskip = __shfl_sync(FULL, (int)skip, last) != 0;
+        S.jbase = __shfl_sync(FULL, base, last);
+        S.n = n0 + nk;
+    }
+    if (__any_sync(FULL, st != LYON_OK)) {
+        const int em = __reduce_max_sync(FULL, st);
+        if (status == LYON_OK) status = em;
+    }
+    vcur += vtot;
+    icur += itot;
     __syncwarp();
 }
 
@@ -687,24 +622,26 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             status = LYON_ERR_INVALID_ARGUMENT;
             break;
         }
-        uint32_t n_kept = 0;
-        uint32_t next_join = 1;
-        bool mnec = false;
-        V2 lastk = V2{0.0f, 0.0f};
-        TCarry tc;
-        tc.verb = 0xFFFFFFFFu;
-        tc.unit = 0;
-        tc.k = 0;
-        tc.t = 0.0f;
+        SubState S;
+        S.n = 0;
+        S.c1 = S.c2 = S.c3 = V2{0.0f, 0.0f};
+        S.f1 = S.f2 = false;
+        S.jtan = V2{0.0f, 0.0f};
+        S.jpn = S.jnn = V2{0.0f, 0.0f};
+        S.jside_valid = false;
+        S.jfneg = S.jfpos = INVALID_ID;
+        S.jfrom_f = EF_ALLINV;
+        S.jsym = true;
+        S.jfast = S.jskip = false;
+        S.jbase = 0;
+        S.mnec = false;
+        S.tc.verb = NO_VERB;
+        S.tc.unit = 0;
+        S.tc.k = 0;
+        S.tc.t = 0.0f;
         bool ended = false, closed = false;
-        bool first_sides_done = false;
-        JCarry jc;
-        jc.pn = jc.nn = V2{0.0f, 0.0f};
-        jc.from_f = EF_NEG_INV | EF_POS_INV | EF_SELF_EQ;
-        jc.fneg = jc.fpos = INVALID_ID;
-        jc.sym = true;
         while (vi < v_end && status == LYON_OK) {
-            // ---- 1. verb window ----
+            // ---- verb window ----
             const uint32_t v = vi + (uint32_t)lane;
             const bool valid = v < v_end;
             int kind = valid ? (int)A.verbs[v] : LYON_VERB_END;
@@ -731,66 +668,11 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             const uint32_t S_w = __shfl_sync(FULL, sincl, 31);
             const int last_kind = __shfl_sync(FULL, kind, nv - 1);
             __syncwarp();
-
-            // ---- 2./3. points, CH at a time ----
-            for (uint32_t cb = 0; cb < S_w; cb += CH) {
-                const uint32_t nsteps = min(CH, S_w - cb);
-                const uint32_t n0 = n_kept;
-                gen_steps(sm, lane, vi, nv, sincl, S_w, cb, n0, tc);
-                // Merge filter (stroke.rs:1530-1536).
-                bool close_any = false;
-                {
-                    const uint32_t g0 = (uint32_t)lane * RUN;
-                    const uint32_t ge = min(g0 + RUN, nsteps);
-                    for (uint32_t g = g0; g < ge; ++g) {
-                        const uint32_t idx = n0 + g;
-                        if (idx == 0) continue;
-                        float2 q = sm.kp[idx & RMASK];
-                        V2 prevp;
-                        if (g == 0) {
-                            prevp = lastk;
-                        } else {
-                            float2 pq = sm.kp[(idx - 1) & RMASK];
-                            prevp = V2{pq.x, pq.y};
-                        }
-                        if (too_close(prevp, V2{q.x, q.y}, P.merge_threshold)) close_any = true;
-                    }
-                }
-                if (__any_sync(FULL, close_any)) {
-                    uint32_t nk = 0;
-                    bool m = mnec;
-                    if (lane == 0) nk = merge_compact(sm, n0, nsteps, lastk, P.merge_threshold, &m);
-                    n_kept = __shfl_sync(FULL, nk, 0);
-                    mnec = __shfl_sync(FULL, m, 0);
-                } else {
-                    n_kept = n0 + nsteps;
-                }
-                __syncwarp();
-                {
-                    float2 lq = sm.kp[(n_kept - 1) & RMASK];
-                    lastk = V2{lq.x, lq.y};
-                }
-                if (!first_sides_done && n_kept >= 2) {
-                    if (lane == 0) {
-                        float2 q0 = sm.kp[0];
-                        float2 q1 = sm.kp[1];
-                        dep_init(sm.first0, V2{q0.x, q0.y}, P.hw, P.line_join, false);
-                        first_point_sides(sm.first0, V2{q1.x, q1.y}, P.hw);
-                    }
-                    first_sides_done = true;
-                    __syncwarp();
-                    jc = carry_from_dep(sm.first0, true);
-                } else if (n_kept == 1 && lane == 0 && !first_sides_done) {
-                    float2 q0 = sm.kp[0];
-                    dep_init(sm.first0, V2{q0.x, q0.y}, P.hw, P.line_join, false);
-                }
-                __syncwarp();
-                // ---- 4. joins, CH at a time ----
-                while (n_kept >= next_join + 2 && n_kept - 1 - next_join >= CH) {
-                    process_joins<EMIT>(sm, lane, next_join, CH, P, po, vcur, icur, status, jc);
-                    next_join += CH;
-                }
+            for (uint32_t cb = 0; cb < S_w; cb += 32) {
+                process_chunk<EMIT>(sm, lane, vi, nv, sincl, S_w, cb, P, po, S, vcur, icur,
+                                    status);
             }
+            __syncwarp();
             vi += nv;
             pc += __shfl_sync(FULL, pincl, 31);
             if (last_kind == LYON_VERB_END || last_kind == LYON_VERB_CLOSE) {
@@ -800,16 +682,13 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             }
         }
         if (!ended || status != LYON_OK) break;
-        // Remaining joins.
-        while (n_kept >= 3 && next_join <= n_kept - 2) {
-            const uint32_t cnt = min(CH, n_kept - 1 - next_join);
-            process_joins<EMIT>(sm, lane, next_join, cnt, P, po, vcur, icur, status, jc);
-            next_join += cnt;
-        }
-        // ---- 5. tail ----
+        // ---- tail ----
         uint32_t tv = 0, ti = 0;
         int tst = LYON_OK;
         if (lane == 0) {
+            if (S.n >= 3)
+                join_dep_with_ids(&sm.last, S.c3, S.c2, S.c1, S.f2, S.jfast, S.jskip, S.jbase, P,
+                                  &tst);
             Sink s;
             s.id_base = po.id_base + vcur;
             s.nv = 0;
@@ -824,7 +703,7 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             s.vcap = cap_left(po.vmax, vcur);
             s.icap = cap_left(po.imax, icur);
             s.overflow = false;
-            subpath_tail(sm, n_kept, closed, mnec, P, s, &tst);
+            subpath_tail(sm, S.n, closed, S.mnec, S.c1, S.f1, P, s, &tst);
             if (s.overflow && tst == LYON_OK) tst = LYON_ERR_INTERNAL;
             tv = s.nv;
             ti = s.ni;
@@ -891,16 +770,22 @@ __global__ void __launch_bounds__(STROKE_WARPS * 32, LG_STROKE_MIN_BLOCKS)
 }
 
 constexpr size_t STROKE_SMEM = sizeof(WarpSmem) * STROKE_WARPS;
+constexpr int MAX_CONFIGURED_DEVICES = 64;
+static bool smem_configured[MAX_CONFIGURED_DEVICES] = {};
 
-static bool smem_configured = false;
-
+// The dynamic shared memory limit is a per-device attribute of each kernel: set it once per
+// device the kernels run on.
 static void configure_smem() {
-    if (smem_configured) return;
-    cudaFuncSetAttribute(stroke_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)STROKE_SMEM);
-    cudaFuncSetAttribute(stroke_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)STROKE_SMEM);
-    smem_configured = true;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_CONFIGURED_DEVICES) return;
+    if (smem_configured[dev]) return;
+    if (STROKE_SMEM > 48 * 1024) {
+        cudaFuncSetAttribute(stroke_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)STROKE_SMEM);
+        cudaFuncSetAttribute(stroke_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)STROKE_SMEM);
+    }
+    smem_configured[dev] = true;
 }
 
 int stroke_blocks_per_sm() {

@@ -8,21 +8,26 @@
 //      lane: lyon's segment counts (`flattened_segments_wang`, quadratic_bezier.rs:943-974,
 //      cubic_bezier.rs:1369-1403) and the sharp-turn split of quadratics (stroke.rs:2755-2779);
 //      a warp scan of the per-verb step counts gives every step its verb;
-//   2. the window's steps are processed 32 at a time, lane = step: the flattened point (lyon's
+//   2. the general joins the window will need, at the end points of its lines and curves, are
+//      computed ahead, one per lane, from the neighbours they will have unless the merge filter
+//      removes one (`speculate_joins`); a join uses that result only after checking that its
+//      actual neighbours are the assumed ones, bit for bit, and computes its own otherwise;
+//   3. the window's steps are processed 32 at a time, lane = step: the flattened point (lyon's
 //      accumulated parameter t is reproduced bit for bit in closed form by accumulate_t, from
 //      the previous chunk's last value), then the merge filter (stroke.rs:1530-1536): a ballot
 //      finds points within the threshold of their predecessor and only then is the chain
 //      replayed and the kept points compacted across lanes;
-//   3. lane L then performs the join at the previous kept point, whose neighbours come from
+//   4. lane L then performs the join at the previous kept point, whose neighbours come from
 //      lanes L-1 and L-2 (or the carry from the previous chunk): flattening-step joins
-//      (stroke.rs:1743-1806) are straight-line register arithmetic; other joins, the first
-//      point's sides and the first join's record go through out-of-line functions;
-//   4. a warp scan of the per-join vertex/index counts places every join's output; each lane
-//      writes its own vertices and indices;
-//   5. lane 0 runs the sub-path tail (caps, closing, empty caps).
-// The count kernel performs steps 1-5 without writing (it proves, by a bound, that the skip test
-// of flattened_step cannot fire instead of evaluating it, see below); a look-back scan turns its
-// per-path counts into offsets; the emit kernel repeats the walk and writes at those offsets.
+//      (stroke.rs:1743-1806) are straight-line register arithmetic; a warp scan of the per-join
+//      vertex/index counts places every join's output and each lane writes its own; the output
+//      of the general joins computed ahead is written at the end of the window, one per lane;
+//   5. the tail of the path's last sub-path (caps, closing, empty caps) is queued; the warp
+//      processes its queue 32 paths at a time, one per lane. Tails of earlier sub-paths of a
+//      multi-sub-path path run at once on lane 0 (the next sub-path's output follows them).
+// The count kernel performs the same walk without writing (it proves, by a bound, that the skip
+// test of flattened_step cannot fire instead of evaluating it, see below); a look-back scan turns
+// its per-path counts into offsets; the emit kernel repeats the walk and writes at those offsets.
 #include "stroke_core.cuh"
 #include "kernels.h"
 
@@ -38,6 +43,7 @@ constexpr int STROKE_WARPS = LG_STROKE_WARPS;
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr uint32_t MAX_VERB_STEPS = 1u << 26;
 constexpr uint32_t NO_VERB = 0xFFFFFFFFu;
+constexpr uint32_t NO_SLOT = 0xFFu;
 constexpr uint32_t EF_ALLINV = EF_NEG_INV | EF_POS_INV | EF_SELF_EQ;
 
 struct VerbSlot {
@@ -49,11 +55,38 @@ struct VerbSlot {
     int kind;
 };
 
+// A general join at the end point of a unit (a line, a curve, or one part of a split quadratic),
+// computed before the window's chunks from the neighbours it assumed.
+struct SpecSlot {
+    V2 prev, cur, next;
+    V2 pn, nn;
+    uint32_t from_f, to_f, fneg_rel, fpos_rel, vcount, jtris;
+    int st;
+    uint32_t flags;  // SPEC_VALID, SPEC_SYM
+};
+constexpr uint32_t SPEC_VALID = 1u, SPEC_SYM = 2u;
+
+// Output of a join computed ahead, written at the end of the window.
+struct EmitJob {
+    uint32_t slot, vo, io, base, pfn, pfp, has_edge;
+};
+
+// Everything the tail of a sub-path needs (stroke.rs:1179-1378): the first three and the last
+// three kept points and how their joins were done.
+struct TailJob {
+    uint32_t path, n, flags, base1, jbase, vcur, icur;
+    V2 p0, p1, p2, c3, c2, c1;
+};
+enum : uint32_t {
+    TJ_CLOSED = 1u, TJ_MNEC = 2u, TJ_FLAT1 = 4u, TJ_FAST1 = 8u, TJ_SKIP1 = 16u, TJ_F1 = 32u,
+    TJ_F2 = 64u, TJ_JFAST = 128u, TJ_JSKIP = 256u
+};
+
 struct WarpSmem {
     VerbSlot verbs[32];
-    DEP first0;  // first kept point of the sub-path, with its side points (lyon's firsts[0])
-    DEP first1;  // the first join after its processing, with ids (lyon's firsts[1])
-    DEP last;    // the last join, with ids (for the tail)
+    SpecSlot spec[64];
+    EmitJob ej[64];
+    TailJob tq[32];
 };
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
@@ -71,6 +104,10 @@ __device__ __forceinline__ V2 shfl_v2(V2 v, int src) {
 __device__ __forceinline__ V2 shfl_up_v2(V2 v, int d) {
     return V2{__shfl_up_sync(FULL, v.x, d), __shfl_up_sync(FULL, v.y, d)};
 }
+__device__ __forceinline__ bool same_bits(V2 a, V2 b) {
+    return __float_as_uint(a.x) == __float_as_uint(b.x) &&
+           __float_as_uint(a.y) == __float_as_uint(b.y);
+}
 
 struct PathOut {
     uint32_t id_base;  // id of the path's first vertex
@@ -82,6 +119,43 @@ struct PathOut {
 
 __device__ __forceinline__ uint32_t cap_left(uint32_t total, uint32_t used) {
     return used < total ? total - used : 0u;
+}
+
+template <bool EMIT>
+__device__ __forceinline__ PathOut path_out(const StrokeArgs& A, uint32_t path) {
+    PathOut po;
+    po.bits = A.index_bits;
+    if (EMIT) {
+        const uint64_t vo = A.vtx_offsets[path];
+        const uint64_t io = A.idx_offsets[path];
+        po.vout = reinterpret_cast<float2*>(A.vertices) + vo;
+        po.iout = A.index_bits == 16 ? (void*)((uint16_t*)A.indices + io)
+                                     : (void*)((uint32_t*)A.indices + io);
+        po.id_base = A.vertex_offset + (A.index_mode == LYON_INDEX_GLOBAL ? (uint32_t)vo : 0u);
+        po.vmax = A.vtx_counts[path];
+        po.imax = A.idx_counts[path];
+    } else {
+        po.vout = nullptr;
+        po.iout = nullptr;
+        po.id_base = 0;
+        po.vmax = 0xFFFFFFFFu;
+        po.imax = 0xFFFFFFFFu;
+    }
+    return po;
+}
+
+// Final per-path bookkeeping: the count pass records counts and status; the emit pass flags a
+// path whose walk disagreed with the count pass (its writes were bounded by the path's range).
+template <bool EMIT>
+__device__ __forceinline__ void finish_path(const StrokeArgs& A, uint32_t path, uint32_t vc,
+                                            uint32_t ic, int st, const PathOut& po) {
+    if (!EMIT) {
+        A.vtx_counts[path] = st == LYON_OK ? vc : 0u;
+        A.idx_counts[path] = st == LYON_OK ? ic : 0u;
+        A.status[path] = st;
+    } else if (st != LYON_OK || vc != po.vmax || ic != po.imax) {
+        A.status[path] = st != LYON_OK ? st : LYON_ERR_INTERNAL;
+    }
 }
 
 // t state carried across step chunks: the chunk's last step.
@@ -97,6 +171,7 @@ struct SubState {
     uint32_t n;      // kept points so far
     V2 c1, c2, c3;   // the last three kept points: P[n-1], P[n-2], P[n-3]
     bool f1, f2;     // flattening-step flags of c1 and c2
+    uint32_t s1;     // spec slot of c1 (NO_SLOT unless it is a unit end point)
     V2 jtan;         // tangent of the edge c2 -> c1
     // The last processed join (at P[n-2]); when n == 2, the first point (its sides only).
     V2 jpn, jnn;        // its side "next" points
@@ -107,6 +182,10 @@ struct SubState {
     bool jfast, jskip;
     uint32_t jbase;         // id of the join's first vertex
     bool mnec;              // lyon's may_need_empty_cap
+    // The first three kept points and the first join (lyon's firsts, stroke.rs:1624-1627).
+    V2 p0, p1, p2;
+    bool flat1, fast1, skip1;
+    uint32_t base1;
     TCarry tc;
 };
 
@@ -188,6 +267,107 @@ __device__ __noinline__ uint32_t setup_verb(VerbSlot& out, int kind, uint32_t po
     return steps;
 }
 
+// The general joins at the end points of the window's units, one verb per lane (slots 2j and
+// 2j + 1 for the two units of verb j). Each assumes that the end point's neighbours are the
+// steps just before and after it (what they are unless the merge filter drops one); the step
+// before a unit's end point is its flattened point m - 1, the step after it the first point of
+// the next unit. `c1` is the sub-path's last kept point before the window, if any.
+__device__ __noinline__ void speculate_joins(WarpSmem& sm, int lane, uint32_t nv, uint32_t S_w,
+                                             const StrokeParams& P, V2 c1, bool have_c1) {
+    if ((uint32_t)lane >= nv) return;
+    const int j = lane;
+    const VerbSlot& sl = sm.verbs[j];
+    sm.spec[2 * j].flags = 0;
+    sm.spec[2 * j + 1].flags = 0;
+    const int kind = sl.kind;
+    if (kind != LYON_VERB_LINE_TO && kind != LYON_VERB_QUADRATIC_TO &&
+        kind != LYON_VERB_CUBIC_TO)
+        return;
+    const uint32_t nunits = kind == LYON_VERB_LINE_TO ? 1u : (sl.mB > 0 ? 2u : 1u);
+    for (uint32_t u = 0; u < nunits; ++u) {
+        const bool line = kind == LYON_VERB_LINE_TO;
+        const uint32_t m = line ? 1u : (u == 0 ? sl.mA : sl.mB);
+        const uint32_t ge = sl.excl + (line ? 0u : (u == 0 ? sl.mA - 1 : sl.mA + sl.mB - 1));
+        if (ge + 1 >= S_w) continue;
+        const V2 E = u == 0 ? sl.toA : sl.toB;
+        V2 next;
+        if (u == 0 && nunits == 2) {
+            next = sl.mB >= 2 ? poly_sample(sl.pB, sl.sB) : sl.toB;
+        } else {
+            const VerbSlot& nx = sm.verbs[j + 1];
+            if (nx.kind == LYON_VERB_LINE_TO) {
+                next = nx.toA;
+            } else if (nx.kind == LYON_VERB_QUADRATIC_TO || nx.kind == LYON_VERB_CUBIC_TO) {
+                next = nx.mA >= 2 ? poly_sample(nx.pA, nx.sA) : nx.toA;
+            } else {
+                continue;
+            }
+        }
+        V2 prev;
+        if (m >= 2) {
+            const float s = u == 0 ? sl.sA : sl.sB;
+            const float t = accumulate_t(s, 0, 0.0f, m - 1);
+            prev = poly_sample(u == 0 ? sl.pA : sl.pB, t);
+        } else if (u == 1) {
+            prev = sl.toA;
+        } else if (j > 0) {
+            const VerbSlot& pv = sm.verbs[j - 1];
+            prev = (pv.kind == LYON_VERB_QUADRATIC_TO && pv.mB > 0) ? pv.toB : pv.toA;
+        } else if (have_c1) {
+            prev = c1;
+        } else {
+            continue;
+        }
+        DEP d;
+        SlowJoin sj;
+        int st = LYON_OK;
+        slow_join_geometry(&d, prev, E, false, next, P, &sj, &st);
+        SpecSlot& o = sm.spec[2 * j + u];
+        o.prev = prev;
+        o.cur = E;
+        o.next = next;
+        o.pn = sj.pn;
+        o.nn = sj.nn;
+        o.from_f = sj.from_f;
+        o.to_f = sj.to_f;
+        o.fneg_rel = sj.from_neg_rel;
+        o.fpos_rel = sj.from_pos_rel;
+        o.vcount = sj.vcount;
+        o.jtris = sj.jtris;
+        o.st = st;
+        o.flags = SPEC_VALID | (sj.sym ? SPEC_SYM : 0u);
+    }
+}
+
+// Writes the output of the joins computed ahead (one per lane). Returns the worst status.
+__device__ __noinline__ int emit_spec_joins(WarpSmem& sm, int lane, uint32_t count,
+                                            const StrokeParams& P, const PathOut& po) {
+    int worst = LYON_OK;
+    for (uint32_t i = (uint32_t)lane; i < count; i += 32) {
+        const EmitJob job = sm.ej[i];
+        const SpecSlot& sp = sm.spec[job.slot];
+        DEP d;
+        SlowJoin sj;
+        int st = LYON_OK;
+        slow_join_geometry(&d, sp.prev, sp.cur, false, sp.next, P, &sj, &st);
+        Sink s;
+        s.id_base = job.base;
+        s.nv = 0;
+        s.ni = 0;
+        s.vout = po.vout + job.vo;
+        s.index_bits = po.bits;
+        s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + job.io)
+                               : (void*)((uint32_t*)po.iout + job.io);
+        s.vcap = cap_left(po.vmax, job.vo);
+        s.icap = cap_left(po.imax, job.io);
+        s.overflow = false;
+        slow_join_emit(&d, &d, s, job.has_edge != 0, job.pfn, job.pfp, true, P, &st);
+        if (s.overflow && st == LYON_OK) st = LYON_ERR_INTERNAL;
+        if (st > worst) worst = st;
+    }
+    return worst;
+}
+
 // A join as lyon's EndpointData after its processing, with vertex ids starting at base_id (the
 // fast layout of flattened_step, or the general layout), for firsts[1] and the tail.
 __device__ __noinline__ void join_dep_with_ids(DEP* out, V2 prev, V2 cur, V2 nxt, bool flat,
@@ -224,38 +404,40 @@ __device__ __noinline__ void fast_join_sides(V2 prev, V2 cur, V2 nxt, float hw, 
     *nn = cur - nrm * hw;
 }
 
-// The first kept point of a sub-path as lyon's EndpointData, with the side points its first
-// edge gives it (stroke.rs:1538-1556) when there is one.
-__device__ __noinline__ void write_first0(DEP* out, V2 pos, bool has_sides, V2 pn, V2 nn,
-                                          const StrokeParams& P) {
-    DEP f;
-    dep_init(f, pos, P.hw, P.line_join, false);
-    if (has_sides) {
-        f.s[SP].next = pn;
-        f.s[SN].next = nn;
+// The tail of a sub-path: stroke.rs:1179-1279 (end, close) and 1322-1378 (end_with_caps), from
+// lyon's firsts (the first kept point with its sides, the first join) and the last join, which
+// are rebuilt here from the recorded points. Writes through `s` (positioned at the tail).
+__device__ __noinline__ void run_tail(const TailJob& j, const StrokeParams& P, Sink& s,
+                                      int* status) {
+    const uint32_t n = j.n;
+    const bool close = (j.flags & TJ_CLOSED) != 0;
+    bool may_need_empty_cap = (j.flags & TJ_MNEC) != 0;
+    DEP first0, first1, last;
+    dep_init(first0, j.p0, P.hw, P.line_join, false);
+    if (n >= 2) first_point_sides(first0, j.p1, P.hw);
+    if (n >= 3) {
+        join_dep_with_ids(&first1, j.p0, j.p1, j.p2, (j.flags & TJ_FLAT1) != 0,
+                          (j.flags & TJ_FAST1) != 0, (j.flags & TJ_SKIP1) != 0, j.base1, P,
+                          status);
+        join_dep_with_ids(&last, j.c3, j.c2, j.c1, (j.flags & TJ_F2) != 0,
+                          (j.flags & TJ_JFAST) != 0, (j.flags & TJ_JSKIP) != 0, j.jbase, P,
+                          status);
     }
-    *out = f;
-}
-
-// The tail of a sub-path on lane 0: stroke.rs:1179-1279 (end, close) and 1322-1378
-// (end_with_caps). `lastp`/`lastflat` are the last kept point P[n-1]; sm.last holds the join at
-// P[n-2] when n >= 3.
-__device__ __noinline__ void subpath_tail(WarpSmem& sm, uint32_t n, bool close,
-                                          bool may_need_empty_cap, V2 lastp, bool lastflat,
-                                          const StrokeParams& P, Sink& s, int* status) {
+    const V2 lastp = j.c1;
+    const bool lastflat = (j.flags & TJ_F1) != 0;
     may_need_empty_cap |= close && n == 1;
     if (close && n > 2) {
         SeqBuffer pb;
-        pb.pts[0] = sm.last;
+        pb.pts[0] = last;
         dep_init(pb.pts[1], lastp, P.hw, P.line_join, lastflat);
         pb.start = 0;
         pb.count = 2;
         pb.n = n;
         bool mnec = false;
-        DEP p = sm.first0;
+        DEP p = first0;
         bool added = seq_step(pb, p, P, s, &mnec, status);
         if (!added) pb.last().pos = p.pos;
-        DEP p2 = sm.first1;
+        DEP p2 = first1;
         seq_step(pb, p2, P, s, &mnec, status);
         DEP& p0 = pb.second_last();
         DEP& p1 = pb.last();
@@ -268,7 +450,7 @@ __device__ __noinline__ void subpath_tail(WarpSmem& sm, uint32_t n, bool close,
         return;
     }
     if (may_need_empty_cap && n == 1) {
-        V2 pos = sm.first0.pos;
+        V2 pos = first0.pos;
         if (P.start_cap == LYON_CAP_SQUARE) {
             tessellate_empty_square_cap(pos, P.hw, s);
         } else if (P.start_cap == LYON_CAP_ROUND) {
@@ -277,7 +459,7 @@ __device__ __noinline__ void subpath_tail(WarpSmem& sm, uint32_t n, bool close,
         return;
     }
     if (n >= 2) {
-        DEP p0 = (n == 2) ? sm.first0 : sm.last;
+        DEP p0 = (n == 2) ? first0 : last;
         DEP p1;
         dep_init(p1, lastp, P.hw, P.line_join, lastflat);
         V2 tan = normalize(p1.pos - p0.pos);
@@ -286,28 +468,72 @@ __device__ __noinline__ void subpath_tail(WarpSmem& sm, uint32_t n, bool close,
         p1.s[SN].prev = p1.pos - nn;
         tessellate_last_edge(p0, p1, n == 2, P, s, status);
         if (n > 2) {
-            p0 = sm.first0;
-            p1 = sm.first1;
+            p0 = first0;
+            p1 = first1;
         }
         tessellate_first_edge(p0, p1, P, s, status);
     }
 }
 
+// Runs a tail at the output position (vcur, icur) of its path. Returns the counts it added.
+__device__ __forceinline__ void tail_at(const TailJob& j, const StrokeParams& P,
+                                        const PathOut& po, uint32_t* tv, uint32_t* ti,
+                                        int* st) {
+    Sink s;
+    s.id_base = po.id_base + j.vcur;
+    s.nv = 0;
+    s.ni = 0;
+    s.vout = po.vout ? po.vout + j.vcur : nullptr;
+    s.iout = nullptr;
+    if (po.vout) {
+        s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + j.icur)
+                               : (void*)((uint32_t*)po.iout + j.icur);
+    }
+    s.index_bits = po.bits;
+    s.vcap = cap_left(po.vmax, j.vcur);
+    s.icap = cap_left(po.imax, j.icur);
+    s.overflow = false;
+    int tst = LYON_OK;
+    run_tail(j, P, s, &tst);
+    if (s.overflow && tst == LYON_OK) tst = LYON_ERR_INTERNAL;
+    *tv = s.nv;
+    *ti = s.ni;
+    *st = tst;
+}
+
+// Processes the warp's queued tails, one per lane, and finishes their paths.
+template <bool EMIT>
+__device__ __noinline__ void flush_tails(WarpSmem& sm, int lane, uint32_t count,
+                                         const StrokeArgs& A) {
+    if ((uint32_t)lane < count) {
+        const TailJob j = sm.tq[lane];
+        const lyon_stroke_options opt = A.options[A.num_options > 1 ? j.path : 0];
+        const StrokeParams P = make_params(opt);
+        const PathOut po = path_out<EMIT>(A, j.path);
+        uint32_t tv, ti;
+        int st;
+        tail_at(j, P, po, &tv, &ti, &st);
+        finish_path<EMIT>(A, j.path, j.vcur + tv, j.icur + ti, st, po);
+    }
+    __syncwarp();
+}
+
 // Steps [cb, cb + 32) of the current verb window (lane = step): flattened points, merge filter,
-// joins, output. See the file comment.
+// joins, output. See the file comment. `ejn` counts the joins queued for emission.
 template <bool EMIT>
 __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, const uint32_t vi,
                                               const uint32_t nv, const uint32_t sincl,
                                               const uint32_t S_w, const uint32_t cb,
                                               const StrokeParams& P, const PathOut& po,
                                               SubState& S, uint32_t& vcur, uint32_t& icur,
-                                              int& status) {
+                                              uint32_t& ejn, int& status) {
     const uint32_t nsteps = min(32u, S_w - cb);
     const bool active = (uint32_t)lane < nsteps;
 
     // ---- 1. the flattened point of step cb + lane ----
     V2 q;
     bool flat = false;
+    uint32_t sid = NO_SLOT;
     uint32_t my_verb = NO_VERB, my_unit = 0, my_k = 0;
     float my_t = 0.0f;
     {
@@ -326,6 +552,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         const int kind = sl.kind;
         if (kind == LYON_VERB_BEGIN || kind == LYON_VERB_LINE_TO) {
             q = sl.toA;
+            if (kind == LYON_VERB_LINE_TO) sid = 2 * lo;
         } else {
             const uint32_t mA = sl.mA;
             const bool unitA = r < mA;
@@ -350,6 +577,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
                 my_t = t;
             } else {
                 q = unitA ? sl.toA : sl.toB;
+                sid = 2 * lo + (unitA ? 0u : 1u);
             }
         }
     }
@@ -390,6 +618,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
             const int src = (uint32_t)lane < nkk ? (int)__fns(km, 0, lane + 1) : 0;
             q = shfl_v2(q, src);
             flat = __shfl_sync(FULL, (int)flat, src) != 0;
+            sid = __shfl_sync(FULL, sid, src);
         }
     }
     const uint32_t nk = __popc(keep);
@@ -401,10 +630,12 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
     V2 cur = shfl_up_v2(q, 1);
     V2 prv = shfl_up_v2(q, 2);
     bool fcur = __shfl_up_sync(FULL, (int)flat, 1) != 0;
+    uint32_t scur = __shfl_up_sync(FULL, sid, 1);
     if (lane == 0) {
         cur = S.c1;
         prv = S.c2;
         fcur = S.f1;
+        scur = S.s1;
     } else if (lane == 1) {
         prv = S.c1;
     }
@@ -422,7 +653,6 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
     bool sym = true, skip = false, have_sides = false;
     V2 pn = V2{0.0f, 0.0f}, nn = V2{0.0f, 0.0f};
     int st = LYON_OK;
-    DEP d;
     if (fast) {
         vcnt = 2;
         from_f = 0;
@@ -436,7 +666,27 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         nn = cur - n;
         have_sides = true;
     }
-    if (slow) {
+    bool spec = false;
+    if (slow && scur != NO_SLOT) {
+        const SpecSlot& sp = sm.spec[scur];
+        spec = (sp.flags & SPEC_VALID) && same_bits(sp.prev, prv) && same_bits(sp.cur, cur) &&
+               same_bits(sp.next, q);
+        if (spec) {
+            vcnt = sp.vcount;
+            jt = sp.jtris;
+            to_f = sp.to_f;
+            from_f = sp.from_f;
+            fneg_rel = sp.fneg_rel;
+            fpos_rel = sp.fpos_rel;
+            sym = (sp.flags & SPEC_SYM) != 0;
+            pn = sp.pn;
+            nn = sp.nn;
+            have_sides = true;
+            st = sp.st;
+        }
+    }
+    DEP d;
+    if (slow && !spec) {
         SlowJoin sj;
         slow_join_geometry(&d, prv, cur, fcur, q, P, &sj, &st);
         vcnt = sj.vcount;
@@ -544,7 +794,21 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
                 if (s.overflow) st = LYON_ERR_INTERNAL;
             }
         }
-        if (slow) {
+        // Joins computed ahead are written at the end of the window.
+        const uint32_t qmask = __ballot_sync(FULL, spec);
+        if (spec) {
+            const uint32_t slot_i = ejn + __popc(qmask & ((1u << lane) - 1u));
+            EmitJob& job = sm.ej[slot_i];
+            job.slot = scur;
+            job.vo = vo;
+            job.io = io;
+            job.base = base;
+            job.pfn = pfn;
+            job.pfp = pfp;
+            job.has_edge = k >= 2 ? 1u : 0u;
+        }
+        ejn += __popc(qmask);
+        if (slow && !spec) {
             Sink s;
             s.id_base = base;
             s.nv = 0;
@@ -561,10 +825,19 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         }
     }
 
-    // ---- lyon's firsts (stroke.rs:1624-1627) ----
-    if (live && k == 0) write_first0(&sm.first0, cur, true, pn, nn, P);
-    if (live && k == -1 && nk == 1) write_first0(&sm.first0, q, false, pn, nn, P);
-    if (live && k == 1) join_dep_with_ids(&sm.first1, prv, cur, q, fcur, fast, skip, base, P, &st);
+    // ---- the first three kept points and the first join (lyon's firsts) ----
+    if (n0 < 3) {
+        if (n0 == 0) S.p0 = shfl_v2(q, 0);
+        if (n0 <= 1 && 1 - (int)n0 < (int)nk) S.p1 = shfl_v2(q, 1 - (int)n0);
+        const int l1 = 2 - (int)n0;  // the lane of the first join (k == 1)
+        if (l1 < (int)nk) {
+            S.p2 = shfl_v2(q, l1);
+            S.flat1 = __shfl_sync(FULL, (int)fcur, l1) != 0;
+            S.fast1 = __shfl_sync(FULL, (int)fast, l1) != 0;
+            S.skip1 = __shfl_sync(FULL, (int)skip, l1) != 0;
+            S.base1 = __shfl_sync(FULL, base, l1);
+        }
+    }
 
     // ---- carry to the next chunk ----
     {
@@ -581,6 +854,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         S.f2 = nk >= 2 ? fl2 : of1;
         S.c1 = q1;
         S.f1 = fl1;
+        S.s1 = __shfl_sync(FULL, sid, last);
         S.jtan = shfl_v2(nt, last);
         S.jpn = shfl_v2(pn, last);
         S.jnn = shfl_v2(nn, last);
@@ -603,10 +877,12 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
     __syncwarp();
 }
 
-// Strokes one path with the whole warp. Returns the path's vertex/index counts via vcur/icur.
+// Strokes one path with the whole warp. On return vcur/icur/status hold the path's counts so
+// far; when the tail of its last sub-path was queued (`deferred`), the queue finishes the path.
 template <bool EMIT>
 __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_t path,
-                            const PathOut& po, uint32_t& vcur, uint32_t& icur, int& status) {
+                            const PathOut& po, uint32_t& vcur, uint32_t& icur, int& status,
+                            uint32_t& tqn, bool& deferred) {
     const uint32_t v_begin = A.verb_offsets[path], v_end = A.verb_offsets[path + 1];
     const uint32_t p_begin = A.point_offsets[path], p_end = A.point_offsets[path + 1];
     const lyon_stroke_options opt = A.options[A.num_options > 1 ? path : 0];
@@ -614,6 +890,7 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
     vcur = 0;
     icur = 0;
     status = LYON_OK;
+    deferred = false;
     uint32_t vi = v_begin;
     uint32_t pc = p_begin;
     while (vi < v_end && status == LYON_OK) {
@@ -626,6 +903,7 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
         S.n = 0;
         S.c1 = S.c2 = S.c3 = V2{0.0f, 0.0f};
         S.f1 = S.f2 = false;
+        S.s1 = NO_SLOT;
         S.jtan = V2{0.0f, 0.0f};
         S.jpn = S.jnn = V2{0.0f, 0.0f};
         S.jside_valid = false;
@@ -635,6 +913,9 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
         S.jfast = S.jskip = false;
         S.jbase = 0;
         S.mnec = false;
+        S.p0 = S.p1 = S.p2 = V2{0.0f, 0.0f};
+        S.flat1 = S.fast1 = S.skip1 = false;
+        S.base1 = 0;
         S.tc.verb = NO_VERB;
         S.tc.unit = 0;
         S.tc.k = 0;
@@ -668,9 +949,18 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             const uint32_t S_w = __shfl_sync(FULL, sincl, 31);
             const int last_kind = __shfl_sync(FULL, kind, nv - 1);
             __syncwarp();
+            speculate_joins(sm, lane, nv, S_w, P, S.c1, S.n > 0);
+            __syncwarp();
+            uint32_t ejn = 0;
             for (uint32_t cb = 0; cb < S_w; cb += 32) {
-                process_chunk<EMIT>(sm, lane, vi, nv, sincl, S_w, cb, P, po, S, vcur, icur,
+                process_chunk<EMIT>(sm, lane, vi, nv, sincl, S_w, cb, P, po, S, vcur, icur, ejn,
                                     status);
+            }
+            if (EMIT && ejn > 0) {
+                __syncwarp();
+                int est = emit_spec_joins(sm, lane, ejn, P, po);
+                est = __reduce_max_sync(FULL, est);
+                if (est != LYON_OK && status == LYON_OK) status = est;
             }
             __syncwarp();
             vi += nv;
@@ -683,31 +973,38 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
         }
         if (!ended || status != LYON_OK) break;
         // ---- tail ----
+        TailJob job;
+        job.path = path;
+        job.n = S.n;
+        job.flags = (closed ? TJ_CLOSED : 0u) | (S.mnec ? TJ_MNEC : 0u) |
+                    (S.flat1 ? TJ_FLAT1 : 0u) | (S.fast1 ? TJ_FAST1 : 0u) |
+                    (S.skip1 ? TJ_SKIP1 : 0u) | (S.f1 ? TJ_F1 : 0u) | (S.f2 ? TJ_F2 : 0u) |
+                    (S.jfast ? TJ_JFAST : 0u) | (S.jskip ? TJ_JSKIP : 0u);
+        job.base1 = S.base1;
+        job.jbase = S.jbase;
+        job.vcur = vcur;
+        job.icur = icur;
+        job.p0 = S.p0;
+        job.p1 = S.p1;
+        job.p2 = S.p2;
+        job.c3 = S.c3;
+        job.c2 = S.c2;
+        job.c1 = S.c1;
+        if (vi >= v_end) {
+            // The path's last sub-path: queue its tail.
+            if (tqn == 32) {
+                flush_tails<EMIT>(sm, lane, tqn, A);
+                tqn = 0;
+            }
+            if (lane == 0) sm.tq[tqn] = job;
+            ++tqn;
+            deferred = true;
+            __syncwarp();
+            break;
+        }
         uint32_t tv = 0, ti = 0;
         int tst = LYON_OK;
-        if (lane == 0) {
-            if (S.n >= 3)
-                join_dep_with_ids(&sm.last, S.c3, S.c2, S.c1, S.f2, S.jfast, S.jskip, S.jbase, P,
-                                  &tst);
-            Sink s;
-            s.id_base = po.id_base + vcur;
-            s.nv = 0;
-            s.ni = 0;
-            s.vout = EMIT ? po.vout + vcur : nullptr;
-            s.iout = nullptr;
-            if (EMIT) {
-                s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + icur)
-                                       : (void*)((uint32_t*)po.iout + icur);
-            }
-            s.index_bits = po.bits;
-            s.vcap = cap_left(po.vmax, vcur);
-            s.icap = cap_left(po.imax, icur);
-            s.overflow = false;
-            subpath_tail(sm, S.n, closed, S.mnec, S.c1, S.f1, P, s, &tst);
-            if (s.overflow && tst == LYON_OK) tst = LYON_ERR_INTERNAL;
-            tv = s.nv;
-            ti = s.ni;
-        }
+        if (lane == 0) tail_at(job, P, po, &tv, &ti, &tst);
         tv = __shfl_sync(FULL, tv, 0);
         ti = __shfl_sync(FULL, ti, 0);
         tst = __shfl_sync(FULL, tst, 0);
@@ -726,47 +1023,23 @@ __global__ void __launch_bounds__(STROKE_WARPS * 32, LG_STROKE_MIN_BLOCKS)
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     WarpSmem& sm = smem[w];
+    uint32_t tqn = 0;  // queued tails
     for (;;) {
         uint32_t item = 0;
         if (lane == 0) item = atomicAdd(A.work_counter, 1u);
         item = __shfl_sync(FULL, item, 0);
         if (item >= A.num_paths) break;
         const uint32_t path = A.order ? A.order[item] : item;
-        PathOut po;
-        po.bits = A.index_bits;
-        if (EMIT) {
-            if (A.status[path] != LYON_OK) continue;
-            const uint64_t vo = A.vtx_offsets[path];
-            const uint64_t io = A.idx_offsets[path];
-            po.vout = reinterpret_cast<float2*>(A.vertices) + vo;
-            po.iout = A.index_bits == 16 ? (void*)((uint16_t*)A.indices + io)
-                                         : (void*)((uint32_t*)A.indices + io);
-            po.id_base = A.vertex_offset +
-                         (A.index_mode == LYON_INDEX_GLOBAL ? (uint32_t)vo : 0u);
-            po.vmax = A.vtx_counts[path];
-            po.imax = A.idx_counts[path];
-        } else {
-            po.vout = nullptr;
-            po.iout = nullptr;
-            po.id_base = 0;
-            po.vmax = 0xFFFFFFFFu;
-            po.imax = 0xFFFFFFFFu;
-        }
+        if (EMIT && A.status[path] != LYON_OK) continue;
+        const PathOut po = path_out<EMIT>(A, path);
         uint32_t vc, ic;
         int st;
-        stroke_path<EMIT>(sm, lane, A, path, po, vc, ic, st);
-        if (!EMIT && lane == 0) {
-            A.vtx_counts[path] = st == LYON_OK ? vc : 0u;
-            A.idx_counts[path] = st == LYON_OK ? ic : 0u;
-            A.status[path] = st;
-        }
-        if (EMIT && lane == 0 && (st != LYON_OK || vc != po.vmax || ic != po.imax)) {
-            // The emit walk disagreed with the count walk: flag the path (its bytes were
-            // bounded by the path's range).
-            A.status[path] = st != LYON_OK ? st : LYON_ERR_INTERNAL;
-        }
+        bool deferred;
+        stroke_path<EMIT>(sm, lane, A, path, po, vc, ic, st, tqn, deferred);
+        if (!deferred && lane == 0) finish_path<EMIT>(A, path, vc, ic, st, po);
         __syncwarp();
     }
+    if (tqn > 0) flush_tails<EMIT>(sm, lane, tqn, A);
 }
 
 constexpr size_t STROKE_SMEM = sizeof(WarpSmem) * STROKE_WARPS;

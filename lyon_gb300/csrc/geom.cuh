@@ -225,15 +225,40 @@ __host__ __device__ __forceinline__ float accumulate_t(float s, uint32_t k0, flo
         const uint32_t W = (uint32_t)((B - t) * inv_u);
         const uint32_t D = (uint32_t)(d * inv_u);
         // m = (W - 1) / D, from a float estimate corrected to the exact quotient.
+#ifdef __CUDA_ARCH__
+        uint32_t m = (uint32_t)__fdividef((float)(W - 1u), (float)D);
+#else
         uint32_t m = (uint32_t)((float)(W - 1u) / (float)D);
+#endif
         while (m > 0 && m * D > W - 1u) --m;
         while ((m + 1) * D <= W - 1u) ++m;
         const uint32_t rem = k - j;
         const uint32_t take = m < rem ? m : rem;
-        t = t + (float)(take * D) * (d / (float)D);
+        // take * d = (take * D) * u, exactly (u is a power of two, take * D < 2^24).
+        const float u = e > 23 ? u2f((uint32_t)(e - 23) << 23) : d / (float)D;
+        t = t + (float)(take * D) * u;
         j += take;
     }
     return t;
+}
+
+// accumulate_t when the value at k0 is known (t0 > 0) and the k - k0 steps stay in t0's binade
+// [2^e, 2^(e+1)): after the first step every step adds the same d (see accumulate_t), so
+// t_k = t_(k0+1) + (k - k0 - 1) * d, with every operation exact. Falls back to the binade walk
+// otherwise.
+__host__ __device__ __forceinline__ float accumulate_t_from(float s, uint32_t k0, float t0,
+                                                            uint32_t k) {
+    if (t0 > 0.0f && k > k0) {
+        const uint32_t e = (f2u(t0) >> 23) & 0xFFu;
+        const float B = u2f((e + 1u) << 23);
+        const float t1 = t0 + s;
+        if (t1 < B) {
+            const float d = (t1 + s) - t1;
+            const float r = t1 + (float)(k - k0 - 1u) * d;
+            if (r < B) return r;
+        }
+    }
+    return accumulate_t(s, k0, t0, k);
 }
 
 // ---- fill ordering predicates (fill.rs:2122-2151) --------------------------------------------

@@ -37,7 +37,7 @@ namespace lg {
 #define LG_STROKE_WARPS 8
 #endif
 #ifndef LG_STROKE_MIN_BLOCKS
-#define LG_STROKE_MIN_BLOCKS 1
+#define LG_STROKE_MIN_BLOCKS 2
 #endif
 constexpr int STROKE_WARPS = LG_STROKE_WARPS;
 constexpr uint32_t FULL = 0xFFFFFFFFu;
@@ -538,14 +538,14 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
     float my_t = 0.0f;
     {
         const uint32_t gq = min(cb + (uint32_t)lane, S_w - 1);
-        // Owner verb: the first whose inclusive step count exceeds gq.
-        uint32_t lo = 0, hi = nv - 1;
-#pragma unroll
-        for (int it = 0; it < 5; ++it) {
-            const uint32_t mid = (lo + hi) >> 1;
-            const uint32_t vmid = __shfl_sync(FULL, sincl, mid);
-            if (vmid > gq) hi = mid; else lo = mid + 1;
-            if (lo > hi) lo = hi;
+        // Owner verb: the number of verbs that end at or before the step (lanes past the
+        // window hold sincl == S_w, which no step reaches). The chunk's steps span the verbs
+        // [vfirst, vlast]; usually one or two.
+        const uint32_t vfirst = __popc(__ballot_sync(FULL, sincl <= cb));
+        const uint32_t vlast = __popc(__ballot_sync(FULL, sincl <= cb + nsteps - 1));
+        uint32_t lo = vfirst;
+        for (uint32_t jv = vfirst; jv < vlast; ++jv) {
+            if (gq >= __shfl_sync(FULL, sincl, (int)jv)) lo = jv + 1;
         }
         const VerbSlot& sl = sm.verbs[lo];
         const uint32_t r = gq - sl.excl;
@@ -567,7 +567,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
                     bk = S.tc.k;
                     bt = S.tc.t;
                 }
-                const float t = accumulate_t(s, bk, bt, kk);
+                const float t = accumulate_t_from(s, bk, bt, kk);
                 const Poly* pp = unitA ? &sl.pA : &sl.pB;
                 q = poly_sample(*pp, t);
                 flat = t != 1.0f;
@@ -779,19 +779,44 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
                 }
             }
             if (k >= 2) {
-                Sink s;
-                s.id_base = base;
-                s.nv = 0;
-                s.ni = 0;
-                s.vout = nullptr;
-                s.index_bits = po.bits;
-                s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + io)
-                                       : (void*)((uint32_t*)po.iout + io);
-                s.icap = cap_left(po.imax, io);
-                s.overflow = false;
-                edge_triangles(pfn, pfp, skip ? INVALID_ID : base + 1, skip ? INVALID_ID : base,
-                               &s);
-                if (s.overflow) st = LYON_ERR_INTERNAL;
+                // add_edge_triangles (stroke.rs:1869-1904) on the resolved ids.
+                const uint32_t pos_id = skip ? INVALID_ID : base;
+                const uint32_t neg_id = skip ? INVALID_ID : base + 1;
+                const bool triA = pfn != pos_id && pfn != pfp && pfp != pos_id;
+                const bool triB = pfn != pos_id && pfn != neg_id && pos_id != neg_id;
+                // Triangle A = (pfn, pfp, pos_id), then B = (pfn, pos_id, neg_id).
+                const uint32_t a1 = triA ? pfp : pos_id, a2 = triA ? pos_id : neg_id;
+                const uint32_t ni = (triA ? 3u : 0u) + (triB ? 3u : 0u);
+                if (io + ni > po.imax) {
+                    st = LYON_ERR_INTERNAL;
+                } else if (po.bits == 32) {
+                    uint32_t* dst = (uint32_t*)po.iout + io;
+                    if (ni == 6 && (reinterpret_cast<uintptr_t>(dst) & 7u) == 0) {
+                        uint2* d2 = reinterpret_cast<uint2*>(dst);
+                        d2[0] = make_uint2(pfn, pfp);
+                        d2[1] = make_uint2(pos_id, pfn);
+                        d2[2] = make_uint2(pos_id, neg_id);
+                    } else if (ni != 0) {
+                        dst[0] = pfn;
+                        dst[1] = a1;
+                        dst[2] = a2;
+                        if (ni == 6) {
+                            dst[3] = pfn;
+                            dst[4] = pos_id;
+                            dst[5] = neg_id;
+                        }
+                    }
+                } else if (ni != 0) {
+                    uint16_t* dst = (uint16_t*)po.iout + io;
+                    dst[0] = (uint16_t)pfn;
+                    dst[1] = (uint16_t)a1;
+                    dst[2] = (uint16_t)a2;
+                    if (ni == 6) {
+                        dst[3] = (uint16_t)pfn;
+                        dst[4] = (uint16_t)pos_id;
+                        dst[5] = (uint16_t)neg_id;
+                    }
+                }
             }
         }
         // Joins computed ahead are written at the end of the window.

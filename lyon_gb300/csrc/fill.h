@@ -11,16 +11,17 @@ namespace lg {
 
 // Device buffers the fill pipeline keeps between its count and emit phases.
 struct FillBuffers {
-    void* scratch = nullptr;        // per-slot sweep arenas
+    void* scratch = nullptr;        // per-thread sweep heaps
     size_t scratch_cap = 0;
     void* stage_v = nullptr;        // staged vertices (f32 x2) per path
     size_t stage_v_cap = 0;
     void* stage_i = nullptr;        // staged indices (u32, path-relative) per path
     size_t stage_i_cap = 0;
-    void* stage_off = nullptr;      // per path: staged vertex/index base (u64 x2) + caps
+    void* stage_off = nullptr;      // per path: staged vertex/index base (u64 x2)
     size_t stage_off_cap = 0;
-    void* work = nullptr;           // per path work estimates, plan arrays
+    void* work = nullptr;           // counters, staging tops and retry lists
     size_t work_cap = 0;
+    uint32_t heap_words = 0;        // per-thread sweep heap size (grows when a path needs more)
 };
 
 // Runs the sweep of every path into staging and writes per-path vertex/index counts and status.

@@ -272,6 +272,81 @@ int lyon_gpu_fill_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* batch
 void lyon_gpu_set_timing(lyon_gpu_context* ctx, int enabled);
 int lyon_gpu_last_timings(lyon_gpu_context* ctx, float* ms4);
 
+/* ----------------------------------------------------------------------------------------- */
+/* Serving loop. No lyon counterpart: lyon is a library called once per path; this is the    */
+/* runtime that turns a stream of tessellation requests into batched launches.               */
+/* ----------------------------------------------------------------------------------------- */
+
+enum { LYON_KIND_STROKE = 0, LYON_KIND_FILL = 1 };
+
+typedef struct lyon_srv lyon_srv;
+
+typedef struct lyon_srv_config {
+    int device;
+    uint32_t num_workers;          /* batches in flight at once, each on its own stream; 0 -> 2 */
+    uint32_t max_batch_paths;      /* most paths coalesced into one launch; 0 -> 65536 */
+    uint64_t device_budget_bytes;  /* device memory for batches and resident outputs; 0 -> 40 GB */
+} lyon_srv_config;
+
+/* A finished request. Its output stays on the device until lyon_srv_release. */
+typedef struct lyon_srv_result {
+    int status;                 /* LYON_OK, or the error that failed the request's batch */
+    uint32_t num_paths;
+    uint32_t num_failed_paths;  /* paths whose own status (path_status) is not LYON_OK */
+    const float* vertices;      /* device: 2 floats per vertex */
+    uint64_t num_vertices;
+    const uint32_t* indices;    /* device: u32 ids counted from the request's first vertex, as
+                                   lyon's BuffersBuilder over one VertexBuffers per request */
+    uint64_t num_indices;
+    const uint64_t* path_vertex_offsets;  /* device, num_paths + 1; subtract vertex_base */
+    const uint64_t* path_index_offsets;   /* device, num_paths + 1; subtract index_base */
+    const int32_t* path_status;           /* device, num_paths */
+    uint64_t vertex_base, index_base;
+    double queue_ms;    /* arrival to the start of its batch */
+    double latency_ms;  /* arrival to its output being resident on the device */
+} lyon_srv_result;
+
+/* Starts the workers. Returns NULL on failure. */
+lyon_srv* lyon_srv_create(const lyon_srv_config* config);
+/* Stops the workers (after their current batch) and frees everything. */
+void lyon_srv_destroy(lyon_srv* srv);
+/* Queues a request: `batch` (host memory) stroked (LYON_KIND_STROKE, lyon_stroke_options) or
+ * filled (LYON_KIND_FILL, lyon_fill_options) with 1 shared or num_paths option records. The
+ * batch and options are read while the request runs: keep them valid until it completes.
+ * Returns a ticket, or 0 for an invalid request. */
+uint64_t lyon_srv_submit(lyon_srv* srv, int kind, const lyon_path_batch* batch,
+                         const void* options, uint32_t num_options);
+/* LYON_OK and *out filled when the request finished; 1 while it is pending. */
+int lyon_srv_poll(lyon_srv* srv, uint64_t ticket, lyon_srv_result* out);
+/* Blocks until the request finishes, then fills *out. */
+int lyon_srv_wait(lyon_srv* srv, uint64_t ticket, lyon_srv_result* out);
+/* Frees a finished request and its share of the device output. */
+int lyon_srv_release(lyon_srv* srv, uint64_t ticket);
+
+/* Open-loop load: requests drawn in turn from `items`, arriving as a Poisson process at
+ * `rate_per_s` for `duration_s` seconds (arrival times from `seed`); each is released as soon as
+ * it completes. Latency is measured from the scheduled arrival. `latencies_ms` (optional)
+ * receives the per-request latencies in arrival order. */
+typedef struct lyon_srv_load_item {
+    int kind;
+    lyon_path_batch batch;
+    const void* options;
+    uint32_t num_options;
+} lyon_srv_load_item;
+
+typedef struct lyon_srv_load_stats {
+    uint32_t submitted, completed, failed;
+    double offered_rate, elapsed_s, achieved_rate;
+    uint64_t paths, vertices, indices;
+    double p50_ms, p99_ms, p999_ms, max_ms;
+    uint64_t batches;
+    double mean_batch_paths;
+} lyon_srv_load_stats;
+
+int lyon_srv_run_load(lyon_srv* srv, const lyon_srv_load_item* items, uint32_t num_items,
+                      double rate_per_s, double duration_s, uint64_t seed,
+                      lyon_srv_load_stats* stats, double* latencies_ms, uint32_t latencies_cap);
+
 /* Synchronise the context's stream. Returns LYON_OK or LYON_ERR_CUDA. */
 int lyon_gpu_synchronize(lyon_gpu_context* ctx);
 

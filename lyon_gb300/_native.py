@@ -37,6 +37,33 @@ class CBatchOutput(ctypes.Structure):
                 ("total_vertices", u64), ("total_indices", u64), ("num_failed_paths", u32)]
 
 
+class CSrvConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
+                ("device_budget_bytes", u64)]
+
+
+class CSrvResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("num_paths", u32), ("num_failed_paths", u32),
+                ("vertices", c_p), ("num_vertices", u64), ("indices", c_p), ("num_indices", u64),
+                ("path_vertex_offsets", c_p), ("path_index_offsets", c_p), ("path_status", c_p),
+                ("vertex_base", u64), ("index_base", u64), ("queue_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double)]
+
+
+class CSrvLoadItem(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("batch", CPathBatch), ("options", c_p),
+                ("num_options", u32)]
+
+
+class CSrvLoadStats(ctypes.Structure):
+    _fields_ = [("submitted", u32), ("completed", u32), ("failed", u32),
+                ("offered_rate", ctypes.c_double), ("elapsed_s", ctypes.c_double),
+                ("achieved_rate", ctypes.c_double), ("paths", u64), ("vertices", u64),
+                ("indices", u64), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("p999_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("batches", u64),
+                ("mean_batch_paths", ctypes.c_double)]
+
+
 class NativeLibraryMissing(RuntimeError):
     pass
 
@@ -96,6 +123,21 @@ def load(build_if_missing: bool = True):
         L.lyon_gpu_flatten_paths.argtypes = [c_p, ctypes.POINTER(CPathBatch), ctypes.c_float,
                                              ctypes.POINTER(c_p), ctypes.POINTER(c_p),
                                              ctypes.POINTER(u64)]
+        L.lyon_srv_create.restype = c_p
+        L.lyon_srv_create.argtypes = [ctypes.POINTER(CSrvConfig)]
+        L.lyon_srv_destroy.argtypes = [c_p]
+        L.lyon_srv_submit.restype = u64
+        L.lyon_srv_submit.argtypes = [c_p, ctypes.c_int, ctypes.POINTER(CPathBatch), c_p, u32]
+        for name in ("lyon_srv_poll", "lyon_srv_wait"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [c_p, u64, ctypes.POINTER(CSrvResult)]
+        L.lyon_srv_release.restype = ctypes.c_int
+        L.lyon_srv_release.argtypes = [c_p, u64]
+        L.lyon_srv_run_load.restype = ctypes.c_int
+        L.lyon_srv_run_load.argtypes = [c_p, ctypes.POINTER(CSrvLoadItem), u32, ctypes.c_double,
+                                        ctypes.c_double, u64, ctypes.POINTER(CSrvLoadStats),
+                                        c_p, u32]
         f = L.lyon_gpu_stroke_paths_noalloc
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.POINTER(CPathBatch), c_p, u32, ctypes.c_int, ctypes.c_int, u32,
@@ -113,4 +155,6 @@ EXPORTED = [
     "lyon_gpu_flatten_counts", "lyon_gpu_flatten_paths", "lyon_gpu_synchronize",
     "lyon_gpu_version", "lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host",
     "lyon_gpu_set_timing", "lyon_gpu_last_timings", "lyon_gpu_stroke_paths_noalloc",
+    "lyon_srv_create", "lyon_srv_destroy", "lyon_srv_submit", "lyon_srv_poll", "lyon_srv_wait",
+    "lyon_srv_release", "lyon_srv_run_load",
 ]

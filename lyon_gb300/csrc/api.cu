@@ -54,6 +54,8 @@ struct lyon_gpu_context {
     // single-path staging
     DevBuf in_verbs, in_points, in_offsets, in_options;
     HostBuf h_verbs, h_points, h_out_v, h_out_i, h_small, h_offs;
+    // optional per-path first path of its request (serving batches: one id space per request)
+    const uint32_t* request_first = nullptr;
     // timing
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -262,6 +264,7 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
     a.index_bits = index_bits;
     a.index_mode = index_mode;
     a.vertex_offset = (uint32_t)vertex_offset;
+    a.request_first = ctx->request_first;
     a.vtx_offsets = as<uint64_t>(ctx->vtx_offsets);
     a.idx_offsets = as<uint64_t>(ctx->idx_offsets);
     return a;
@@ -325,7 +328,7 @@ int pipeline_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
                                    as<uint32_t>(ctx->idx_counts), as<int32_t>(ctx->status),
                                    as<uint64_t>(ctx->vtx_offsets),
                                    as<uint64_t>(ctx->idx_offsets), vout, iout, index_bits,
-                                   index_mode, (uint32_t)vertex_offset, s)))
+                                   index_mode, (uint32_t)vertex_offset, ctx->request_first, s)))
             return LYON_ERR_CUDA;
     }
     mark(ctx, 3);
@@ -547,6 +550,38 @@ int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t 
 }
 
 }  // namespace
+
+// Entry points for the serving loop (serve.cu): one batched call split in its count and emit
+// halves, u32 indices, one id space per request (`request_first`).
+namespace lg {
+
+int srv_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
+              uint32_t num_options, const uint32_t* request_first, uint64_t* tv, uint64_t* ti,
+              uint32_t* failed) {
+    cudaSetDevice(ctx->device);
+    ctx->request_first = request_first;
+    int r = pipeline_count(ctx, kind, batch, options, num_options, 32, LYON_INDEX_GLOBAL, 0, tv,
+                           ti, failed);
+    ctx->request_first = nullptr;
+    return r;
+}
+
+int srv_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
+             uint32_t num_options, const uint32_t* request_first, float* vout, void* iout,
+             uint64_t tv) {
+    ctx->request_first = request_first;
+    int r = pipeline_emit(ctx, kind, batch, options, num_options, 32, LYON_INDEX_GLOBAL, 0, vout,
+                          iout, tv);
+    ctx->request_first = nullptr;
+    return r;
+}
+
+const uint64_t* srv_vtx_offsets(lyon_gpu_context* ctx) { return as<uint64_t>(ctx->vtx_offsets); }
+const uint64_t* srv_idx_offsets(lyon_gpu_context* ctx) { return as<uint64_t>(ctx->idx_offsets); }
+const int32_t* srv_status(lyon_gpu_context* ctx) { return as<int32_t>(ctx->status); }
+cudaStream_t srv_stream(lyon_gpu_context* ctx) { return ctx->stream; }
+
+}  // namespace lg
 
 extern "C" {
 

@@ -1377,7 +1377,8 @@ __global__ void fill_emit_kernel(uint32_t n, const uint32_t* vtx_counts,
                                  const unsigned long long* stage_off, const float2* stage_v,
                                  const uint32_t* stage_i, const uint64_t* vtx_offsets,
                                  const uint64_t* idx_offsets, float2* vertices, void* indices,
-                                 int index_bits, int index_mode, uint32_t vertex_offset) {
+                                 int index_bits, int index_mode, uint32_t vertex_offset,
+                                 const uint32_t* request_first) {
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; p < n; p += warps) {
@@ -1385,8 +1386,9 @@ __global__ void fill_emit_kernel(uint32_t n, const uint32_t* vtx_counts,
         const uint32_t nv = vtx_counts[p], ni = idx_counts[p];
         const unsigned long long sv = stage_off[2 * (size_t)p], si = stage_off[2 * (size_t)p + 1];
         const uint64_t vo = vtx_offsets[p], io = idx_offsets[p];
+        const uint64_t rb = request_first ? vtx_offsets[request_first[p]] : 0ull;
         const uint32_t base =
-            vertex_offset + (index_mode == LYON_INDEX_GLOBAL ? (uint32_t)vo : 0u);
+            vertex_offset + (index_mode == LYON_INDEX_GLOBAL ? (uint32_t)(vo - rb) : 0u);
         for (uint32_t i = lane; i < nv; i += 32) vertices[vo + i] = stage_v[sv + i];
         if (index_bits == 16) {
             uint16_t* d = reinterpret_cast<uint16_t*>(indices) + io;
@@ -1539,7 +1541,7 @@ cudaError_t fill_emit(FillBuffers& fb, uint32_t n, const uint32_t* vtx_counts,
                       const uint32_t* idx_counts, const int32_t* status,
                       const uint64_t* vtx_offsets, const uint64_t* idx_offsets, float* vertices,
                       void* indices, int index_bits, int index_mode, uint32_t vertex_offset,
-                      cudaStream_t stream) {
+                      const uint32_t* request_first, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
     const uint32_t blocks = std::min<uint32_t>((n + 7) / 8, 4096u);
     fillk::fill_emit_kernel<<<blocks, 256, 0, stream>>>(
@@ -1547,7 +1549,7 @@ cudaError_t fill_emit(FillBuffers& fb, uint32_t n, const uint32_t* vtx_counts,
         reinterpret_cast<const unsigned long long*>(fb.stage_off),
         reinterpret_cast<const float2*>(fb.stage_v), reinterpret_cast<const uint32_t*>(fb.stage_i),
         vtx_offsets, idx_offsets, reinterpret_cast<float2*>(vertices), indices, index_bits,
-        index_mode, vertex_offset);
+        index_mode, vertex_offset, request_first);
     return cudaGetLastError();
 }
 

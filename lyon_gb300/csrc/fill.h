@@ -30,12 +30,13 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
                int32_t* status, uint32_t* small_words, cudaStream_t stream,
                std::string* error);
 
-// Copies the staged output of every successful path to its final offsets, rebasing indices.
+// Copies the staged output of every successful path to its final offsets, rebasing indices
+// (`request_first`: optional per-path first path of its request, as in StrokeArgs).
 cudaError_t fill_emit(FillBuffers& fb, uint32_t n, const uint32_t* vtx_counts,
                       const uint32_t* idx_counts, const int32_t* status,
                       const uint64_t* vtx_offsets, const uint64_t* idx_offsets, float* vertices,
                       void* indices, int index_bits, int index_mode, uint32_t vertex_offset,
-                      cudaStream_t stream);
+                      const uint32_t* request_first, cudaStream_t stream);
 
 void fill_free(FillBuffers& fb);
 

@@ -29,30 +29,9 @@ struct StrokeArgs {
     int index_bits;
     int index_mode;
     uint32_t vertex_offset;
-};
-
-struct FillArgs {
-    const uint8_t* verbs;
-    const float* points;
-    const uint32_t* verb_offsets;
-    const uint32_t* point_offsets;
-    uint32_t num_paths;
-    const lyon_fill_options* options;
-    uint32_t num_options;
-    const uint32_t* order;
-    uint32_t* work_counter;
-    // per-path scratch arena (events, edges, spans, output staging)
-    unsigned char* scratch;
-    uint64_t scratch_per_thread;
-    uint32_t num_slots;
-    // outputs of the sweep pass (staged vertices/indices per path) and counts
-    float* stage_vertices;
-    uint32_t* stage_indices;
-    const uint64_t* stage_vtx_offsets;
-    const uint64_t* stage_idx_offsets;
-    uint32_t* vtx_counts;
-    uint32_t* idx_counts;
-    int32_t* status;
+    // Optional, per path: the first path of the request it belongs to. In LYON_INDEX_GLOBAL mode
+    // ids then count from that path's first vertex (one VertexBuffers per request of a batch).
+    const uint32_t* request_first;
 };
 
 int stroke_blocks_per_sm();

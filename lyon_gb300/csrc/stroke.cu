@@ -131,7 +131,9 @@ __device__ __forceinline__ PathOut path_out(const StrokeArgs& A, uint32_t path) 
         po.vout = reinterpret_cast<float2*>(A.vertices) + vo;
         po.iout = A.index_bits == 16 ? (void*)((uint16_t*)A.indices + io)
                                      : (void*)((uint32_t*)A.indices + io);
-        po.id_base = A.vertex_offset + (A.index_mode == LYON_INDEX_GLOBAL ? (uint32_t)vo : 0u);
+        const uint64_t rb = A.request_first ? A.vtx_offsets[A.request_first[path]] : 0ull;
+        po.id_base =
+            A.vertex_offset + (A.index_mode == LYON_INDEX_GLOBAL ? (uint32_t)(vo - rb) : 0u);
         po.vmax = A.vtx_counts[path];
         po.imax = A.idx_counts[path];
     } else {

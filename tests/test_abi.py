@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     hdr = open(os.path.join(ROOT, "include", "lyon_gpu.h")).read()
-    return sorted(set(re.findall(r"\b(lyon_gpu_\w+)\s*\(", hdr)))
+    return sorted(set(re.findall(r"\b(lyon_(?:gpu|srv)_\w+)\s*\(", hdr)))
 
 
 def test_library_exports_every_declared_symbol():

@@ -47,6 +47,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=100_000)
+    ap.add_argument("--fill-paths", type=int, default=200_000)
+    ap.add_argument("--no-fill", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--profile-fill", action="store_true",
+                    help="only run the fill warm-up and timed steps (for profilers)")
     ap.add_argument("--profile", action="store_true",
                     help="only run the warm-up and timed device steps (for profilers)")
     return ap.parse_args()
@@ -155,10 +161,10 @@ def cpu_baseline(batch, opts, sample_paths: int):
     """The oracle on a bounded sample, all host threads."""
     from oracle import lyon_oracle as orc
     n = min(sample_paths, batch.num_paths)
-    sub = batch.subset(range(n))
+    sub = batch.head(n)
     sub_opts = opts[:n] if len(opts) > 1 else opts
     threads = os.cpu_count() or 1
-    orc.batch("stroke", sub.subset(range(min(n, 2000))),
+    orc.batch("stroke", sub.head(min(n, 2000)),
               sub_opts[:min(n, 2000)] if len(sub_opts) > 1 else sub_opts, 32, threads, False)
     t0 = time.perf_counter()
     r = orc.batch("stroke", sub, sub_opts, 32, threads, want_output=False)
@@ -179,11 +185,11 @@ def run_reference(args):
     from oracle import lyon_oracle as orc
     sample = min(args.paths, 100_000)
     batch, opts = workloads.batched_stroke(args.paths, seed=2)
-    sub = batch.subset(range(sample))
+    sub = batch.head(sample)
     sub_opts = opts[:sample]
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        orc.batch("stroke", sub.subset(range(min(sample, 5000))), sub_opts[:min(sample, 5000)],
+        orc.batch("stroke", sub.head(min(sample, 5000)), sub_opts[:min(sample, 5000)],
                   32, threads, want_output=False)
     verts = 0
     t0 = time.perf_counter()
@@ -222,6 +228,14 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
 
+    if args.profile_fill:
+        ctx = T.Context(dev)
+        lib = ctx.lib
+        lib.lyon_gpu_set_timing(ctx.h, 1)
+        out = run_fill(ctx, args, T, world)
+        print(json.dumps({k: v for k, v in out.items() if k != "config"}))
+        ctx.close()
+        return 0
     batch, opts = workloads.batched_stroke(args.paths, seed=2)
     ctx = T.Context(dev)
     lib = ctx.lib
@@ -304,11 +318,119 @@ def main():
         line["cpu_baseline"] = cpu_baseline(batch, opts, args.cpu_sample)
     if rank == 0:
         line["plain_per_path"] = plain_per_path(ctx, batch, opts, T)
+        if not args.no_fill:
+            line["fill"] = run_fill(ctx, args, T, world)
+        if not args.no_serve and world == 1:
+            del db, od
+            ctx.close()
+            ctx = None
+            torch.cuda.empty_cache()
+            line["serving"] = run_serving(args)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     return 0
+
+
+def run_fill(ctx, args, T, world, batch=None):
+    """Batched fill of the glyph workload (200,000 closed paths, tolerance 0.1, u32 global
+    indices), non-zero and even-odd; inputs resident; CPU baseline: the oracle on a sample."""
+    import torch
+    from lyon_gb300 import workloads
+    from lyon_gb300.options import FILL_OPTIONS_DTYPE, FillRule
+    from oracle import lyon_oracle as orc
+    if batch is None:
+        batch, _ = workloads.glyph_fill(args.fill_paths, seed=3)
+    db = T.DeviceBatch.upload(batch, 0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    out = {"workload": f"glyph_fill_{batch.num_paths}_paths",
+           "config": {"paths": batch.num_paths, "contours": "1-6 of 8-40 quadratics; 10% stars",
+                      "tolerance": 0.1, "index_bits": 32, "index_mode": "global", "seed": 3}}
+    threads = os.cpu_count() or 1
+    for name, rule in (("non_zero", FillRule.NonZero), ("even_odd", FillRule.EvenOdd)):
+        opts = np.zeros(1, dtype=FILL_OPTIONS_DTYPE)
+        opts[0] = (0.1, rule, 0, 1)
+        od = T.upload_options(opts, 0)
+        for _ in range(2):
+            res = T.tessellate_paths("fill", db, od, 1, 32, T.INDEX_GLOBAL, 0, ctx)
+        ctx.synchronize()
+        steps = max(1, args.steps)
+        sweep_ms, phases = [], []
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(steps):
+            res = T.tessellate_paths("fill", db, od, 1, 32, T.INDEX_GLOBAL, 0, ctx)
+            ms4 = (ctypes.c_float * 4)()
+            ctx.lib.lyon_gpu_last_timings(ctx.h, ms4)
+            sweep_ms.append(ms4[0])
+            phases.append([ms4[0], ms4[1], ms4[2], ms4[3]])
+        end.record(stream)
+        end.synchronize()
+        ms = start.elapsed_time(end) / steps
+        v = res.total_vertices
+        entry = {"metric": "output vertices/s", "value": v / (ms / 1e3), "unit": "vertices/s",
+                 "ms_per_step": ms, "vertices_per_step": v, "indices_per_step": res.total_indices,
+                 "failed_paths": res.num_failed_paths,
+                 "sweep_kernel_ms": statistics.median(sweep_ms),
+                 "phases_ms": {"sweep": phases[-1][0], "scan": phases[-1][1],
+                               "emit": phases[-1][2], "call": phases[-1][3]},
+                 "gpu_launches": 4 * steps}
+        if args.profile_fill:
+            out[name] = entry
+            continue
+        n = min(20_000, batch.num_paths)
+        sub = batch.head(n)
+        orc.batch("fill", sub.head(min(n, 1000)), opts, 32, threads, want_output=False)
+        t0 = time.perf_counter()
+        r = orc.batch("fill", sub, opts, 32, threads, want_output=False)
+        dt = time.perf_counter() - t0
+        cv = int(r["vtx_counts"].sum())
+        entry["cpu_baseline"] = {"value": cv / dt, "unit": "vertices/s", "cores": threads,
+                                 "kind": "port",
+                                 "sample": f"first {n} paths, {cv} output vertices, "
+                                           f"{dt:.2f} s wall on {threads} threads"}
+        out[name] = entry
+    return out
+
+
+def run_serving(args):
+    """Serving loop: Poisson arrivals of scenes of 1-5,000 paths (log-uniform), 70 % strokes from
+    the plain-stroke generator, 30 % fills from the glyph generator; outputs stay resident; each
+    request released on completion. Offered load 50,000 requests/s, plus a load below
+    saturation; p50/p99/p99.9 latency from the scheduled arrival to the output on the device."""
+    from lyon_gb300 import serving, workloads
+    sp, so = workloads.plain_stroke(20_000, seed=1)
+    fp, fo = workloads.glyph_fill(5_000, seed=3)
+    reqs = serving.mixed_requests(sp, so, fp, fo, 4096, seed=5, max_paths=5000)
+    small = [r for r in reqs if r.count <= 1000]
+    srv = serving.Server(0, num_workers=3)
+    try:
+        srv.run_load(reqs[:64], rate_per_s=2000.0, duration_s=0.2, seed=1)  # warm-up
+        offered = srv.run_load(reqs, rate_per_s=50_000.0, duration_s=args.serve_seconds, seed=2)
+        cap_paths = offered["paths"] / max(offered["elapsed_s"], 1e-9)
+        mean_paths = float(np.mean([r.count for r in reqs]))
+        moderate_rate = max(50.0, 0.3 * cap_paths / mean_paths)
+        moderate = srv.run_load(reqs, rate_per_s=moderate_rate, duration_s=2.0, seed=3)
+        small_load = srv.run_load(small, rate_per_s=moderate_rate, duration_s=2.0, seed=4)
+    finally:
+        srv.close()
+
+    def brief(st):
+        return {k: st[k] for k in ("offered_rate", "submitted", "completed", "failed",
+                                   "achieved_rate", "elapsed_s", "p50_ms", "p99_ms", "p999_ms",
+                                   "max_ms", "batches", "mean_batch_paths")} | {
+            "vertices_per_s": st["vertices"] / max(st["elapsed_s"], 1e-9),
+            "paths_per_s": st["paths"] / max(st["elapsed_s"], 1e-9)}
+
+    return {"workload": "Poisson scenes of 1-5000 paths, 70% plain-stroke / 30% glyph-fill, "
+                        "u32, device-resident outputs",
+            "requests_in_pool": len(reqs), "mean_paths_per_request": mean_paths,
+            "offered_50k_per_s": brief(offered),
+            "below_saturation": brief(moderate),
+            "below_saturation_requests_le_1000_paths": brief(small_load)}
 
 
 def plain_per_path(ctx, batch, opts, T, count: int = 300):

@@ -18,13 +18,29 @@ constexpr uint32_t NONE = 0xFFFFFFFFu;
 constexpr int LEFT = 0, RIGHT = 1;
 constexpr int FILL_ERR_HEAP = 1000;  // internal: the path's heap was too small (retried)
 
-// ---- per-thread heap and growable arrays ------------------------------------------------------
+// ---- per-path heap and growable arrays --------------------------------------------------------
+
+__host__ __device__ __forceinline__ uint32_t ceil_log2(uint32_t x) {
+    uint32_t c = 0;
+    while ((1u << c) < x) ++c;
+    return c;
+}
+
+// Bump allocation of power-of-two blocks (8 words and up) with one free list per size, so the
+// arrays a path outgrows and the state of ended spans are reused.
+constexpr uint32_t HEAP_CLASSES = 28;
 
 struct Heap {
     uint32_t* w;
     uint32_t cap, top;
     bool oom;
-    __device__ __forceinline__ uint32_t alloc(uint32_t words) {
+    uint32_t free_head[HEAP_CLASSES];
+    __host__ __device__ void reset() {
+        top = 0;
+        oom = false;
+        for (uint32_t c = 0; c < HEAP_CLASSES; ++c) free_head[c] = NONE;
+    }
+    __host__ __device__ __forceinline__ uint32_t alloc(uint32_t words) {
         const uint32_t start = (top + 1u) & ~1u;  // 8-byte alignment for float2 members
         if (oom || start > cap || words > cap - start) {
             oom = true;
@@ -33,35 +49,61 @@ struct Heap {
         top = start + words;
         return start;
     }
+    // A block of at least `words` words; *cls receives its size class (2^cls words).
+    __host__ __device__ uint32_t alloc_block(uint32_t words, uint32_t* cls) {
+        uint32_t c = ceil_log2(words < 8 ? 8 : words);
+        *cls = c;
+        if (c < HEAP_CLASSES && free_head[c] != NONE) {
+            const uint32_t o = free_head[c];
+            free_head[c] = w[o];
+            return o;
+        }
+        return alloc(1u << c);
+    }
+    __host__ __device__ void free_block(uint32_t off, uint32_t c) {
+        if (c >= HEAP_CLASSES || oom) return;
+        w[off] = free_head[c];
+        free_head[c] = off;
+    }
 };
 
 template <class T>
 struct Vec {
     uint32_t off, n, cap;
-    __device__ __forceinline__ void init() { off = 0; n = 0; cap = 0; }
-    __device__ __forceinline__ T* p(const Heap& h) const {
+    __host__ __device__ __forceinline__ void init() { off = 0; n = 0; cap = 0; }
+    __host__ __device__ __forceinline__ T* p(const Heap& h) const {
         return reinterpret_cast<T*>(h.w + off);
     }
-    __device__ __forceinline__ T& at(const Heap& h, uint32_t i) const { return p(h)[i]; }
-    __device__ bool reserve(Heap& h, uint32_t want) {
+    __host__ __device__ __forceinline__ T& at(const Heap& h, uint32_t i) const { return p(h)[i]; }
+    static constexpr uint32_t WPE = (uint32_t)((sizeof(T) + 3) / 4);  // words per element
+    __host__ __device__ bool reserve(Heap& h, uint32_t want) {
         if (want <= cap) return true;
         uint32_t nc = cap < 4 ? 4 : cap * 2;
         while (nc < want) nc *= 2;
-        const uint32_t o = h.alloc(nc * (uint32_t)((sizeof(T) + 3) / 4));
+        uint32_t cls;
+        const uint32_t o = h.alloc_block(nc * WPE, &cls);
         if (h.oom) return false;
         T* dst = reinterpret_cast<T*>(h.w + o);
         const T* src = p(h);
         for (uint32_t i = 0; i < n; ++i) dst[i] = src[i];
+        if (cap > 0) h.free_block(off, ceil_log2(cap * WPE));
         off = o;
-        cap = nc;
+        cap = (1u << cls) / WPE;
         return true;
     }
-    __device__ __forceinline__ bool push(Heap& h, const T& v) {
+    // Returns the array's block to the heap (the array becomes empty).
+    __host__ __device__ void release(Heap& h) {
+        if (cap > 0) h.free_block(off, ceil_log2(cap * WPE));
+        off = 0;
+        cap = 0;
+        n = 0;
+    }
+    __host__ __device__ __forceinline__ bool push(Heap& h, const T& v) {
         if (!reserve(h, n + 1)) return false;
         p(h)[n++] = v;
         return true;
     }
-    __device__ bool insert(Heap& h, uint32_t i, const T& v) {
+    __host__ __device__ bool insert(Heap& h, uint32_t i, const T& v) {
         if (!reserve(h, n + 1)) return false;
         T* d = p(h);
         for (uint32_t k = n; k > i; --k) d[k] = d[k - 1];
@@ -69,12 +111,12 @@ struct Vec {
         ++n;
         return true;
     }
-    __device__ void erase(Heap& h, uint32_t i) {
+    __host__ __device__ void erase(Heap& h, uint32_t i) {
         T* d = p(h);
         for (uint32_t k = i; k + 1 < n; ++k) d[k] = d[k + 1];
         --n;
     }
-    __device__ __forceinline__ void clear() { n = 0; }
+    __host__ __device__ __forceinline__ void clear() { n = 0; }
 };
 
 // ---- event queue (event_queue.rs) ---------------------------------------------------------------
@@ -90,7 +132,7 @@ struct EdgeData {  // event_queue.rs:28-36
     uint32_t is_edge;
 };
 
-__device__ __forceinline__ int16_t w16(int v) { return (int16_t)v; }
+__host__ __device__ __forceinline__ int16_t w16(int v) { return (int16_t)v; }
 
 // ---- monotone tessellators (monotone.rs) ------------------------------------------------------
 
@@ -128,10 +170,10 @@ struct ActiveEdge {  // fill.rs:153-170
     uint32_t from_id, src_edge;
     float range_end;
     uint32_t pad;
-    __device__ __forceinline__ float min_x() const { return fminf(from.x, to.x); }
-    __device__ __forceinline__ float max_x() const { return from.x > to.x ? from.x : to.x; }
+    __host__ __device__ __forceinline__ float min_x() const { return fminf(from.x, to.x); }
+    __host__ __device__ __forceinline__ float max_x() const { return from.x > to.x ? from.x : to.x; }
     // fill.rs:185-200 with geom line.rs:56-71
-    __device__ __forceinline__ float solve_x_for_y(float y) const {
+    __host__ __device__ __forceinline__ float solve_x_for_y(float y) const {
         float dy = to.y - from.y;
         float t = dy == 0.0f ? 0.0f : (y - from.y) / dy;
         float x = from.x * (1.0f - t) + to.x * t;
@@ -152,9 +194,9 @@ struct VertexEvent {
     int32_t side;
 };
 
-__device__ __forceinline__ float fmax_lyon(float a, float b) { return a > b ? a : b; }
-__device__ __forceinline__ float slope(V2 v) { return v.x / fmaxf(v.y, 1.17549435e-38f); }
-__device__ __forceinline__ bool fill_rule_is_in(int rule, int16_t w) {  // path/src/lib.rs:267-281
+__host__ __device__ __forceinline__ float fmax_lyon(float a, float b) { return a > b ? a : b; }
+__host__ __device__ __forceinline__ float slope(V2 v) { return v.x / fmaxf(v.y, 1.17549435e-38f); }
+__host__ __device__ __forceinline__ bool fill_rule_is_in(int rule, int16_t w) {  // path/src/lib.rs:267-281
     if (rule == LYON_FILL_EVEN_ODD) return (w % 2) != 0;
     return w != 0;
 }
@@ -163,12 +205,12 @@ struct WindingState {  // fill.rs:88-113
     int32_t span_index;
     int16_t number;
     bool is_in;
-    __device__ __forceinline__ void reset() {
+    __host__ __device__ __forceinline__ void reset() {
         span_index = -1;
         number = 0;
         is_in = false;
     }
-    __device__ __forceinline__ void update(int rule, int16_t w) {
+    __host__ __device__ __forceinline__ void update(int rule, int16_t w) {
         number = w16(number + w);
         is_in = fill_rule_is_in(rule, number);
         if (is_in) span_index += 1;
@@ -176,7 +218,7 @@ struct WindingState {  // fill.rs:88-113
 };
 
 // fill.rs:2339-2347
-__device__ __forceinline__ float remap_t_in_range(float val, float start, float end) {
+__host__ __device__ __forceinline__ float remap_t_in_range(float val, float start, float end) {
     if (end > start) {
         float d = end - start;
         return start + val * d;
@@ -185,8 +227,32 @@ __device__ __forceinline__ float remap_t_in_range(float val, float start, float 
     return end + (1.0f - val) * d;
 }
 
+// Side of p relative to the line a -> b, (a - p) x (b - a), in f32 with a bound on its rounding
+// error: (a.x - p.x) and (a.y - p.y) round once, the products and the difference once more, so
+// the error stays below 4 * 2^-24 * (|t1| + |t2|); 1e-5 leaves a wide margin, and 1e-30 covers
+// underflow. NaN or infinite terms compare false and leave the sign unknown.
+__host__ __device__ __forceinline__ float orient_f32(V2 p, V2 a, V2 b, float* bound) {
+    const float t1 = (a.x - p.x) * (b.y - a.y);
+    const float t2 = (a.y - p.y) * (b.x - a.x);
+    *bound = 1e-5f * (fabsf(t1) + fabsf(t2)) + 1e-30f;
+    return t1 - t2;
+}
+
+// False only when segments s and o certainly do not intersect: both end points of one lie
+// strictly on the same side of the other's line, beyond the rounding bound. lyon's f64 test
+// (below) computes the same two orientations per segment, so it returns false in exactly
+// those cases; pairs that pass this filter go through the f64 test unchanged.
+__host__ __device__ __forceinline__ bool may_intersect(V2 sf, V2 st, V2 of, V2 ot) {
+    float b1, b2, b3, b4;
+    const float o1 = orient_f32(sf, of, ot, &b1), o2 = orient_f32(st, of, ot, &b2);
+    if ((o1 > b1 && o2 > b2) || (o1 < -b1 && o2 < -b2)) return false;
+    const float o3 = orient_f32(of, sf, st, &b3), o4 = orient_f32(ot, sf, st, &b4);
+    if ((o3 > b3 && o4 > b4) || (o3 < -b3 && o4 < -b4)) return false;
+    return true;
+}
+
 // geom line.rs:217-253 with S = f64
-static __device__ bool segment_intersection_t(double sfx, double sfy, double stx, double sty,
+static __host__ __device__ bool segment_intersection_t(double sfx, double sfy, double stx, double sty,
                                        double ofx, double ofy, double otx, double oty,
                                        double* ta, double* tb) {
     if ((stx == otx && sty == oty) || (sfx == ofx && sfy == ofy) ||

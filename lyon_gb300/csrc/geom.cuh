@@ -30,11 +30,11 @@ __host__ __device__ __forceinline__ V2 operator-(V2 a) { return V2{-a.x, -a.y}; 
 __host__ __device__ __forceinline__ float dot(V2 a, V2 b) { return a.x * b.x + a.y * b.y; }
 __host__ __device__ __forceinline__ float cross(V2 a, V2 b) { return a.x * b.y - a.y * b.x; }
 __host__ __device__ __forceinline__ float sqlen(V2 a) { return a.x * a.x + a.y * a.y; }
-__device__ __forceinline__ float vlength(V2 a) { return sqrtf(sqlen(a)); }
-__device__ __forceinline__ V2 normalize(V2 a) { return a / vlength(a); }
+__host__ __device__ __forceinline__ float vlength(V2 a) { return sqrtf(sqlen(a)); }
+__host__ __device__ __forceinline__ V2 normalize(V2 a) { return a / vlength(a); }
 __host__ __device__ __forceinline__ bool peq(V2 a, V2 b) { return a.x == b.x && a.y == b.y; }
 __host__ __device__ __forceinline__ V2 perp(V2 v) { return V2{-v.y, v.x}; }  // utils.rs:15-17
-__device__ __forceinline__ V2 lerp(V2 a, V2 b, float t) {
+__host__ __device__ __forceinline__ V2 lerp(V2 a, V2 b, float t) {
     float one_t = 1.0f - t;
     return V2{one_t * a.x + t * b.x, one_t * a.y + t * b.y};
 }
@@ -47,7 +47,7 @@ __device__ __forceinline__ float angle_to(float from, float to) {
     if (d < -LG_PI_F) d += two_pi;
     return d;
 }
-__device__ __forceinline__ bool isnan_f(float v) { return v != v; }
+__host__ __device__ __forceinline__ bool isnan_f(float v) { return v != v; }
 
 __device__ __forceinline__ V2 load_pt(const float* pts, uint32_t i) {
     float2 p = reinterpret_cast<const float2*>(pts)[i];
@@ -55,19 +55,19 @@ __device__ __forceinline__ V2 load_pt(const float* pts, uint32_t i) {
 }
 
 // Rust `as u32` on f32 (saturating, NaN -> 0).
-__device__ __forceinline__ uint32_t sat_u32(float v) {
+__host__ __device__ __forceinline__ uint32_t sat_u32(float v) {
     if (!(v == v) || v <= 0.0f) return 0u;
     if (v >= 4294967295.0f) return 0xFFFFFFFFu;
     return (uint32_t)v;
 }
 // NumCast::to_u32 on f32: None (-> 1 in lyon's unwrap_or) outside (-1, 2^32).
-__device__ __forceinline__ uint32_t to_u32_or1(float n) {
+__host__ __device__ __forceinline__ uint32_t to_u32_or1(float n) {
     if (n > -1.0f && n < 4294967296.0f) return (uint32_t)n;
     return 1u;
 }
 
 // ---- flattening segment counts (quadratic_bezier.rs:943-974, cubic_bezier.rs:1369-1403) -----
-__device__ __forceinline__ float wang_from_err4(float err4) {
+__host__ __device__ __forceinline__ float wang_from_err4(float err4) {
     // i^4 for i in 1..=24; the first i with err4 <= i^4 is ceil(err4^(1/4)).
     if (err4 <= 331776.0f) {
 #pragma unroll 1
@@ -80,14 +80,14 @@ __device__ __forceinline__ float wang_from_err4(float err4) {
     return fmaxf(sqrtf(sqrtf(err4)), 1.0f);
 }
 
-__device__ __forceinline__ float quad_wang(V2 from, V2 ctrl, V2 to, float tol) {
+__host__ __device__ __forceinline__ float quad_wang(V2 from, V2 ctrl, V2 to, float tol) {
     V2 l = ((from - ctrl * 2.0f) + to) * 2.0f;
     float d = 1.0f / (8.0f * tol);
     float err4 = dot(l, l) * d * d;
     return wang_from_err4(err4);
 }
 
-__device__ __forceinline__ float cubic_wang(V2 from, V2 c1, V2 c2, V2 to, float tol) {
+__host__ __device__ __forceinline__ float cubic_wang(V2 from, V2 c1, V2 c2, V2 to, float tol) {
     V2 v1 = ((from - c1 * 2.0f) + c2) * 6.0f;
     V2 v2_ = ((c1 - c2 * 2.0f) + to) * 6.0f;
     float l = fmaxf(dot(v1, v1), dot(v2_, v2_));
@@ -102,7 +102,7 @@ struct Poly {
     V2 a0, a1, a2, a3;
     bool cubic;
 };
-__device__ __forceinline__ Poly quad_poly(V2 from, V2 ctrl, V2 to) {
+__host__ __device__ __forceinline__ Poly quad_poly(V2 from, V2 ctrl, V2 to) {
     Poly p;
     p.a0 = from;
     p.a1 = (ctrl - from) * 2.0f;
@@ -111,7 +111,7 @@ __device__ __forceinline__ Poly quad_poly(V2 from, V2 ctrl, V2 to) {
     p.cubic = false;
     return p;
 }
-__device__ __forceinline__ Poly cubic_poly(V2 from, V2 c1, V2 c2, V2 to) {
+__host__ __device__ __forceinline__ Poly cubic_poly(V2 from, V2 c1, V2 c2, V2 to) {
     Poly p;
     p.a0 = from;
     p.a1 = (c1 - from) * 3.0f;
@@ -120,7 +120,7 @@ __device__ __forceinline__ Poly cubic_poly(V2 from, V2 c1, V2 c2, V2 to) {
     p.cubic = true;
     return p;
 }
-__device__ __forceinline__ V2 poly_sample(const Poly& p, float t) {
+__host__ __device__ __forceinline__ V2 poly_sample(const Poly& p, float t) {
     V2 v = p.a0;
     float t2 = t;
     v = v + p.a1 * t2;
@@ -134,7 +134,7 @@ __device__ __forceinline__ V2 poly_sample(const Poly& p, float t) {
 }
 
 // quadratic_bezier.rs:35-41
-__device__ __forceinline__ V2 quad_sample(V2 from, V2 ctrl, V2 to, float t) {
+__host__ __device__ __forceinline__ V2 quad_sample(V2 from, V2 ctrl, V2 to, float t) {
     float t2 = t * t;
     float one_t = 1.0f - t;
     float one_t2 = one_t * one_t;
@@ -262,16 +262,16 @@ __host__ __device__ __forceinline__ float accumulate_t_from(float s, uint32_t k0
 }
 
 // ---- fill ordering predicates (fill.rs:2122-2151) --------------------------------------------
-__device__ __forceinline__ int compare_positions(V2 a, V2 b) {
+__host__ __device__ __forceinline__ int compare_positions(V2 a, V2 b) {
     if (a.y > b.y) return 1;
     if (a.y < b.y) return -1;
     if (a.x > b.x) return 1;
     if (a.x < b.x) return -1;
     return 0;
 }
-__device__ __forceinline__ bool is_after(V2 a, V2 b) {
+__host__ __device__ __forceinline__ bool is_after(V2 a, V2 b) {
     return a.y > b.y || (a.y == b.y && a.x > b.x);
 }
-__device__ __forceinline__ bool is_near(V2 a, V2 b) { return sqlen(a - b) < 0.000000001f; }
+__host__ __device__ __forceinline__ bool is_near(V2 a, V2 b) { return sqlen(a - b) < 0.000000001f; }
 
 }  // namespace lg

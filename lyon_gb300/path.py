@@ -189,6 +189,13 @@ class PathBatch:
         p0, p1 = int(self.point_offsets[i]), int(self.point_offsets[i + 1])
         return Path(self.verbs[v0:v1], self.points[p0:p1])
 
+    def head(self, n: int) -> "PathBatch":
+        """The first n paths (array slices, offsets unchanged)."""
+        n = min(n, self.num_paths)
+        vo = self.verb_offsets[:n + 1]
+        po = self.point_offsets[:n + 1]
+        return PathBatch(self.verbs[:int(vo[-1])], self.points[:int(po[-1])], vo, po)
+
     def subset(self, idx: Sequence[int]) -> "PathBatch":
         return PathBatch.from_paths(self.path(int(i)) for i in idx)
 

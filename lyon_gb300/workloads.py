@@ -105,71 +105,72 @@ def batched_stroke(n_paths: int = 1_000_000, seed: int = 2):
     return batch, opts
 
 
+def _star_step(m: int) -> int:
+    """k of the star polygon {m/k}: coprime to m, so the outline visits every vertex."""
+    if m <= 4:
+        return 1
+    k = max(2, m // 2 - (1 if m % 2 == 0 else 0))
+    while math.gcd(m, k) != 1:
+        k -= 1
+    return max(k, 2)
+
+
 def glyph_fill(n_paths: int = 200_000, seed: int = 3, fill_rule: int = FillRule.NonZero):
     """Closed glyph-like paths; see the module docstring."""
     rng = np.random.default_rng(seed)
-    verbs_l = []
-    pts_l = []
-    vo = [0]
-    po = [0]
     is_star = rng.random(n_paths) < 0.10
-    n_contours = rng.integers(1, 7, size=n_paths)
-    for i in range(n_paths):
-        cx, cy = rng.uniform(0, 1024, size=2)
-        R = rng.uniform(5, 200)
-        v = []
-        p = []
-        if is_star[i]:
-            m = int(rng.integers(5, 51))
-            # A star polygon {m/k} with k coprime to m visits every vertex and self-intersects.
-            k = max(2, m // 2 - (1 if m % 2 == 0 else 0))
-            while math.gcd(m, k) != 1:
-                k -= 1
-            k = max(k, 2) if m > 4 else 1
-            ang = 2 * math.pi * ((np.arange(m) * k) % m) / m
-            rad = R * (1 + rng.uniform(-0.3, 0.3, size=m))
-            xs = cx + rad * np.cos(ang)
-            ys = cy + rad * np.sin(ang)
-            v.append(Verb.BEGIN)
-            p.append((xs[0], ys[0]))
-            for j in range(1, m):
-                v.append(Verb.LINE_TO)
-                p.append((xs[j], ys[j]))
-            v.append(Verb.CLOSE)
-            p.append((xs[0], ys[0]))
-        else:
-            for c in range(int(n_contours[i])):
-                if c == 0:
-                    ox, oy, r = cx, cy, R
-                    reverse = False
-                else:
-                    ox = cx + rng.uniform(-0.3, 0.3) * R
-                    oy = cy + rng.uniform(-0.3, 0.3) * R
-                    r = R * rng.uniform(0.1, 0.45)
-                    reverse = rng.random() < 0.30
-                m = int(rng.integers(8, 41))
-                ang = 2 * math.pi * np.arange(2 * m) / (2 * m)
-                if reverse:
-                    ang = -ang
-                rad = r * (1 + rng.uniform(-0.3, 0.3, size=2 * m))
-                xs = ox + rad * np.cos(ang)
-                ys = oy + rad * np.sin(ang)
-                v.append(Verb.BEGIN)
-                p.append((xs[0], ys[0]))
-                for j in range(m):
-                    c_idx = 2 * j + 1
-                    t_idx = (2 * j + 2) % (2 * m)
-                    v.append(Verb.QUADRATIC_TO)
-                    p.append((xs[c_idx], ys[c_idx]))
-                    p.append((xs[t_idx], ys[t_idx]))
-                v.append(Verb.CLOSE)
-                p.append((xs[0], ys[0]))
-        verbs_l.append(np.asarray(v, np.uint8))
-        pts_l.append(np.asarray(p, np.float32))
-        vo.append(vo[-1] + len(v))
-        po.append(po[-1] + len(p))
-    batch = PathBatch(np.concatenate(verbs_l), np.concatenate(pts_l).reshape(-1, 2),
-                      np.asarray(vo, np.uint32), np.asarray(po, np.uint32))
+    n_contours = np.where(is_star, 1, rng.integers(1, 7, size=n_paths)).astype(np.int64)
+    centre = rng.uniform(0, 1024, size=(n_paths, 2))
+    R = rng.uniform(5, 200, size=n_paths)
+    # One row per contour (a star path is one contour of lines).
+    n_c = int(n_contours.sum())
+    cpath = np.repeat(np.arange(n_paths, dtype=np.int64), n_contours)
+    cfirst = np.zeros(n_paths + 1, dtype=np.int64)
+    cfirst[1:] = np.cumsum(n_contours)
+    cidx = np.arange(n_c, dtype=np.int64) - cfirst[cpath]
+    cstar = is_star[cpath]
+    inner = cidx > 0
+    cR = R[cpath]
+    off = rng.uniform(-0.3, 0.3, size=(n_c, 2)) * cR[:, None]
+    ox = centre[cpath, 0] + np.where(inner, off[:, 0], 0.0)
+    oy = centre[cpath, 1] + np.where(inner, off[:, 1], 0.0)
+    r = np.where(inner, cR * rng.uniform(0.1, 0.45, size=n_c), cR)
+    reverse = inner & (rng.random(n_c) < 0.30)
+    m = np.where(cstar, rng.integers(5, 51, size=n_c), rng.integers(8, 41, size=n_c))
+    k = np.array([_star_step(int(x)) for x in range(51)], dtype=np.int64)[m]
+    # Raw outline points: m star vertices, or 2m alternating on-curve / control points.
+    n_raw = np.where(cstar, m, 2 * m)
+    raw_first = np.zeros(n_c + 1, dtype=np.int64)
+    raw_first[1:] = np.cumsum(n_raw)
+    rc = np.repeat(np.arange(n_c, dtype=np.int64), n_raw)
+    j = np.arange(int(raw_first[-1]), dtype=np.int64) - raw_first[rc]
+    ang = np.where(cstar[rc], 2 * math.pi * ((j * k[rc]) % m[rc]) / m[rc],
+                   2 * math.pi * j / (2 * m[rc]))
+    ang = np.where(reverse[rc], -ang, ang)
+    rad = r[rc] * (1 + rng.uniform(-0.3, 0.3, size=rc.shape[0]))
+    raw = np.stack([ox[rc] + rad * np.cos(ang), oy[rc] + rad * np.sin(ang)], axis=1)
+    # Emitted points: the raw points, then the first point again (the end of the last quadratic
+    # of a curved contour, and the point Close stores).
+    extra = np.where(cstar, 1, 2)
+    n_out = n_raw + extra
+    out_first = np.zeros(n_c + 1, dtype=np.int64)
+    out_first[1:] = np.cumsum(n_out)
+    oc = np.repeat(np.arange(n_c, dtype=np.int64), n_out)
+    oj = np.arange(int(out_first[-1]), dtype=np.int64) - out_first[oc]
+    src = raw_first[oc] + np.where(oj < n_raw[oc], oj, 0)
+    points = raw[src].astype(np.float32)
+    # Verbs: Begin, m - 1 lines (star) or m quadratics, Close.
+    n_verbs = np.where(cstar, m + 1, m + 2)
+    verb_first = np.zeros(n_c + 1, dtype=np.int64)
+    verb_first[1:] = np.cumsum(n_verbs)
+    vc = np.repeat(np.arange(n_c, dtype=np.int64), n_verbs)
+    vj = np.arange(int(verb_first[-1]), dtype=np.int64) - verb_first[vc]
+    body = np.where(cstar[vc], Verb.LINE_TO, Verb.QUADRATIC_TO)
+    verbs = np.where(vj == 0, Verb.BEGIN,
+                     np.where(vj == n_verbs[vc] - 1, Verb.CLOSE, body)).astype(np.uint8)
+    vo = verb_first[cfirst].astype(np.uint32)
+    po = out_first[cfirst].astype(np.uint32)
+    batch = PathBatch(verbs, points, vo, po)
     opts = np.zeros(1, dtype=FILL_OPTIONS_DTYPE)
     opts[0] = (0.1, fill_rule, Orientation.Vertical, 1)
     return batch, opts

@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--fill-paths", type=int, default=200_000)
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-seconds", type=float, default=0.1)
     ap.add_argument("--profile-fill", action="store_true",
                     help="only run the fill warm-up and timed steps (for profilers)")
     ap.add_argument("--profile", action="store_true",
@@ -413,8 +413,8 @@ def run_serving(args):
         cap_paths = offered["paths"] / max(offered["elapsed_s"], 1e-9)
         mean_paths = float(np.mean([r.count for r in reqs]))
         moderate_rate = max(50.0, 0.3 * cap_paths / mean_paths)
-        moderate = srv.run_load(reqs, rate_per_s=moderate_rate, duration_s=2.0, seed=3)
-        small_load = srv.run_load(small, rate_per_s=moderate_rate, duration_s=2.0, seed=4)
+        moderate = srv.run_load(reqs, rate_per_s=moderate_rate, duration_s=1.0, seed=3)
+        small_load = srv.run_load(small, rate_per_s=moderate_rate, duration_s=1.0, seed=4)
     finally:
         srv.close()
 

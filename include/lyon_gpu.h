@@ -245,7 +245,8 @@ int lyon_gpu_flatten_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch, 
 /* Batched stroke with HOST buffers (the end-to-end form of lyon_gpu_stroke_paths): the batch
  * and options live in host memory, outputs are written to host memory. The call processes the
  * paths in chunks, overlapping each chunk's host->device copy, kernels and device->host copy with
- * its neighbours', and returns when every output byte is on the host. `vertices`/`indices` must
+ * its neighbours', and returns when every output byte is on the host (pinned host buffers let
+ * the copies run at the link's full rate). `vertices`/`indices` must
  * hold `vertex_capacity` vertices and `index_capacity` indices; if they are too small the call
  * returns LYON_ERR_CAPACITY after setting *total_vertices / *total_indices to the sizes needed.
  * `status` (host, num_paths entries) receives the per-path status and may be NULL.

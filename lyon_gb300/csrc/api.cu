@@ -6,6 +6,7 @@
 // totals) -> emit. The host-buffer form runs that pipeline per chunk of paths and overlaps each
 // chunk's device->host copy (second stream) with the next chunk's kernels.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -39,12 +40,15 @@ struct lyon_gpu_context {
     std::string last_error;
     // per-path work arrays
     DevBuf vtx_counts, idx_counts, status, vtx_offsets, idx_offsets, scan_state;
-    DevBuf small;  // [0] work counter, [1] scan counter, [2] error flag, [3] failed paths
+    DevBuf small;  // [0] work counter, [1] scan counter, [2] error flag, [3] failed paths,
+                   // [4..5] processing-order counters
+    DevBuf order;  // processing order of the current stroke batch (long paths first)
+    bool order_valid = false;
     // outputs of device-buffer batched calls
     DevBuf out_vertices, out_indices;
     // host-buffer calls: inputs and double-buffered outputs
     DevBuf h_in_verbs, h_in_points, h_in_voff, h_in_poff, h_in_opts;
-    DevBuf slot_v[2], slot_i[2];
+    DevBuf slot_v[2], slot_i[2], slot_status[2];
     cudaEvent_t slot_done[2] = {nullptr, nullptr};
     cudaEvent_t emitted = nullptr;
     // fill scratch / staging
@@ -53,7 +57,7 @@ struct lyon_gpu_context {
     DevBuf flat_counts, flat_offsets, flat_points;
     // single-path staging
     DevBuf in_verbs, in_points, in_offsets, in_options;
-    HostBuf h_verbs, h_points, h_out_v, h_out_i, h_small, h_offs;
+    HostBuf h_verbs, h_points, h_out_v, h_out_i, h_small, h_offs, h_status;
     // optional per-path first path of its request (serving batches: one id space per request)
     const uint32_t* request_first = nullptr;
     // timing
@@ -119,6 +123,19 @@ T* as(DevBuf& b) {
 }
 
 uint64_t max_index_for(int bits) { return bits == 16 ? 65535ull : 0xFFFFFFFEull; }
+
+// The device address of a pinned, mapped host buffer, or null for any other memory.
+template <class T>
+T* direct_host_pointer(void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return reinterpret_cast<T*>(a.devicePointer);
+}
 
 uint32_t* small_words(lyon_gpu_context* ctx) { return as<uint32_t>(ctx->small); }
 
@@ -204,9 +221,16 @@ bool finish_counts(lyon_gpu_context* ctx, uint32_t n, int index_bits, int index_
             return false;
         if (!ensure_host(ctx, ctx->h_small, 64)) return false;
         uint64_t* hs = reinterpret_cast<uint64_t*>(ctx->h_small.ptr);
-        cudaMemcpyAsync(hs, as<uint64_t>(ctx->vtx_offsets) + n, 8, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(hs + 1, as<uint64_t>(ctx->idx_offsets) + n, 8, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(hs + 2, sw + 2, 8, cudaMemcpyDeviceToHost, s);
+        uint64_t* hs_dev = direct_host_pointer<uint64_t>(hs);
+        if (hs_dev) {
+            lg::launch_read_totals(as<uint64_t>(ctx->vtx_offsets) + n,
+                                   as<uint64_t>(ctx->idx_offsets) + n, sw + 2, hs_dev, s);
+        } else {
+            cudaMemcpyAsync(hs, as<uint64_t>(ctx->vtx_offsets) + n, 8, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(hs + 1, as<uint64_t>(ctx->idx_offsets) + n, 8, cudaMemcpyDeviceToHost,
+                            s);
+            cudaMemcpyAsync(hs + 2, sw + 2, 8, cudaMemcpyDeviceToHost, s);
+        }
         if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return false;
         *tv = hs[0];
         *ti = hs[1];
@@ -256,7 +280,7 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
     a.num_paths = batch->num_paths;
     a.options = options;
     a.num_options = num_options;
-    a.order = nullptr;
+    a.order = ctx->order_valid ? as<uint32_t>(ctx->order) : nullptr;
     a.work_counter = small_words(ctx);
     a.vtx_counts = as<uint32_t>(ctx->vtx_counts);
     a.idx_counts = as<uint32_t>(ctx->idx_counts);
@@ -284,7 +308,13 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     if (!alloc_path_arrays(ctx, n)) return LYON_ERR_OUT_OF_MEMORY;
     cudaStream_t s = ctx->stream;
     mark(ctx, 0);
+    ctx->order_valid = false;
     if (kind == KIND_STROKE) {
+        // Long paths first, so that no single long path is left running at the end of a launch.
+        if (n > 0 && ensure(ctx, ctx->order, (size_t)n * 4) &&
+            lg::launch_big_first_order(batch->point_offsets, n, 1024, as<uint32_t>(ctx->order),
+                                       small_words(ctx) + 4, s) == cudaSuccess)
+            ctx->order_valid = true;
         lg::StrokeArgs a = stroke_args(ctx, batch, (const lyon_stroke_options*)options,
                                        num_options, index_bits, index_mode, vertex_offset);
         if (n > 0) {
@@ -382,8 +412,14 @@ int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, con
     cudaSetDevice(ctx->device);
     const uint32_t n = hb->num_paths;
     const size_t isz = index_bits / 8;
-    // Chunks of at most CH paths and ~64 MB of points.
-    const uint32_t CH = 1u << 17;
+    // Chunks of at most CH paths (LYON_GB300_HOST_CHUNK_PATHS overrides) and ~64 MB of points.
+    uint32_t CH = 1u << 17;
+    if (const char* env = getenv("LYON_GB300_HOST_CHUNK_PATHS")) {
+        long v = atol(env);
+        if (v > 0 && v < (1l << 30)) CH = (uint32_t)v;
+    }
+    if (hstatus && n > 0 && !ensure_host(ctx, ctx->h_status, (size_t)n * 4))
+        return LYON_ERR_OUT_OF_MEMORY;
     uint64_t run_v = 0, run_i = 0;
     bool capacity_ok = true;
     int slot = 0;
@@ -447,9 +483,11 @@ int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, con
                               index_bits, index_mode, voff, as<float>(ctx->slot_v[slot]),
                               ctx->slot_i[slot].ptr, tv);
             if (r != LYON_OK) return r;
-            if (hstatus)
-                cudaMemcpyAsync(hstatus + c0, ctx->status.ptr, (size_t)cn * 4,
-                                cudaMemcpyDeviceToHost, s);
+            if (hstatus) {
+                if (!ensure(ctx, ctx->slot_status[slot], (size_t)cn * 4)) return LYON_ERR_OUT_OF_MEMORY;
+                cudaMemcpyAsync(ctx->slot_status[slot].ptr, ctx->status.ptr, (size_t)cn * 4,
+                                cudaMemcpyDeviceToDevice, s);
+            }
             cudaEventRecord(ctx->emitted, s);
             cudaStreamWaitEvent(ctx->copy_stream, ctx->emitted, 0);
             if (tv)
@@ -459,6 +497,10 @@ int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, con
                 cudaMemcpyAsync(reinterpret_cast<unsigned char*>(hi) + run_i * isz,
                                 ctx->slot_i[slot].ptr, ti * isz, cudaMemcpyDeviceToHost,
                                 ctx->copy_stream);
+            if (hstatus)  // into pinned staging: a copy into pageable memory would block
+                cudaMemcpyAsync(reinterpret_cast<int32_t*>(ctx->h_status.ptr) + c0,
+                                ctx->slot_status[slot].ptr, (size_t)cn * 4,
+                                cudaMemcpyDeviceToHost, ctx->copy_stream);
             cudaEventRecord(ctx->slot_done[slot], ctx->copy_stream);
             slot ^= 1;
         }
@@ -470,6 +512,7 @@ int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, con
     if (!set_err(ctx, "sync", cudaStreamSynchronize(ctx->copy_stream)) ||
         !set_err(ctx, "sync", cudaStreamSynchronize(ctx->stream)))
         return LYON_ERR_CUDA;
+    if (hstatus && capacity_ok && n > 0) std::memcpy(hstatus, ctx->h_status.ptr, (size_t)n * 4);
     if (total_v) *total_v = run_v;
     if (total_i) *total_i = run_i;
     if (!capacity_ok) {
@@ -625,11 +668,12 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->h_in_poff,  &ctx->h_in_opts,   &ctx->slot_v[0],   &ctx->slot_v[1],
                       &ctx->slot_i[0],  &ctx->slot_i[1],   &ctx->flat_counts, &ctx->flat_offsets,
                       &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
-                      &ctx->in_options};
+                      &ctx->in_options, &ctx->order, &ctx->slot_status[0],
+                      &ctx->slot_status[1]};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
     HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v, &ctx->h_out_i, &ctx->h_small,
-                     &ctx->h_offs};
+                     &ctx->h_offs, &ctx->h_status};
     for (HostBuf* b : hb) free_host(*b);
     for (int i = 0; i < 4; ++i)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);

@@ -25,6 +25,15 @@ namespace fillk {
 
 constexpr int32_t STATUS_RETRY = -1;
 
+#ifndef LG_FILL_SWEEPERS_PER_SM
+#define LG_FILL_SWEEPERS_PER_SM 32
+#endif
+#ifndef LG_FILL_MIN_BLOCKS
+#define LG_FILL_MIN_BLOCKS 32
+#endif
+// One sweeper per 32-thread block (its first lane runs the path).
+constexpr uint32_t FILL_SWEEPERS_PER_SM = LG_FILL_SWEEPERS_PER_SM;
+
 struct SweepArgs {
     const uint8_t* verbs;
     const float* points;
@@ -49,11 +58,11 @@ struct SweepArgs {
     int final_attempt;
 };
 
-__global__ void __launch_bounds__(128) fill_sweep_kernel(SweepArgs A) {
-    // One path per warp, run by its first lane: the sweep's control flow depends on the path,
-    // and 32 different paths in one warp would run one after the other anyway.
-    if ((threadIdx.x & 31) != 0) return;
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(32, LG_FILL_MIN_BLOCKS) fill_sweep_kernel(SweepArgs A) {
+    // One path per block of one warp, run by its first lane: the sweep's control flow depends on
+    // the path, and 32 different paths in one warp would run one after the other anyway.
+    if (threadIdx.x != 0) return;
+    const uint32_t wid = blockIdx.x;
     Filler f;
     f.h.w = A.heaps + (size_t)wid * A.heap_words;
     f.h.cap = A.heap_words;
@@ -172,9 +181,9 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         reinterpret_cast<char*>(fb.work) + 16);
     uint32_t* lists[2] = {reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(fb.work) + 64),
                           reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(fb.work) + 64) + n};
-    // Sweepers (one per warp) and heaps: 128-thread blocks, 4 per SM; heaps start at 64 K words
-    // (256 KB), which covers nearly every glyph-sized path.
-    const uint32_t threads = (uint32_t)(num_sms > 0 ? num_sms : 1) * 16u;
+    // Sweepers (one per warp) and heaps; heaps start at 64 K words (256 KB), which covers nearly
+    // every glyph-sized path.
+    const uint32_t threads = (uint32_t)(num_sms > 0 ? num_sms : 1) * fillk::FILL_SWEEPERS_PER_SM;
     if (fb.heap_words == 0) fb.heap_words = 65536;
     // Staging: start from a guess of 4 vertices and 12 indices per input point.
     if (fb.stage_v_cap == 0) {
@@ -228,8 +237,7 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         a.status = status;
         a.retry_list = lists[attempt & 1];
         a.final_attempt = attempt == MAX_ATTEMPTS - 1;
-        const uint32_t blocks = (nthreads + 3) / 4;  // 4 sweepers per 128-thread block
-        fillk::fill_sweep_kernel<<<blocks, 128, 0, stream>>>(a);
+        fillk::fill_sweep_kernel<<<nthreads, 32, 0, stream>>>(a);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             if (error) *error = std::string("fill sweep: ") + cudaGetErrorString(e);

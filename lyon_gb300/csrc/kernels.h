@@ -53,4 +53,16 @@ cudaError_t launch_per_path_limit(uint32_t* vtx_counts, uint32_t* idx_counts, in
 
 cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cudaStream_t s);
 
+// Writes out_a[n], out_b[n] (the scan totals) and the two u32 words at `words` into `host_dst`
+// (mapped pinned host memory) with a kernel, so that the read-back does not queue behind large
+// device->host copies on the copy engines.
+cudaError_t launch_read_totals(const uint64_t* a_total, const uint64_t* b_total,
+                               const uint32_t* words, uint64_t* host_dst, cudaStream_t s);
+
+// Processing order for a batch: paths with more than `big_points` points first (their work can
+// exceed the rest of a launch), then the others. `counters` holds two u32 and is reset here.
+// Outputs do not depend on the order (offsets come from the scan by path index).
+cudaError_t launch_big_first_order(const uint32_t* point_offsets, uint32_t n, uint32_t big_points,
+                                   uint32_t* order, uint32_t* counters, cudaStream_t s);
+
 }  // namespace lg

@@ -183,6 +183,54 @@ __global__ void narrow_u64_kernel(const uint64_t* in, uint32_t* out, uint32_t n)
     if (i < n) out[i] = (uint32_t)in[i];
 }
 
+__global__ void read_totals_kernel(const uint64_t* a_total, const uint64_t* b_total,
+                                   const uint32_t* words, uint64_t* host_dst) {
+    host_dst[0] = *a_total;
+    host_dst[1] = *b_total;
+    host_dst[2] = (uint64_t)words[0] | ((uint64_t)words[1] << 32);
+}
+
+cudaError_t launch_read_totals(const uint64_t* a_total, const uint64_t* b_total,
+                               const uint32_t* words, uint64_t* host_dst, cudaStream_t s) {
+    read_totals_kernel<<<1, 1, 0, s>>>(a_total, b_total, words, host_dst);
+    return cudaGetLastError();
+}
+
+__global__ void big_first_order_kernel(const uint32_t* point_offsets, uint32_t n,
+                                       uint32_t big_points, uint32_t* order, uint32_t* counters) {
+    // Every lane of every warp takes part in the votes (the grid is a whole number of warps).
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    const bool big = valid && point_offsets[i + 1] - point_offsets[i] > big_points;
+    const bool small = valid && !big;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t bmask = __ballot_sync(0xFFFFFFFFu, big);
+    const uint32_t smask = __ballot_sync(0xFFFFFFFFu, small);
+    // One atomic per warp and class.
+    const int leader_b = bmask ? __ffs(bmask) - 1 : 0, leader_s = smask ? __ffs(smask) - 1 : 0;
+    uint32_t base_b = 0, base_s = 0;
+    if (bmask && (int)lane == leader_b) base_b = atomicAdd(&counters[0], __popc(bmask));
+    if (smask && (int)lane == leader_s) base_s = atomicAdd(&counters[1], __popc(smask));
+    base_b = __shfl_sync(0xFFFFFFFFu, base_b, leader_b);
+    base_s = __shfl_sync(0xFFFFFFFFu, base_s, leader_s);
+    if (!valid) return;
+    const uint32_t below = (1u << lane) - 1u;
+    if (big) {
+        order[base_b + __popc(bmask & below)] = i;
+    } else {
+        order[n - 1 - (base_s + __popc(smask & below))] = i;
+    }
+}
+
+cudaError_t launch_big_first_order(const uint32_t* point_offsets, uint32_t n, uint32_t big_points,
+                                   uint32_t* order, uint32_t* counters, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    cudaMemsetAsync(counters, 0, 8, s);
+    big_first_order_kernel<<<(n + 255) / 256, 256, 0, s>>>(point_offsets, n, big_points, order,
+                                                           counters);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     narrow_u64_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, out, n);

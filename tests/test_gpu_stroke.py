@@ -172,3 +172,48 @@ def test_flatten_counts_and_points(gpu):
         assert np.array_equal(gc, oc)
         assert gp.shape == op.shape
         assert np.array_equal(gp, op)
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_buffer_entry_point_matches_device(gpu, pinned, monkeypatch):
+    # lyon_gpu_stroke_paths_host in several chunks (staged copies for pageable buffers, direct
+    # writes for pinned ones) equals the device-buffer call; too-small buffers give CAPACITY.
+    import ctypes
+    import torch
+    from lyon_gb300 import _native
+    monkeypatch.setenv("LYON_GB300_HOST_CHUNK_PATHS", "700")
+    batch, opts = workloads.batched_stroke(3000, seed=41)
+    g = gpu.gpu_batch("stroke", batch, opts, index_bits=32, index_mode=T.INDEX_GLOBAL)
+    tv, ti = int(g["total_vertices"]), int(g["total_indices"])
+    if pinned:
+        hv_t = torch.empty(2 * tv, dtype=torch.float32, pin_memory=True)
+        hi_t = torch.empty(ti, dtype=torch.int32, pin_memory=True)
+        vptr, iptr = hv_t.data_ptr(), hi_t.data_ptr()
+        get = lambda: (hv_t.numpy().reshape(-1, 2), hi_t.numpy().view(np.uint32))  # noqa: E731
+    else:
+        hv = np.empty(2 * tv, np.float32)
+        hi = np.empty(ti, np.uint32)
+        vptr, iptr = hv.ctypes.data, hi.ctypes.data
+        get = lambda: (hv.reshape(-1, 2), hi)  # noqa: E731
+    lib = gpu.ctx().lib
+    vs = np.ascontiguousarray(batch.verbs)
+    ps = np.ascontiguousarray(batch.points)
+    vo = np.ascontiguousarray(batch.verb_offsets)
+    po = np.ascontiguousarray(batch.point_offsets)
+    hb = _native.CPathBatch(vs.ctypes.data, ps.ctypes.data, vo.ctypes.data, po.ctypes.data,
+                            batch.num_paths)
+    oh = np.ascontiguousarray(opts)
+    status = np.full(batch.num_paths, -7, np.int32)
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    r = lib.lyon_gpu_stroke_paths_host(gpu.ctx().h, ctypes.byref(hb), oh.ctypes.data, len(oh),
+                                       32, T.INDEX_GLOBAL, 0, vptr, tv, iptr, ti,
+                                       status.ctypes.data, ctypes.byref(a), ctypes.byref(b))
+    assert r == 0 and a.value == tv and b.value == ti
+    v, i = get()
+    assert np.array_equal(i, g["indices"])
+    assert np.array_equal(v, g["vertices"])
+    assert np.array_equal(status, g["status"])
+    r = lib.lyon_gpu_stroke_paths_host(gpu.ctx().h, ctypes.byref(hb), oh.ctypes.data, len(oh),
+                                       32, T.INDEX_GLOBAL, 0, vptr, tv // 2, iptr, ti, None,
+                                       ctypes.byref(a), ctypes.byref(b))
+    assert r == T.LYON_ERR_CAPACITY and a.value == tv and b.value == ti

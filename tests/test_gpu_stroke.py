@@ -217,3 +217,24 @@ def test_host_buffer_entry_point_matches_device(gpu, pinned, monkeypatch):
                                        32, T.INDEX_GLOBAL, 0, vptr, tv // 2, iptr, ti, None,
                                        ctypes.byref(a), ctypes.byref(b))
     assert r == T.LYON_ERR_CAPACITY and a.value == tv and b.value == ti
+
+
+def test_batched_stroke_full_size_counts(gpu):
+    # The full 1,000,000-path batched workload: every path's vertex and index counts and status
+    # equal the oracle's (all host threads run the oracle).
+    import os
+    batch, opts = workloads.batched_stroke(1_000_000, seed=2)
+    ref = orc.batch("stroke", batch, opts, 32, os.cpu_count() or 1, want_output=False)
+    c = gpu.ctx()
+    db = T.DeviceBatch.upload(batch, 0)
+    od = T.upload_options(opts, 0)
+    res = T.tessellate_paths("stroke", db, od, len(opts), 32, T.INDEX_PER_PATH, 0, c)
+    c.synchronize()
+    vo, io = res.offsets()
+    gv = np.diff(vo.cpu().numpy())
+    gi = np.diff(io.cpu().numpy())
+    st = res.statuses().cpu().numpy()
+    assert np.array_equal(st, ref["status"])
+    bad = np.nonzero((gv != ref["vtx_counts"]) | (gi != ref["idx_counts"]))[0]
+    assert len(bad) == 0, bad[:10]
+    assert int(gv.sum()) == int(ref["vtx_counts"].sum())

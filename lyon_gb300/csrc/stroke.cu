@@ -642,9 +642,10 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         prv = S.c1;
     }
     const V2 ne = q - cur;
-    const V2 nt = ne / vlength(ne);
-    V2 pt = shfl_up_v2(nt, 1);
-    if (lane == 0) pt = S.jtan;
+    // Tangent of the edge cur -> q. The count pass needs tangents only at a sub-path's first
+    // point and when it evaluates the skip test exactly (below), so it computes them there.
+    V2 nt = V2{0.0f, 0.0f};
+    if (EMIT || (live && k == 0)) nt = ne / vlength(ne);
     const V2 pe = cur - prv;
     const bool isjoin = live && k >= 1;
     const bool fast = isjoin && fcur && dot(pe, ne) > 0.0f;
@@ -722,6 +723,18 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         exact = __any_sync(FULL, !ok);
     }
     if (exact) {
+        if (!EMIT) nt = ne / vlength(ne);
+        V2 pt = shfl_up_v2(nt, 1);
+        if (lane == 0) {
+            // The previous edge's tangent: carried by the emit pass, recomputed by the count
+            // pass with the same operations (c2 -> c1 is the edge into lane 0's join point).
+            if (EMIT) {
+                pt = S.jtan;
+            } else {
+                const V2 e = S.c1 - S.c2;
+                pt = e / vlength(e);
+            }
+        }
         if (fast) {
             const V2 nrm = compute_normal(pt, nt);
             pn = cur + nrm * P.hw;
@@ -882,7 +895,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         S.c1 = q1;
         S.f1 = fl1;
         S.s1 = __shfl_sync(FULL, sid, last);
-        S.jtan = shfl_v2(nt, last);
+        if (EMIT) S.jtan = shfl_v2(nt, last);
         S.jpn = shfl_v2(pn, last);
         S.jnn = shfl_v2(nn, last);
         S.jside_valid = __shfl_sync(FULL, (int)have_sides, last) != 0;

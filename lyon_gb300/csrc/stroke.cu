@@ -39,7 +39,15 @@ namespace lg {
 #ifndef LG_STROKE_MIN_BLOCKS
 #define LG_STROKE_MIN_BLOCKS 2
 #endif
+#ifndef LG_WINDOW_VERBS
+#define LG_WINDOW_VERBS 32
+#endif
+#ifndef LG_TAIL_QUEUE
+#define LG_TAIL_QUEUE 32
+#endif
 constexpr int STROKE_WARPS = LG_STROKE_WARPS;
+constexpr uint32_t WINDOW = LG_WINDOW_VERBS;  // verbs decoded per window (<= 32)
+constexpr uint32_t TAILQ = LG_TAIL_QUEUE;     // sub-path tails queued per warp (<= 32)
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr uint32_t MAX_VERB_STEPS = 1u << 26;
 constexpr uint32_t NO_VERB = 0xFFFFFFFFu;
@@ -83,10 +91,10 @@ enum : uint32_t {
 };
 
 struct WarpSmem {
-    VerbSlot verbs[32];
-    SpecSlot spec[64];
-    EmitJob ej[64];
-    TailJob tq[32];
+    VerbSlot verbs[WINDOW];
+    SpecSlot spec[2 * WINDOW];
+    EmitJob ej[2 * WINDOW];
+    TailJob tq[TAILQ];
 };
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
@@ -969,7 +977,7 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             const bool is_end = valid && (kind == LYON_VERB_END || kind == LYON_VERB_CLOSE);
             const bool bad_begin = valid && lane > 0 && kind == LYON_VERB_BEGIN;
             const uint32_t endmask = __ballot_sync(FULL, is_end || bad_begin);
-            uint32_t nv = min(32u, v_end - vi);
+            uint32_t nv = min(WINDOW, v_end - vi);
             if (endmask) nv = min(nv, (uint32_t)(__ffs(endmask)));
             const bool inwin = (uint32_t)lane < nv;
             if (inwin && bad_begin) kind = -1;
@@ -1032,7 +1040,7 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
         job.c1 = S.c1;
         if (vi >= v_end) {
             // The path's last sub-path: queue its tail.
-            if (tqn == 32) {
+            if (tqn == TAILQ) {
                 flush_tails<EMIT>(sm, lane, tqn, A);
                 tqn = 0;
             }

@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--fill-paths", type=int, default=200_000)
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-polylines", action="store_true")
+    ap.add_argument("--polyline-paths", type=int, default=2_000_000)
     ap.add_argument("--serve-seconds", type=float, default=0.1)
     ap.add_argument("--profile-fill", action="store_true",
                     help="only run the fill warm-up and timed steps (for profilers)")
@@ -320,6 +322,8 @@ def main():
         line["plain_per_path"] = plain_per_path(ctx, batch, opts, T)
         if not args.no_fill:
             line["fill"] = run_fill(ctx, args, T, world)
+        if not args.no_polylines:
+            line["polylines_autotuned"] = run_polylines(ctx, args, T)
         if not args.no_serve and world == 1:
             del db, od
             ctx.close()
@@ -393,6 +397,66 @@ def run_fill(ctx, args, T, world, batch=None):
                                  "sample": f"first {n} paths, {cv} output vertices, "
                                            f"{dt:.2f} s wall on {threads} threads"}
         out[name] = entry
+    return out
+
+
+def run_polylines(ctx, args, T):
+    """Map-like strokes (2,000,000 open polylines, Pareto lengths up to 20,000 points, mixed
+    joins, widths 1-8) at tolerances 0.01, 0.1 and 1.0; for each, the autotuner picks the stroke
+    launch settings on a 200,000-path sample, then the whole batch is timed with them."""
+    import torch
+    from lyon_gb300 import _native, workloads
+    from oracle import lyon_oracle as orc
+    batch, opts = workloads.map_polylines(args.polyline_paths, seed=4)
+    db = T.DeviceBatch.upload(batch, 0)
+    cb = db.c()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    saved = _native.CStrokeTuning()
+    ctx.lib.lyon_gpu_get_stroke_tuning(ctx.h, ctypes.byref(saved))
+    out = {"workload": f"map_polylines_{batch.num_paths}_paths",
+           "config": {"lengths": "Pareto alpha 1.2, 2..20000 points", "joins": "miter/bevel/round",
+                      "widths": "U[1, 8]", "index_bits": 32, "index_mode": "global", "seed": 4,
+                      "autotune_sample_paths": 200_000}}
+    threads = os.cpu_count() or 1
+    for tol in (0.01, 0.1, 1.0):
+        o = opts.copy()
+        o["tolerance"] = tol
+        od = T.upload_options(o, 0)
+        best = _native.CStrokeTuning()
+        times = (ctypes.c_float * 8)()
+        nc = ctypes.c_uint32()
+        ctx.lib.lyon_gpu_autotune_stroke(ctx.h, ctypes.byref(cb), od.data_ptr(), len(o), 200_000,
+                                         ctypes.byref(best), times, ctypes.byref(nc))
+        res = T.tessellate_paths("stroke", db, od, len(o), 32, T.INDEX_GLOBAL, 0, ctx)
+        ctx.synchronize()
+        steps = max(1, args.steps)
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(steps):
+            res = T.tessellate_paths("stroke", db, od, len(o), 32, T.INDEX_GLOBAL, 0, ctx)
+        end.record(stream)
+        end.synchronize()
+        ms = start.elapsed_time(end) / steps
+        entry = {"metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
+                 "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
+                 "chosen": {"long_path_points": best.long_path_points,
+                            "blocks_per_sm": best.blocks_per_sm},
+                 "candidate_ms": [round(float(t), 3) for t in times[:nc.value]],
+                 "gpu_launches": 5 * steps}
+        if tol == 0.1:
+            n = min(100_000, batch.num_paths)
+            sub = batch.head(n)
+            t0 = time.perf_counter()
+            r = orc.batch("stroke", sub, o[:n], 32, threads, want_output=False)
+            dt = time.perf_counter() - t0
+            cv = int(r["vtx_counts"].sum())
+            entry["cpu_baseline"] = {"value": cv / dt, "unit": "vertices/s", "cores": threads,
+                                     "kind": "port",
+                                     "sample": f"first {n} paths, {cv} output vertices, "
+                                               f"{dt:.2f} s wall on {threads} threads"}
+        out[f"tolerance_{tol}"] = entry
+    ctx.lib.lyon_gpu_set_stroke_tuning(ctx.h, ctypes.byref(saved))
     return out
 
 

@@ -348,6 +348,31 @@ int lyon_srv_run_load(lyon_srv* srv, const lyon_srv_load_item* items, uint32_t n
                       double rate_per_s, double duration_s, uint64_t seed,
                       lyon_srv_load_stats* stats, double* latencies_ms, uint32_t latencies_cap);
 
+/* ---- Stroke launch settings and autotuner (no lyon counterpart) ---------------------------- */
+
+/* Runtime settings of the stroke kernels on a context. */
+typedef struct lyon_gpu_stroke_tuning {
+    uint32_t long_path_points;  /* paths with more points are scheduled first (so that no long
+                                   path is left running alone at the end of a launch);
+                                   0: path order. Default 1024. */
+    uint32_t blocks_per_sm;     /* resident blocks per SM of the persistent grid; 0: as many as
+                                   fit (default) */
+} lyon_gpu_stroke_tuning;
+
+int lyon_gpu_set_stroke_tuning(lyon_gpu_context* ctx, const lyon_gpu_stroke_tuning* tuning);
+int lyon_gpu_get_stroke_tuning(lyon_gpu_context* ctx, lyon_gpu_stroke_tuning* tuning);
+
+/* Times the batched stroke (device buffers, u32 per-path indices) on the first `sample_paths`
+ * paths of `batch` (0: all) for each candidate setting — long_path_points in {0, 256, 1024,
+ * 8192} x blocks_per_sm in {as many as fit, 1} — and keeps the fastest on the context, so that
+ * later calls on paths of the same length distribution use it. `best` receives the choice;
+ * `times_ms` (optional, 8 entries) the candidates' times in that order (points vary fastest);
+ * `num_candidates` the count. Outputs of later calls do not depend on the settings. */
+int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                             const lyon_stroke_options* options, uint32_t num_options,
+                             uint32_t sample_paths, lyon_gpu_stroke_tuning* best,
+                             float* times_ms, uint32_t* num_candidates);
+
 /* Synchronise the context's stream. Returns LYON_OK or LYON_ERR_CUDA. */
 int lyon_gpu_synchronize(lyon_gpu_context* ctx);
 

@@ -64,6 +64,10 @@ class CSrvLoadStats(ctypes.Structure):
                 ("mean_batch_paths", ctypes.c_double)]
 
 
+class CStrokeTuning(ctypes.Structure):
+    _fields_ = [("long_path_points", u32), ("blocks_per_sm", u32)]
+
+
 class NativeLibraryMissing(RuntimeError):
     pass
 
@@ -138,6 +142,15 @@ def load(build_if_missing: bool = True):
         L.lyon_srv_run_load.argtypes = [c_p, ctypes.POINTER(CSrvLoadItem), u32, ctypes.c_double,
                                         ctypes.c_double, u64, ctypes.POINTER(CSrvLoadStats),
                                         c_p, u32]
+        for name in ("lyon_gpu_set_stroke_tuning", "lyon_gpu_get_stroke_tuning"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [c_p, ctypes.POINTER(CStrokeTuning)]
+        L.lyon_gpu_autotune_stroke.restype = ctypes.c_int
+        L.lyon_gpu_autotune_stroke.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
+                                               ctypes.POINTER(CStrokeTuning),
+                                               ctypes.POINTER(ctypes.c_float),
+                                               ctypes.POINTER(u32)]
         f = L.lyon_gpu_stroke_paths_noalloc
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.POINTER(CPathBatch), c_p, u32, ctypes.c_int, ctypes.c_int, u32,
@@ -156,5 +169,6 @@ EXPORTED = [
     "lyon_gpu_version", "lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host",
     "lyon_gpu_set_timing", "lyon_gpu_last_timings", "lyon_gpu_stroke_paths_noalloc",
     "lyon_srv_create", "lyon_srv_destroy", "lyon_srv_submit", "lyon_srv_poll", "lyon_srv_wait",
-    "lyon_srv_release", "lyon_srv_run_load",
+    "lyon_srv_release", "lyon_srv_run_load", "lyon_gpu_set_stroke_tuning",
+    "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke",
 ]

@@ -44,6 +44,9 @@ struct lyon_gpu_context {
                    // [4..5] processing-order counters
     DevBuf order;  // processing order of the current stroke batch (long paths first)
     bool order_valid = false;
+    // stroke launch settings (the autotuner's knobs)
+    uint32_t long_path_points = 1024;  // paths with more points go first; 0: path order
+    uint32_t blocks_per_sm = 0;        // 0: as many as fit
     // outputs of device-buffer batched calls
     DevBuf out_vertices, out_indices;
     // host-buffer calls: inputs and double-buffered outputs
@@ -295,7 +298,10 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
 }
 
 int stroke_grid(lyon_gpu_context* ctx, uint32_t n) {
-    const int max_grid = ctx->num_sms * ctx->stroke_bps;
+    const int bps = ctx->blocks_per_sm > 0 && (int)ctx->blocks_per_sm < ctx->stroke_bps
+                        ? (int)ctx->blocks_per_sm
+                        : ctx->stroke_bps;
+    const int max_grid = ctx->num_sms * bps;
     const int needed = (int)((n + 3) / 4);
     return needed < max_grid ? (needed > 0 ? needed : 1) : max_grid;
 }
@@ -311,9 +317,10 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     ctx->order_valid = false;
     if (kind == KIND_STROKE) {
         // Long paths first, so that no single long path is left running at the end of a launch.
-        if (n > 0 && ensure(ctx, ctx->order, (size_t)n * 4) &&
-            lg::launch_big_first_order(batch->point_offsets, n, 1024, as<uint32_t>(ctx->order),
-                                       small_words(ctx) + 4, s) == cudaSuccess)
+        if (n > 0 && ctx->long_path_points > 0 && ensure(ctx, ctx->order, (size_t)n * 4) &&
+            lg::launch_big_first_order(batch->point_offsets, n, ctx->long_path_points,
+                                       as<uint32_t>(ctx->order), small_words(ctx) + 4,
+                                       s) == cudaSuccess)
             ctx->order_valid = true;
         lg::StrokeArgs a = stroke_args(ctx, batch, (const lyon_stroke_options*)options,
                                        num_options, index_bits, index_mode, vertex_offset);
@@ -689,6 +696,82 @@ void* lyon_gpu_stream(lyon_gpu_context* ctx) { return ctx ? (void*)ctx->stream :
 
 const char* lyon_gpu_last_error(lyon_gpu_context* ctx) {
     return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int lyon_gpu_set_stroke_tuning(lyon_gpu_context* ctx, const lyon_gpu_stroke_tuning* t) {
+    if (!ctx || !t) return LYON_ERR_INVALID_ARGUMENT;
+    ctx->long_path_points = t->long_path_points;
+    ctx->blocks_per_sm = t->blocks_per_sm;
+    return LYON_OK;
+}
+
+int lyon_gpu_get_stroke_tuning(lyon_gpu_context* ctx, lyon_gpu_stroke_tuning* t) {
+    if (!ctx || !t) return LYON_ERR_INVALID_ARGUMENT;
+    t->long_path_points = ctx->long_path_points;
+    t->blocks_per_sm = ctx->blocks_per_sm;
+    return LYON_OK;
+}
+
+int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                             const lyon_stroke_options* options, uint32_t num_options,
+                             uint32_t sample_paths, lyon_gpu_stroke_tuning* best,
+                             float* times_ms, uint32_t* num_candidates) {
+    if (!ctx || !batch || !options || (num_options != 1 && num_options != batch->num_paths))
+        return LYON_ERR_INVALID_ARGUMENT;
+    static const uint32_t kPoints[] = {0u, 256u, 1024u, 8192u};
+    static const uint32_t kBlocks[] = {0u, 1u};
+    const uint32_t nc = 8;
+    if (num_candidates) *num_candidates = nc;
+    lyon_path_batch sample = *batch;
+    if (sample_paths > 0 && sample_paths < batch->num_paths) sample.num_paths = sample_paths;
+    const uint32_t sopts = num_options > 1 ? sample.num_paths : 1;
+    const uint32_t saved_points = ctx->long_path_points, saved_blocks = ctx->blocks_per_sm;
+    const bool saved_timing = ctx->timing;
+    ctx->timing = false;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = -1.0f;
+    lyon_gpu_stroke_tuning b{saved_points, saved_blocks};
+    int rc = LYON_OK;
+    for (uint32_t c = 0; c < nc && rc == LYON_OK; ++c) {
+        ctx->long_path_points = kPoints[c % 4];
+        ctx->blocks_per_sm = kBlocks[c / 4];
+        lyon_gpu_batch_output out;
+        rc = batched_device(ctx, KIND_STROKE, &sample, options, sopts, 32, LYON_INDEX_PER_PATH, 0,
+                            &out);  // warm-up (and buffer growth)
+        if (rc != LYON_OK) break;
+        float ms = 0.0f;
+        for (int rep = 0; rep < 2 && rc == LYON_OK; ++rep) {
+            cudaEventRecord(e0, ctx->stream);
+            rc = batched_device(ctx, KIND_STROKE, &sample, options, sopts, 32,
+                                LYON_INDEX_PER_PATH, 0, &out);
+            cudaEventRecord(e1, ctx->stream);
+            cudaEventSynchronize(e1);
+            float m = 0.0f;
+            cudaEventElapsedTime(&m, e0, e1);
+            ms += m;
+        }
+        ms *= 0.5f;
+        if (times_ms) times_ms[c] = ms;
+        if (best_ms < 0.0f || ms < best_ms) {
+            best_ms = ms;
+            b.long_path_points = ctx->long_path_points;
+            b.blocks_per_sm = ctx->blocks_per_sm;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->timing = saved_timing;
+    if (rc != LYON_OK) {
+        ctx->long_path_points = saved_points;
+        ctx->blocks_per_sm = saved_blocks;
+        return rc;
+    }
+    ctx->long_path_points = b.long_path_points;
+    ctx->blocks_per_sm = b.blocks_per_sm;
+    if (best) *best = b;
+    return LYON_OK;
 }
 
 int lyon_gpu_synchronize(lyon_gpu_context* ctx) {

@@ -238,3 +238,44 @@ def test_batched_stroke_full_size_counts(gpu):
     bad = np.nonzero((gv != ref["vtx_counts"]) | (gi != ref["idx_counts"]))[0]
     assert len(bad) == 0, bad[:10]
     assert int(gv.sum()) == int(ref["vtx_counts"].sum())
+
+
+@pytest.mark.parametrize("tol", [0.01, 0.1, 1.0])
+def test_map_polylines_subset(gpu, tol):
+    # The map-polyline generator (open polylines, Pareto lengths, miter/bevel/round joins, widths
+    # 1-8, coordinates up to 65536) at each tolerance of its sweep.
+    batch, opts = workloads.map_polylines(3000, seed=4, tolerance=tol, max_len=3000)
+    s = gpu.compare_per_path("stroke", batch, opts, index_bits=32)
+    _report(s)
+    assert not s["mismatches"], s["mismatches"][:10]
+    assert s["near_tie_mismatches"] <= max(2, batch.num_paths // 1000)
+
+
+def test_autotuner_picks_a_setting_and_keeps_outputs(gpu):
+    import ctypes
+    from lyon_gb300 import _native
+    batch, opts = workloads.map_polylines(4000, seed=44, max_len=5000)
+    before = gpu.gpu_batch("stroke", batch, opts, index_bits=32)
+    c = gpu.ctx()
+    db = T.DeviceBatch.upload(batch, 0)
+    od = T.upload_options(opts, 0)
+    cb = db.c()
+    best = _native.CStrokeTuning()
+    times = (ctypes.c_float * 8)()
+    nc = ctypes.c_uint32()
+    saved = _native.CStrokeTuning()
+    assert c.lib.lyon_gpu_get_stroke_tuning(c.h, ctypes.byref(saved)) == 0
+    try:
+        r = c.lib.lyon_gpu_autotune_stroke(c.h, ctypes.byref(cb), od.data_ptr(), len(opts), 2000,
+                                           ctypes.byref(best), times, ctypes.byref(nc))
+        assert r == 0 and nc.value == 8
+        assert all(t > 0.0 for t in times)
+        cur = _native.CStrokeTuning()
+        c.lib.lyon_gpu_get_stroke_tuning(c.h, ctypes.byref(cur))
+        assert (cur.long_path_points, cur.blocks_per_sm) == (best.long_path_points,
+                                                             best.blocks_per_sm)
+        after = gpu.gpu_batch("stroke", batch, opts, index_bits=32)
+        assert np.array_equal(after["indices"], before["indices"])
+        assert np.array_equal(after["vertices"], before["vertices"])
+    finally:
+        c.lib.lyon_gpu_set_stroke_tuning(c.h, ctypes.byref(saved))

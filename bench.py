@@ -258,6 +258,7 @@ def main():
     emit_ms = []
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
+    launches0 = lib.lyon_gpu_kernel_launches()
     with ClockSampler(dev) as clocks:
         start.record(stream)
         t0 = time.perf_counter()
@@ -269,6 +270,7 @@ def main():
         end.record(stream)
         end.synchronize()
         wall = time.perf_counter() - t0
+    launches = lib.lyon_gpu_kernel_launches() - launches0
     torch.cuda.synchronize()
     elapsed_ms = start.elapsed_time(end)
     if world > 1:
@@ -310,7 +312,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)", "config": workload_config(args.paths),
         "roofline": roofline, "clocks": clocks.summary(),
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": launches,
         "wall_ms_per_step": wall / args.steps * 1e3,
         "output_vertices_per_step": verts_per_step, "output_indices_per_step": idx_per_step,
     }
@@ -364,6 +366,7 @@ def run_fill(ctx, args, T, world, batch=None):
         sweep_ms, phases = [], []
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
+        launches0 = ctx.lib.lyon_gpu_kernel_launches()
         start.record(stream)
         for _ in range(steps):
             res = T.tessellate_paths("fill", db, od, 1, 32, T.INDEX_GLOBAL, 0, ctx)
@@ -381,7 +384,7 @@ def run_fill(ctx, args, T, world, batch=None):
                  "sweep_kernel_ms": statistics.median(sweep_ms),
                  "phases_ms": {"sweep": phases[-1][0], "scan": phases[-1][1],
                                "emit": phases[-1][2], "call": phases[-1][3]},
-                 "gpu_launches": 4 * steps}
+                 "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
         if args.profile_fill:
             out[name] = entry
             continue
@@ -423,7 +426,7 @@ def run_polylines(ctx, args, T):
         o["tolerance"] = tol
         od = T.upload_options(o, 0)
         best = _native.CStrokeTuning()
-        times = (ctypes.c_float * 8)()
+        times = (ctypes.c_float * 16)()
         nc = ctypes.c_uint32()
         ctx.lib.lyon_gpu_autotune_stroke(ctx.h, ctypes.byref(cb), od.data_ptr(), len(o), 200_000,
                                          ctypes.byref(best), times, ctypes.byref(nc))
@@ -432,6 +435,7 @@ def run_polylines(ctx, args, T):
         steps = max(1, args.steps)
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
+        launches0 = ctx.lib.lyon_gpu_kernel_launches()
         start.record(stream)
         for _ in range(steps):
             res = T.tessellate_paths("stroke", db, od, len(o), 32, T.INDEX_GLOBAL, 0, ctx)
@@ -441,9 +445,10 @@ def run_polylines(ctx, args, T):
         entry = {"metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
                  "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
                  "chosen": {"long_path_points": best.long_path_points,
-                            "blocks_per_sm": best.blocks_per_sm},
+                            "blocks_per_sm": best.blocks_per_sm,
+                            "short_path_points": best.short_path_points},
                  "candidate_ms": [round(float(t), 3) for t in times[:nc.value]],
-                 "gpu_launches": 5 * steps}
+                 "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
         if tol == 0.1:
             n = min(100_000, batch.num_paths)
             sub = batch.head(n)
@@ -550,15 +555,17 @@ def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
     lib.lyon_gpu_set_timing(ctx.h, 0)
     call()
     steps = max(1, min(args.steps, 3))
+    launches0 = lib.lyon_gpu_kernel_launches()
     t0 = time.perf_counter()
     for _ in range(steps):
         call()
     dt = (time.perf_counter() - t0) / steps
+    launches = lib.lyon_gpu_kernel_launches() - launches0
     h2d = batch.input_bytes(options_bytes_per_path=24)
     d2h = int(tv) * 8 + int(ti) * 4 + batch.num_paths * 4
     return {"value": int(tvo.value) / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3, "steps": steps,
-            "host_buffers": host_kind}
+            "host_buffers": host_kind, "gpu_launches": launches}
 
 
 if __name__ == "__main__":

@@ -357,6 +357,9 @@ typedef struct lyon_gpu_stroke_tuning {
                                    0: path order. Default 1024. */
     uint32_t blocks_per_sm;     /* resident blocks per SM of the persistent grid; 0: as many as
                                    fit (default) */
+    uint32_t short_path_points; /* line-only paths of at most this many points are stroked one
+                                   path per thread instead of one per warp; 0: none, at most 64.
+                                   Default 32. */
 } lyon_gpu_stroke_tuning;
 
 int lyon_gpu_set_stroke_tuning(lyon_gpu_context* ctx, const lyon_gpu_stroke_tuning* tuning);
@@ -364,10 +367,11 @@ int lyon_gpu_get_stroke_tuning(lyon_gpu_context* ctx, lyon_gpu_stroke_tuning* tu
 
 /* Times the batched stroke (device buffers, u32 per-path indices) on the first `sample_paths`
  * paths of `batch` (0: all) for each candidate setting — long_path_points in {0, 256, 1024,
- * 8192} x blocks_per_sm in {as many as fit, 1} — and keeps the fastest on the context, so that
- * later calls on paths of the same length distribution use it. `best` receives the choice;
- * `times_ms` (optional, 8 entries) the candidates' times in that order (points vary fastest);
- * `num_candidates` the count. Outputs of later calls do not depend on the settings. */
+ * 8192} x blocks_per_sm in {as many as fit, 1} x short_path_points in {0, 32} — and keeps the
+ * fastest on the context, so that later calls on paths of the same length distribution use it.
+ * `best` receives the choice; `times_ms` (optional, 16 entries) the candidates' times in that
+ * order (long_path_points varies fastest, short_path_points slowest); `num_candidates` the
+ * count. Outputs of later calls do not depend on the settings. */
 int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                              const lyon_stroke_options* options, uint32_t num_options,
                              uint32_t sample_paths, lyon_gpu_stroke_tuning* best,
@@ -378,6 +382,10 @@ int lyon_gpu_synchronize(lyon_gpu_context* ctx);
 
 /* Library version and build information (static string). */
 const char* lyon_gpu_version(void);
+
+/* Number of kernel launches this library has issued in this process so far (all contexts and
+ * threads; no lyon counterpart). The difference across a call is that call's launch count. */
+uint64_t lyon_gpu_kernel_launches(void);
 
 #ifdef __cplusplus
 }

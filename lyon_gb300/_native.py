@@ -65,7 +65,7 @@ class CSrvLoadStats(ctypes.Structure):
 
 
 class CStrokeTuning(ctypes.Structure):
-    _fields_ = [("long_path_points", u32), ("blocks_per_sm", u32)]
+    _fields_ = [("long_path_points", u32), ("blocks_per_sm", u32), ("short_path_points", u32)]
 
 
 class NativeLibraryMissing(RuntimeError):
@@ -93,6 +93,8 @@ def load(build_if_missing: bool = True):
             raise NativeLibraryMissing(f"{path} is missing; run lyon_gb300.build.build()")
         L = ctypes.CDLL(path)
         L.lyon_gpu_version.restype = ctypes.c_char_p
+        L.lyon_gpu_kernel_launches.restype = u64
+        L.lyon_gpu_kernel_launches.argtypes = []
         L.lyon_gpu_create.restype = c_p
         L.lyon_gpu_create.argtypes = [ctypes.c_int]
         L.lyon_gpu_destroy.argtypes = [c_p]
@@ -170,5 +172,5 @@ EXPORTED = [
     "lyon_gpu_set_timing", "lyon_gpu_last_timings", "lyon_gpu_stroke_paths_noalloc",
     "lyon_srv_create", "lyon_srv_destroy", "lyon_srv_submit", "lyon_srv_poll", "lyon_srv_wait",
     "lyon_srv_release", "lyon_srv_run_load", "lyon_gpu_set_stroke_tuning",
-    "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke",
+    "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
 ]

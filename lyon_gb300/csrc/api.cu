@@ -44,9 +44,12 @@ struct lyon_gpu_context {
                    // [4..5] processing-order counters
     DevBuf order;  // processing order of the current stroke batch (long paths first)
     bool order_valid = false;
+    DevBuf path_class, class_counters;  // classification for the one-thread-per-path phase
+    bool split_valid = false;           // class_counters holds the first short item
     // stroke launch settings (the autotuner's knobs)
     uint32_t long_path_points = 1024;  // paths with more points go first; 0: path order
     uint32_t blocks_per_sm = 0;        // 0: as many as fit
+    uint32_t short_path_points = 32;   // line-only paths up to this size: one per thread
     // outputs of device-buffer batched calls
     DevBuf out_vertices, out_indices;
     // host-buffer calls: inputs and double-buffered outputs
@@ -292,6 +295,10 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
     a.index_mode = index_mode;
     a.vertex_offset = (uint32_t)vertex_offset;
     a.request_first = ctx->request_first;
+    if (ctx->split_valid) {
+        a.item_split = as<uint32_t>(ctx->class_counters) + 2 * (3 + ctx->short_path_points);
+        a.seq_counter = small_words(ctx) + 6;
+    }
     a.vtx_offsets = as<uint64_t>(ctx->vtx_offsets);
     a.idx_offsets = as<uint64_t>(ctx->idx_offsets);
     return a;
@@ -315,17 +322,30 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     cudaStream_t s = ctx->stream;
     mark(ctx, 0);
     ctx->order_valid = false;
+    ctx->split_valid = false;
     if (kind == KIND_STROKE) {
-        // Long paths first, so that no single long path is left running at the end of a launch.
-        if (n > 0 && ctx->long_path_points > 0 && ensure(ctx, ctx->order, (size_t)n * 4) &&
-            lg::launch_big_first_order(batch->point_offsets, n, ctx->long_path_points,
-                                       as<uint32_t>(ctx->order), small_words(ctx) + 4,
-                                       s) == cudaSuccess)
+        // Long paths first, so that no single long path is left running at the end of a launch;
+        // short line-only paths last, for the one-thread-per-path phase.
+        if (n > 0 && ctx->short_path_points > 0) {
+            if (ensure(ctx, ctx->order, (size_t)n * 4) && ensure(ctx, ctx->path_class, n) &&
+                ensure(ctx, ctx->class_counters, lg::CLASSIFY_COUNTER_WORDS * 4) &&
+                lg::launch_classify_paths(batch->verbs, batch->verb_offsets,
+                                          batch->point_offsets, n, ctx->long_path_points,
+                                          ctx->short_path_points,
+                                          as<uint8_t>(ctx->path_class), as<uint32_t>(ctx->order),
+                                          as<uint32_t>(ctx->class_counters), s) == cudaSuccess)
+                ctx->order_valid = ctx->split_valid = true;
+        } else if (n > 0 && ctx->long_path_points > 0 && ensure(ctx, ctx->order, (size_t)n * 4) &&
+                   lg::launch_big_first_order(batch->point_offsets, n, ctx->long_path_points,
+                                              as<uint32_t>(ctx->order), small_words(ctx) + 4,
+                                              s) == cudaSuccess) {
             ctx->order_valid = true;
+        }
         lg::StrokeArgs a = stroke_args(ctx, batch, (const lyon_stroke_options*)options,
                                        num_options, index_bits, index_mode, vertex_offset);
         if (n > 0) {
             cudaMemsetAsync(small_words(ctx), 0, 4, s);
+            if (a.seq_counter) cudaMemsetAsync(a.seq_counter, 0, 4, s);
             if (!set_err(ctx, "stroke count", lg::launch_stroke(a, false, stroke_grid(ctx, n), s)))
                 return LYON_ERR_CUDA;
         }
@@ -356,6 +376,7 @@ int pipeline_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
         a.indices = iout;
         if (n > 0 && tv > 0) {
             cudaMemsetAsync(small_words(ctx), 0, 4, s);
+            if (a.seq_counter) cudaMemsetAsync(a.seq_counter, 0, 4, s);
             if (!set_err(ctx, "stroke emit", lg::launch_stroke(a, true, stroke_grid(ctx, n), s)))
                 return LYON_ERR_CUDA;
         }
@@ -637,6 +658,8 @@ extern "C" {
 
 const char* lyon_gpu_version(void) { return kVersion; }
 
+uint64_t lyon_gpu_kernel_launches(void) { return lg::launches_total(); }
+
 lyon_gpu_context* lyon_gpu_create(int device) {
     lyon_gpu_context* ctx = new lyon_gpu_context();
     ctx->device = device;
@@ -676,7 +699,7 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->slot_i[0],  &ctx->slot_i[1],   &ctx->flat_counts, &ctx->flat_offsets,
                       &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
                       &ctx->in_options, &ctx->order, &ctx->slot_status[0],
-                      &ctx->slot_status[1]};
+                      &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
     HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v, &ctx->h_out_i, &ctx->h_small,
@@ -700,8 +723,13 @@ const char* lyon_gpu_last_error(lyon_gpu_context* ctx) {
 
 int lyon_gpu_set_stroke_tuning(lyon_gpu_context* ctx, const lyon_gpu_stroke_tuning* t) {
     if (!ctx || !t) return LYON_ERR_INVALID_ARGUMENT;
+    if (t->short_path_points > lg::CLASSIFY_MAX_SHORT_POINTS) {
+        ctx->last_error = "short_path_points above 64";
+        return LYON_ERR_INVALID_ARGUMENT;
+    }
     ctx->long_path_points = t->long_path_points;
     ctx->blocks_per_sm = t->blocks_per_sm;
+    ctx->short_path_points = t->short_path_points;
     return LYON_OK;
 }
 
@@ -709,6 +737,7 @@ int lyon_gpu_get_stroke_tuning(lyon_gpu_context* ctx, lyon_gpu_stroke_tuning* t)
     if (!ctx || !t) return LYON_ERR_INVALID_ARGUMENT;
     t->long_path_points = ctx->long_path_points;
     t->blocks_per_sm = ctx->blocks_per_sm;
+    t->short_path_points = ctx->short_path_points;
     return LYON_OK;
 }
 
@@ -720,23 +749,26 @@ int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch
         return LYON_ERR_INVALID_ARGUMENT;
     static const uint32_t kPoints[] = {0u, 256u, 1024u, 8192u};
     static const uint32_t kBlocks[] = {0u, 1u};
-    const uint32_t nc = 8;
+    static const uint32_t kShort[] = {0u, 32u};
+    const uint32_t nc = 16;
     if (num_candidates) *num_candidates = nc;
     lyon_path_batch sample = *batch;
     if (sample_paths > 0 && sample_paths < batch->num_paths) sample.num_paths = sample_paths;
     const uint32_t sopts = num_options > 1 ? sample.num_paths : 1;
-    const uint32_t saved_points = ctx->long_path_points, saved_blocks = ctx->blocks_per_sm;
+    lyon_gpu_stroke_tuning saved;
+    lyon_gpu_get_stroke_tuning(ctx, &saved);
     const bool saved_timing = ctx->timing;
     ctx->timing = false;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best_ms = -1.0f;
-    lyon_gpu_stroke_tuning b{saved_points, saved_blocks};
+    lyon_gpu_stroke_tuning b = saved;
     int rc = LYON_OK;
     for (uint32_t c = 0; c < nc && rc == LYON_OK; ++c) {
         ctx->long_path_points = kPoints[c % 4];
-        ctx->blocks_per_sm = kBlocks[c / 4];
+        ctx->blocks_per_sm = kBlocks[(c / 4) % 2];
+        ctx->short_path_points = kShort[c / 8];
         lyon_gpu_batch_output out;
         rc = batched_device(ctx, KIND_STROKE, &sample, options, sopts, 32, LYON_INDEX_PER_PATH, 0,
                             &out);  // warm-up (and buffer growth)
@@ -756,20 +788,17 @@ int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch
         if (times_ms) times_ms[c] = ms;
         if (best_ms < 0.0f || ms < best_ms) {
             best_ms = ms;
-            b.long_path_points = ctx->long_path_points;
-            b.blocks_per_sm = ctx->blocks_per_sm;
+            lyon_gpu_get_stroke_tuning(ctx, &b);
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ctx->timing = saved_timing;
     if (rc != LYON_OK) {
-        ctx->long_path_points = saved_points;
-        ctx->blocks_per_sm = saved_blocks;
+        lyon_gpu_set_stroke_tuning(ctx, &saved);
         return rc;
     }
-    ctx->long_path_points = b.long_path_points;
-    ctx->blocks_per_sm = b.blocks_per_sm;
+    lyon_gpu_set_stroke_tuning(ctx, &b);
     if (best) *best = b;
     return LYON_OK;
 }

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "fill.h"
+#include "kernels.h"
 #include "fill_sweep.cuh"
 
 namespace lg {
@@ -238,6 +239,7 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         a.retry_list = lists[attempt & 1];
         a.final_attempt = attempt == MAX_ATTEMPTS - 1;
         fillk::fill_sweep_kernel<<<nthreads, 32, 0, stream>>>(a);
+        lg::note_launches(1);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             if (error) *error = std::string("fill sweep: ") + cudaGetErrorString(e);
@@ -289,6 +291,7 @@ cudaError_t fill_emit(FillBuffers& fb, uint32_t n, const uint32_t* vtx_counts,
         reinterpret_cast<const float2*>(fb.stage_v), reinterpret_cast<const uint32_t*>(fb.stage_i),
         vtx_offsets, idx_offsets, reinterpret_cast<float2*>(vertices), indices, index_bits,
         index_mode, vertex_offset, request_first);
+    lg::note_launches(1);
     return cudaGetLastError();
 }
 

@@ -8,6 +8,7 @@
 // accumulated parameter (crates/geom/src/quadratic_bezier.rs:1004-1033 and
 // crates/geom/src/cubic_bezier.rs:1434-1459 iterators).
 #include "geom.cuh"
+#include "kernels.h"
 #include "kernels_flatten.h"
 
 namespace lg {
@@ -127,8 +128,10 @@ __global__ void flatten_kernel(FlattenArgs A) {
 cudaError_t launch_flatten(const FlattenArgs& a, bool write_points, int grid, cudaStream_t s) {
     if (write_points) {
         flatten_kernel<true><<<grid, 256, 0, s>>>(a);
+        note_launches(1);
     } else {
         flatten_kernel<false><<<grid, 256, 0, s>>>(a);
+        note_launches(1);
     }
     return cudaGetLastError();
 }

@@ -8,6 +8,11 @@
 
 namespace lg {
 
+// Kernel launches issued by this library in this process (every context and thread): each
+// launch site notes its launches here.
+void note_launches(uint32_t k);
+uint64_t launches_total();
+
 struct StrokeArgs {
     const uint8_t* verbs;
     const float* points;
@@ -32,6 +37,11 @@ struct StrokeArgs {
     // Optional, per path: the first path of the request it belongs to. In LYON_INDEX_GLOBAL mode
     // ids then count from that path's first vertex (one VertexBuffers per request of a batch).
     const uint32_t* request_first;
+    // Optional, with `order`: items [0, *item_split) of the order are stroked one path per warp,
+    // the rest (short line-only paths) one path per thread, 32 per warp, once a warp finds no
+    // warp items left; `seq_counter` (zeroed before each launch) hands out those.
+    const uint32_t* item_split;
+    uint32_t* seq_counter;
 };
 
 int stroke_blocks_per_sm();
@@ -58,6 +68,19 @@ cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cud
 // device->host copies on the copy engines.
 cudaError_t launch_read_totals(const uint64_t* a_total, const uint64_t* b_total,
                                const uint32_t* words, uint64_t* host_dst, cudaStream_t s);
+
+// Processing order by class: paths with more than `big_points` points (0: none) first, then the
+// other paths, then line-only paths of at most `short_points` points (0: none; at most
+// CLASSIFY_MAX_SHORT_POINTS) by decreasing point count: the one-thread-per-path phase of the
+// stroke kernel takes those. `path_class` holds one byte per path; `counters` 2 * (3 +
+// short_points) + 1 words (bin sizes, placement cursors, then the first short item), reset here.
+constexpr uint32_t CLASSIFY_MAX_SHORT_POINTS = 64;
+constexpr uint32_t CLASSIFY_MAX_BINS = 3 + CLASSIFY_MAX_SHORT_POINTS;
+constexpr uint32_t CLASSIFY_COUNTER_WORDS = 2 * CLASSIFY_MAX_BINS + 1;
+cudaError_t launch_classify_paths(const uint8_t* verbs, const uint32_t* verb_offsets,
+                                  const uint32_t* point_offsets, uint32_t n, uint32_t big_points,
+                                  uint32_t short_points, uint8_t* path_class, uint32_t* order,
+                                  uint32_t* counters, cudaStream_t s);
 
 // Processing order for a batch: paths with more than `big_points` points first (their work can
 // exceed the rest of a launch), then the others. `counters` holds two u32 and is reset here.

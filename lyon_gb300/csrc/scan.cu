@@ -6,9 +6,15 @@
 // until it meets an inclusive prefix, and publishes its own inclusive prefix. States pack a 2-bit
 // flag with a 62-bit value in one u64 so that a single load sees a consistent pair. Waits are
 // bounded: past the bound the kernel records an error and returns without hanging the GPU.
+#include <atomic>
+
 #include "kernels.h"
 
 namespace lg {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launches(uint32_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+uint64_t launches_total() { return g_launches.load(std::memory_order_relaxed); }
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
@@ -162,6 +168,7 @@ cudaError_t launch_scan_pairs(const uint32_t* a, const uint32_t* b, uint64_t* ou
     cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
     scan_pairs_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, stream>>>(a, b, out_a, out_b, n,
                                                                    tile_state, counter, error);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -171,6 +178,7 @@ cudaError_t launch_per_path_limit(uint32_t* vtx_counts, uint32_t* idx_counts, in
     if (n == 0) return cudaSuccess;
     per_path_limit_kernel<<<(n + 255) / 256, 256, 0, stream>>>(vtx_counts, idx_counts, status, n,
                                                               vertex_offset, max_index, failed);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -193,6 +201,96 @@ __global__ void read_totals_kernel(const uint64_t* a_total, const uint64_t* b_to
 cudaError_t launch_read_totals(const uint64_t* a_total, const uint64_t* b_total,
                                const uint32_t* words, uint64_t* host_dst, cudaStream_t s) {
     read_totals_kernel<<<1, 1, 0, s>>>(a_total, b_total, words, host_dst);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+// Class of a path for the processing order: 0 = more than `big_points` points (when big_points
+// > 0), 2 + short_points - points for a line-only path of at most `short_points` points (when
+// short_points > 0; fewer points, later), 1 = any other path.
+__device__ __forceinline__ uint32_t path_class_of(const uint8_t* verbs, const uint32_t* verb_offsets,
+                                                  const uint32_t* point_offsets, uint32_t i,
+                                                  uint32_t big_points, uint32_t short_points) {
+    const uint32_t pts = point_offsets[i + 1] - point_offsets[i];
+    if (big_points && pts > big_points) return 0;
+    if (short_points && pts <= short_points) {
+        bool lines = true;
+        for (uint32_t v = verb_offsets[i]; v < verb_offsets[i + 1] && lines; ++v) {
+            const uint8_t k = verbs[v];
+            lines = k == LYON_VERB_BEGIN || k == LYON_VERB_LINE_TO || k == LYON_VERB_CLOSE ||
+                    k == LYON_VERB_END;
+        }
+        if (lines) return 2 + short_points - pts;
+    }
+    return 1;
+}
+
+constexpr uint32_t CLASSIFY_THREADS = 256;
+
+__global__ void classify_count_kernel(const uint8_t* verbs, const uint32_t* verb_offsets,
+                                      const uint32_t* point_offsets, uint32_t n,
+                                      uint32_t big_points, uint32_t short_points,
+                                      uint8_t* path_class, uint32_t* counters) {
+    __shared__ uint32_t hist[CLASSIFY_MAX_BINS];
+    const uint32_t nb = 3 + short_points;
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const uint32_t c = path_class_of(verbs, verb_offsets, point_offsets, i, big_points,
+                                         short_points);
+        path_class[i] = (uint8_t)c;
+        atomicAdd(&hist[c], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x)
+        if (hist[b]) atomicAdd(&counters[b], hist[b]);
+}
+
+__global__ void classify_place_kernel(const uint8_t* path_class, uint32_t n,
+                                      uint32_t short_points, uint32_t* order,
+                                      uint32_t* counters) {
+    __shared__ uint32_t start[CLASSIFY_MAX_BINS];
+    __shared__ uint32_t local[CLASSIFY_MAX_BINS];
+    const uint32_t nb = 3 + short_points;
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (uint32_t b = 0; b < nb; ++b) {
+            start[b] = acc;
+            acc += counters[b];
+        }
+        if (blockIdx.x == 0) counters[2 * nb] = start[2];
+    }
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) local[b] = 0;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t c = 0, rank = 0;
+    if (i < n) {
+        c = path_class[i];
+        rank = atomicAdd(&local[c], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x)
+        if (local[b]) local[b] = atomicAdd(&counters[nb + b], local[b]);
+    __syncthreads();
+    if (i < n) order[start[c] + local[c] + rank] = i;
+}
+
+cudaError_t launch_classify_paths(const uint8_t* verbs, const uint32_t* verb_offsets,
+                                  const uint32_t* point_offsets, uint32_t n, uint32_t big_points,
+                                  uint32_t short_points, uint8_t* path_class, uint32_t* order,
+                                  uint32_t* counters, cudaStream_t s) {
+    if (short_points > CLASSIFY_MAX_SHORT_POINTS) return cudaErrorInvalidValue;
+    const uint32_t nb = 3 + short_points;
+    cudaMemsetAsync(counters, 0, (2 * nb + 1) * sizeof(uint32_t), s);
+    if (n == 0) return cudaGetLastError();
+    const uint32_t blocks = (n + CLASSIFY_THREADS - 1) / CLASSIFY_THREADS;
+    classify_count_kernel<<<blocks, CLASSIFY_THREADS, 0, s>>>(
+        verbs, verb_offsets, point_offsets, n, big_points, short_points, path_class, counters);
+    note_launches(1);
+    classify_place_kernel<<<blocks, CLASSIFY_THREADS, 0, s>>>(path_class, n, short_points, order,
+                                                             counters);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -228,12 +326,14 @@ cudaError_t launch_big_first_order(const uint32_t* point_offsets, uint32_t n, ui
     cudaMemsetAsync(counters, 0, 8, s);
     big_first_order_kernel<<<(n + 255) / 256, 256, 0, s>>>(point_offsets, n, big_points, order,
                                                            counters);
+    note_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     narrow_u64_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, out, n);
+    note_launches(1);
     return cudaGetLastError();
 }
 

@@ -1063,6 +1063,120 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
     }
 }
 
+// One thread strokes one short line-only path: lyon's sequential step (seq_step, the
+// fixed_width_step_impl of stroke.rs:1521-1632) over its points, then the sub-path tail through
+// run_tail, as the warp walk does. Verbs are checked per window of up to WINDOW verbs ending at
+// an End/Close (a Begin inside it, or points missing for it, fail the path before any of its
+// steps), so that a path fails with the status the warp walk gives it.
+template <bool EMIT>
+__device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path) {
+    const PathOut po = path_out<EMIT>(A, path);
+    const uint32_t v_begin = A.verb_offsets[path], v_end = A.verb_offsets[path + 1];
+    const uint32_t p_end = A.point_offsets[path + 1];
+    const StrokeParams P = make_params(A.options[A.num_options > 1 ? path : 0]);
+    Sink s;
+    s.id_base = po.id_base;
+    s.nv = 0;
+    s.ni = 0;
+    s.vout = po.vout;
+    s.iout = po.iout;
+    s.index_bits = po.bits;
+    s.vcap = po.vmax;
+    s.icap = po.imax;
+    s.overflow = false;
+    int status = LYON_OK;
+    uint32_t vi = v_begin, pc = A.point_offsets[path];
+    while (vi < v_end && status == LYON_OK) {
+        if (A.verbs[vi] != LYON_VERB_BEGIN) {
+            status = LYON_ERR_INVALID_ARGUMENT;
+            break;
+        }
+        SeqBuffer pb;
+        pb.start = 0;
+        pb.count = 0;
+        pb.n = 0;
+        TailJob job;
+        job.path = path;
+        job.base1 = job.jbase = 0;
+        job.p0 = job.p1 = job.p2 = job.c3 = job.c2 = job.c1 = V2{0.0f, 0.0f};
+        bool mnec = false, ended = false, closed = false;
+        while (vi < v_end && status == LYON_OK) {
+            uint32_t nv = 0, need = 0;
+            int last_kind = LYON_VERB_END;
+            while (nv < WINDOW && vi + nv < v_end) {
+                const int k = A.verbs[vi + nv];
+                ++nv;
+                last_kind = k;
+                if (nv > 1 && k == LYON_VERB_BEGIN) {
+                    status = LYON_ERR_INVALID_ARGUMENT;
+                    break;
+                }
+                need += points_of_verb(k);
+                if (k == LYON_VERB_END || k == LYON_VERB_CLOSE) break;
+            }
+            if (status != LYON_OK || pc + need > p_end) {
+                status = LYON_ERR_INVALID_ARGUMENT;
+                break;
+            }
+            for (uint32_t j = 0; j < nv; ++j) {
+                const int k = A.verbs[vi + j];
+                if (k == LYON_VERB_CLOSE) ++pc;
+                if (k != LYON_VERB_BEGIN && k != LYON_VERB_LINE_TO) continue;
+                const V2 p = load_pt(A.points, pc++);
+                DEP d;
+                dep_init(d, p, P.hw, P.line_join, false);
+                const uint32_t base = s.id_base + s.nv;
+                if (!seq_step(pb, d, P, s, &mnec, &status)) continue;
+                job.c3 = job.c2;
+                job.c2 = job.c1;
+                job.c1 = p;
+                if (pb.n == 1) {
+                    job.p0 = p;
+                } else if (pb.n == 2) {
+                    job.p1 = p;
+                } else {
+                    if (pb.n == 3) {
+                        job.p2 = p;
+                        job.base1 = base;
+                    }
+                    job.jbase = base;
+                }
+            }
+            vi += nv;
+            if (last_kind == LYON_VERB_END || last_kind == LYON_VERB_CLOSE) {
+                ended = true;
+                closed = last_kind == LYON_VERB_CLOSE;
+                break;
+            }
+        }
+        if (!ended || status != LYON_OK) break;
+        job.n = pb.n;
+        job.flags = (closed ? TJ_CLOSED : 0u) | (mnec ? TJ_MNEC : 0u);
+        int tst = LYON_OK;
+        run_tail(job, P, s, &tst);
+        if (tst != LYON_OK) status = tst;
+    }
+    if (s.overflow && status == LYON_OK) status = LYON_ERR_INTERNAL;
+    finish_path<EMIT>(A, path, s.nv, s.ni, status, po);
+}
+
+// The short line-only paths (items [split, num_paths) of the order): 32 per warp, one per lane.
+template <bool EMIT>
+__device__ __noinline__ void stroke_short_paths(const StrokeArgs& A, uint32_t split, int lane) {
+    for (;;) {
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(A.seq_counter, 32u);
+        first = __shfl_sync(FULL, first, 0);
+        if (first >= A.num_paths - split) break;
+        const uint32_t item = split + first + (uint32_t)lane;
+        if (item < A.num_paths) {
+            const uint32_t path = A.order[item];
+            if (!EMIT || A.status[path] == LYON_OK) stroke_path_seq<EMIT>(A, path);
+        }
+        __syncwarp();
+    }
+}
+
 template <bool EMIT>
 __global__ void __launch_bounds__(STROKE_WARPS * 32, LG_STROKE_MIN_BLOCKS)
     stroke_kernel(StrokeArgs A) {
@@ -1072,11 +1186,12 @@ __global__ void __launch_bounds__(STROKE_WARPS * 32, LG_STROKE_MIN_BLOCKS)
     const int w = threadIdx.x >> 5;
     WarpSmem& sm = smem[w];
     uint32_t tqn = 0;  // queued tails
+    const uint32_t split = A.item_split ? min(*A.item_split, A.num_paths) : A.num_paths;
     for (;;) {
         uint32_t item = 0;
         if (lane == 0) item = atomicAdd(A.work_counter, 1u);
         item = __shfl_sync(FULL, item, 0);
-        if (item >= A.num_paths) break;
+        if (item >= split) break;
         const uint32_t path = A.order ? A.order[item] : item;
         if (EMIT && A.status[path] != LYON_OK) continue;
         const PathOut po = path_out<EMIT>(A, path);
@@ -1088,6 +1203,7 @@ __global__ void __launch_bounds__(STROKE_WARPS * 32, LG_STROKE_MIN_BLOCKS)
         __syncwarp();
     }
     if (tqn > 0) flush_tails<EMIT>(sm, lane, tqn, A);
+    if (split < A.num_paths) stroke_short_paths<EMIT>(A, split, lane);
 }
 
 constexpr size_t STROKE_SMEM = sizeof(WarpSmem) * STROKE_WARPS;
@@ -1121,8 +1237,10 @@ cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStrea
     configure_smem();
     if (emit) {
         stroke_kernel<true><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
+        note_launches(1);
     } else {
         stroke_kernel<false><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
+        note_launches(1);
     }
     return cudaGetLastError();
 }

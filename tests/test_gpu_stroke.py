@@ -261,19 +261,19 @@ def test_autotuner_picks_a_setting_and_keeps_outputs(gpu):
     od = T.upload_options(opts, 0)
     cb = db.c()
     best = _native.CStrokeTuning()
-    times = (ctypes.c_float * 8)()
+    times = (ctypes.c_float * 16)()
     nc = ctypes.c_uint32()
     saved = _native.CStrokeTuning()
     assert c.lib.lyon_gpu_get_stroke_tuning(c.h, ctypes.byref(saved)) == 0
     try:
         r = c.lib.lyon_gpu_autotune_stroke(c.h, ctypes.byref(cb), od.data_ptr(), len(opts), 2000,
                                            ctypes.byref(best), times, ctypes.byref(nc))
-        assert r == 0 and nc.value == 8
+        assert r == 0 and nc.value == 16
         assert all(t > 0.0 for t in times)
         cur = _native.CStrokeTuning()
         c.lib.lyon_gpu_get_stroke_tuning(c.h, ctypes.byref(cur))
-        assert (cur.long_path_points, cur.blocks_per_sm) == (best.long_path_points,
-                                                             best.blocks_per_sm)
+        assert (cur.long_path_points, cur.blocks_per_sm, cur.short_path_points) == (
+            best.long_path_points, best.blocks_per_sm, best.short_path_points)
         after = gpu.gpu_batch("stroke", batch, opts, index_bits=32)
         assert np.array_equal(after["indices"], before["indices"])
         assert np.array_equal(after["vertices"], before["vertices"])

@@ -150,6 +150,26 @@ int lyon_gpu_stroke_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t n
                          const lyon_stroke_options* options, int index_bits, uint32_t index_base,
                          lyon_gpu_result* result);
 
+/* One stroke output vertex with the attributes lyon's StrokeVertex hands a vertex constructor
+ * (crates/tessellation/src/stroke.rs:2667-2720): position(), normal() (the length that inflates
+ * the stroke by 1 on each side, not a unit vector at miters), advancement() (distance along the
+ * path, carried from one sub-path to the next as lyon does) and side() (0 = Side::Positive,
+ * 1 = Side::Negative, crates/path/src/lib.rs:224-227). 24 bytes. */
+typedef struct lyon_stroke_vertex {
+    float x, y;
+    float normal_x, normal_y;
+    float advancement;
+    uint32_t side;
+} lyon_stroke_vertex;
+
+/* lyon_gpu_stroke_path with a BuffersBuilder whose vertex constructor reads the StrokeVertex
+ * attributes: `result->vertices` points at `num_vertices` lyon_stroke_vertex records (cast the
+ * pointer). Indices, statuses and positions are those of lyon_gpu_stroke_path. */
+int lyon_gpu_stroke_path_attributes(lyon_gpu_context* ctx, const uint8_t* verbs,
+                                    uint32_t num_verbs, const float* points, uint32_t num_points,
+                                    const lyon_stroke_options* options, int index_bits,
+                                    uint32_t index_base, lyon_gpu_result* result);
+
 /* FillTessellator::tessellate_path(path, options, &mut BuffersBuilder)
  * (crates/tessellation/src/fill.rs:628-641), `Positions` vertices. Same conventions as above. */
 int lyon_gpu_fill_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
@@ -186,6 +206,14 @@ int lyon_gpu_stroke_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                           const lyon_stroke_options* options, uint32_t num_options,
                           int index_bits, int index_mode, uint32_t vertex_offset,
                           lyon_gpu_batch_output* out);
+
+/* lyon_gpu_stroke_paths with lyon_stroke_vertex records (position, normal, advancement, side):
+ * `out->vertices` points at `total_vertices` records in device memory (cast the pointer); the
+ * rest of `out` is as for lyon_gpu_stroke_paths. */
+int lyon_gpu_stroke_paths_attributes(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                                     const lyon_stroke_options* options, uint32_t num_options,
+                                     int index_bits, int index_mode, uint32_t vertex_offset,
+                                     lyon_gpu_batch_output* out);
 
 /* Largest batch lyon_gpu_stroke_paths_noalloc accepts (its fixed scratch holds this many paths). */
 #define LYON_NOALLOC_MAX_PATHS 262144u

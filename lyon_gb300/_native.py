@@ -104,12 +104,14 @@ def load(build_if_missing: bool = True):
         L.lyon_gpu_last_error.argtypes = [c_p]
         L.lyon_gpu_synchronize.restype = ctypes.c_int
         L.lyon_gpu_synchronize.argtypes = [c_p]
-        for name in ("lyon_gpu_stroke_path", "lyon_gpu_fill_path"):
+        for name in ("lyon_gpu_stroke_path", "lyon_gpu_fill_path",
+                     "lyon_gpu_stroke_path_attributes"):
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [c_p, c_p, u32, c_p, u32, c_p, ctypes.c_int, u32,
                           ctypes.POINTER(CResult)]
-        for name in ("lyon_gpu_stroke_paths", "lyon_gpu_fill_paths"):
+        for name in ("lyon_gpu_stroke_paths", "lyon_gpu_fill_paths",
+                     "lyon_gpu_stroke_paths_attributes"):
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, ctypes.c_int, ctypes.c_int,
@@ -173,4 +175,5 @@ EXPORTED = [
     "lyon_srv_create", "lyon_srv_destroy", "lyon_srv_submit", "lyon_srv_poll", "lyon_srv_wait",
     "lyon_srv_release", "lyon_srv_run_load", "lyon_gpu_set_stroke_tuning",
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
+    "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",
 ]

@@ -50,6 +50,7 @@ struct lyon_gpu_context {
     uint32_t long_path_points = 1024;  // paths with more points go first; 0: path order
     uint32_t blocks_per_sm = 0;        // 0: as many as fit
     uint32_t short_path_points = 32;   // line-only paths up to this size: one per thread
+    bool vertex_attrs = false;  // during a *_attributes call: lyon_stroke_vertex records
     // outputs of device-buffer batched calls
     DevBuf out_vertices, out_indices;
     // host-buffer calls: inputs and double-buffered outputs
@@ -294,6 +295,7 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
     a.index_bits = index_bits;
     a.index_mode = index_mode;
     a.vertex_offset = (uint32_t)vertex_offset;
+    a.vertex_attrs = ctx->vertex_attrs ? 1 : 0;
     a.request_first = ctx->request_first;
     if (ctx->split_valid) {
         a.item_split = as<uint32_t>(ctx->class_counters) + 2 * (3 + ctx->short_path_points);
@@ -412,7 +414,8 @@ int batched_device(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     int r = pipeline_count(ctx, kind, batch, options, num_options, index_bits, index_mode,
                            vertex_offset, &tv, &ti, &failed);
     if (r != LYON_OK) return r;
-    if (!ensure(ctx, ctx->out_vertices, tv * 8 + 16) ||
+    const size_t vbytes = ctx->vertex_attrs ? sizeof(lyon_stroke_vertex) : 8;
+    if (!ensure(ctx, ctx->out_vertices, tv * vbytes + 16) ||
         !ensure(ctx, ctx->out_indices, ti * (index_bits / 8) + 16))
         return LYON_ERR_OUT_OF_MEMORY;
     r = pipeline_emit(ctx, kind, batch, options, num_options, index_bits, index_mode,
@@ -452,8 +455,12 @@ int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, con
     bool capacity_ok = true;
     int slot = 0;
     uint32_t c0 = 0;
+    // The first chunk's kernels run before any copy can start, so chunks start small and double
+    // up to CH: the copy stream, which bounds the call, starts sooner.
+    uint32_t ch = CH < 16384u ? CH : 16384u;
     while (c0 < n || (n == 0 && c0 == 0)) {
-        uint32_t c1 = c0 + CH < n ? c0 + CH : n;
+        uint32_t c1 = c0 + ch < n ? c0 + ch : n;
+        ch = ch < CH / 2 ? ch * 2 : CH;
         while (c1 > c0 + 1 &&
                (uint64_t)(hb->point_offsets[c1] - hb->point_offsets[c0]) * 8 > (64ull << 20))
             c1 = c0 + (c1 - c0) / 2;
@@ -603,7 +610,8 @@ int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t 
     if (r != LYON_OK) return r;
     cudaStream_t s = ctx->stream;
     if (!ensure_host(ctx, ctx->h_small, 64)) return LYON_ERR_OUT_OF_MEMORY;
-    size_t vb = bo.total_vertices * 8, ib = bo.total_indices * (index_bits / 8);
+    size_t vb = bo.total_vertices * (ctx->vertex_attrs ? sizeof(lyon_stroke_vertex) : 8);
+    size_t ib = bo.total_indices * (index_bits / 8);
     if (!ensure_host(ctx, ctx->h_out_v, vb + 16) || !ensure_host(ctx, ctx->h_out_i, ib + 16))
         return LYON_ERR_OUT_OF_MEMORY;
     cudaMemcpyAsync(ctx->h_small.ptr, bo.status, 4, cudaMemcpyDeviceToHost, s);
@@ -828,6 +836,18 @@ int lyon_gpu_stroke_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                           vertex_offset, out);
 }
 
+int lyon_gpu_stroke_paths_attributes(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                                     const lyon_stroke_options* options, uint32_t num_options,
+                                     int index_bits, int index_mode, uint32_t vertex_offset,
+                                     lyon_gpu_batch_output* out) {
+    if (!ctx) return LYON_ERR_INVALID_ARGUMENT;
+    ctx->vertex_attrs = true;
+    int r = batched_device(ctx, KIND_STROKE, batch, options, num_options, index_bits, index_mode,
+                           vertex_offset, out);
+    ctx->vertex_attrs = false;
+    return r;
+}
+
 int lyon_gpu_fill_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                         const lyon_fill_options* options, uint32_t num_options, int index_bits,
                         int index_mode, uint32_t vertex_offset, lyon_gpu_batch_output* out) {
@@ -864,6 +884,18 @@ int lyon_gpu_stroke_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t n
                          lyon_gpu_result* result) {
     return single_path(ctx, KIND_STROKE, verbs, num_verbs, points, num_points, options,
                        sizeof(lyon_stroke_options), index_bits, index_base, result);
+}
+
+int lyon_gpu_stroke_path_attributes(lyon_gpu_context* ctx, const uint8_t* verbs,
+                                    uint32_t num_verbs, const float* points, uint32_t num_points,
+                                    const lyon_stroke_options* options, int index_bits,
+                                    uint32_t index_base, lyon_gpu_result* result) {
+    if (!ctx) return LYON_ERR_INVALID_ARGUMENT;
+    ctx->vertex_attrs = true;
+    int r = single_path(ctx, KIND_STROKE, verbs, num_verbs, points, num_points, options,
+                        sizeof(lyon_stroke_options), index_bits, index_base, result);
+    ctx->vertex_attrs = false;
+    return r;
 }
 
 int lyon_gpu_fill_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,

@@ -34,6 +34,9 @@ struct StrokeArgs {
     int index_bits;
     int index_mode;
     uint32_t vertex_offset;
+    // Non-zero: `vertices` receives lyon_stroke_vertex records (position, normal, advancement,
+    // side) instead of positions.
+    int vertex_attrs;
     // Optional, per path: the first path of the request it belongs to. In LYON_INDEX_GLOBAL mode
     // ids then count from that path's first vertex (one VertexBuffers per request of a batch).
     const uint32_t* request_first;

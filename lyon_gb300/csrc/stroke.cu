@@ -77,6 +77,7 @@ constexpr uint32_t SPEC_VALID = 1u, SPEC_SYM = 2u;
 // Output of a join computed ahead, written at the end of the window.
 struct EmitJob {
     uint32_t slot, vo, io, base, pfn, pfp, has_edge;
+    float adv;  // the join's advancement (attribute output)
 };
 
 // Everything the tail of a sub-path needs (stroke.rs:1179-1378): the first three and the last
@@ -84,6 +85,7 @@ struct EmitJob {
 struct TailJob {
     uint32_t path, n, flags, base1, jbase, vcur, icur;
     V2 p0, p1, p2, c3, c2, c1;
+    float adv0, adv2, adv1;  // advancements of p0, c2 and c1 (read by the attribute output only)
 };
 enum : uint32_t {
     TJ_CLOSED = 1u, TJ_MNEC = 2u, TJ_FLAT1 = 4u, TJ_FAST1 = 8u, TJ_SKIP1 = 16u, TJ_F1 = 32u,
@@ -119,7 +121,8 @@ __device__ __forceinline__ bool same_bits(V2 a, V2 b) {
 
 struct PathOut {
     uint32_t id_base;  // id of the path's first vertex
-    float2* vout;      // null when counting
+    float2* vout;      // positions; null when counting or writing attribute records
+    lyon_stroke_vertex* rout;  // attribute records (the attribute output), else null
     void* iout;
     int bits;
     uint32_t vmax, imax;  // the path's counts from the count pass (write bounds when emitting)
@@ -129,14 +132,15 @@ __device__ __forceinline__ uint32_t cap_left(uint32_t total, uint32_t used) {
     return used < total ? total - used : 0u;
 }
 
-template <bool EMIT>
+template <bool EMIT, bool ATTR>
 __device__ __forceinline__ PathOut path_out(const StrokeArgs& A, uint32_t path) {
     PathOut po;
     po.bits = A.index_bits;
     if (EMIT) {
         const uint64_t vo = A.vtx_offsets[path];
         const uint64_t io = A.idx_offsets[path];
-        po.vout = reinterpret_cast<float2*>(A.vertices) + vo;
+        po.vout = ATTR ? nullptr : reinterpret_cast<float2*>(A.vertices) + vo;
+        po.rout = ATTR ? reinterpret_cast<lyon_stroke_vertex*>(A.vertices) + vo : nullptr;
         po.iout = A.index_bits == 16 ? (void*)((uint16_t*)A.indices + io)
                                      : (void*)((uint32_t*)A.indices + io);
         const uint64_t rb = A.request_first ? A.vtx_offsets[A.request_first[path]] : 0ull;
@@ -146,6 +150,7 @@ __device__ __forceinline__ PathOut path_out(const StrokeArgs& A, uint32_t path) 
         po.imax = A.idx_counts[path];
     } else {
         po.vout = nullptr;
+        po.rout = nullptr;
         po.iout = nullptr;
         po.id_base = 0;
         po.vmax = 0xFFFFFFFFu;
@@ -197,6 +202,8 @@ struct SubState {
     bool flat1, fast1, skip1;
     uint32_t base1;
     TCarry tc;
+    // Advancements (attribute output only): of the first point, of c1 and of c2.
+    float adv0, adv1, adv2;
 };
 
 __device__ __forceinline__ uint32_t points_of_verb(int kind) {
@@ -350,6 +357,7 @@ __device__ __noinline__ void speculate_joins(WarpSmem& sm, int lane, uint32_t nv
 }
 
 // Writes the output of the joins computed ahead (one per lane). Returns the worst status.
+template <bool ATTR>
 __device__ __noinline__ int emit_spec_joins(WarpSmem& sm, int lane, uint32_t count,
                                             const StrokeParams& P, const PathOut& po) {
     int worst = LYON_OK;
@@ -360,11 +368,13 @@ __device__ __noinline__ int emit_spec_joins(WarpSmem& sm, int lane, uint32_t cou
         SlowJoin sj;
         int st = LYON_OK;
         slow_join_geometry(&d, sp.prev, sp.cur, false, sp.next, P, &sj, &st);
-        Sink s;
+        SinkT<ATTR> s;
         s.id_base = job.base;
         s.nv = 0;
         s.ni = 0;
-        s.vout = po.vout + job.vo;
+        s.vout = po.vout ? po.vout + job.vo : nullptr;
+        s.rout = po.rout ? po.rout + job.vo : nullptr;
+        s.adv = job.adv;
         s.index_bits = po.bits;
         s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + job.io)
                                : (void*)((uint32_t*)po.iout + job.io);
@@ -417,13 +427,15 @@ __device__ __noinline__ void fast_join_sides(V2 prev, V2 cur, V2 nxt, float hw, 
 // The tail of a sub-path: stroke.rs:1179-1279 (end, close) and 1322-1378 (end_with_caps), from
 // lyon's firsts (the first kept point with its sides, the first join) and the last join, which
 // are rebuilt here from the recorded points. Writes through `s` (positioned at the tail).
-__device__ __noinline__ void run_tail(const TailJob& j, const StrokeParams& P, Sink& s,
+template <class SK>
+__device__ __noinline__ void run_tail(const TailJob& j, const StrokeParams& P, SK& s,
                                       int* status) {
     const uint32_t n = j.n;
     const bool close = (j.flags & TJ_CLOSED) != 0;
     bool may_need_empty_cap = (j.flags & TJ_MNEC) != 0;
     DEP first0, first1, last;
     dep_init(first0, j.p0, P.hw, P.line_join, false);
+    first0.adv = j.adv0;
     if (n >= 2) first_point_sides(first0, j.p1, P.hw);
     if (n >= 3) {
         join_dep_with_ids(&first1, j.p0, j.p1, j.p2, (j.flags & TJ_FLAT1) != 0,
@@ -432,6 +444,7 @@ __device__ __noinline__ void run_tail(const TailJob& j, const StrokeParams& P, S
         join_dep_with_ids(&last, j.c3, j.c2, j.c1, (j.flags & TJ_F2) != 0,
                           (j.flags & TJ_JFAST) != 0, (j.flags & TJ_JSKIP) != 0, j.jbase, P,
                           status);
+        last.adv = j.adv2;
     }
     const V2 lastp = j.c1;
     const bool lastflat = (j.flags & TJ_F1) != 0;
@@ -440,27 +453,36 @@ __device__ __noinline__ void run_tail(const TailJob& j, const StrokeParams& P, S
         SeqBuffer pb;
         pb.pts[0] = last;
         dep_init(pb.pts[1], lastp, P.hw, P.line_join, lastflat);
+        // The last point's advancement is known to lyon here only when the join before it was
+        // a flattening step (stroke.rs:1765-1769); otherwise it is computed again from the
+        // point's position, which the merge below may have moved (stroke.rs:1225-1236).
+        if (j.flags & TJ_JFAST) pb.pts[1].adv = j.adv1;
         pb.start = 0;
         pb.count = 2;
         pb.n = n;
         bool mnec = false;
+        // close (stroke.rs:1206-1279): the first point is stepped again with its advancement
+        // recomputed; the two vertices re-made for the first edge keep the starting one.
         DEP p = first0;
+        p.adv = __int_as_float(0x7fc00000);
         bool added = seq_step(pb, p, P, s, &mnec, status);
         if (!added) pb.last().pos = p.pos;
         DEP p2 = first1;
         seq_step(pb, p2, P, s, &mnec, status);
         DEP& p0 = pb.second_last();
         DEP& p1 = pb.last();
+        s.adv = j.adv0;
         for (int side = 0; side < 2; ++side) {
             V2 sp = p0.s[side].has_single ? p0.s[side].single : p0.s[side].next;
             V2 normal = (sp - p0.pos) / p0.hw;
-            p0.s[side].next_vertex = s.vertex(p0.pos + normal * p0.hw);
+            p0.s[side].next_vertex = s.vertex(p0.pos + normal * p0.hw, normal, side);
         }
         add_edge_triangles(p0, p1, s);
         return;
     }
     if (may_need_empty_cap && n == 1) {
         V2 pos = first0.pos;
+        s.adv = first0.adv;
         if (P.start_cap == LYON_CAP_SQUARE) {
             tessellate_empty_square_cap(pos, P.hw, s);
         } else if (P.start_cap == LYON_CAP_ROUND) {
@@ -472,6 +494,7 @@ __device__ __noinline__ void run_tail(const TailJob& j, const StrokeParams& P, S
         DEP p0 = (n == 2) ? first0 : last;
         DEP p1;
         dep_init(p1, lastp, P.hw, P.line_join, lastflat);
+        p1.adv = j.adv1;
         V2 tan = normalize(p1.pos - p0.pos);
         V2 nn = V2{-tan.y, tan.x} * p1.hw;
         p1.s[SP].prev = p1.pos + nn;
@@ -486,16 +509,18 @@ __device__ __noinline__ void run_tail(const TailJob& j, const StrokeParams& P, S
 }
 
 // Runs a tail at the output position (vcur, icur) of its path. Returns the counts it added.
+template <bool ATTR>
 __device__ __forceinline__ void tail_at(const TailJob& j, const StrokeParams& P,
                                         const PathOut& po, uint32_t* tv, uint32_t* ti,
                                         int* st) {
-    Sink s;
+    SinkT<ATTR> s;
     s.id_base = po.id_base + j.vcur;
     s.nv = 0;
     s.ni = 0;
     s.vout = po.vout ? po.vout + j.vcur : nullptr;
+    s.rout = po.rout ? po.rout + j.vcur : nullptr;
     s.iout = nullptr;
-    if (po.vout) {
+    if (po.vout || po.rout) {
         s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + j.icur)
                                : (void*)((uint32_t*)po.iout + j.icur);
     }
@@ -512,17 +537,17 @@ __device__ __forceinline__ void tail_at(const TailJob& j, const StrokeParams& P,
 }
 
 // Processes the warp's queued tails, one per lane, and finishes their paths.
-template <bool EMIT>
+template <bool EMIT, bool ATTR>
 __device__ __noinline__ void flush_tails(WarpSmem& sm, int lane, uint32_t count,
                                          const StrokeArgs& A) {
     if ((uint32_t)lane < count) {
         const TailJob j = sm.tq[lane];
         const lyon_stroke_options opt = A.options[A.num_options > 1 ? j.path : 0];
         const StrokeParams P = make_params(opt);
-        const PathOut po = path_out<EMIT>(A, j.path);
+        const PathOut po = path_out<EMIT, ATTR>(A, j.path);
         uint32_t tv, ti;
         int st;
-        tail_at(j, P, po, &tv, &ti, &st);
+        tail_at<ATTR>(j, P, po, &tv, &ti, &st);
         finish_path<EMIT>(A, j.path, j.vcur + tv, j.icur + ti, st, po);
     }
     __syncwarp();
@@ -530,7 +555,7 @@ __device__ __noinline__ void flush_tails(WarpSmem& sm, int lane, uint32_t count,
 
 // Steps [cb, cb + 32) of the current verb window (lane = step): flattened points, merge filter,
 // joins, output. See the file comment. `ejn` counts the joins queued for emission.
-template <bool EMIT>
+template <bool EMIT, bool ATTR>
 __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, const uint32_t vi,
                                               const uint32_t nv, const uint32_t sincl,
                                               const uint32_t S_w, const uint32_t cb,
@@ -653,7 +678,24 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
     // Tangent of the edge cur -> q. The count pass needs tangents only at a sub-path's first
     // point and when it evaluates the skip test exactly (below), so it computes them there.
     V2 nt = V2{0.0f, 0.0f};
-    if (EMIT || (live && k == 0)) nt = ne / vlength(ne);
+    float len_ne = 0.0f;
+    if (EMIT || (live && k == 0)) {
+        len_ne = vlength(ne);
+        nt = ne / len_ne;
+    }
+    // Advancement of each kept point (attribute output): lyon adds the edge lengths one after
+    // the other in f32 (stroke.rs:1546-1550, 1657-1662, 1759-1771), so the sum runs through the
+    // lanes in order; a sub-path's first point starts from the carried advancement.
+    float adv_q = 0.0f, adv_join = 0.0f;
+    if (EMIT && ATTR) {
+        float carry = S.adv1;
+        for (int i = 0; i < (int)nk; ++i) {
+            if (lane == i) adv_q = k < 0 ? S.adv0 : carry + len_ne;
+            carry = __shfl_sync(FULL, adv_q, i);
+        }
+        adv_join = __shfl_up_sync(FULL, adv_q, 1);
+        if (lane == 0) adv_join = S.adv1;
+    }
     const V2 pe = cur - prv;
     const bool isjoin = live && k >= 1;
     const bool fast = isjoin && fcur && dot(pe, ne) > 0.0f;
@@ -718,6 +760,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
     // joins' side points), so when every fast lane's edge is longer the test cannot fire;
     // otherwise the count pass evaluates it exactly as well.
     bool exact = EMIT;
+    V2 fast_nrm = V2{0.0f, 0.0f};
     if (!EMIT) {
         bool psym = __shfl_up_sync(FULL, (int)sym, 1) != 0;
         if (lane == 0) psym = S.jsym;
@@ -747,6 +790,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
             const V2 nrm = compute_normal(pt, nt);
             pn = cur + nrm * P.hw;
             nn = cur - nrm * P.hw;
+            fast_nrm = nrm;
             have_sides = true;
         }
         V2 ppn = shfl_up_v2(pn, 1), pnn = shfl_up_v2(nn, 1);
@@ -788,7 +832,20 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         const uint32_t vo = vcur + vrel;
         const uint32_t io = icur + irel;
         if (fast) {
-            if (!skip) {
+            if (ATTR && !skip) {
+                // flattened_step's two vertices, + then - (stroke.rs:1791-1797).
+                if (vo + 2 <= po.vmax) {
+                    float2* dst = reinterpret_cast<float2*>(po.rout + vo);
+                    dst[0] = make_float2(pn.x, pn.y);
+                    dst[1] = make_float2(fast_nrm.x, fast_nrm.y);
+                    dst[2] = make_float2(adv_join, __uint_as_float((uint32_t)SP));
+                    dst[3] = make_float2(nn.x, nn.y);
+                    dst[4] = make_float2(-fast_nrm.x, -fast_nrm.y);
+                    dst[5] = make_float2(adv_join, __uint_as_float((uint32_t)SN));
+                } else {
+                    st = LYON_ERR_INTERNAL;
+                }
+            } else if (!skip) {
                 if (vo + 2 <= po.vmax) {
                     float2* dst = po.vout + vo;
                     if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
@@ -854,14 +911,17 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
             job.pfn = pfn;
             job.pfp = pfp;
             job.has_edge = k >= 2 ? 1u : 0u;
+            job.adv = ATTR ? adv_join : 0.0f;
         }
         ejn += __popc(qmask);
         if (slow && !spec) {
-            Sink s;
+            SinkT<ATTR> s;
             s.id_base = base;
             s.nv = 0;
             s.ni = 0;
-            s.vout = po.vout + vo;
+            s.vout = po.vout ? po.vout + vo : nullptr;
+            s.rout = po.rout ? po.rout + vo : nullptr;
+            s.adv = adv_join;
             s.index_bits = po.bits;
             s.iout = po.bits == 16 ? (void*)((uint16_t*)po.iout + io)
                                    : (void*)((uint32_t*)po.iout + io);
@@ -897,6 +957,12 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         const bool fl1 = __shfl_sync(FULL, (int)flat, last) != 0;
         const V2 oc1 = S.c1, oc2 = S.c2;
         const bool of1 = S.f1;
+        if (EMIT && ATTR) {
+            const float a2 = __shfl_sync(FULL, adv_q, last >= 1 ? last - 1 : 0);
+            const float a1 = __shfl_sync(FULL, adv_q, last);
+            S.adv2 = nk >= 2 ? a2 : S.adv1;
+            S.adv1 = a1;
+        }
         S.c3 = nk >= 3 ? q3 : (nk == 2 ? oc1 : oc2);
         S.c2 = nk >= 2 ? q2 : oc1;
         S.f2 = nk >= 2 ? fl2 : of1;
@@ -927,7 +993,7 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
 
 // Strokes one path with the whole warp. On return vcur/icur/status hold the path's counts so
 // far; when the tail of its last sub-path was queued (`deferred`), the queue finishes the path.
-template <bool EMIT>
+template <bool EMIT, bool ATTR>
 __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_t path,
                             const PathOut& po, uint32_t& vcur, uint32_t& icur, int& status,
                             uint32_t& tqn, bool& deferred) {
@@ -941,6 +1007,7 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
     deferred = false;
     uint32_t vi = v_begin;
     uint32_t pc = p_begin;
+    float start_adv = 0.0f;  // sub_path_start_advancement (stroke.rs:585, 1359)
     while (vi < v_end && status == LYON_OK) {
         // A sub-path starts with Begin (crates/path/src/path.rs:843-909).
         if (A.verbs[vi] != LYON_VERB_BEGIN) {
@@ -968,6 +1035,8 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
         S.tc.unit = 0;
         S.tc.k = 0;
         S.tc.t = 0.0f;
+        S.adv0 = start_adv;
+        S.adv1 = S.adv2 = 0.0f;
         bool ended = false, closed = false;
         while (vi < v_end && status == LYON_OK) {
             // ---- verb window ----
@@ -1001,12 +1070,12 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             __syncwarp();
             uint32_t ejn = 0;
             for (uint32_t cb = 0; cb < S_w; cb += 32) {
-                process_chunk<EMIT>(sm, lane, vi, nv, sincl, S_w, cb, P, po, S, vcur, icur, ejn,
+                process_chunk<EMIT, ATTR>(sm, lane, vi, nv, sincl, S_w, cb, P, po, S, vcur, icur, ejn,
                                     status);
             }
             if (EMIT && ejn > 0) {
                 __syncwarp();
-                int est = emit_spec_joins(sm, lane, ejn, P, po);
+                int est = emit_spec_joins<ATTR>(sm, lane, ejn, P, po);
                 est = __reduce_max_sync(FULL, est);
                 if (est != LYON_OK && status == LYON_OK) status = est;
             }
@@ -1038,10 +1107,18 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
         job.c3 = S.c3;
         job.c2 = S.c2;
         job.c1 = S.c1;
+        job.adv0 = job.adv1 = job.adv2 = 0.0f;
+        if (ATTR) {
+            job.adv0 = S.adv0;
+            job.adv1 = S.adv1;
+            job.adv2 = S.adv2;
+            // end_with_caps carries the last advancement to the next sub-path (stroke.rs:1359).
+            if (S.n >= 2 && !(closed && S.n > 2)) start_adv = S.adv1;
+        }
         if (vi >= v_end) {
             // The path's last sub-path: queue its tail.
             if (tqn == TAILQ) {
-                flush_tails<EMIT>(sm, lane, tqn, A);
+                flush_tails<EMIT, ATTR>(sm, lane, tqn, A);
                 tqn = 0;
             }
             if (lane == 0) sm.tq[tqn] = job;
@@ -1052,7 +1129,7 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
         }
         uint32_t tv = 0, ti = 0;
         int tst = LYON_OK;
-        if (lane == 0) tail_at(job, P, po, &tv, &ti, &tst);
+        if (lane == 0) tail_at<ATTR>(job, P, po, &tv, &ti, &tst);
         tv = __shfl_sync(FULL, tv, 0);
         ti = __shfl_sync(FULL, ti, 0);
         tst = __shfl_sync(FULL, tst, 0);
@@ -1068,17 +1145,18 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
 // run_tail, as the warp walk does. Verbs are checked per window of up to WINDOW verbs ending at
 // an End/Close (a Begin inside it, or points missing for it, fail the path before any of its
 // steps), so that a path fails with the status the warp walk gives it.
-template <bool EMIT>
+template <bool EMIT, bool ATTR>
 __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path) {
-    const PathOut po = path_out<EMIT>(A, path);
+    const PathOut po = path_out<EMIT, ATTR>(A, path);
     const uint32_t v_begin = A.verb_offsets[path], v_end = A.verb_offsets[path + 1];
     const uint32_t p_end = A.point_offsets[path + 1];
     const StrokeParams P = make_params(A.options[A.num_options > 1 ? path : 0]);
-    Sink s;
+    SinkT<ATTR> s;
     s.id_base = po.id_base;
     s.nv = 0;
     s.ni = 0;
     s.vout = po.vout;
+    s.rout = po.rout;
     s.iout = po.iout;
     s.index_bits = po.bits;
     s.vcap = po.vmax;
@@ -1086,6 +1164,7 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
     s.overflow = false;
     int status = LYON_OK;
     uint32_t vi = v_begin, pc = A.point_offsets[path];
+    float start_adv = 0.0f;  // sub_path_start_advancement (stroke.rs:585, 1359)
     while (vi < v_end && status == LYON_OK) {
         if (A.verbs[vi] != LYON_VERB_BEGIN) {
             status = LYON_ERR_INVALID_ARGUMENT;
@@ -1125,6 +1204,7 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
                 const V2 p = load_pt(A.points, pc++);
                 DEP d;
                 dep_init(d, p, P.hw, P.line_join, false);
+                if (k == LYON_VERB_BEGIN) d.adv = start_adv;
                 const uint32_t base = s.id_base + s.nv;
                 if (!seq_step(pb, d, P, s, &mnec, &status)) continue;
                 job.c3 = job.c2;
@@ -1152,6 +1232,15 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
         if (!ended || status != LYON_OK) break;
         job.n = pb.n;
         job.flags = (closed ? TJ_CLOSED : 0u) | (mnec ? TJ_MNEC : 0u);
+        job.adv0 = start_adv;
+        job.adv1 = job.adv2 = start_adv;
+        if (ATTR && pb.n >= 2) {
+            const DEP& l = pb.last();
+            const DEP& sl = pb.second_last();
+            job.adv2 = sl.adv;
+            job.adv1 = isnan(l.adv) ? sl.adv + vlength(l.pos - sl.pos) : l.adv;
+            if (!(closed && pb.n > 2)) start_adv = job.adv1;
+        }
         int tst = LYON_OK;
         run_tail(job, P, s, &tst);
         if (tst != LYON_OK) status = tst;
@@ -1161,7 +1250,7 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
 }
 
 // The short line-only paths (items [split, num_paths) of the order): 32 per warp, one per lane.
-template <bool EMIT>
+template <bool EMIT, bool ATTR>
 __device__ __noinline__ void stroke_short_paths(const StrokeArgs& A, uint32_t split, int lane) {
     for (;;) {
         uint32_t first = 0;
@@ -1171,13 +1260,13 @@ __device__ __noinline__ void stroke_short_paths(const StrokeArgs& A, uint32_t sp
         const uint32_t item = split + first + (uint32_t)lane;
         if (item < A.num_paths) {
             const uint32_t path = A.order[item];
-            if (!EMIT || A.status[path] == LYON_OK) stroke_path_seq<EMIT>(A, path);
+            if (!EMIT || A.status[path] == LYON_OK) stroke_path_seq<EMIT, ATTR>(A, path);
         }
         __syncwarp();
     }
 }
 
-template <bool EMIT>
+template <bool EMIT, bool ATTR>
 __global__ void __launch_bounds__(STROKE_WARPS * 32, LG_STROKE_MIN_BLOCKS)
     stroke_kernel(StrokeArgs A) {
     extern __shared__ unsigned char smem_raw[];
@@ -1194,16 +1283,16 @@ __global__ void __launch_bounds__(STROKE_WARPS * 32, LG_STROKE_MIN_BLOCKS)
         if (item >= split) break;
         const uint32_t path = A.order ? A.order[item] : item;
         if (EMIT && A.status[path] != LYON_OK) continue;
-        const PathOut po = path_out<EMIT>(A, path);
+        const PathOut po = path_out<EMIT, ATTR>(A, path);
         uint32_t vc, ic;
         int st;
         bool deferred;
-        stroke_path<EMIT>(sm, lane, A, path, po, vc, ic, st, tqn, deferred);
+        stroke_path<EMIT, ATTR>(sm, lane, A, path, po, vc, ic, st, tqn, deferred);
         if (!deferred && lane == 0) finish_path<EMIT>(A, path, vc, ic, st, po);
         __syncwarp();
     }
-    if (tqn > 0) flush_tails<EMIT>(sm, lane, tqn, A);
-    if (split < A.num_paths) stroke_short_paths<EMIT>(A, split, lane);
+    if (tqn > 0) flush_tails<EMIT, ATTR>(sm, lane, tqn, A);
+    if (split < A.num_paths) stroke_short_paths<EMIT, ATTR>(A, split, lane);
 }
 
 constexpr size_t STROKE_SMEM = sizeof(WarpSmem) * STROKE_WARPS;
@@ -1217,10 +1306,12 @@ static void configure_smem() {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_CONFIGURED_DEVICES) return;
     if (smem_configured[dev]) return;
     if (STROKE_SMEM > 48 * 1024) {
-        cudaFuncSetAttribute(stroke_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)STROKE_SMEM);
-        cudaFuncSetAttribute(stroke_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)STROKE_SMEM);
+        cudaFuncSetAttribute(stroke_kernel<true, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STROKE_SMEM);
+        cudaFuncSetAttribute(stroke_kernel<true, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STROKE_SMEM);
+        cudaFuncSetAttribute(stroke_kernel<false, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STROKE_SMEM);
     }
     smem_configured[dev] = true;
 }
@@ -1228,20 +1319,23 @@ static void configure_smem() {
 int stroke_blocks_per_sm() {
     configure_smem();
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stroke_kernel<true>, STROKE_WARPS * 32,
-                                                  STROKE_SMEM);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stroke_kernel<true, false>,
+                                                  STROKE_WARPS * 32, STROKE_SMEM);
     return n > 0 ? n : 1;
 }
 
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream) {
     configure_smem();
-    if (emit) {
-        stroke_kernel<true><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
-        note_launches(1);
+    // The attribute output is its own instantiation, so the positions kernel carries none of
+    // its work (the advancement chain, the record stores).
+    if (emit && args.vertex_attrs) {
+        stroke_kernel<true, true><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
+    } else if (emit) {
+        stroke_kernel<true, false><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
     } else {
-        stroke_kernel<false><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
-        note_launches(1);
+        stroke_kernel<false, false><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
     }
+    note_launches(1);
     return cudaGetLastError();
 }
 

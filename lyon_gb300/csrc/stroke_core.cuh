@@ -25,9 +25,10 @@ struct SidePts {  // stroke.rs:300-307
     bool has_single;
 };
 
-struct DEP {  // EndpointData, stroke.rs:309-342 (advancement is not tracked: no output uses it)
+struct DEP {  // EndpointData, stroke.rs:309-342
     V2 pos;
     float hw;
+    float adv;  // advancement: NaN until computed (only the vertex attribute output reads it)
     int join;
     bool is_flat;
     bool fold[2];
@@ -37,6 +38,7 @@ struct DEP {  // EndpointData, stroke.rs:309-342 (advancement is not tracked: no
 __device__ __forceinline__ void dep_init(DEP& d, V2 pos, float hw, int join, bool flat) {
     d.pos = pos;
     d.hw = hw;
+    d.adv = __int_as_float(0x7fc00000);
     d.join = join;
     d.is_flat = flat;
     d.fold[0] = d.fold[1] = false;
@@ -51,11 +53,16 @@ __device__ __forceinline__ void dep_init(DEP& d, V2 pos, float hw, int join, boo
     }
 }
 
-// Output sink: vertices get consecutive ids starting at `id_base`; when `vout`/`iout` are null
-// only the counters move (count pass). `vcap`/`icap` bound the writes to what the count pass
-// measured for this sink's range, so a disagreement between the passes can never write outside
-// the caller's buffers (it is reported through `overflow`).
-struct Sink {
+// Output sink: vertices get consecutive ids starting at `id_base`; when `vout`/`rout`/`iout`
+// are null only the counters move (count pass). `vcap`/`icap` bound the writes to what the count
+// pass measured for this sink's range, so a disagreement between the passes can never write
+// outside the caller's buffers (it is reported through `overflow`). With `rout`, every vertex
+// is a lyon_stroke_vertex record: the position, the normal and side the emission site gives and
+// the advancement of the join or end being emitted (`adv`, set by the caller), as lyon's
+// StrokeVertexData holds them when the vertex is added (stroke.rs:2656-2720).
+template <bool REC>
+struct SinkT {
+    static constexpr bool kRec = REC;
     uint32_t id_base;
     uint32_t nv, ni;
     float2* vout;
@@ -63,10 +70,21 @@ struct Sink {
     int index_bits;
     uint32_t vcap = 0xFFFFFFFFu, icap = 0xFFFFFFFFu;
     bool overflow = false;
+    lyon_stroke_vertex* rout = nullptr;
+    float adv = 0.0f;
 
-    __device__ __forceinline__ uint32_t vertex(V2 p) {
+    __device__ __forceinline__ uint32_t vertex(V2 p, V2 n, int side) {
         uint32_t id = id_base + nv;
-        if (vout) {
+        if constexpr (REC) {
+            if (nv < vcap) {
+                float2* d = reinterpret_cast<float2*>(rout + nv);
+                d[0] = make_float2(p.x, p.y);
+                d[1] = make_float2(n.x, n.y);
+                d[2] = make_float2(adv, __uint_as_float((uint32_t)side));
+            } else {
+                overflow = true;
+            }
+        } else if (vout) {
             if (nv < vcap) vout[nv] = make_float2(p.x, p.y);
             else overflow = true;
         }
@@ -92,6 +110,8 @@ struct Sink {
         ni += 3;
     }
 };
+using Sink = SinkT<false>;     // positions
+using RecSink = SinkT<true>;  // lyon_stroke_vertex records
 
 struct StrokeParams {
     float hw;          // line_width * 0.5
@@ -364,8 +384,10 @@ __device__ __forceinline__ uint32_t arc_vertex_count(uint32_t depth) {
 }
 
 // stroke.rs:2612-2653 (pre-order recursion, made iterative with an explicit stack).
+template <class SK>
 __device__ __noinline__ void tessellate_arc(V2 center, float radius, float a0, float a1, uint32_t va,
-                                            uint32_t vb, uint32_t depth, bool cr, Sink& sink) {
+                                            uint32_t vb, uint32_t depth, bool cr, int side,
+                                            SK& sink) {
     if (depth == 0) return;
     struct Frame {
         float a0, a1;
@@ -379,7 +401,7 @@ __device__ __noinline__ void tessellate_arc(V2 center, float radius, float a0, f
         if (f.n == 0) continue;
         float mid = (f.a0 + f.a1) * 0.5f;
         V2 normal = cr ? V2{cr_cos(mid), cr_sin(mid)} : V2{cosf(mid), sinf(mid)};
-        uint32_t vid = sink.vertex(center + normal * radius);
+        uint32_t vid = sink.vertex(center + normal * radius, normal, side);
         sink.tri(f.va, vid, f.vb);
         st[sp++] = Frame{mid, f.a1, vid, f.vb, f.n - 1};
         st[sp++] = Frame{f.a0, mid, f.va, vid, f.n - 1};
@@ -389,28 +411,30 @@ __device__ __noinline__ void tessellate_arc(V2 center, float radius, float a0, f
 // ---- emission ---------------------------------------------------------------------------------
 
 // stroke.rs:2024-2055
-__device__ __forceinline__ void add_join_base_vertices(DEP& j, int side, Sink& sink) {
+template <class SK>
+__device__ __forceinline__ void add_join_base_vertices(DEP& j, int side, SK& sink) {
     if (j.s[side].has_single) {
         V2 normal = (j.s[side].single - j.pos) / j.hw;
-        uint32_t v = sink.vertex(j.pos + normal * j.hw);
+        uint32_t v = sink.vertex(j.pos + normal * j.hw, normal, side);
         j.s[side].prev_vertex = v;
         j.s[side].next_vertex = v;
     } else {
         V2 n0 = (j.s[side].prev - j.pos) / j.hw;
-        uint32_t pv = sink.vertex(j.pos + n0 * j.hw);
+        uint32_t pv = sink.vertex(j.pos + n0 * j.hw, n0, side);
         V2 n1 = (j.s[side].next - j.pos) / j.hw;
-        uint32_t nv = sink.vertex(j.pos + n1 * j.hw);
+        uint32_t nv = sink.vertex(j.pos + n1 * j.hw, n1, side);
         j.s[side].prev_vertex = pv;
         j.s[side].next_vertex = nv;
     }
 }
 
 // Base vertices of a join: fast path +,- (stroke.rs:1791-1797) or regular -,+ (:1595-1608).
-__device__ __forceinline__ void emit_join_base(DEP& j, const JoinGeo& g, Sink& sink) {
+template <class SK>
+__device__ __forceinline__ void emit_join_base(DEP& j, const JoinGeo& g, SK& sink) {
     if (g.fast) {
         if (g.skip) return;
-        uint32_t pv = sink.vertex(j.pos + g.normal * j.hw);
-        uint32_t nv = sink.vertex(j.pos + (-g.normal) * j.hw);
+        uint32_t pv = sink.vertex(j.pos + g.normal * j.hw, g.normal, SP);
+        uint32_t nv = sink.vertex(j.pos + (-g.normal) * j.hw, -g.normal, SN);
         j.s[SP].prev_vertex = pv;
         j.s[SP].next_vertex = pv;
         j.s[SN].prev_vertex = nv;
@@ -440,8 +464,9 @@ __device__ __forceinline__ void edge_ids_to(const DEP& p1, uint32_t* neg, uint32
 }
 
 // stroke.rs:1869-1904 on already-resolved ids. Returns the number of triangles.
+template <class SK>
 __device__ __forceinline__ uint32_t edge_triangles(uint32_t p0_neg, uint32_t p0_pos,
-                                                   uint32_t p1_neg, uint32_t p1_pos, Sink* sink) {
+                                                   uint32_t p1_neg, uint32_t p1_pos, SK* sink) {
     if (p0_neg == p1_pos) return 0;
     uint32_t n = 0;
     if (p0_neg != p0_pos && p0_pos != p1_pos) {
@@ -455,7 +480,8 @@ __device__ __forceinline__ uint32_t edge_triangles(uint32_t p0_neg, uint32_t p0_
     return n;
 }
 
-__device__ __forceinline__ void add_edge_triangles(const DEP& p0, const DEP& p1, Sink& sink) {
+template <class SK>
+__device__ __forceinline__ void add_edge_triangles(const DEP& p0, const DEP& p1, SK& sink) {
     uint32_t a, b, c, d;
     edge_ids_from(p0, &a, &b);
     edge_ids_to(p1, &c, &d);
@@ -463,7 +489,8 @@ __device__ __forceinline__ void add_edge_triangles(const DEP& p0, const DEP& p1,
 }
 
 // stroke.rs:1907-1965 (interior triangles then round arcs).
-__device__ __forceinline__ void tessellate_join(const DEP& j, const StrokeParams& P, Sink& sink,
+template <class SK>
+__device__ __forceinline__ void tessellate_join(const DEP& j, const StrokeParams& P, SK& sink,
                                                 int* status) {
     bool nj[2];
     side_needs_join(j, nj);
@@ -485,7 +512,7 @@ __device__ __forceinline__ void tessellate_join(const DEP& j, const StrokeParams
             ArcPlan a = round_join_plan(j, side, P.tolerance, status);
             uint32_t va = side == SN ? j.s[side].next_vertex : j.s[side].prev_vertex;
             uint32_t vb = side == SN ? j.s[side].prev_vertex : j.s[side].next_vertex;
-            tessellate_arc(j.pos, j.hw, a.a0, a.a1, va, vb, a.depth, a.cr, sink);
+            tessellate_arc(j.pos, j.hw, a.a0, a.a1, va, vb, a.depth, a.cr, side, sink);
         }
     }
 }
@@ -506,12 +533,14 @@ __device__ __forceinline__ uint32_t join_arc_vertices(const DEP& j, const Stroke
 }
 
 // stroke.rs:2459-2524
+template <class SK>
 __device__ __noinline__ void tessellate_round_cap(V2 center, float radius, V2 start_normal,
                                                   uint32_t start_vertex, uint32_t end_vertex,
                                                   V2 edge_normal, bool is_start,
-                                                  const StrokeParams& P, Sink& sink,
+                                                  const StrokeParams& P, SK& sink,
                                                   int* status) {
     if (radius < P.tolerance) return;
+    const int first_side = (is_start ^ (cross(edge_normal, start_normal) >= 0.0f)) ? SP : SN;
     bool cr = false;
     float start_angle, diff, step;
     for (;;) {
@@ -528,29 +557,33 @@ __device__ __noinline__ void tessellate_round_cap(V2 center, float radius, V2 st
     float mid_angle = start_angle + diff;
     float end_angle = mid_angle + diff;
     uint32_t depth = depth_of(fabsf(diff) / step, status);
-    uint32_t mid_vertex = sink.vertex(center + normalize(edge_normal) * radius);
+    const V2 mid_normal = normalize(edge_normal);
+    uint32_t mid_vertex = sink.vertex(center + mid_normal * radius, mid_normal, first_side);
     sink.tri(start_vertex, mid_vertex, end_vertex);
     tessellate_arc(center, radius, start_angle, mid_angle, start_vertex, mid_vertex, depth, cr,
-                   sink);
-    tessellate_arc(center, radius, mid_angle, end_angle, mid_vertex, end_vertex, depth, cr, sink);
+                   first_side, sink);
+    tessellate_arc(center, radius, mid_angle, end_angle, mid_vertex, end_vertex, depth, cr,
+                   1 - first_side, sink);
 }
 
 // stroke.rs:2526-2560
-__device__ __forceinline__ void tessellate_empty_square_cap(V2 pos, float hw, Sink& sink) {
-    uint32_t a = sink.vertex(pos + V2{1.0f, 1.0f} * hw);
-    uint32_t b = sink.vertex(pos + V2{1.0f, -1.0f} * hw);
-    uint32_t c = sink.vertex(pos + V2{-1.0f, -1.0f} * hw);
-    uint32_t d = sink.vertex(pos + V2{-1.0f, 1.0f} * hw);
+template <class SK>
+__device__ __forceinline__ void tessellate_empty_square_cap(V2 pos, float hw, SK& sink) {
+    uint32_t a = sink.vertex(pos + V2{1.0f, 1.0f} * hw, V2{1.0f, 1.0f}, SN);
+    uint32_t b = sink.vertex(pos + V2{1.0f, -1.0f} * hw, V2{1.0f, -1.0f}, SP);
+    uint32_t c = sink.vertex(pos + V2{-1.0f, -1.0f} * hw, V2{-1.0f, -1.0f}, SP);
+    uint32_t d = sink.vertex(pos + V2{-1.0f, 1.0f} * hw, V2{-1.0f, 1.0f}, SN);
     sink.tri(a, b, c);
     sink.tri(a, c, d);
 }
 
 // stroke.rs:2562-2609
+template <class SK>
 __device__ __forceinline__ void tessellate_empty_round_cap(V2 center, float hw,
-                                                           const StrokeParams& P, Sink& sink,
+                                                           const StrokeParams& P, SK& sink,
                                                            int* status) {
-    uint32_t left_id = sink.vertex(center + V2{-1.0f, 0.0f} * hw);
-    uint32_t right_id = sink.vertex(center + V2{1.0f, 0.0f} * hw);
+    uint32_t left_id = sink.vertex(center + V2{-1.0f, 0.0f} * hw, V2{-1.0f, 0.0f}, SP);
+    uint32_t right_id = sink.vertex(center + V2{1.0f, 0.0f} * hw, V2{1.0f, 0.0f}, SN);
     tessellate_round_cap(center, hw, V2{-1.0f, 0.0f}, left_id, right_id, V2{0.0f, 1.0f}, true, P,
                          sink, status);
     tessellate_round_cap(center, hw, V2{1.0f, 0.0f}, right_id, left_id, V2{0.0f, -1.0f}, false,
@@ -558,10 +591,15 @@ __device__ __forceinline__ void tessellate_empty_round_cap(V2 center, float hw,
 }
 
 // stroke.rs:2130-2206
+template <class SK>
 __device__ __forceinline__ void tessellate_last_edge(const DEP& p0, DEP& p1, bool is_first_edge,
-                                                     const StrokeParams& P, Sink& sink,
+                                                     const StrokeParams& P, SK& sink,
                                                      int* status) {
     V2 v = p1.pos - p0.pos;
+    if constexpr (SK::kRec) {
+        p1.adv = p0.adv + vlength(v);
+        sink.adv = p1.adv;
+    }
     for (int side = 0; side < 2; ++side) {
         V2 side_position = p1.s[side].prev;
         if (P.end_cap == LYON_CAP_SQUARE || P.end_cap == LYON_CAP_BUTT) {
@@ -575,7 +613,7 @@ __device__ __forceinline__ void tessellate_last_edge(const DEP& p0, DEP& p1, boo
             }
         }
         V2 normal = (p1.s[side].prev - p1.pos) / p1.hw;
-        p1.s[side].prev_vertex = sink.vertex(p1.pos + normal * p1.hw);
+        p1.s[side].prev_vertex = sink.vertex(p1.pos + normal * p1.hw, normal, side);
     }
     if (!is_first_edge) add_edge_triangles(p0, p1, sink);
     if (P.end_cap == LYON_CAP_ROUND) {
@@ -585,9 +623,11 @@ __device__ __forceinline__ void tessellate_last_edge(const DEP& p0, DEP& p1, boo
 }
 
 // stroke.rs:2208-2276
+template <class SK>
 __device__ __forceinline__ void tessellate_first_edge(DEP& first, const DEP& second,
-                                                      const StrokeParams& P, Sink& sink,
+                                                      const StrokeParams& P, SK& sink,
                                                       int* status) {
+    sink.adv = first.adv;
     for (int side = 0; side < 2; ++side) {
         V2 side_position = first.s[side].next;
         if (P.start_cap == LYON_CAP_SQUARE || P.start_cap == LYON_CAP_BUTT) {
@@ -603,7 +643,7 @@ __device__ __forceinline__ void tessellate_first_edge(DEP& first, const DEP& sec
             }
         }
         V2 normal = (side_position - first.pos) / first.hw;
-        first.s[side].next_vertex = sink.vertex(first.pos + normal * first.hw);
+        first.s[side].next_vertex = sink.vertex(first.pos + normal * first.hw, normal, side);
     }
     add_edge_triangles(first, second, sink);
     if (P.start_cap == LYON_CAP_ROUND) {
@@ -689,7 +729,8 @@ __device__ __noinline__ void slow_join_geometry(DEP* dep, V2 prev, V2 cur, bool 
 
 // Emission of a general join: base vertices (- then +), the edge triangles from the previous
 // join, then tessellate_join. *out receives the join with its ids (for the tail).
-__device__ __noinline__ void slow_join_emit(const DEP* dep, DEP* out, Sink& s, bool has_edge,
+template <class SK>
+__device__ __noinline__ void slow_join_emit(const DEP* dep, DEP* out, SK& s, bool has_edge,
                                             uint32_t pfn, uint32_t pfp, bool emit_tris,
                                             const StrokeParams& P, int* status) {
     DEP J = *dep;
@@ -738,7 +779,8 @@ struct SeqBuffer {
     }
 };
 
-__device__ __noinline__ bool seq_step(SeqBuffer& pb, DEP next, const StrokeParams& P, Sink& sink,
+template <class SK>
+__device__ __noinline__ bool seq_step(SeqBuffer& pb, DEP next, const StrokeParams& P, SK& sink,
                                       bool* may_need_empty_cap, int* status) {
     uint32_t count = pb.n;
     if (count > 0) {
@@ -746,12 +788,22 @@ __device__ __noinline__ bool seq_step(SeqBuffer& pb, DEP next, const StrokeParam
             if (count == 1) *may_need_empty_cap = true;
             return false;
         }
-        if (count == 1) first_point_sides(pb.last(), next.pos, next.hw);
+        if (count == 1) {
+            DEP& first = pb.last();
+            first_point_sides(first, next.pos, next.hw);
+            if (SK::kRec && isnan(next.adv)) next.adv = first.adv + vlength(next.pos - first.pos);
+        }
     }
     if (count > 1) {
         DEP& prev = pb.second_last();
         DEP& join = pb.last();
+        // Advancements (stroke.rs:1657-1662, 1759-1771): the join's from its predecessor, and
+        // on a flattening step the next point's from the join.
+        if (SK::kRec && isnan(join.adv)) join.adv = prev.adv + vlength(join.pos - prev.pos);
         JoinGeo g = join_geometry(prev.pos, join, next.pos, P.miter_limit);
+        if (SK::kRec && g.fast && isnan(next.adv))
+            next.adv = join.adv + vlength(next.pos - join.pos);
+        sink.adv = join.adv;
         if (g.fast) g.skip = flattened_skip(prev.pos, prev.s[SP].next, prev.s[SN].next, join);
         emit_join_base(join, g, sink);
         if (count > 2) add_edge_triangles(prev, join, sink);

@@ -39,6 +39,11 @@ LYON_ERR_UNSUPPORTED = 104
 INDEX_GLOBAL = 0
 INDEX_PER_PATH = 1
 
+# lyon_stroke_vertex: the StrokeVertex attributes a vertex constructor reads
+# (crates/tessellation/src/stroke.rs:2667-2720); side 0 = Positive, 1 = Negative.
+STROKE_VERTEX_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("normal_x", "<f4"),
+                                ("normal_y", "<f4"), ("advancement", "<f4"), ("side", "<u4")])
+
 _ERROR_NAMES = {
     LYON_ERR_POSITION_IS_NAN: "UnsupportedParamater(PositionIsNaN)",
     LYON_ERR_TOLERANCE_IS_NAN: "UnsupportedParamater(ToleranceIsNaN)",
@@ -77,11 +82,18 @@ class VertexBuffers:
 
 
 class BuffersBuilder:
-    """`BuffersBuilder::new(&mut buffers, Positions)` with an optional vertex offset."""
+    """`BuffersBuilder::new(&mut buffers, ctor)` with an optional vertex offset.
 
-    def __init__(self, buffers: VertexBuffers, vertex_offset: int = 0):
+    Without `vertex_ctor` the vertices are positions (lyon's `Positions` constructor). With it,
+    a stroke hands the constructor every vertex as a STROKE_VERTEX_DTYPE record array (position,
+    normal, advancement, side: what lyon's StrokeVertex exposes) and a fill hands it the (N, 2)
+    positions; the constructor returns one output row per vertex (vectorised, where lyon calls
+    it once per vertex)."""
+
+    def __init__(self, buffers: VertexBuffers, vertex_offset: int = 0, vertex_ctor=None):
         self.buffers = buffers
         self.vertex_offset = vertex_offset
+        self.vertex_ctor = vertex_ctor
 
     def with_vertex_offset(self, offset: int) -> "BuffersBuilder":
         self.vertex_offset = offset
@@ -92,7 +104,11 @@ class BuffersBuilder:
 
     def append(self, vertices: np.ndarray, indices: np.ndarray) -> None:
         b = self.buffers
-        b.vertices = np.concatenate([b.vertices, vertices.reshape(-1, 2)])
+        if self.vertex_ctor is not None:
+            made = np.asarray(self.vertex_ctor(vertices))
+            b.vertices = made.copy() if len(b.vertices) == 0 else np.concatenate([b.vertices, made])
+        else:
+            b.vertices = np.concatenate([b.vertices, vertices.reshape(-1, 2)])
         b.indices = np.concatenate([b.indices, indices.astype(b.indices.dtype)])
 
 
@@ -148,12 +164,26 @@ def _single(kind: str, ctx: Context, path: Path, options, builder: BuffersBuilde
     pts = np.ascontiguousarray(path.points, dtype=np.float32)
     opt = options.to_c()
     res = _native.CResult()
-    fn = ctx.lib.lyon_gpu_stroke_path if kind == "stroke" else ctx.lib.lyon_gpu_fill_path
+    records = kind == "stroke" and builder.vertex_ctor is not None
+    if records:
+        fn = ctx.lib.lyon_gpu_stroke_path_attributes
+    else:
+        fn = ctx.lib.lyon_gpu_stroke_path if kind == "stroke" else ctx.lib.lyon_gpu_fill_path
     r = fn(ctx.h, _ptr(verbs), len(verbs), _ptr(pts), len(pts), ctypes.byref(opt), bits,
            builder.next_index(), ctypes.byref(res))
     if r != LYON_OK:
         raise TessellationError(r, ctx.last_error() if r >= 100 else "")
     nv, ni = res.num_vertices, res.num_indices
+    if records:
+        raw = np.ctypeslib.as_array(ctypes.cast(res.vertices, ctypes.POINTER(ctypes.c_uint8)),
+                                    shape=(nv * STROKE_VERTEX_DTYPE.itemsize,)).copy() \
+            if nv else np.zeros(0, np.uint8)
+        v = raw.view(STROKE_VERTEX_DTYPE)
+        ctype = ctypes.c_uint16 if bits == 16 else ctypes.c_uint32
+        i = np.ctypeslib.as_array(ctypes.cast(res.indices, ctypes.POINTER(ctype)),
+                                  shape=(ni,)).copy() if ni else np.zeros(0, builder.buffers.indices.dtype)
+        builder.append(v, i)
+        return
     v = np.ctypeslib.as_array(ctypes.cast(res.vertices, ctypes.POINTER(ctypes.c_float)),
                               shape=(nv * 2,)).copy() if nv else np.zeros(0, np.float32)
     ctype = ctypes.c_uint16 if bits == 16 else ctypes.c_uint32
@@ -249,6 +279,7 @@ class BatchResult:
     num_paths: int
     vertex_offsets_ptr: int = 0
     index_offsets_ptr: int = 0
+    vertex_floats: int = 2  # 6 when the vertices are lyon_stroke_vertex records
 
     def offsets(self):
         """(vertex_offsets, index_offsets) as int64 torch tensors of num_paths + 1 entries."""
@@ -260,8 +291,18 @@ class BatchResult:
         return v, i
 
     def vertices(self):
+        """Positions, (V, 2) f32 (a strided view when the output holds records)."""
         import torch
-        return torch.as_tensor(_CudaArray(self.vertices_ptr, (self.total_vertices, 2), "<f4"),
+        t = torch.as_tensor(_CudaArray(self.vertices_ptr, (self.total_vertices, self.vertex_floats),
+                                       "<f4"), device="cuda")
+        return t if self.vertex_floats == 2 else t[:, :2]
+
+    def records(self):
+        """lyon_stroke_vertex records as a (V, 6) f32 tensor (column 5 holds the side's u32
+        bits); `.cpu().numpy().view(STROKE_VERTEX_DTYPE)` gives the structured records."""
+        import torch
+        assert self.vertex_floats == 6, "not an attribute output"
+        return torch.as_tensor(_CudaArray(self.vertices_ptr, (self.total_vertices, 6), "<f4"),
                                device="cuda")
 
     def indices(self):
@@ -283,13 +324,20 @@ class BatchResult:
 
 def tessellate_paths(kind: str, dbatch: DeviceBatch, options_dev, num_options: int,
                      index_bits: int = 32, index_mode: int = INDEX_GLOBAL,
-                     vertex_offset: int = 0, ctx: Optional[Context] = None) -> BatchResult:
+                     vertex_offset: int = 0, ctx: Optional[Context] = None,
+                     attributes: bool = False) -> BatchResult:
     """Batched stroke or fill of every path of a DeviceBatch (results stay on the device,
-    owned by the context until its next batched call)."""
+    owned by the context until its next batched call). With `attributes` (strokes), the
+    vertices are lyon_stroke_vertex records (BatchResult.records)."""
     ctx = ctx or Context.default()
     out = _native.CBatchOutput()
     cb = dbatch.c()
-    fn = ctx.lib.lyon_gpu_stroke_paths if kind == "stroke" else ctx.lib.lyon_gpu_fill_paths
+    if attributes and kind != "stroke":
+        raise ValueError("vertex attributes are a stroke output")
+    if attributes:
+        fn = ctx.lib.lyon_gpu_stroke_paths_attributes
+    else:
+        fn = ctx.lib.lyon_gpu_stroke_paths if kind == "stroke" else ctx.lib.lyon_gpu_fill_paths
     r = fn(ctx.h, ctypes.byref(cb), options_dev.data_ptr(), num_options, index_bits, index_mode,
            vertex_offset, ctypes.byref(out))
     if r != LYON_OK:
@@ -297,4 +345,5 @@ def tessellate_paths(kind: str, dbatch: DeviceBatch, options_dev, num_options: i
     return BatchResult(r, int(out.total_vertices), int(out.total_indices),
                        int(out.num_failed_paths), int(out.vertices or 0), int(out.indices or 0),
                        int(out.status or 0), index_bits, dbatch.num_paths,
-                       int(out.vertex_offsets or 0), int(out.index_offsets or 0))
+                       int(out.vertex_offsets or 0), int(out.index_offsets or 0),
+                       6 if attributes else 2)

@@ -336,6 +336,10 @@ static const uint32_t INVALID_ID = 0xFFFFFFFFu;
 struct Output {
     std::vector<float> vertices;     // x, y
     std::vector<uint32_t> indices;   // VertexId values; exported as u16 (truncating) or u32
+    // With want_attributes, the stroke vertex attributes (StrokeVertex, stroke.rs:2667-2720):
+    // normal x, normal y, advancement (f32 bits) and side, four words per vertex.
+    bool want_attributes = false;
+    std::vector<uint32_t> attributes;
     uint64_t max_index = 0xFFFFFFFEull;
     uint64_t vertex_offset = 0;
     size_t first_vertex = 0, first_index = 0;
@@ -360,6 +364,7 @@ struct Output {
     void abort_geometry() {
         vertices.resize(first_vertex * 2);
         indices.resize(first_index);
+        if (want_attributes) attributes.resize(first_vertex * 4);
     }
 };
 
@@ -537,6 +542,14 @@ struct Stroker {
         P pos = add(vertex.position_on_path, mul(vertex.normal, vertex.half_width));
         uint32_t id;
         if (!out->add_vertex(pos, &id)) throw TessError{LYON_ERR_TOO_MANY_VERTICES, 0};
+        if (out->want_attributes) {
+            uint32_t w[3];
+            std::memcpy(&w[0], &vertex.normal.x, 4);
+            std::memcpy(&w[1], &vertex.normal.y, 4);
+            std::memcpy(&w[2], &vertex.advancement, 4);
+            out->attributes.insert(out->attributes.end(), w, w + 3);
+            out->attributes.push_back((uint32_t)vertex.side);
+        }
         return id;
     }
 
@@ -2443,7 +2456,16 @@ void lyon_oracle_out_free(lyon_oracle_out* o) { delete o; }
 void lyon_oracle_out_clear(lyon_oracle_out* o) {
     o->out.vertices.clear();
     o->out.indices.clear();
+    o->out.attributes.clear();
     o->near_ties = 0;
+}
+// Stroke vertex attributes (four words per vertex: normal x, normal y, advancement, side),
+// recorded from the next call on.
+void lyon_oracle_out_set_attributes(lyon_oracle_out* o, int enabled) {
+    o->out.want_attributes = enabled != 0;
+}
+const uint32_t* lyon_oracle_out_attributes(const lyon_oracle_out* o) {
+    return o->out.attributes.data();
 }
 uint64_t lyon_oracle_out_num_vertices(const lyon_oracle_out* o) { return o->out.vertices.size() / 2; }
 uint64_t lyon_oracle_out_num_indices(const lyon_oracle_out* o) { return o->out.indices.size(); }
@@ -2562,6 +2584,43 @@ int lyon_oracle_batch(int kind, const lyon_path_batch* batch, const void* option
         for (int t = 0; t < num_threads; ++t) th.emplace_back(worker);
         for (auto& t : th) t.join();
     }
+    return LYON_OK;
+}
+
+// The stroke vertex attributes of every path of a batch (four words per vertex, see
+// lyon_oracle_out_set_attributes), written at `vtx_offsets` (from a counting call).
+int lyon_oracle_batch_stroke_attributes(const lyon_path_batch* batch, const void* options,
+                                        uint32_t num_options, int num_threads,
+                                        const uint64_t* vtx_offsets, uint32_t* attributes) {
+    uint32_t n = batch->num_paths;
+    if (num_threads < 1) num_threads = 1;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        lyon_oracle_out o;
+        o.out.want_attributes = true;
+        for (;;) {
+            uint32_t begin = next.fetch_add(64);
+            if (begin >= n) break;
+            uint32_t end = std::min(n, begin + 64);
+            for (uint32_t i = begin; i < end; ++i) {
+                o.out.vertices.clear();
+                o.out.indices.clear();
+                o.out.attributes.clear();
+                uint32_t v0 = batch->verb_offsets[i], v1 = batch->verb_offsets[i + 1];
+                uint32_t p0 = batch->point_offsets[i], p1 = batch->point_offsets[i + 1];
+                const lyon_stroke_options* so =
+                    (const lyon_stroke_options*)options + (num_options > 1 ? i : 0);
+                lyon_oracle_stroke_path(&o, batch->verbs + v0, v1 - v0,
+                                        batch->points + 2 * (size_t)p0, p1 - p0, so);
+                std::memcpy(attributes + 4 * vtx_offsets[i], o.out.attributes.data(),
+                            o.out.attributes.size() * sizeof(uint32_t));
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < num_threads; ++t) th.emplace_back(worker);
+    worker();
+    for (auto& t : th) t.join();
     return LYON_OK;
 }
 

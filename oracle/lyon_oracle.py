@@ -59,6 +59,12 @@ def lib():
                                                    ctypes.c_float, c_p, c_p, ctypes.c_uint64]
             L.lyon_oracle_wang.restype = ctypes.c_float
             L.lyon_oracle_wang.argtypes = [c_p, ctypes.c_int, ctypes.c_float]
+            L.lyon_oracle_out_set_attributes.argtypes = [c_p, ctypes.c_int]
+            L.lyon_oracle_out_attributes.restype = ctypes.POINTER(ctypes.c_uint32)
+            L.lyon_oracle_out_attributes.argtypes = [c_p]
+            L.lyon_oracle_batch_stroke_attributes.restype = ctypes.c_int
+            L.lyon_oracle_batch_stroke_attributes.argtypes = [c_p, c_p, ctypes.c_uint32,
+                                                              ctypes.c_int, c_p, c_p]
             L.lyon_oracle_batch.restype = ctypes.c_int
             L.lyon_oracle_batch.argtypes = [ctypes.c_int, c_p, c_p, ctypes.c_uint32, ctypes.c_int,
                                             ctypes.c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
@@ -73,9 +79,12 @@ def _ptr(a: np.ndarray):
 class Result:
     """Output of one oracle call: positions, indices (u32 VertexId values), status."""
 
-    def __init__(self, status, vertices, indices, near_ties, index_bits):
+    def __init__(self, status, vertices, indices, near_ties, index_bits, attributes=None):
         self.status = status
         self.vertices = vertices
+        # Stroke vertex attributes when requested: (V, 4) u32 words (normal x, normal y,
+        # advancement as f32 bits; side 0 positive / 1 negative).
+        self.attributes = attributes
         self.indices = indices if index_bits == 32 else indices.astype(np.uint16)
         self.indices32 = indices
         self.near_ties = near_ties
@@ -88,10 +97,13 @@ class Result:
 class Output:
     """A VertexBuffers + BuffersBuilder pair on the oracle side (append semantics)."""
 
-    def __init__(self, index_bits: int = 32, vertex_offset: int = 0):
+    def __init__(self, index_bits: int = 32, vertex_offset: int = 0, attributes: bool = False):
         self.L = lib()
         self.h = self.L.lyon_oracle_out_new(index_bits, vertex_offset)
         self.index_bits = index_bits
+        self.attributes = attributes
+        if attributes:
+            self.L.lyon_oracle_out_set_attributes(self.h, 1)
 
     def __del__(self):
         try:
@@ -109,8 +121,13 @@ class Output:
             if nv else np.zeros(0, np.float32)
         i = np.ctypeslib.as_array(self.L.lyon_oracle_out_indices32(self.h), shape=(ni,)).copy() \
             if ni else np.zeros(0, np.uint32)
+        a = None
+        if self.attributes:
+            a = np.ctypeslib.as_array(self.L.lyon_oracle_out_attributes(self.h),
+                                      shape=(nv * 4,)).copy().reshape(-1, 4) \
+                if nv else np.zeros((0, 4), np.uint32)
         return Result(status, v.reshape(-1, 2), i, self.L.lyon_oracle_out_near_ties(self.h),
-                      self.index_bits)
+                      self.index_bits, a)
 
     def stroke(self, path, options):
         o = options.to_c()
@@ -127,8 +144,9 @@ class Output:
                                             ctypes.byref(o))
 
 
-def stroke(path, options, index_bits: int = 32, vertex_offset: int = 0) -> Result:
-    out = Output(index_bits, vertex_offset)
+def stroke(path, options, index_bits: int = 32, vertex_offset: int = 0,
+           attributes: bool = False) -> Result:
+    out = Output(index_bits, vertex_offset, attributes)
     st = out.stroke(path, options)
     return out.snapshot(st)
 
@@ -165,11 +183,12 @@ class _CBatch(ctypes.Structure):
 
 
 def batch(kind: str, pb, options_records: np.ndarray, index_bits: int = 32,
-          num_threads: int = 1, want_output: bool = True):
+          num_threads: int = 1, want_output: bool = True, want_attributes: bool = False):
     """Tessellates every path of a PathBatch with the oracle (per-path buffers).
 
     Returns dict with per-path vertex/index counts, statuses, near-tie counts and, when
-    `want_output`, the concatenated outputs with per-path offsets."""
+    `want_output`, the concatenated outputs with per-path offsets (and, for strokes with
+    `want_attributes`, the (V, 4) vertex attribute words of `Result.attributes`)."""
     L = lib()
     n = pb.num_paths
     cb = _CBatch(_ptr(pb.verbs), _ptr(pb.points), _ptr(pb.verb_offsets),
@@ -193,4 +212,9 @@ def batch(kind: str, pb, options_records: np.ndarray, index_bits: int = 32,
         L.lyon_oracle_batch(k, ctypes.byref(cb), _ptr(opts), len(opts), index_bits, num_threads,
                             None, None, None, None, _ptr(verts), _ptr(idx), _ptr(vo), _ptr(io))
         res.update(vertices=verts, indices=idx, vtx_offsets=vo, idx_offsets=io)
+        if want_attributes and kind == "stroke":
+            attrs = np.zeros((int(vo[-1]), 4), np.uint32)
+            L.lyon_oracle_batch_stroke_attributes(ctypes.byref(cb), _ptr(opts), len(opts),
+                                                  num_threads, _ptr(vo), _ptr(attrs))
+            res["attributes"] = attrs
     return res

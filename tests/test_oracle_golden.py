@@ -137,9 +137,14 @@ STROKE_CASES = load("lyon_stroke_cases.json")
 
 
 def check_stroke_builder_asserts(r):
-    """The TestBuilder of stroke.rs:2787-2849: distinct indices, cross >= -0.035, no NaN."""
+    """The TestBuilder of stroke.rs:2787-2849: distinct indices, cross >= -0.035, no NaN; with
+    attributes, no NaN normal or advancement and no zero normal (stroke.rs:2817-2826)."""
     v = r.vertices.astype(np.float32)
     assert not np.isnan(v).any()
+    if r.attributes is not None:
+        f = r.attributes[:, :3].copy().view(np.float32)
+        assert not np.isnan(f).any()
+        assert ((f[:, 0] * f[:, 0] + f[:, 1] * f[:, 1]) != 0.0).all()
     t = r.indices32.reshape(-1, 3).astype(np.int64)
     assert (t[:, 0] != t[:, 1]).all() and (t[:, 0] != t[:, 2]).all() and (t[:, 1] != t[:, 2]).all()
     pa, pb, pc = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
@@ -154,7 +159,7 @@ def check_stroke_builder_asserts(r):
 def test_stroke_kat(case):
     path = case_path(case)
     opts = stroke_options_from_case(case["options"])
-    r = orc.stroke(path, opts, index_bits=16)
+    r = orc.stroke(path, opts, index_bits=16, attributes=True)
     assert r.status == 0, case["src"]
     if case["name"] in ("test_square", "test_empty_caps", "test_empty_path"):
         # These go through stroke.rs `test_path`, whose TestBuilder asserts per triangle.
@@ -176,6 +181,59 @@ def test_stroke_kat(case):
             assert np.min(np.abs(allowed - p).max(axis=1)) < 1e-5
     if "max_y" in case:
         assert float(r.vertices[:, 1].max()) == case["max_y"]
+
+
+def _adv(r):
+    return r.attributes[:, 2].copy().view(np.float32)
+
+
+def test_stroke_attributes_advancement_and_sides():
+    # A right angle, miter join within the limit, butt caps: the join's two vertices at
+    # advancement 10, the end's at 20, the start's at 0; one vertex per side each time.
+    p = Path.builder()
+    p.begin((0.0, 0.0))
+    p.line_to((10.0, 0.0))
+    p.line_to((10.0, 10.0))
+    p.end(False)
+    r = orc.stroke(p.build(), StrokeOptions(line_width=2.0), attributes=True)
+    assert r.status == 0
+    assert sorted(_adv(r).tolist()) == [0.0, 0.0, 10.0, 10.0, 20.0, 20.0]
+    for a in (0.0, 10.0, 20.0):
+        assert sorted(r.attributes[_adv(r) == a, 3].tolist()) == [0, 1]
+    # Positions are position_on_path + normal * half_width.
+    n = r.attributes[:, :2].copy().view(np.float32)
+    on_path = {0.0: (0.0, 0.0), 10.0: (10.0, 0.0), 20.0: (10.0, 10.0)}
+    for k in range(len(r.vertices)):
+        c = np.array(on_path[float(_adv(r)[k])], np.float32)
+        assert np.allclose(r.vertices[k], c + n[k] * np.float32(1.0), atol=1e-6)
+
+
+def test_stroke_attributes_advancement_across_sub_paths():
+    # end_with_caps carries the end advancement into the next sub-path (stroke.rs:1359); a
+    # closed sub-path does not (close() leaves sub_path_start_advancement alone).
+    p = Path.builder()
+    p.begin((0.0, 0.0))
+    p.line_to((10.0, 0.0))
+    p.end(False)
+    p.begin((0.0, 5.0))
+    p.line_to((0.0, 8.0))
+    p.end(False)
+    r = orc.stroke(p.build(), StrokeOptions(line_width=2.0), attributes=True)
+    assert sorted(set(_adv(r).tolist())) == [0.0, 10.0, 13.0]
+    p = Path.builder()
+    p.begin((0.0, 0.0))
+    p.line_to((10.0, 0.0))
+    p.line_to((10.0, 10.0))
+    p.end(True)
+    p.begin((0.0, 20.0))
+    p.line_to((5.0, 20.0))
+    p.end(False)
+    r = orc.stroke(p.build(), StrokeOptions(line_width=2.0), attributes=True)
+    a = _adv(r)
+    # The closed triangle: 0, 10, 20 and the closing join at 20 + 10*sqrt(2); then 0 and 5.
+    tail = a[-4:]
+    assert sorted(tail.tolist()) == [0.0, 0.0, 5.0, 5.0]
+    assert np.isclose(a.max(), 20.0 + 10.0 * math.sqrt(2.0), atol=1e-4)
 
 
 def test_stroke_too_many_vertices():

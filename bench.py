@@ -57,6 +57,10 @@ def parse():
                     help="only run the fill warm-up and timed steps (for profilers)")
     ap.add_argument("--profile", action="store_true",
                     help="only run the warm-up and timed device steps (for profilers)")
+    ap.add_argument("--profile-polylines", action="store_true",
+                    help="only run the map-polyline stroke (tolerance 0.1, default launch "
+                         "settings, --polyline-paths paths) for --warmup + --steps calls "
+                         "(for profilers)")
     return ap.parse_args()
 
 
@@ -230,6 +234,27 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
 
+    if args.profile_polylines:
+        ctx = T.Context(dev)
+        pb, popts = workloads.map_polylines(args.polyline_paths, seed=4)
+        popts["tolerance"] = 0.1
+        pdb = T.DeviceBatch.upload(pb, dev)
+        pod = T.upload_options(popts, dev)
+        stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", dev))
+        for _ in range(args.warmup):
+            res = T.tessellate_paths("stroke", pdb, pod, len(popts), 32, T.INDEX_GLOBAL, 0, ctx)
+        ctx.synchronize()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            res = T.tessellate_paths("stroke", pdb, pod, len(popts), 32, T.INDEX_GLOBAL, 0, ctx)
+        end.record(stream)
+        end.synchronize()
+        print(json.dumps({"profile_polylines_ms_per_step": start.elapsed_time(end) / args.steps,
+                          "paths": pb.num_paths, "vertices": res.total_vertices}))
+        ctx.close()
+        return 0
     if args.profile_fill:
         ctx = T.Context(dev)
         lib = ctx.lib
@@ -450,7 +475,7 @@ def run_polylines(ctx, args, T):
                  "candidate_ms": [round(float(t), 3) for t in times[:nc.value]],
                  "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
         if tol == 0.1:
-            n = min(100_000, batch.num_paths)
+            n = batch.num_paths  # the whole batch: well under a second on the host cores
             sub = batch.head(n)
             t0 = time.perf_counter()
             r = orc.batch("stroke", sub, o[:n], 32, threads, want_output=False)

@@ -257,6 +257,7 @@ struct Evt {
     EvtKind kind;
     P from, ctrl1, ctrl2, to;  // Begin: to = at. End: from = last, to = first.
     bool close;
+    float w_from = NAN, w_to = NAN;  // endpoint width factors (variable line width only)
 };
 
 struct PathIter {
@@ -264,47 +265,67 @@ struct PathIter {
     uint32_t nverbs;
     const float* pts;
     uint32_t npts;
+    // Optional per-point width factors (the endpoint attribute that
+    // StrokeOptions::variable_line_width names, stroke.rs:646-767); indexed like the points.
+    const float* widths = nullptr;
     uint32_t vi = 0, pi = 0;
     P current{0, 0}, first{0, 0};
+    float cur_w = NAN, first_w = NAN;
+    uint32_t last_idx = 0;
     bool bad = false;
     P take() {
         if (pi >= npts) {
             bad = true;
+            last_idx = npts;
             return P{NAN, NAN};
         }
         P p{pts[2 * pi], pts[2 * pi + 1]};
+        last_idx = pi;
         ++pi;
         return p;
     }
+    float width_at(uint32_t idx) const { return widths && idx < npts ? widths[idx] : NAN; }
     bool next(Evt* e) {
         if (vi >= nverbs) return false;
         uint8_t v = verbs[vi++];
         switch (v) {
             case LYON_VERB_BEGIN:
                 current = take();
+                cur_w = width_at(last_idx);
                 first = current;
+                first_w = cur_w;
+                e->w_to = cur_w;
                 e->kind = EV_BEGIN;
                 e->to = current;
                 return true;
             case LYON_VERB_LINE_TO:
                 e->kind = EV_LINE;
                 e->from = current;
+                e->w_from = cur_w;
                 current = take();
+                cur_w = width_at(last_idx);
+                e->w_to = cur_w;
                 e->to = current;
                 return true;
             case LYON_VERB_QUADRATIC_TO:
                 e->kind = EV_QUAD;
                 e->from = current;
+                e->w_from = cur_w;
                 e->ctrl1 = take();
                 current = take();
+                cur_w = width_at(last_idx);
+                e->w_to = cur_w;
                 e->to = current;
                 return true;
             case LYON_VERB_CUBIC_TO:
                 e->kind = EV_CUBIC;
                 e->from = current;
+                e->w_from = cur_w;
                 e->ctrl1 = take();
                 e->ctrl2 = take();
                 current = take();
+                cur_w = width_at(last_idx);
+                e->w_to = cur_w;
                 e->to = current;
                 return true;
             case LYON_VERB_CLOSE:
@@ -312,6 +333,8 @@ struct PathIter {
                 e->from = current;
                 (void)take();
                 e->to = first;
+                e->w_from = cur_w;
+                e->w_to = first_w;
                 e->close = true;
                 return true;
             case LYON_VERB_END:
@@ -319,6 +342,9 @@ struct PathIter {
                 e->from = current;
                 current = first;
                 e->to = first;
+                e->w_from = cur_w;
+                e->w_to = first_w;
+                cur_w = first_w;
                 e->close = false;
                 return true;
             default:
@@ -418,6 +444,11 @@ struct PointBuffer {  // stroke.rs:2371-2457
         start += 1;
         if (start == 3) start = 0;
     }
+    void replace_last(const EndpointData& p) {  // stroke.rs:2400-2406
+        size_t idx = start;
+        if (idx == 0) idx = count;
+        points[idx - 1] = p;
+    }
     void clear() { count = 0, start = 0; }
     EndpointData& get(size_t idx) { return points[(idx + start) % 3]; }
     EndpointData& last() { return get(count - 1); }
@@ -511,6 +542,7 @@ static inline float cr_atan2(float y, float x) { return (float)atan2((double)y, 
 static inline float cr_acos(float x) { return (float)acos((double)x); }
 static inline float cr_cos(float x) { return (float)cos((double)x); }
 static inline float cr_sin(float x) { return (float)sin((double)x); }
+static inline float cr_asin(float x) { return (float)asin((double)x); }
 
 struct Stroker {
     lyon_stroke_options options;
@@ -522,6 +554,7 @@ struct Stroker {
     float sub_path_start_advancement = 0.0f;
     float square_merge_threshold;
     bool may_need_empty_cap = false;
+    bool vw = false;  // StrokeOptions::variable_line_width set
 
     // stroke.rs:591-631
     Stroker(const lyon_stroke_options& o, Output* output) : options(o), out(output) {
@@ -823,6 +856,188 @@ struct Stroker {
         }
     }
 
+    // ---- Variable line width (StrokeOptions::variable_line_width) --------------------------
+    // The edge's attachment angles use atan2/asin/cos/sin; lyon takes them from the platform's
+    // f32 libm, whose last bit varies between platforms. Here (and on the GPU) they are
+    // evaluated in f64 and rounded once, so both sides agree bit for bit.
+
+    // stroke.rs:1842-1866
+    static void compute_side_attachment_positions(EndpointData& p0, EndpointData& p1,
+                                                  float edge_angle, float vwidth_angle,
+                                                  int side) {
+        float nl = side == SIDE_NEGATIVE ? -1.0f : 1.0f;
+        float normal_angle = edge_angle + nl * (PI_F * 0.5f + vwidth_angle);
+        P normal = P{cr_cos(normal_angle), cr_sin(normal_angle)};
+        p0.side[side].next = add(p0.position, mul(normal, p0.half_width));
+        p1.side[side].prev = add(p1.position, mul(normal, p1.half_width));
+    }
+
+    // stroke.rs:1808-1840
+    static void compute_edge_attachment_positions(EndpointData& p0, EndpointData& p1) {
+        P edge = sub(p1.position, p0.position);
+        float d = length(edge);
+        float edge_angle = cr_atan2(edge.y, edge.x);
+        float sin_vwidth_angle = (p1.half_width - p0.half_width) / d;
+        float vwidth_angle = cr_asin(sin_vwidth_angle);
+        if (is_nan_f(vwidth_angle)) vwidth_angle = 0.0f;
+        compute_side_attachment_positions(p0, p1, edge_angle, vwidth_angle, SIDE_POSITIVE);
+        compute_side_attachment_positions(p0, p1, edge_angle, vwidth_angle, SIDE_NEGATIVE);
+        if (is_nan_f(p1.advancement)) p1.advancement = p0.advancement + d;
+    }
+
+    // stroke.rs:2060-2128
+    static void compute_join_side_positions_vw(const EndpointData& prev, EndpointData& join,
+                                               const EndpointData& next, float miter_limit,
+                                               int side) {
+        float sign = side == SIDE_NEGATIVE ? -1.0f : 1.0f;
+        P v0 = normalize(sub(join.side[side].prev, prev.side[side].next));
+        P v1 = normalize(sub(next.side[side].prev, join.side[side].next));
+        bool inward = cross(v0, v1) * sign > 0.0f;
+        bool forward = dot(v0, v1) > 0.0f;
+        P normal = mul(compute_normal(v0, v1), sign);
+        P path_v0 = normalize(sub(join.position, prev.position));
+        P path_v1 = normalize(sub(next.position, join.position));
+        bool normal_same_side = dot(add(v0, v1), add(path_v0, path_v1)) >= 0.0f;
+        bool angle_is_sharp = inward && !forward && normal_same_side;
+        if (angle_is_sharp) {
+            P extruded_normal = mul(normal, join.half_width);
+            float prev_length = join.advancement - prev.advancement;
+            float next_length = next.advancement - join.advancement;
+            float d_next = dot(extruded_normal, v1) - next_length;
+            float d_prev = dot(extruded_normal, neg(v0)) - prev_length;
+            if (fminf(d_next, d_prev) > 0.0f || sqlen(normal) < 1e-5f) join.fold[side] = true;
+        }
+        bool concave = inward && normal_same_side && !join.fold[side];
+        if (concave || ((join.line_join == LYON_JOIN_MITER || join.line_join == LYON_JOIN_MITER_CLIP) &&
+                        !miter_limit_is_exceeded(normal, miter_limit))) {
+            join.side[side].has_single = true;
+            join.side[side].single = add(join.position, mul(normal, join.half_width));
+        } else if (join.line_join == LYON_JOIN_MITER_CLIP) {
+            P n0 = sub(join.side[side].prev, join.position);
+            P n1 = sub(join.side[side].next, join.position);
+            P pn, nn;
+            get_clip_intersections(n0, n1, normal, miter_limit * join.half_width, &pn, &nn);
+            join.side[side].prev = add(join.position, pn);
+            join.side[side].next = add(join.position, nn);
+        }
+    }
+
+    // stroke.rs:1380-1512 (step_impl)
+    bool step_vw_impl(EndpointData next) {
+        size_t count = point_buffer.count;
+        if (count > 0 && points_are_too_close(point_buffer.last().position, next.position)) {
+            if (count == 1) may_need_empty_cap = true;
+            return false;
+        }
+        if (count > 0) {
+            EndpointData& join = point_buffer.last();
+            if (!join.is_flattening_step || !next.is_flattening_step)
+                compute_edge_attachment_positions(join, next);
+        }
+        bool skip = false;
+        if (count > 1) {
+            EndpointData& prev = point_buffer.second_last();
+            EndpointData& join = point_buffer.last();
+            vertex.position_on_path = join.position;
+            vertex.half_width = join.half_width;
+            vertex.advancement = join.advancement;
+            bool fast_path = false;
+            if (join.is_flattening_step) {
+                P v0 = sub(join.position, prev.position);
+                P v1 = sub(next.position, join.position);
+                fast_path = dot(v0, v1) > 0.0f;
+            }
+            if (fast_path) {
+                join.line_join = LYON_JOIN_MITER;
+                skip = flattened_step(prev, join, next);
+            } else {
+                compute_join_side_positions_vw(prev, join, next, options.miter_limit,
+                                               SIDE_POSITIVE);
+                compute_join_side_positions_vw(prev, join, next, options.miter_limit,
+                                               SIDE_NEGATIVE);
+                // Prevent folding when the other side is concave.
+                if (join.side[SIDE_POSITIVE].has_single) join.fold[SIDE_NEGATIVE] = false;
+                if (join.side[SIDE_NEGATIVE].has_single) join.fold[SIDE_POSITIVE] = false;
+                add_join_base_vertices(join, SIDE_NEGATIVE);
+                add_join_base_vertices(join, SIDE_POSITIVE);
+            }
+            if (!skip) {
+                if (count > 2) add_edge_triangles(prev, join);
+                tessellate_join(join);
+                if (count == 2) {
+                    firsts.push_back(prev);
+                    firsts.push_back(join);
+                }
+            }
+        }
+        if (skip) {
+            point_buffer.replace_last(next);
+        } else {
+            point_buffer.push(next);
+        }
+        return true;
+    }
+
+    // The step of the active mode: fixed width (stroke.rs:1521-1632) or variable.
+    bool step_impl(const EndpointData& next) {
+        return vw ? step_vw_impl(next) : fixed_width_step_impl(next);
+    }
+
+    void step(const EndpointData& next) {  // stroke.rs:1515-1519
+        try {
+            step_impl(next);
+        } catch (const TessError& e) {
+            set_error(e.code);
+        }
+    }
+
+    // Events of tessellate_with_ids_vw (stroke.rs:654-767): the half width of an endpoint is
+    // line_width x its factor x 0.5; along a curve the width is interpolated linearly in t
+    // (stroke.rs:996-1067, with flatten_quad's t mapping, stroke.rs:2755-2779).
+    void begin_vw(P position, float w) {
+        may_need_empty_cap = false;
+        EndpointData d = make_point(position);
+        d.half_width = options.line_width * w * 0.5f;
+        d.advancement = sub_path_start_advancement;
+        step(d);
+    }
+    void line_to_vw(P to, float w) {
+        EndpointData d = make_point(to);
+        d.half_width = options.line_width * w * 0.5f;
+        step(d);
+    }
+    void curve_point_vw(P position, float t, bool is_flattening_step, float start_width,
+                        float end_width) {
+        EndpointData d = make_point(position);
+        d.half_width = (start_width * (1.0f - t) + end_width * t) * 0.5f;
+        d.is_flattening_step = is_flattening_step;
+        step(d);
+    }
+    void quadratic_bezier_to_vw(const Quad& curve, float w0, float w1) {
+        float sw = options.line_width * w0, ew = options.line_width * w1;
+        float t_split;
+        if (find_sharp_turn(curve, &t_split)) {
+            Quad before, after;
+            quad_split(curve, t_split, &before, &after);
+            quad_flatten_with_t(before, options.tolerance, [&](P, P to, float, float t1) {
+                curve_point_vw(to, t1 * t_split, t1 != 1.0f, sw, ew);
+            });
+            quad_flatten_with_t(after, options.tolerance, [&](P, P to, float, float t1) {
+                curve_point_vw(to, t_split + t1 * (1.0f - t_split), t1 != 1.0f, sw, ew);
+            });
+        } else {
+            quad_flatten_with_t(curve, options.tolerance, [&](P, P to, float, float t1) {
+                curve_point_vw(to, t1, t1 != 1.0f, sw, ew);
+            });
+        }
+    }
+    void cubic_bezier_to_vw(const Cubic& curve, float w0, float w1) {
+        float sw = options.line_width * w0, ew = options.line_width * w1;
+        cubic_flatten_with_t(curve, options.tolerance, [&](P, P to, float, float t1) {
+            curve_point_vw(to, t1, t1 != 1.0f, sw, ew);
+        });
+    }
+
     EndpointData make_point(P position) const {
         EndpointData d;
         d.position = position;
@@ -1063,10 +1278,13 @@ struct Stroker {
         if (count >= 2) {
             EndpointData p0 = point_buffer.second_last();
             EndpointData p1 = point_buffer.last();
-            P tan = normalize(sub(p1.position, p0.position));
-            P n = mul(P{-tan.y, tan.x}, p1.half_width);
-            p1.side[SIDE_POSITIVE].prev = add(p1.position, n);
-            p1.side[SIDE_NEGATIVE].prev = sub(p1.position, n);
+            if (!vw) {
+                // With a fixed width only the joins have side points so far (stroke.rs:1338-1346).
+                P tan = normalize(sub(p1.position, p0.position));
+                P n = mul(P{-tan.y, tan.x}, p1.half_width);
+                p1.side[SIDE_POSITIVE].prev = add(p1.position, n);
+                p1.side[SIDE_NEGATIVE].prev = sub(p1.position, n);
+            }
             bool is_first = count == 2;
             tessellate_last_edge(p0, p1, is_first);
             sub_path_start_advancement = p1.advancement;
@@ -1085,11 +1303,11 @@ struct Stroker {
         EndpointData p = firsts[0];
         float advancement = p.advancement;
         p.advancement = NAN;
-        bool segment_added = fixed_width_step_impl(p);
+        bool segment_added = step_impl(p);
         if (!segment_added) point_buffer.last().position = p.position;
         if (firsts.size() >= 2) {
             EndpointData p2 = firsts[1];
-            fixed_width_step_impl(p2);
+            step_impl(p2);
             EndpointData& p0 = point_buffer.second_last();
             EndpointData& p1 = point_buffer.last();
             vertex.position_on_path = p0.position;
@@ -1130,16 +1348,20 @@ struct Stroker {
         while (it.next(&e)) {
             switch (e.kind) {
                 case EV_BEGIN:
-                    begin_fw(e.to);
+                    if (vw) begin_vw(e.to, e.w_to);
+                    else begin_fw(e.to);
                     break;
                 case EV_LINE:
-                    line_to_fw(e.to);
+                    if (vw) line_to_vw(e.to, e.w_to);
+                    else line_to_fw(e.to);
                     break;
                 case EV_QUAD:
-                    quadratic_bezier_to_fw(Quad{e.from, e.ctrl1, e.to});
+                    if (vw) quadratic_bezier_to_vw(Quad{e.from, e.ctrl1, e.to}, e.w_from, e.w_to);
+                    else quadratic_bezier_to_fw(Quad{e.from, e.ctrl1, e.to});
                     break;
                 case EV_CUBIC:
-                    cubic_bezier_to_fw(Cubic{e.from, e.ctrl1, e.ctrl2, e.to});
+                    if (vw) cubic_bezier_to_vw(Cubic{e.from, e.ctrl1, e.ctrl2, e.to}, e.w_from, e.w_to);
+                    else cubic_bezier_to_fw(Cubic{e.from, e.ctrl1, e.ctrl2, e.to});
                     break;
                 case EV_END:
                     end(e.close);
@@ -2484,6 +2706,22 @@ int lyon_oracle_stroke_path(lyon_oracle_out* o, const uint8_t* verbs, uint32_t n
     return r;
 }
 
+// The same with StrokeOptions::variable_line_width: `widths` holds one factor per point (only
+// the endpoints' are read); an endpoint's line width is options->line_width times its factor
+// (stroke.rs:646-767).
+int lyon_oracle_stroke_path_vw(lyon_oracle_out* o, const uint8_t* verbs, uint32_t num_verbs,
+                               const float* points, uint32_t num_points, const float* widths,
+                               const lyon_stroke_options* options) {
+    g_near_ties = 0;
+    Stroker s(*options, &o->out);
+    s.vw = true;
+    PathIter it{verbs, num_verbs, points, num_points};
+    it.widths = widths;
+    int r = s.tessellate(it);
+    o->near_ties += g_near_ties;
+    return r;
+}
+
 // FillTessellator::tessellate_path appending to the output.
 int lyon_oracle_fill_path(lyon_oracle_out* o, const uint8_t* verbs, uint32_t num_verbs,
                           const float* points, uint32_t num_points,
@@ -2527,17 +2765,19 @@ float lyon_oracle_wang(const float* pts, int n_ctrl, float tolerance) {
 // index counts, statuses and near-tie counts; when `vertices`/`indices` are non-NULL the
 // outputs are concatenated in path order (indices per path, i.e. LYON_INDEX_PER_PATH) and the
 // caller must size them from a previous counting call. kind: 0 = stroke, 1 = fill.
-int lyon_oracle_batch(int kind, const lyon_path_batch* batch, const void* options,
-                      uint32_t num_options, int index_bits, int num_threads,
+static int batch_impl(int kind, const lyon_path_batch* batch, const float* widths,
+                      const void* options, uint32_t num_options, int index_bits, int num_threads,
                       uint32_t* vtx_counts, uint32_t* idx_counts, int32_t* status,
                       uint32_t* near_ties, float* vertices, uint32_t* indices,
-                      const uint64_t* vtx_offsets, const uint64_t* idx_offsets) {
+                      const uint64_t* vtx_offsets, const uint64_t* idx_offsets,
+                      uint32_t* attributes) {
     uint32_t n = batch->num_paths;
     if (num_threads < 1) num_threads = 1;
     std::atomic<uint32_t> next{0};
     auto worker = [&]() {
         lyon_oracle_out o;
         o.out.max_index = index_bits == 16 ? 65535ull : 0xFFFFFFFEull;
+        o.out.want_attributes = attributes != nullptr;
         for (;;) {
             uint32_t begin = next.fetch_add(64);
             if (begin >= n) break;
@@ -2545,6 +2785,7 @@ int lyon_oracle_batch(int kind, const lyon_path_batch* batch, const void* option
             for (uint32_t i = begin; i < end; ++i) {
                 o.out.vertices.clear();
                 o.out.indices.clear();
+                o.out.attributes.clear();
                 o.near_ties = 0;
                 uint32_t v0 = batch->verb_offsets[i], v1 = batch->verb_offsets[i + 1];
                 uint32_t p0 = batch->point_offsets[i], p1 = batch->point_offsets[i + 1];
@@ -2552,8 +2793,14 @@ int lyon_oracle_batch(int kind, const lyon_path_batch* batch, const void* option
                 if (kind == 0) {
                     const lyon_stroke_options* so =
                         (const lyon_stroke_options*)options + (num_options > 1 ? i : 0);
-                    r = lyon_oracle_stroke_path(&o, batch->verbs + v0, v1 - v0,
-                                                batch->points + 2 * (size_t)p0, p1 - p0, so);
+                    if (widths) {
+                        r = lyon_oracle_stroke_path_vw(&o, batch->verbs + v0, v1 - v0,
+                                                       batch->points + 2 * (size_t)p0, p1 - p0,
+                                                       widths + p0, so);
+                    } else {
+                        r = lyon_oracle_stroke_path(&o, batch->verbs + v0, v1 - v0,
+                                                    batch->points + 2 * (size_t)p0, p1 - p0, so);
+                    }
                 } else {
                     const lyon_fill_options* fo =
                         (const lyon_fill_options*)options + (num_options > 1 ? i : 0);
@@ -2574,6 +2821,10 @@ int lyon_oracle_batch(int kind, const lyon_path_batch* batch, const void* option
                     std::memcpy(indices + idx_offsets[i], o.out.indices.data(),
                                 o.out.indices.size() * sizeof(uint32_t));
                 }
+                if (attributes && vtx_offsets) {
+                    std::memcpy(attributes + 4 * vtx_offsets[i], o.out.attributes.data(),
+                                o.out.attributes.size() * sizeof(uint32_t));
+                }
             }
         }
     };
@@ -2585,6 +2836,29 @@ int lyon_oracle_batch(int kind, const lyon_path_batch* batch, const void* option
         for (auto& t : th) t.join();
     }
     return LYON_OK;
+}
+
+int lyon_oracle_batch(int kind, const lyon_path_batch* batch, const void* options,
+                      uint32_t num_options, int index_bits, int num_threads,
+                      uint32_t* vtx_counts, uint32_t* idx_counts, int32_t* status,
+                      uint32_t* near_ties, float* vertices, uint32_t* indices,
+                      const uint64_t* vtx_offsets, const uint64_t* idx_offsets) {
+    return batch_impl(kind, batch, nullptr, options, num_options, index_bits, num_threads,
+                      vtx_counts, idx_counts, status, near_ties, vertices, indices, vtx_offsets,
+                      idx_offsets, nullptr);
+}
+
+// Batched stroke with a variable line width (`widths`: one factor per point of the batch) and,
+// when `attributes` is set, the stroke vertex attributes (four words per vertex).
+int lyon_oracle_batch_stroke_vw(const lyon_path_batch* batch, const float* widths,
+                                const void* options, uint32_t num_options, int index_bits,
+                                int num_threads, uint32_t* vtx_counts, uint32_t* idx_counts,
+                                int32_t* status, uint32_t* near_ties, float* vertices,
+                                uint32_t* indices, const uint64_t* vtx_offsets,
+                                const uint64_t* idx_offsets, uint32_t* attributes) {
+    return batch_impl(0, batch, widths, options, num_options, index_bits, num_threads,
+                      vtx_counts, idx_counts, status, near_ties, vertices, indices, vtx_offsets,
+                      idx_offsets, attributes);
 }
 
 // The stroke vertex attributes of every path of a batch (four words per vertex, see

@@ -65,6 +65,12 @@ def lib():
             L.lyon_oracle_batch_stroke_attributes.restype = ctypes.c_int
             L.lyon_oracle_batch_stroke_attributes.argtypes = [c_p, c_p, ctypes.c_uint32,
                                                               ctypes.c_int, c_p, c_p]
+            L.lyon_oracle_stroke_path_vw.restype = ctypes.c_int
+            L.lyon_oracle_stroke_path_vw.argtypes = [c_p, c_p, ctypes.c_uint32, c_p,
+                                                     ctypes.c_uint32, c_p, c_p]
+            L.lyon_oracle_batch_stroke_vw.restype = ctypes.c_int
+            L.lyon_oracle_batch_stroke_vw.argtypes = [c_p, c_p, c_p, ctypes.c_uint32,
+                                                      ctypes.c_int, ctypes.c_int] + [c_p] * 9
             L.lyon_oracle_batch.restype = ctypes.c_int
             L.lyon_oracle_batch.argtypes = [ctypes.c_int, c_p, c_p, ctypes.c_uint32, ctypes.c_int,
                                             ctypes.c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
@@ -129,10 +135,17 @@ class Output:
         return Result(status, v.reshape(-1, 2), i, self.L.lyon_oracle_out_near_ties(self.h),
                       self.index_bits, a)
 
-    def stroke(self, path, options):
+    def stroke(self, path, options, widths=None):
+        """`widths`: one variable-line-width factor per point (StrokeOptions::
+        variable_line_width), or None for a fixed width."""
         o = options.to_c()
         v = np.ascontiguousarray(path.verbs, dtype=np.uint8)
         p = np.ascontiguousarray(path.points, dtype=np.float32)
+        if widths is not None:
+            w = np.ascontiguousarray(widths, dtype=np.float32)
+            assert len(w) == len(p)
+            return self.L.lyon_oracle_stroke_path_vw(self.h, _ptr(v), len(v), _ptr(p), len(p),
+                                                     _ptr(w), ctypes.byref(o))
         return self.L.lyon_oracle_stroke_path(self.h, _ptr(v), len(v), _ptr(p), len(p),
                                               ctypes.byref(o))
 
@@ -145,9 +158,9 @@ class Output:
 
 
 def stroke(path, options, index_bits: int = 32, vertex_offset: int = 0,
-           attributes: bool = False) -> Result:
+           attributes: bool = False, widths=None) -> Result:
     out = Output(index_bits, vertex_offset, attributes)
-    st = out.stroke(path, options)
+    st = out.stroke(path, options, widths)
     return out.snapshot(st)
 
 
@@ -183,7 +196,8 @@ class _CBatch(ctypes.Structure):
 
 
 def batch(kind: str, pb, options_records: np.ndarray, index_bits: int = 32,
-          num_threads: int = 1, want_output: bool = True, want_attributes: bool = False):
+          num_threads: int = 1, want_output: bool = True, want_attributes: bool = False,
+          widths=None):
     """Tessellates every path of a PathBatch with the oracle (per-path buffers).
 
     Returns dict with per-path vertex/index counts, statuses, near-tie counts and, when
@@ -199,6 +213,30 @@ def batch(kind: str, pb, options_records: np.ndarray, index_bits: int = 32,
     st = np.zeros(n, np.int32)
     nt = np.zeros(n, np.uint32)
     k = 0 if kind == "stroke" else 1
+    if widths is not None:
+        # Variable line width: one factor per point of the batch.
+        assert kind == "stroke"
+        w = np.ascontiguousarray(widths, dtype=np.float32)
+        assert len(w) == len(pb.points)
+        L.lyon_oracle_batch_stroke_vw(ctypes.byref(cb), _ptr(w), _ptr(opts), len(opts),
+                                      index_bits, num_threads, _ptr(vc), _ptr(ic), _ptr(st),
+                                      _ptr(nt), None, None, None, None, None)
+        res = {"vtx_counts": vc, "idx_counts": ic, "status": st, "near_ties": nt}
+        if want_output:
+            vo = np.zeros(n + 1, np.uint64)
+            io = np.zeros(n + 1, np.uint64)
+            vo[1:] = np.cumsum(vc, dtype=np.uint64)
+            io[1:] = np.cumsum(ic, dtype=np.uint64)
+            verts = np.zeros((int(vo[-1]), 2), np.float32)
+            idx = np.zeros(int(io[-1]), np.uint32)
+            attrs = np.zeros((int(vo[-1]), 4), np.uint32) if want_attributes else None
+            L.lyon_oracle_batch_stroke_vw(ctypes.byref(cb), _ptr(w), _ptr(opts), len(opts),
+                                          index_bits, num_threads, None, None, None, None,
+                                          _ptr(verts), _ptr(idx), _ptr(vo), _ptr(io), _ptr(attrs))
+            res.update(vertices=verts, indices=idx, vtx_offsets=vo, idx_offsets=io)
+            if want_attributes:
+                res["attributes"] = attrs
+        return res
     L.lyon_oracle_batch(k, ctypes.byref(cb), _ptr(opts), len(opts), index_bits, num_threads,
                         _ptr(vc), _ptr(ic), _ptr(st), _ptr(nt), None, None, None, None)
     res = {"vtx_counts": vc, "idx_counts": ic, "status": st, "near_ties": nt}

@@ -58,30 +58,40 @@ class PathBuild:
     def __init__(self):
         self.verbs = []
         self.points = []
+        # The first endpoint attribute of every point (lyon stores attributes per endpoint;
+        # control points get 0.0, which nothing reads).
+        self.widths = []
         self.first = None
+        self.first_w = 0.0
         self.open = False
 
-    def begin(self, p):
+    def begin(self, p, w=0.0):
         self.first = p
+        self.first_w = w
         self.points.append(p)
+        self.widths.append(w)
         self.verbs.append(VERB_BEGIN)
         self.open = True
 
-    def line_to(self, p):
+    def line_to(self, p, w=0.0):
         self.points.append(p)
+        self.widths.append(w)
         self.verbs.append(VERB_LINE)
 
-    def quad_to(self, c, p):
+    def quad_to(self, c, p, w=0.0):
         self.points += [c, p]
+        self.widths += [0.0, w]
         self.verbs.append(VERB_QUAD)
 
-    def cubic_to(self, c1, c2, p):
+    def cubic_to(self, c1, c2, p, w=0.0):
         self.points += [c1, c2, p]
+        self.widths += [0.0, 0.0, w]
         self.verbs.append(VERB_CUBIC)
 
     def end(self, close):
         if close:
             self.points.append(self.first)
+            self.widths.append(self.first_w)
         self.verbs.append(VERB_CLOSE if close else VERB_END)
         self.open = False
 
@@ -127,10 +137,12 @@ def parse_builder_calls(body):
         args = body[m.end():i - 1]
         pos = i
         pts = [(f32(a), f32(b)) for a, b in re.findall(POINT, args)]
+        attr = re.search(r"&\[\s*(" + NUM + r")", args)
+        w = f32(attr.group(1)) if attr else 0.0
         if method == "begin":
             if len(pts) != 1:
                 return None
-            pb.begin(pts[0])
+            pb.begin(pts[0], w)
         elif method == "move_to":
             if len(pts) != 1:
                 return None
@@ -141,15 +153,15 @@ def parse_builder_calls(body):
         elif method == "line_to":
             if len(pts) != 1 or not pb.open:
                 return None
-            pb.line_to(pts[0])
+            pb.line_to(pts[0], w)
         elif method == "quadratic_bezier_to":
             if len(pts) != 2 or not pb.open:
                 return None
-            pb.quad_to(*pts)
+            pb.quad_to(*pts, w)
         elif method == "cubic_bezier_to":
             if len(pts) != 3 or not pb.open:
                 return None
-            pb.cubic_to(*pts)
+            pb.cubic_to(*pts, w)
         elif method == "end":
             a = args.strip()
             if a not in ("true", "false"):
@@ -253,6 +265,27 @@ def stroke_cases(ref):
     pb = parse_builder_calls(body)
     add("test_line_width", pb, {"line_width": 2.0}, None,
         vertices_in=[[0.0, 0.0], [0.0, 2.0], [2.0, 0.0], [2.0, 2.0]])
+
+    # The variable-line-width runs of test_square and test_empty_caps (the same expectations,
+    # StrokeOptions::default().with_variable_line_width(0)) and the variable-width regressions.
+    for name in ("test_square", "test_empty_caps"):
+        line, body = tests[name]
+        assert "with_variable_line_width(0)" in body
+        pb = parse_builder_calls(body)
+        for c in [c for c in out if c["name"] == name]:
+            d = dict(c)
+            d["options"] = dict(c["options"], variable_line_width=True)
+            d["widths"] = pb.widths
+            out.append(d)
+    for name, tol_re in (("issue_821", r"with_tolerance\((" + NUM + r")\)"),
+                         ("issue_894", r"StrokeOptions::tolerance\((" + NUM + r")\)")):
+        line, body = tests[name]
+        assert "with_variable_line_width" in body and "LineCap::Round" in body
+        pb = parse_builder_calls(body)
+        tol = re.search(tol_re, body).group(1)
+        add(name, pb, {"tolerance": f32(tol), "line_cap": "Round",
+                       "variable_line_width": True}, None,
+            widths=pb.widths, must_succeed=(name == "issue_821"), no_internal_error=True)
 
     line, body = tests["correct_miter_clip_length"]
     pb = PathBuild()

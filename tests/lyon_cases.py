@@ -41,6 +41,8 @@ def stroke_options_from_case(opts: dict) -> StrokeOptions:
             o = o.with_miter_limit(float(v))
         elif k == "line_width":
             o = o.with_line_width(float(v))
+        elif k == "variable_line_width":
+            pass  # the case's per-point `widths` carry the attribute
         else:
             raise KeyError(k)
     return o

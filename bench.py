@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-polylines", action="store_true")
+    ap.add_argument("--no-variable-width", action="store_true")
+    ap.add_argument("--vw-paths", type=int, default=200_000)
     ap.add_argument("--polyline-paths", type=int, default=2_000_000)
     ap.add_argument("--serve-seconds", type=float, default=0.1)
     ap.add_argument("--profile-fill", action="store_true",
@@ -351,6 +353,8 @@ def main():
             line["fill"] = run_fill(ctx, args, T, world)
         if not args.no_polylines:
             line["polylines_autotuned"] = run_polylines(ctx, args, T)
+        if not args.no_variable_width:
+            line["variable_width"] = run_variable_width(ctx, args, T)
         if not args.no_serve and world == 1:
             del db, od
             ctx.close()
@@ -425,6 +429,55 @@ def run_fill(ctx, args, T, world, batch=None):
                                  "sample": f"first {n} paths, {cv} output vertices, "
                                            f"{dt:.2f} s wall on {threads} threads"}
         out[name] = entry
+    return out
+
+
+def run_variable_width(ctx, args, T):
+    """Variable line width (StrokeOptions::variable_line_width): the batched-stroke generator's
+    paths (seed 2, round joins and caps, tolerance 0.05) with a width factor per point drawn from
+    U[0.5, 2]; one thread per path. CPU baseline: the oracle on a sample."""
+    import torch
+    from lyon_gb300 import workloads
+    from oracle import lyon_oracle as orc
+    batch, opts = workloads.batched_stroke(args.vw_paths, seed=2)
+    widths = np.random.default_rng(21).uniform(0.5, 2.0, size=len(batch.points)).astype(
+        np.float32)
+    db = T.DeviceBatch.upload(batch, 0)
+    od = T.upload_options(opts, 0)
+    wd = torch.from_numpy(widths).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    res = T.tessellate_paths("stroke", db, od, len(opts), 32, T.INDEX_GLOBAL, 0, ctx, widths=wd)
+    ctx.synchronize()
+    steps = max(1, args.steps)
+    launches0 = ctx.lib.lyon_gpu_kernel_launches()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        res = T.tessellate_paths("stroke", db, od, len(opts), 32, T.INDEX_GLOBAL, 0, ctx,
+                                 widths=wd)
+    end.record(stream)
+    end.synchronize()
+    ms = start.elapsed_time(end) / steps
+    out = {"workload": f"variable_width_{batch.num_paths}_paths",
+           "config": {"paths": batch.num_paths, "generator": "batched stroke, seed 2",
+                      "width_factors": "U[0.5, 2] per point, seed 21", "index_bits": 32,
+                      "index_mode": "global"},
+           "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
+           "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
+           "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
+    threads = os.cpu_count() or 1
+    n = min(20_000, batch.num_paths)
+    sub = batch.head(n)
+    t0 = time.perf_counter()
+    r = orc.batch("stroke", sub, opts[:n], 32, threads, want_output=False,
+                  widths=widths[:int(batch.point_offsets[n])])
+    dt = time.perf_counter() - t0
+    cv = int(r["vtx_counts"].sum())
+    out["cpu_baseline"] = {"value": cv / dt, "unit": "vertices/s", "cores": threads,
+                           "kind": "port",
+                           "sample": f"first {n} paths, {cv} output vertices, "
+                                     f"{dt:.2f} s wall on {threads} threads"}
     return out
 
 

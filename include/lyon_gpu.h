@@ -170,6 +170,16 @@ int lyon_gpu_stroke_path_attributes(lyon_gpu_context* ctx, const uint8_t* verbs,
                                     const lyon_stroke_options* options, int index_bits,
                                     uint32_t index_base, lyon_gpu_result* result);
 
+/* lyon_gpu_stroke_path with StrokeOptions::variable_line_width: `widths` (host memory) holds one
+ * width factor per point, as for lyon_gpu_stroke_paths_variable_width. `vertex_attributes`
+ * non-zero makes `result->vertices` point at lyon_stroke_vertex records. */
+int lyon_gpu_stroke_path_variable_width(lyon_gpu_context* ctx, const uint8_t* verbs,
+                                        uint32_t num_verbs, const float* points,
+                                        uint32_t num_points, const float* widths,
+                                        const lyon_stroke_options* options, int index_bits,
+                                        uint32_t index_base, int vertex_attributes,
+                                        lyon_gpu_result* result);
+
 /* FillTessellator::tessellate_path(path, options, &mut BuffersBuilder)
  * (crates/tessellation/src/fill.rs:628-641), `Positions` vertices. Same conventions as above. */
 int lyon_gpu_fill_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
@@ -214,6 +224,20 @@ int lyon_gpu_stroke_paths_attributes(lyon_gpu_context* ctx, const lyon_path_batc
                                      const lyon_stroke_options* options, uint32_t num_options,
                                      int index_bits, int index_mode, uint32_t vertex_offset,
                                      lyon_gpu_batch_output* out);
+
+/* StrokeTessellator::tessellate_path with StrokeOptions::variable_line_width
+ * (crates/tessellation/src/stroke.rs:646-767, 954-1067, 1380-1512): the path's endpoints carry a
+ * width factor and an endpoint's line width is options.line_width times its factor (linearly
+ * interpolated along curves). `widths` (device memory) holds one factor per point of the batch,
+ * indexed like `points`; entries of control points and of Close's repeated point are not read.
+ * `vertex_attributes` non-zero writes lyon_stroke_vertex records instead of positions. The rest
+ * is as for lyon_gpu_stroke_paths. Each path is stroked by one thread. */
+int lyon_gpu_stroke_paths_variable_width(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                                         const float* widths,
+                                         const lyon_stroke_options* options,
+                                         uint32_t num_options, int index_bits, int index_mode,
+                                         uint32_t vertex_offset, int vertex_attributes,
+                                         lyon_gpu_batch_output* out);
 
 /* Largest batch lyon_gpu_stroke_paths_noalloc accepts (its fixed scratch holds this many paths). */
 #define LYON_NOALLOC_MAX_PATHS 262144u

@@ -150,6 +150,13 @@ def load(build_if_missing: bool = True):
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [c_p, ctypes.POINTER(CStrokeTuning)]
+        L.lyon_gpu_stroke_paths_variable_width.restype = ctypes.c_int
+        L.lyon_gpu_stroke_paths_variable_width.argtypes = [c_p, c_p, c_p, c_p, u32,
+                                                           ctypes.c_int, ctypes.c_int, u32,
+                                                           ctypes.c_int, c_p]
+        L.lyon_gpu_stroke_path_variable_width.restype = ctypes.c_int
+        L.lyon_gpu_stroke_path_variable_width.argtypes = [c_p, c_p, u32, c_p, u32, c_p, c_p,
+                                                          ctypes.c_int, u32, ctypes.c_int, c_p]
         L.lyon_gpu_autotune_stroke.restype = ctypes.c_int
         L.lyon_gpu_autotune_stroke.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
                                                ctypes.POINTER(CStrokeTuning),
@@ -176,4 +183,5 @@ EXPORTED = [
     "lyon_srv_release", "lyon_srv_run_load", "lyon_gpu_set_stroke_tuning",
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
     "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",
+    "lyon_gpu_stroke_paths_variable_width", "lyon_gpu_stroke_path_variable_width",
 ]

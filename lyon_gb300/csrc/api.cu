@@ -51,6 +51,7 @@ struct lyon_gpu_context {
     uint32_t blocks_per_sm = 0;        // 0: as many as fit
     uint32_t short_path_points = 32;   // line-only paths up to this size: one per thread
     bool vertex_attrs = false;  // during a *_attributes call: lyon_stroke_vertex records
+    const float* vw_widths = nullptr;  // during a variable-width call: width factors (device)
     // outputs of device-buffer batched calls
     DevBuf out_vertices, out_indices;
     // host-buffer calls: inputs and double-buffered outputs
@@ -63,7 +64,7 @@ struct lyon_gpu_context {
     // flatten outputs
     DevBuf flat_counts, flat_offsets, flat_points;
     // single-path staging
-    DevBuf in_verbs, in_points, in_offsets, in_options;
+    DevBuf in_verbs, in_points, in_offsets, in_options, in_widths;
     HostBuf h_verbs, h_points, h_out_v, h_out_i, h_small, h_offs, h_status;
     // optional per-path first path of its request (serving batches: one id space per request)
     const uint32_t* request_first = nullptr;
@@ -296,6 +297,7 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
     a.index_mode = index_mode;
     a.vertex_offset = (uint32_t)vertex_offset;
     a.vertex_attrs = ctx->vertex_attrs ? 1 : 0;
+    a.widths = ctx->vw_widths;
     a.request_first = ctx->request_first;
     if (ctx->split_valid) {
         a.item_split = as<uint32_t>(ctx->class_counters) + 2 * (3 + ctx->short_path_points);
@@ -328,7 +330,9 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     if (kind == KIND_STROKE) {
         // Long paths first, so that no single long path is left running at the end of a launch;
         // short line-only paths last, for the one-thread-per-path phase.
-        if (n > 0 && ctx->short_path_points > 0) {
+        if (ctx->vw_widths) {
+            // The variable-width kernel takes paths in index order.
+        } else if (n > 0 && ctx->short_path_points > 0) {
             if (ensure(ctx, ctx->order, (size_t)n * 4) && ensure(ctx, ctx->path_class, n) &&
                 ensure(ctx, ctx->class_counters, lg::CLASSIFY_COUNTER_WORDS * 4) &&
                 lg::launch_classify_paths(batch->verbs, batch->verb_offsets,
@@ -560,13 +564,15 @@ int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, con
 // Copies a host path into the context's device input arena (one-path batch).
 bool stage_single_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
                        const float* points, uint32_t num_points, const void* options,
-                       size_t options_size, lyon_path_batch* batch) {
+                       size_t options_size, lyon_path_batch* batch,
+                       const float* widths = nullptr) {
     cudaStream_t s = ctx->stream;
-    size_t vb = num_verbs, pb = (size_t)num_points * 8;
+    size_t vb = num_verbs, pb = (size_t)num_points * 8, wb = widths ? (size_t)num_points * 4 : 0;
     if (!ensure(ctx, ctx->in_verbs, vb + 16) || !ensure(ctx, ctx->in_points, pb + 16) ||
         !ensure(ctx, ctx->in_offsets, 64) || !ensure(ctx, ctx->in_options, 64) ||
+        (widths && !ensure(ctx, ctx->in_widths, wb + 16)) ||
         !ensure_host(ctx, ctx->h_verbs, vb + 128 + options_size) ||
-        !ensure_host(ctx, ctx->h_points, pb + 16))
+        !ensure_host(ctx, ctx->h_points, pb + wb + 16))
         return false;
     cudaStreamSynchronize(s);
     unsigned char* hv = reinterpret_cast<unsigned char*>(ctx->h_verbs.ptr);
@@ -583,6 +589,11 @@ bool stage_single_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num
     if (num_verbs) cudaMemcpyAsync(ctx->in_verbs.ptr, hv + 64, vb, cudaMemcpyHostToDevice, s);
     if (num_points)
         cudaMemcpyAsync(ctx->in_points.ptr, ctx->h_points.ptr, pb, cudaMemcpyHostToDevice, s);
+    if (widths && num_points) {
+        unsigned char* hw = reinterpret_cast<unsigned char*>(ctx->h_points.ptr) + pb;
+        memcpy(hw, widths, wb);
+        cudaMemcpyAsync(ctx->in_widths.ptr, hw, wb, cudaMemcpyHostToDevice, s);
+    }
     batch->verbs = as<uint8_t>(ctx->in_verbs);
     batch->points = as<float>(ctx->in_points);
     batch->verb_offsets = as<uint32_t>(ctx->in_offsets);
@@ -593,7 +604,8 @@ bool stage_single_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num
 
 int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t num_verbs,
                 const float* points, uint32_t num_points, const void* options, size_t opt_size,
-                int index_bits, uint32_t index_base, lyon_gpu_result* result) {
+                int index_bits, uint32_t index_base, lyon_gpu_result* result,
+                const float* widths = nullptr) {
     if (!ctx || !options || !result || (index_bits != 16 && index_bits != 32) ||
         (num_verbs && !verbs) || (num_points && !points)) {
         if (ctx) ctx->last_error = "invalid argument";
@@ -602,8 +614,10 @@ int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t 
     cudaSetDevice(ctx->device);
     memset(result, 0, sizeof(*result));
     lyon_path_batch b;
-    if (!stage_single_path(ctx, verbs, num_verbs, points, num_points, options, opt_size, &b))
+    if (!stage_single_path(ctx, verbs, num_verbs, points, num_points, options, opt_size, &b,
+                           widths))
         return LYON_ERR_OUT_OF_MEMORY;
+    if (widths) ctx->vw_widths = as<float>(ctx->in_widths);
     lyon_gpu_batch_output bo;
     int r = batched_device(ctx, kind, &b, ctx->in_options.ptr, 1, index_bits,
                            LYON_INDEX_PER_PATH, index_base, &bo);
@@ -707,7 +721,8 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->slot_i[0],  &ctx->slot_i[1],   &ctx->flat_counts, &ctx->flat_offsets,
                       &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
                       &ctx->in_options, &ctx->order, &ctx->slot_status[0],
-                      &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters};
+                      &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters,
+                      &ctx->in_widths};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
     HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v, &ctx->h_out_i, &ctx->h_small,
@@ -848,6 +863,22 @@ int lyon_gpu_stroke_paths_attributes(lyon_gpu_context* ctx, const lyon_path_batc
     return r;
 }
 
+int lyon_gpu_stroke_paths_variable_width(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                                         const float* widths,
+                                         const lyon_stroke_options* options,
+                                         uint32_t num_options, int index_bits, int index_mode,
+                                         uint32_t vertex_offset, int vertex_attributes,
+                                         lyon_gpu_batch_output* out) {
+    if (!ctx || (!widths && batch && batch->num_paths > 0)) return LYON_ERR_INVALID_ARGUMENT;
+    ctx->vertex_attrs = vertex_attributes != 0;
+    ctx->vw_widths = widths;
+    int r = batched_device(ctx, KIND_STROKE, batch, options, num_options, index_bits, index_mode,
+                           vertex_offset, out);
+    ctx->vertex_attrs = false;
+    ctx->vw_widths = nullptr;
+    return r;
+}
+
 int lyon_gpu_fill_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                         const lyon_fill_options* options, uint32_t num_options, int index_bits,
                         int index_mode, uint32_t vertex_offset, lyon_gpu_batch_output* out) {
@@ -895,6 +926,23 @@ int lyon_gpu_stroke_path_attributes(lyon_gpu_context* ctx, const uint8_t* verbs,
     int r = single_path(ctx, KIND_STROKE, verbs, num_verbs, points, num_points, options,
                         sizeof(lyon_stroke_options), index_bits, index_base, result);
     ctx->vertex_attrs = false;
+    return r;
+}
+
+int lyon_gpu_stroke_path_variable_width(lyon_gpu_context* ctx, const uint8_t* verbs,
+                                        uint32_t num_verbs, const float* points,
+                                        uint32_t num_points, const float* widths,
+                                        const lyon_stroke_options* options, int index_bits,
+                                        uint32_t index_base, int vertex_attributes,
+                                        lyon_gpu_result* result) {
+    if (!ctx || (num_points && !widths)) return LYON_ERR_INVALID_ARGUMENT;
+    static const float kNoPoints = 1.0f;
+    ctx->vertex_attrs = vertex_attributes != 0;
+    int r = single_path(ctx, KIND_STROKE, verbs, num_verbs, points, num_points, options,
+                        sizeof(lyon_stroke_options), index_bits, index_base, result,
+                        num_points ? widths : &kNoPoints);
+    ctx->vertex_attrs = false;
+    ctx->vw_widths = nullptr;
     return r;
 }
 

@@ -37,6 +37,9 @@ struct StrokeArgs {
     // Non-zero: `vertices` receives lyon_stroke_vertex records (position, normal, advancement,
     // side) instead of positions.
     int vertex_attrs;
+    // Non-null: variable line width, one width factor per point of the batch (indexed like
+    // `points`); the paths are stroked by the variable-width kernel (one thread per path).
+    const float* widths;
     // Optional, per path: the first path of the request it belongs to. In LYON_INDEX_GLOBAL mode
     // ids then count from that path's first vertex (one VertexBuffers per request of a batch).
     const uint32_t* request_first;

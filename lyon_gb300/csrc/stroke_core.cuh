@@ -186,6 +186,7 @@ __device__ __forceinline__ float cr_atan2(float y, float x) { return (float)atan
 __device__ __forceinline__ float cr_acos(float x) { return (float)acos((double)x); }
 __device__ __forceinline__ float cr_cos(float x) { return (float)cos((double)x); }
 __device__ __forceinline__ float cr_sin(float x) { return (float)sin((double)x); }
+__device__ __forceinline__ float cr_asin(float x) { return (float)asin((double)x); }
 
 // An arc's subdivision count is ceil(|diff| / step) with diff from two atan2 values and step from
 // acos (stroke.rs:1986-2004, 2482-2490, 2749-2753). f32 libms differ by an ulp between
@@ -777,6 +778,12 @@ struct SeqBuffer {
         }
         ++n;
     }
+    __device__ __forceinline__ DEP& first() { return pts[start % 3]; }
+    // PointBuffer::replace_last (stroke.rs:2400-2406).
+    __device__ __forceinline__ void replace_last(const DEP& p) {
+        const uint32_t idx = start == 0 ? count : start;
+        pts[idx - 1] = p;
+    }
 };
 
 template <class SK>
@@ -811,6 +818,207 @@ __device__ __noinline__ bool seq_step(SeqBuffer& pb, DEP next, const StrokeParam
     }
     pb.push(next);
     return true;
+}
+
+
+// ---- variable line width (StrokeOptions::variable_line_width) -------------------------------
+// One thread strokes a whole path with lyon's sequential variable-width stepper. The edge
+// attachment angles are evaluated in f64 with one rounding (cr_*), as in the oracle; lyon takes
+// them from the platform's f32 libm.
+
+struct VwState {
+    SeqBuffer pb;
+    DEP firsts[2];
+    uint32_t nfirsts;
+    bool mnec;          // may_need_empty_cap
+    float start_adv;    // sub_path_start_advancement
+};
+
+// stroke.rs:1842-1866
+__device__ __forceinline__ void vw_side_attachment(DEP& p0, DEP& p1, float edge_angle,
+                                                   float vwidth_angle, int side) {
+    const float nl = side == SN ? -1.0f : 1.0f;
+    const float normal_angle = edge_angle + nl * (LG_PI_F * 0.5f + vwidth_angle);
+    const V2 normal = V2{cr_cos(normal_angle), cr_sin(normal_angle)};
+    p0.s[side].next = p0.pos + normal * p0.hw;
+    p1.s[side].prev = p1.pos + normal * p1.hw;
+}
+
+// stroke.rs:1808-1840
+__device__ __noinline__ void vw_edge_attachments(DEP& p0, DEP& p1) {
+    const V2 edge = p1.pos - p0.pos;
+    const float d = vlength(edge);
+    const float edge_angle = cr_atan2(edge.y, edge.x);
+    const float sin_vwidth_angle = (p1.hw - p0.hw) / d;
+    float vwidth_angle = cr_asin(sin_vwidth_angle);
+    if (isnan(vwidth_angle)) vwidth_angle = 0.0f;
+    vw_side_attachment(p0, p1, edge_angle, vwidth_angle, SP);
+    vw_side_attachment(p0, p1, edge_angle, vwidth_angle, SN);
+    if (isnan(p1.adv)) p1.adv = p0.adv + d;
+}
+
+// stroke.rs:2060-2128
+__device__ __noinline__ void vw_join_sides(const DEP& prev, DEP& join, const DEP& next,
+                                           float miter_limit, int side) {
+    const float sign = side == SN ? -1.0f : 1.0f;
+    const V2 v0 = normalize(join.s[side].prev - prev.s[side].next);
+    const V2 v1 = normalize(next.s[side].prev - join.s[side].next);
+    const bool inward = cross(v0, v1) * sign > 0.0f;
+    const bool forward = dot(v0, v1) > 0.0f;
+    const V2 normal = compute_normal(v0, v1) * sign;
+    const V2 path_v0 = normalize(join.pos - prev.pos);
+    const V2 path_v1 = normalize(next.pos - join.pos);
+    const bool normal_same_side = dot(v0 + v1, path_v0 + path_v1) >= 0.0f;
+    const bool angle_is_sharp = inward && !forward && normal_same_side;
+    if (angle_is_sharp) {
+        const V2 extruded_normal = normal * join.hw;
+        const float prev_length = join.adv - prev.adv;
+        const float next_length = next.adv - join.adv;
+        const float d_next = dot(extruded_normal, v1) - next_length;
+        const float d_prev = dot(extruded_normal, -v0) - prev_length;
+        if (fminf(d_next, d_prev) > 0.0f || sqlen(normal) < 1e-5f) join.fold[side] = true;
+    }
+    const bool concave = inward && normal_same_side && !join.fold[side];
+    if (concave || ((join.join == LYON_JOIN_MITER || join.join == LYON_JOIN_MITER_CLIP) &&
+                    !miter_limit_exceeded(normal, miter_limit))) {
+        join.s[side].has_single = true;
+        join.s[side].single = join.pos + normal * join.hw;
+    } else if (join.join == LYON_JOIN_MITER_CLIP) {
+        const V2 n0 = join.s[side].prev - join.pos;
+        const V2 n1 = join.s[side].next - join.pos;
+        V2 pn, nn;
+        get_clip_intersections(n0, n1, normal, miter_limit * join.hw, &pn, &nn);
+        join.s[side].prev = join.pos + pn;
+        join.s[side].next = join.pos + nn;
+    }
+}
+
+// step_impl (stroke.rs:1380-1512). Returns false when `next` merged into the last point.
+template <class SK>
+__device__ __noinline__ bool vw_step(VwState& W, DEP next, const StrokeParams& P, SK& sink,
+                                     int* status) {
+    SeqBuffer& pb = W.pb;
+    const uint32_t count = pb.count;
+    if (count > 0 && too_close(pb.last().pos, next.pos, P.merge_threshold)) {
+        if (count == 1) W.mnec = true;
+        return false;
+    }
+    if (count > 0) {
+        DEP& join = pb.last();
+        if (!join.is_flat || !next.is_flat) vw_edge_attachments(join, next);
+    }
+    bool skip = false;
+    if (count > 1) {
+        DEP& prev = pb.second_last();
+        DEP& join = pb.last();
+        sink.adv = join.adv;
+        bool fast = false;
+        if (join.is_flat) fast = dot(join.pos - prev.pos, next.pos - join.pos) > 0.0f;
+        if (fast) {
+            // flattened_step (stroke.rs:1743-1806)
+            join.join = LYON_JOIN_MITER;
+            const V2 prev_edge = join.pos - prev.pos;
+            const float prev_length = vlength(prev_edge);
+            const V2 prev_tangent = prev_edge / prev_length;
+            const V2 next_edge = next.pos - join.pos;
+            const float next_length = vlength(next_edge);
+            const V2 next_tangent = next_edge / next_length;
+            const V2 normal = compute_normal(prev_tangent, next_tangent);
+            if (isnan(join.adv)) join.adv = prev.adv + prev_length;
+            if (isnan(next.adv)) next.adv = join.adv + next_length;
+            sink.adv = join.adv;
+            const V2 p0 = join.pos + normal * join.hw;
+            const V2 p1 = join.pos - normal * join.hw;
+            join.s[SP].prev = join.s[SP].next = join.s[SP].single = p0;
+            join.s[SP].has_single = true;
+            join.s[SN].prev = join.s[SN].next = join.s[SN].single = p1;
+            join.s[SN].has_single = true;
+            const V2 v0 = p0 - prev.s[SP].next;
+            const V2 v1 = p1 - prev.s[SN].next;
+            if (dot(prev_edge, v0) < 0.0f && dot(prev_edge, v1) < 0.0f) {
+                skip = true;
+            } else {
+                const uint32_t pv = sink.vertex(join.pos + normal * join.hw, normal, SP);
+                const uint32_t nv = sink.vertex(join.pos + (-normal) * join.hw, -normal, SN);
+                join.s[SP].prev_vertex = join.s[SP].next_vertex = pv;
+                join.s[SN].prev_vertex = join.s[SN].next_vertex = nv;
+            }
+        } else {
+            vw_join_sides(prev, join, next, P.miter_limit, SP);
+            vw_join_sides(prev, join, next, P.miter_limit, SN);
+            // Prevent folding when the other side is concave.
+            if (join.s[SP].has_single) join.fold[SN] = false;
+            if (join.s[SN].has_single) join.fold[SP] = false;
+            add_join_base_vertices(join, SN, sink);
+            add_join_base_vertices(join, SP, sink);
+        }
+        if (!skip) {
+            if (count > 2) add_edge_triangles(prev, join, sink);
+            tessellate_join(join, P, sink, status);
+            if (count == 2) {
+                W.firsts[0] = prev;
+                W.firsts[1] = join;
+                W.nfirsts = 2;
+            }
+        }
+    }
+    if (skip) {
+        pb.replace_last(next);
+    } else {
+        pb.push(next);
+    }
+    return true;
+}
+
+// end (stroke.rs:1179-1193) with close (1206-1279), end_with_caps (1322-1378) and the empty
+// cap (1282-1316), on the stepper's own points.
+template <class SK>
+__device__ __noinline__ void vw_end(VwState& W, bool close, const StrokeParams& P, SK& sink,
+                                    int* status) {
+    SeqBuffer& pb = W.pb;
+    const uint32_t count = pb.count;
+    W.mnec |= close && count == 1;
+    if (close && count > 2) {
+        DEP p = W.firsts[0];
+        const float start_adv = p.adv;
+        p.adv = __int_as_float(0x7fc00000);
+        if (!vw_step(W, p, P, sink, status)) pb.last().pos = p.pos;
+        if (W.nfirsts >= 2) {
+            vw_step(W, W.firsts[1], P, sink, status);
+            DEP& p0 = pb.second_last();
+            DEP& p1 = pb.last();
+            sink.adv = start_adv;
+            for (int side = 0; side < 2; ++side) {
+                const V2 sp = p0.s[side].has_single ? p0.s[side].single : p0.s[side].next;
+                const V2 normal = (sp - p0.pos) / p0.hw;
+                p0.s[side].next_vertex = sink.vertex(p0.pos + normal * p0.hw, normal, side);
+            }
+            add_edge_triangles(p0, p1, sink);
+        }
+    } else if (W.mnec && count == 1) {
+        const DEP& point = pb.first();
+        sink.adv = point.adv;
+        if (P.start_cap == LYON_CAP_SQUARE) {
+            tessellate_empty_square_cap(point.pos, point.hw, sink);
+        } else if (P.start_cap == LYON_CAP_ROUND) {
+            tessellate_empty_round_cap(point.pos, point.hw, P, sink, status);
+        }
+    } else if (count >= 2) {
+        DEP p0 = pb.second_last();
+        DEP p1 = pb.last();
+        // tessellate_last_edge sets the last point's advancement (stroke.rs:2140), which the
+        // next sub-path starts from.
+        p1.adv = p0.adv + vlength(p1.pos - p0.pos);
+        tessellate_last_edge(p0, p1, count == 2, P, sink, status);
+        W.start_adv = p1.adv;
+        if (count > 2) {
+            p0 = W.firsts[0];
+            p1 = W.firsts[1];
+        }
+        tessellate_first_edge(p0, p1, P, sink, status);
+    }
+    pb.start = pb.count = pb.n = 0;
+    W.nfirsts = 0;
 }
 
 }  // namespace lg

@@ -158,19 +158,28 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
 
 
-def _single(kind: str, ctx: Context, path: Path, options, builder: BuffersBuilder) -> None:
+def _single(kind: str, ctx: Context, path: Path, options, builder: BuffersBuilder,
+            widths=None) -> None:
     bits = builder.buffers.index_bits
     verbs = np.ascontiguousarray(path.verbs, dtype=np.uint8)
     pts = np.ascontiguousarray(path.points, dtype=np.float32)
     opt = options.to_c()
     res = _native.CResult()
     records = kind == "stroke" and builder.vertex_ctor is not None
-    if records:
-        fn = ctx.lib.lyon_gpu_stroke_path_attributes
+    if widths is not None:
+        w = np.ascontiguousarray(widths, dtype=np.float32)
+        if len(w) != len(pts):
+            raise ValueError("one width factor per point")
+        r = ctx.lib.lyon_gpu_stroke_path_variable_width(
+            ctx.h, _ptr(verbs), len(verbs), _ptr(pts), len(pts), _ptr(w), ctypes.byref(opt), bits,
+            builder.next_index(), 1 if records else 0, ctypes.byref(res))
     else:
-        fn = ctx.lib.lyon_gpu_stroke_path if kind == "stroke" else ctx.lib.lyon_gpu_fill_path
-    r = fn(ctx.h, _ptr(verbs), len(verbs), _ptr(pts), len(pts), ctypes.byref(opt), bits,
-           builder.next_index(), ctypes.byref(res))
+        if records:
+            fn = ctx.lib.lyon_gpu_stroke_path_attributes
+        else:
+            fn = ctx.lib.lyon_gpu_stroke_path if kind == "stroke" else ctx.lib.lyon_gpu_fill_path
+        r = fn(ctx.h, _ptr(verbs), len(verbs), _ptr(pts), len(pts), ctypes.byref(opt), bits,
+               builder.next_index(), ctypes.byref(res))
     if r != LYON_OK:
         raise TessellationError(r, ctx.last_error() if r >= 100 else "")
     nv, ni = res.num_vertices, res.num_indices
@@ -198,8 +207,11 @@ class StrokeTessellator:
     def __init__(self, ctx: Optional[Context] = None):
         self.ctx = ctx or Context.default()
 
-    def tessellate_path(self, path: Path, options: StrokeOptions, builder: BuffersBuilder) -> None:
-        _single("stroke", self.ctx, path, options, builder)
+    def tessellate_path(self, path: Path, options: StrokeOptions, builder: BuffersBuilder,
+                        widths=None) -> None:
+        """`widths`: one width factor per point for StrokeOptions::variable_line_width (lyon
+        reads it from the path's endpoint attribute); None strokes with the fixed width."""
+        _single("stroke", self.ctx, path, options, builder, widths)
 
     tessellate = tessellate_path
 
@@ -325,21 +337,27 @@ class BatchResult:
 def tessellate_paths(kind: str, dbatch: DeviceBatch, options_dev, num_options: int,
                      index_bits: int = 32, index_mode: int = INDEX_GLOBAL,
                      vertex_offset: int = 0, ctx: Optional[Context] = None,
-                     attributes: bool = False) -> BatchResult:
+                     attributes: bool = False, widths=None) -> BatchResult:
     """Batched stroke or fill of every path of a DeviceBatch (results stay on the device,
     owned by the context until its next batched call). With `attributes` (strokes), the
     vertices are lyon_stroke_vertex records (BatchResult.records)."""
     ctx = ctx or Context.default()
     out = _native.CBatchOutput()
     cb = dbatch.c()
-    if attributes and kind != "stroke":
-        raise ValueError("vertex attributes are a stroke output")
-    if attributes:
-        fn = ctx.lib.lyon_gpu_stroke_paths_attributes
+    if (attributes or widths is not None) and kind != "stroke":
+        raise ValueError("vertex attributes and variable widths are stroke options")
+    if widths is not None:
+        # Variable line width: `widths` is a device tensor of one f32 factor per point.
+        r = ctx.lib.lyon_gpu_stroke_paths_variable_width(
+            ctx.h, ctypes.byref(cb), widths.data_ptr(), options_dev.data_ptr(), num_options,
+            index_bits, index_mode, vertex_offset, 1 if attributes else 0, ctypes.byref(out))
     else:
-        fn = ctx.lib.lyon_gpu_stroke_paths if kind == "stroke" else ctx.lib.lyon_gpu_fill_paths
-    r = fn(ctx.h, ctypes.byref(cb), options_dev.data_ptr(), num_options, index_bits, index_mode,
-           vertex_offset, ctypes.byref(out))
+        if attributes:
+            fn = ctx.lib.lyon_gpu_stroke_paths_attributes
+        else:
+            fn = ctx.lib.lyon_gpu_stroke_paths if kind == "stroke" else ctx.lib.lyon_gpu_fill_paths
+        r = fn(ctx.h, ctypes.byref(cb), options_dev.data_ptr(), num_options, index_bits,
+               index_mode, vertex_offset, ctypes.byref(out))
     if r != LYON_OK:
         raise TessellationError(r, ctx.last_error())
     return BatchResult(r, int(out.total_vertices), int(out.total_indices),

@@ -239,6 +239,19 @@ int lyon_gpu_stroke_paths_variable_width(lyon_gpu_context* ctx, const lyon_path_
                                          uint32_t vertex_offset, int vertex_attributes,
                                          lyon_gpu_batch_output* out);
 
+/* Basic shapes: FillTessellator::tessellate_rectangle and tessellate_circle
+ * (crates/tessellation/src/fill.rs:654-673 with crates/tessellation/src/basic_shapes.rs:12-124),
+ * which fill without the sweep, over a batch of shapes. `params` (device memory) holds 4 floats
+ * per rectangle (min x, min y, max x, max y) or 3 per circle (center x, center y, radius);
+ * `options` 1 shared record or one per shape (circles read the tolerance). Each shape is one
+ * "path" of `out` (per-shape offsets, statuses, index modes as for lyon_gpu_fill_paths). A circle
+ * that would need more than 2^20 bisections per quarter fails with LYON_ERR_UNSUPPORTED. */
+enum { LYON_SHAPE_RECTANGLE = 0, LYON_SHAPE_CIRCLE = 1 };
+int lyon_gpu_fill_shapes(lyon_gpu_context* ctx, int shape_kind, const float* params,
+                         uint32_t num_shapes, const lyon_fill_options* options,
+                         uint32_t num_options, int index_bits, int index_mode,
+                         uint32_t vertex_offset, lyon_gpu_batch_output* out);
+
 /* Largest batch lyon_gpu_stroke_paths_noalloc accepts (its fixed scratch holds this many paths). */
 #define LYON_NOALLOC_MAX_PATHS 262144u
 

@@ -150,6 +150,9 @@ def load(build_if_missing: bool = True):
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [c_p, ctypes.POINTER(CStrokeTuning)]
+        L.lyon_gpu_fill_shapes.restype = ctypes.c_int
+        L.lyon_gpu_fill_shapes.argtypes = [c_p, ctypes.c_int, c_p, u32, c_p, u32, ctypes.c_int,
+                                           ctypes.c_int, u32, c_p]
         L.lyon_gpu_stroke_paths_variable_width.restype = ctypes.c_int
         L.lyon_gpu_stroke_paths_variable_width.argtypes = [c_p, c_p, c_p, c_p, u32,
                                                            ctypes.c_int, ctypes.c_int, u32,
@@ -184,4 +187,5 @@ EXPORTED = [
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
     "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",
     "lyon_gpu_stroke_paths_variable_width", "lyon_gpu_stroke_path_variable_width",
+    "lyon_gpu_fill_shapes",
 ]

@@ -879,6 +879,72 @@ int lyon_gpu_stroke_paths_variable_width(lyon_gpu_context* ctx, const lyon_path_
     return r;
 }
 
+int lyon_gpu_fill_shapes(lyon_gpu_context* ctx, int shape_kind, const float* params,
+                         uint32_t num_shapes, const lyon_fill_options* options,
+                         uint32_t num_options, int index_bits, int index_mode,
+                         uint32_t vertex_offset, lyon_gpu_batch_output* out) {
+    const uint32_t n = num_shapes;
+    const bool circles = shape_kind == LYON_SHAPE_CIRCLE;
+    if (!ctx || !out || (shape_kind != LYON_SHAPE_RECTANGLE && !circles) || (n && !params) ||
+        (index_bits != 16 && index_bits != 32) ||
+        (index_mode != LYON_INDEX_GLOBAL && index_mode != LYON_INDEX_PER_PATH) ||
+        (circles && (!options || (num_options != 1 && num_options != n)))) {
+        if (ctx) ctx->last_error = "invalid argument";
+        return LYON_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(ctx->device);
+    memset(out, 0, sizeof(*out));
+    if (!alloc_path_arrays(ctx, n)) return LYON_ERR_OUT_OF_MEMORY;
+    cudaStream_t s = ctx->stream;
+    lg::ShapeArgs a;
+    memset(&a, 0, sizeof a);
+    a.kind = shape_kind;
+    a.params = params;
+    a.n = n;
+    a.options = options;
+    a.num_options = num_options;
+    a.vtx_counts = as<uint32_t>(ctx->vtx_counts);
+    a.idx_counts = as<uint32_t>(ctx->idx_counts);
+    a.status = as<int32_t>(ctx->status);
+    a.index_bits = index_bits;
+    a.index_mode = index_mode;
+    a.vertex_offset = vertex_offset;
+    mark(ctx, 0);
+    if (!set_err(ctx, "shapes count", lg::launch_shapes(a, false, s))) return LYON_ERR_CUDA;
+    mark(ctx, 1);
+    uint64_t tv = 0, ti = 0;
+    uint32_t failed = 0;
+    if (!finish_counts(ctx, n, index_bits, index_mode, vertex_offset, &tv, &ti, &failed))
+        return LYON_ERR_CUDA;
+    mark(ctx, 2);
+    if (!ensure(ctx, ctx->out_vertices, tv * 8 + 16) ||
+        !ensure(ctx, ctx->out_indices, ti * (index_bits / 8) + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    a.vtx_offsets = as<uint64_t>(ctx->vtx_offsets);
+    a.idx_offsets = as<uint64_t>(ctx->idx_offsets);
+    a.vertices = as<float>(ctx->out_vertices);
+    a.indices = ctx->out_indices.ptr;
+    if (tv > 0 && !set_err(ctx, "shapes emit", lg::launch_shapes(a, true, s)))
+        return LYON_ERR_CUDA;
+    mark(ctx, 3);
+    if (ctx->timing) {
+        cudaEventSynchronize(ctx->ev[3]);
+        cudaEventElapsedTime(&ctx->last_ms[0], ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&ctx->last_ms[1], ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&ctx->last_ms[2], ctx->ev[2], ctx->ev[3]);
+        cudaEventElapsedTime(&ctx->last_ms[3], ctx->ev[0], ctx->ev[3]);
+    }
+    out->vertices = as<float>(ctx->out_vertices);
+    out->indices = ctx->out_indices.ptr;
+    out->vertex_offsets = as<uint64_t>(ctx->vtx_offsets);
+    out->index_offsets = as<uint64_t>(ctx->idx_offsets);
+    out->status = as<int32_t>(ctx->status);
+    out->total_vertices = tv;
+    out->total_indices = ti;
+    out->num_failed_paths = failed;
+    return LYON_OK;
+}
+
 int lyon_gpu_fill_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                         const lyon_fill_options* options, uint32_t num_options, int index_bits,
                         int index_mode, uint32_t vertex_offset, lyon_gpu_batch_output* out) {

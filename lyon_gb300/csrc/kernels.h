@@ -50,6 +50,27 @@ struct StrokeArgs {
     uint32_t* seq_counter;
 };
 
+// Basic shapes (shapes.cu): `params` holds 4 floats per rectangle (min x, min y, max x, max y)
+// or 3 per circle (center x, center y, radius).
+struct ShapeArgs {
+    int kind;  // LYON_SHAPE_RECTANGLE or LYON_SHAPE_CIRCLE
+    const float* params;
+    uint32_t n;
+    const lyon_fill_options* options;
+    uint32_t num_options;
+    uint32_t* vtx_counts;
+    uint32_t* idx_counts;
+    int32_t* status;
+    const uint64_t* vtx_offsets;
+    const uint64_t* idx_offsets;
+    float* vertices;
+    void* indices;
+    int index_bits;
+    int index_mode;
+    uint32_t vertex_offset;
+};
+cudaError_t launch_shapes(const ShapeArgs& args, bool emit, cudaStream_t stream);
+
 int stroke_blocks_per_sm();
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);
 

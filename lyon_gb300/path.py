@@ -152,6 +152,105 @@ class PathBuilder:
     def close(self) -> None:
         self.end(True)
 
+    # ---- shapes (crates/path/src/builder.rs:560-680, 1508-1548, 1551-1660) ----------------
+    # Arithmetic is f32, as in lyon; `winding` is +1 (Winding::Positive) or -1 (Negative).
+
+    def add_polygon(self, points, closed: bool = True) -> None:
+        """builder.rs:560-573: begin at the first point, a line to each next one."""
+        pts = np.asarray(points, dtype=np.float32).reshape(-1, 2)
+        if len(pts) == 0:
+            return
+        self.begin(pts[0])
+        for p in pts[1:]:
+            self.line_to(p)
+        self.end(closed)
+
+    def add_rectangle(self, rect, winding: int = 1) -> None:
+        """builder.rs:649-675; rect = (min_x, min_y, max_x, max_y)."""
+        x0, y0, x1, y1 = [np.float32(v) for v in rect]
+        if winding >= 0:
+            self.add_polygon([(x0, y0), (x1, y0), (x1, y1), (x0, y1)], True)
+        else:
+            self.add_polygon([(x0, y0), (x0, y1), (x1, y1), (x1, y0)], True)
+
+    def add_circle(self, center, radius: float, winding: int = 1) -> None:
+        """builder.rs:1508-1548: four cubic arcs with the 0.55191505 control factor."""
+        f = np.float32
+        r = abs(f(radius))
+        d_dir = f(1.0) if winding >= 0 else f(-1.0)
+        cx, cy = f(center[0]), f(center[1])
+        d = r * f(0.55191505)
+
+        def at(dx, dy):
+            return (cx + f(dx), cy + f(dy))
+        self.begin(at(-r, f(0.0)))
+        self.cubic_bezier_to(at(-r, -d * d_dir), at(-d, -r * d_dir), at(f(0.0), -r * d_dir))
+        self.cubic_bezier_to(at(d, -r * d_dir), at(r, -d * d_dir), at(r, f(0.0)))
+        self.cubic_bezier_to(at(r, d * d_dir), at(d, r * d_dir), at(f(0.0), r * d_dir))
+        self.cubic_bezier_to(at(-d, r * d_dir), at(-r, d * d_dir), at(-r, f(0.0)))
+        self.close()
+
+    def add_rounded_rectangle(self, rect, radii, winding: int = 1) -> None:
+        """builder.rs:1551-1660; radii = (top_left, top_right, bottom_left, bottom_right)."""
+        f = np.float32
+        x_min, y_min, x_max, y_max = [f(v) for v in rect]
+        w = x_max - x_min
+        h = y_max - y_min
+        min_wh = min(w, h)
+        tl, tr, bl, br = [min(abs(f(r)), min_wh) for r in radii]
+        if tl + tr > w:
+            x = (tl + tr - w) * f(0.5)
+            tl, tr = tl - x, tr - x
+        if bl + br > w:
+            x = (bl + br - w) * f(0.5)
+            bl, br = bl - x, br - x
+        if tr + br > h:
+            x = (tr + br - h) * f(0.5)
+            tr, br = tr - x, br - x
+        if tl + bl > h:
+            x = (tl + bl - h) * f(0.5)
+            tl, bl = tl - x, bl - x
+        k = f(0.55191505)
+        tl_d, tr_d, br_d, bl_d = tl * k, tr * k, br * k, bl * k
+        z = f(0.0)
+        pts = [
+            (x_min, y_min + tl), (x_min + z, y_min + (tl - tl_d)), (x_min + (tl - tl_d), y_min + z),
+            (x_min + tl, y_min + z),
+            (x_max - tr, y_min), (x_max + (-tr + tr_d), y_min + z), (x_max + z, y_min + (tr - tr_d)),
+            (x_max + z, y_min + tr),
+            (x_max, y_max - br), (x_max + z, y_max + (-br + br_d)), (x_max + (-br + br_d), y_max + z),
+            (x_max + -br, y_max + z),
+            (x_min + bl, y_max), (x_min + (bl - bl_d), y_max + z), (x_min + z, y_max + (-bl + bl_d)),
+            (x_min + z, y_max + -bl),
+        ]
+        if winding >= 0:
+            self.begin(pts[0])
+            if tl > 0:
+                self.cubic_bezier_to(pts[1], pts[2], pts[3])
+            self.line_to(pts[4])
+            if tr > 0:
+                self.cubic_bezier_to(pts[5], pts[6], pts[7])
+            self.line_to(pts[8])
+            if br > 0:
+                self.cubic_bezier_to(pts[9], pts[10], pts[11])
+            self.line_to(pts[12])
+            if bl > 0:
+                self.cubic_bezier_to(pts[13], pts[14], pts[15])
+        else:
+            self.begin(pts[15])
+            if bl > 0:
+                self.cubic_bezier_to(pts[14], pts[13], pts[12])
+            self.line_to(pts[11])
+            if br > 0:
+                self.cubic_bezier_to(pts[10], pts[9], pts[8])
+            self.line_to(pts[7])
+            if tr > 0:
+                self.cubic_bezier_to(pts[6], pts[5], pts[4])
+            self.line_to(pts[3])
+            if tl > 0:
+                self.cubic_bezier_to(pts[2], pts[1], pts[0])
+        self.end(True)
+
     def build(self) -> Path:
         if self._open:
             self.end(False)

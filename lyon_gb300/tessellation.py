@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _native
 from .options import (FILL_OPTIONS_DTYPE, STROKE_OPTIONS_DTYPE, FillOptions, StrokeOptions)
-from .path import Path, PathBatch
+from .path import Path, PathBatch, PathBuilder
 
 LYON_OK = 0
 LYON_ERR_POSITION_IS_NAN = 1
@@ -201,6 +201,44 @@ def _single(kind: str, ctx: Context, path: Path, options, builder: BuffersBuilde
     builder.append(v.reshape(-1, 2), i)
 
 
+def _append_result(res: "BatchResult", builder: BuffersBuilder) -> None:
+    import torch  # noqa: F401  (device copies)
+    if res.num_failed_paths:
+        st = int(res.statuses().cpu().numpy()[0])
+        raise TessellationError(st)
+    v = res.vertices().cpu().numpy() if res.total_vertices else np.zeros((0, 2), np.float32)
+    if res.total_indices:
+        i = res.indices().cpu().numpy()
+        i = i.view(np.uint16) if res.index_bits == 16 else i.view(np.uint32)
+    else:
+        i = np.zeros(0, builder.buffers.indices.dtype)
+    builder.append(v.reshape(-1, 2), i)
+
+
+def fill_shapes(kind: int, params_dev, num_shapes: int, options_dev=None, num_options: int = 0,
+                index_bits: int = 32, index_mode: int = INDEX_GLOBAL, vertex_offset: int = 0,
+                ctx: Optional[Context] = None) -> "BatchResult":
+    """Batched basic shapes (lyon_gpu_fill_shapes): SHAPE_RECTANGLE params are (min x, min y,
+    max x, max y) per shape, SHAPE_CIRCLE (center x, center y, radius); device tensors."""
+    ctx = ctx or Context.default()
+    out = _native.CBatchOutput()
+    r = ctx.lib.lyon_gpu_fill_shapes(ctx.h, kind, params_dev.data_ptr() if num_shapes else None,
+                                     num_shapes,
+                                     options_dev.data_ptr() if options_dev is not None else None,
+                                     num_options, index_bits, index_mode, vertex_offset,
+                                     ctypes.byref(out))
+    if r != LYON_OK:
+        raise TessellationError(r, ctx.last_error())
+    return BatchResult(r, int(out.total_vertices), int(out.total_indices),
+                       int(out.num_failed_paths), int(out.vertices or 0), int(out.indices or 0),
+                       int(out.status or 0), index_bits, num_shapes,
+                       int(out.vertex_offsets or 0), int(out.index_offsets or 0))
+
+
+SHAPE_RECTANGLE = 0
+SHAPE_CIRCLE = 1
+
+
 class StrokeTessellator:
     """lyon's StrokeTessellator (fixed line width, `Positions` vertices)."""
 
@@ -213,6 +251,26 @@ class StrokeTessellator:
         reads it from the path's endpoint attribute); None strokes with the fixed width."""
         _single("stroke", self.ctx, path, options, builder, widths)
 
+    def tessellate_polygon(self, points, closed: bool, options: StrokeOptions,
+                           builder: BuffersBuilder) -> None:
+        """stroke.rs:255-263."""
+        b = PathBuilder()
+        b.add_polygon(points, closed)
+        self.tessellate_path(b.build(), options, builder)
+
+    def tessellate_rectangle(self, rect, options: StrokeOptions, builder: BuffersBuilder) -> None:
+        """stroke.rs:265-278: the rectangle as a path (Winding::Positive)."""
+        b = PathBuilder()
+        b.add_rectangle(rect, 1)
+        self.tessellate_path(b.build(), options, builder)
+
+    def tessellate_circle(self, center, radius: float, options: StrokeOptions,
+                          builder: BuffersBuilder) -> None:
+        """stroke.rs:280-292: the circle as a path of four cubics (Winding::Positive)."""
+        b = PathBuilder()
+        b.add_circle(center, radius, 1)
+        self.tessellate_path(b.build(), options, builder)
+
     tessellate = tessellate_path
 
 
@@ -221,6 +279,31 @@ class FillTessellator:
 
     def __init__(self, ctx: Optional[Context] = None):
         self.ctx = ctx or Context.default()
+
+    def tessellate_polygon(self, points, closed: bool, options: FillOptions,
+                           builder: BuffersBuilder) -> None:
+        """fill.rs:643-651."""
+        b = PathBuilder()
+        b.add_polygon(points, closed)
+        self.tessellate_path(b.build(), options, builder)
+
+    def _shape(self, kind, params, options, builder):
+        import torch
+        p = torch.tensor(np.asarray(params, np.float32).reshape(-1), device="cuda")
+        od = upload_options(options.to_record())
+        res = fill_shapes(kind, p, 1, od, 1, builder.buffers.index_bits, INDEX_PER_PATH,
+                          builder.next_index(), self.ctx)
+        self.ctx.synchronize()
+        _append_result(res, builder)
+
+    def tessellate_rectangle(self, rect, options: FillOptions, builder: BuffersBuilder) -> None:
+        """fill.rs:653-661 (basic_shapes.rs:12-38); rect = (min_x, min_y, max_x, max_y)."""
+        self._shape(SHAPE_RECTANGLE, rect, options, builder)
+
+    def tessellate_circle(self, center, radius: float, options: FillOptions,
+                          builder: BuffersBuilder) -> None:
+        """fill.rs:663-672 (basic_shapes.rs:40-124)."""
+        self._shape(SHAPE_CIRCLE, [center[0], center[1], radius], options, builder)
 
     def tessellate_path(self, path: Path, options: FillOptions, builder: BuffersBuilder) -> None:
         _single("fill", self.ctx, path, options, builder)

@@ -2651,6 +2651,81 @@ static void flatten_path(const uint8_t* verbs, uint32_t nverbs, const float* pts
     }
 }
 
+// --------------------------------------------------------------------------------------------
+// Basic shapes (crates/tessellation/src/basic_shapes.rs): FillTessellator::tessellate_rectangle
+// and tessellate_circle, which bypass the sweep.
+// --------------------------------------------------------------------------------------------
+// basic_shapes.rs:12-38
+static int fill_rectangle(Output* out, P min, P max) {
+    out->begin_geometry();
+    P corners[4] = {min, P{min.x, max.y}, max, P{max.x, min.y}};
+    uint32_t id[4];
+    for (int k = 0; k < 4; ++k) {
+        if (!out->add_vertex(corners[k], &id[k])) {
+            out->abort_geometry();
+            return LYON_ERR_TOO_MANY_VERTICES;
+        }
+    }
+    out->add_triangle(id[0], id[1], id[2]);
+    out->add_triangle(id[0], id[2], id[3]);
+    return LYON_OK;
+}
+
+// basic_shapes.rs:151-155
+static float circle_flattening_step_fill(float radius, float tolerance) {
+    tolerance = fminf(tolerance, radius);
+    return 2.0f * sqrtf(2.0f * tolerance * radius - tolerance * tolerance);
+}
+
+// basic_shapes.rs:158-207
+static bool fill_border_radius(Output* out, P center, float a0, float a1, float radius,
+                               uint32_t va, uint32_t vb, uint32_t num_recursions) {
+    if (num_recursions == 0) return true;
+    float mid_angle = (a0 + a1) * 0.5f;
+    P normal = P{cosf(mid_angle), sinf(mid_angle)};
+    P position = add(center, mul(normal, radius));
+    uint32_t v;
+    if (!out->add_vertex(position, &v)) return false;
+    out->add_triangle(vb, v, va);
+    return fill_border_radius(out, center, a0, mid_angle, radius, va, v, num_recursions - 1) &&
+           fill_border_radius(out, center, mid_angle, a1, radius, v, vb, num_recursions - 1);
+}
+
+// basic_shapes.rs:40-124
+static int fill_circle(Output* out, P center, float radius, float tolerance) {
+    radius = fabsf(radius);
+    if (radius == 0.0f) return LYON_OK;
+    float arc_len = 0.5f * PI_F * radius;
+    float step = circle_flattening_step_fill(radius, tolerance);
+    float num_segments = ceilf(arc_len / step);
+    uint32_t num_recursions = sat_u32(log2f(num_segments));  // `as u32`
+    // More than four million vertices for one circle: reported as unsupported (the GPU's bound).
+    if (num_recursions > 20) return LYON_ERR_UNSUPPORTED;
+    out->begin_geometry();
+    const P dirs[4] = {P{-1.0f, 0.0f}, P{0.0f, -1.0f}, P{1.0f, 0.0f}, P{0.0f, 1.0f}};
+    uint32_t v[4];
+    for (int k = 0; k < 4; ++k) {
+        if (!out->add_vertex(add(center, mul(dirs[k], radius)), &v[k])) {
+            out->abort_geometry();
+            return LYON_ERR_TOO_MANY_VERTICES;
+        }
+    }
+    out->add_triangle(v[0], v[3], v[1]);
+    out->add_triangle(v[1], v[3], v[2]);
+    const float angles[4][2] = {{PI_F, 1.5f * PI_F},
+                                {1.5f * PI_F, 2.0f * PI_F},
+                                {0.0f, PI_F * 0.5f},
+                                {PI_F * 0.5f, PI_F}};
+    for (int k = 0; k < 4; ++k) {
+        if (!fill_border_radius(out, center, angles[k][0], angles[k][1], radius, v[k],
+                                v[(k + 1) % 4], num_recursions)) {
+            out->abort_geometry();
+            return LYON_ERR_TOO_MANY_VERTICES;
+        }
+    }
+    return LYON_OK;
+}
+
 }  // namespace lo
 
 // ============================================================================================
@@ -2720,6 +2795,16 @@ int lyon_oracle_stroke_path_vw(lyon_oracle_out* o, const uint8_t* verbs, uint32_
     int r = s.tessellate(it);
     o->near_ties += g_near_ties;
     return r;
+}
+
+// FillTessellator::tessellate_rectangle / tessellate_circle appending to the output.
+int lyon_oracle_fill_rectangle(lyon_oracle_out* o, float min_x, float min_y, float max_x,
+                               float max_y) {
+    return fill_rectangle(&o->out, P{min_x, min_y}, P{max_x, max_y});
+}
+int lyon_oracle_fill_circle(lyon_oracle_out* o, float cx, float cy, float radius,
+                            float tolerance) {
+    return fill_circle(&o->out, P{cx, cy}, radius, tolerance);
 }
 
 // FillTessellator::tessellate_path appending to the output.

@@ -65,6 +65,10 @@ def lib():
             L.lyon_oracle_batch_stroke_attributes.restype = ctypes.c_int
             L.lyon_oracle_batch_stroke_attributes.argtypes = [c_p, c_p, ctypes.c_uint32,
                                                               ctypes.c_int, c_p, c_p]
+            L.lyon_oracle_fill_rectangle.restype = ctypes.c_int
+            L.lyon_oracle_fill_rectangle.argtypes = [c_p] + [ctypes.c_float] * 4
+            L.lyon_oracle_fill_circle.restype = ctypes.c_int
+            L.lyon_oracle_fill_circle.argtypes = [c_p] + [ctypes.c_float] * 4
             L.lyon_oracle_stroke_path_vw.restype = ctypes.c_int
             L.lyon_oracle_stroke_path_vw.argtypes = [c_p, c_p, ctypes.c_uint32, c_p,
                                                      ctypes.c_uint32, c_p, c_p]
@@ -161,6 +165,23 @@ def stroke(path, options, index_bits: int = 32, vertex_offset: int = 0,
            attributes: bool = False, widths=None) -> Result:
     out = Output(index_bits, vertex_offset, attributes)
     st = out.stroke(path, options, widths)
+    return out.snapshot(st)
+
+
+def fill_rectangle(rect, index_bits: int = 32, vertex_offset: int = 0) -> Result:
+    """FillTessellator::tessellate_rectangle (basic_shapes.rs:12-38); rect = (min_x, min_y,
+    max_x, max_y)."""
+    out = Output(index_bits, vertex_offset)
+    st = out.L.lyon_oracle_fill_rectangle(out.h, *[float(x) for x in rect])
+    return out.snapshot(st)
+
+
+def fill_circle(center, radius, tolerance, index_bits: int = 32,
+                vertex_offset: int = 0) -> Result:
+    """FillTessellator::tessellate_circle (basic_shapes.rs:40-124)."""
+    out = Output(index_bits, vertex_offset)
+    st = out.L.lyon_oracle_fill_circle(out.h, float(center[0]), float(center[1]), float(radius),
+                                       float(tolerance))
     return out.snapshot(st)
 
 

@@ -445,6 +445,38 @@ int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch
 /* Synchronise the context's stream. Returns LYON_OK or LYON_ERR_CUDA. */
 int lyon_gpu_synchronize(lyon_gpu_context* ctx);
 
+/* ---- SVG path data (no lyon_gpu counterpart; lyon_extra's PathParser) ----------------------- */
+
+/* Parse errors of lyon's PathParser (crates/extra/src/parser.rs:14-33), per string. */
+#define LYON_SVG_ERR_NUMBER 110          /* expected a number */
+#define LYON_SVG_ERR_FLAG 111            /* expected an arc flag (0/1) */
+#define LYON_SVG_ERR_COMMAND 112         /* invalid command */
+#define LYON_SVG_ERR_MISSING_MOVE_TO 113 /* a command after Z other than M */
+
+typedef struct lyon_svg_parse_options {
+    uint32_t num_attributes; /* per endpoint (ParserOptions::num_attributes): 0, or 1 to read a
+                                width factor per endpoint into `widths` */
+    int32_t stop_at;         /* ParserOptions::stop_at: a character that ends parsing, or -1 */
+    uint32_t num_threads;    /* host threads; 0: all */
+} lyon_svg_parse_options;
+
+/* PathParser::parse (crates/extra/src/parser.rs:154-490) of `num_strings` SVG path data strings
+ * (UTF-8; string i is text[string_offsets[i] .. string_offsets[i + 1]]) into one host path batch:
+ * path i gets verbs[verb_offsets[i] ..], points[point_offsets[i] ..] as lyon's Path builder
+ * would hold them (arcs as quadratic beziers, crates/geom/src/arc.rs:58-138,668-703). `status[i]`
+ * is LYON_OK or a LYON_SVG_ERR_* code with its line and column (as lyon reports them); a failed
+ * string keeps what was built before the error, ended, as lyon's builder does. Call with null
+ * output arrays (or too small capacities) to get *total_verbs / *total_points: the call then
+ * returns LYON_ERR_CAPACITY. `widths` (optional, one float per point) receives the endpoint
+ * attribute when options->num_attributes is 1 (control points get 0). All buffers are host
+ * memory; the strings are parsed on the host's threads. */
+int lyon_svg_parse_paths(const char* text, const uint64_t* string_offsets, uint32_t num_strings,
+                         const lyon_svg_parse_options* options, uint8_t* verbs,
+                         uint64_t verb_capacity, float* points, uint64_t point_capacity,
+                         float* widths, uint32_t* verb_offsets, uint32_t* point_offsets,
+                         int32_t* status, int32_t* error_line, int32_t* error_column,
+                         uint64_t* total_verbs, uint64_t* total_points);
+
 /* Library version and build information (static string). */
 const char* lyon_gpu_version(void);
 

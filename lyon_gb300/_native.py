@@ -64,6 +64,10 @@ class CSrvLoadStats(ctypes.Structure):
                 ("mean_batch_paths", ctypes.c_double)]
 
 
+class CSvgParseOptions(ctypes.Structure):
+    _fields_ = [("num_attributes", u32), ("stop_at", ctypes.c_int32), ("num_threads", u32)]
+
+
 class CStrokeTuning(ctypes.Structure):
     _fields_ = [("long_path_points", u32), ("blocks_per_sm", u32), ("short_path_points", u32)]
 
@@ -150,6 +154,9 @@ def load(build_if_missing: bool = True):
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [c_p, ctypes.POINTER(CStrokeTuning)]
+        L.lyon_svg_parse_paths.restype = ctypes.c_int
+        L.lyon_svg_parse_paths.argtypes = [c_p, c_p, u32, c_p, c_p, u64, c_p, u64, c_p, c_p, c_p,
+                                           c_p, c_p, c_p, c_p, c_p]
         L.lyon_gpu_fill_shapes.restype = ctypes.c_int
         L.lyon_gpu_fill_shapes.argtypes = [c_p, ctypes.c_int, c_p, u32, c_p, u32, ctypes.c_int,
                                            ctypes.c_int, u32, c_p]
@@ -187,5 +194,5 @@ EXPORTED = [
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
     "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",
     "lyon_gpu_stroke_paths_variable_width", "lyon_gpu_stroke_path_variable_width",
-    "lyon_gpu_fill_shapes",
+    "lyon_gpu_fill_shapes", "lyon_svg_parse_paths",
 ]

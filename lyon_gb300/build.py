@@ -21,10 +21,11 @@ LIB_NAME = "liblyon_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
 SOURCES = ["stroke.cu", "scan.cu", "flatten.cu", "fill.cu", "api.cu", "noalloc.cu", "serve.cu",
-           "shapes.cu"]
+           "shapes.cu", "svg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-prec-div=true",
-              "-prec-sqrt=true", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
+              "-prec-sqrt=true", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math",
+              "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:

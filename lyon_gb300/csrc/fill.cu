@@ -171,7 +171,8 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
     if (n == 0) return LYON_OK;
     // Counters: [0] work, [1] retries, [2] heap overflows; two u64 staging tops; two retry
     // lists.
-    const size_t ctl_bytes = 64 + (size_t)n * 8;
+    // After them: the size-order scratch (counters, one byte per path).
+    const size_t ctl_bytes = 64 + (size_t)n * 8 + 2 * SIZE_ORDER_BINS * 4 + (size_t)n;
     if (!grow(&fb.work, &fb.work_cap, ctl_bytes, 0, stream) ||
         !grow(&fb.stage_off, &fb.stage_off_cap, (size_t)n * 16, 0, stream)) {
         if (error) *error = "cudaMalloc (fill control arrays)";
@@ -199,7 +200,15 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         }
     }
     cudaMemsetAsync(tops, 0, 16, stream);
+    // Big paths first, so that the last paths a sweeper takes are short ones and the launch
+    // does not end on one long sweep. The order lives in the second retry list, which the first
+    // attempt does not write.
+    uint32_t* size_counters = lists[1] + n;
+    uint8_t* size_cls = reinterpret_cast<uint8_t*>(size_counters + 2 * SIZE_ORDER_BINS);
     const uint32_t* order = nullptr;
+    if (launch_size_order(batch->point_offsets, n, size_cls, lists[1], size_counters, stream) ==
+        cudaSuccess)
+        order = lists[1];
     uint32_t items = n;
     const int MAX_ATTEMPTS = 4;
     for (int attempt = 0; attempt < MAX_ATTEMPTS; ++attempt) {

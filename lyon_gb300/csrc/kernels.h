@@ -109,6 +109,13 @@ cudaError_t launch_classify_paths(const uint8_t* verbs, const uint32_t* verb_off
                                   uint32_t short_points, uint8_t* path_class, uint32_t* order,
                                   uint32_t* counters, cudaStream_t s);
 
+// Processing order by decreasing size (powers of two of the point count, largest first), for
+// work queues whose last items should be the cheap ones. `cls` holds one byte per path,
+// `counters` 2 * SIZE_ORDER_BINS words; both are scratch.
+constexpr uint32_t SIZE_ORDER_BINS = 33;
+cudaError_t launch_size_order(const uint32_t* point_offsets, uint32_t n, uint8_t* cls,
+                              uint32_t* order, uint32_t* counters, cudaStream_t s);
+
 // Processing order for a batch: paths with more than `big_points` points first (their work can
 // exceed the rest of a launch), then the others. `counters` holds two u32 and is reset here.
 // Outputs do not depend on the order (offsets come from the scan by path index).

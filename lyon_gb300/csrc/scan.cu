@@ -276,6 +276,62 @@ __global__ void classify_place_kernel(const uint8_t* path_class, uint32_t n,
     if (i < n) order[start[c] + local[c] + rank] = i;
 }
 
+// Order by size: bin 31 - floor(log2(points)) (0 points: bin 32), so bigger paths come first.
+__global__ void size_count_kernel(const uint32_t* point_offsets, uint32_t n, uint8_t* cls,
+                                  uint32_t* counters) {
+    __shared__ uint32_t hist[SIZE_ORDER_BINS];
+    for (uint32_t b = threadIdx.x; b < SIZE_ORDER_BINS; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const uint32_t pts = point_offsets[i + 1] - point_offsets[i];
+        const uint32_t c = pts == 0 ? 32u : (uint32_t)__clz(pts);
+        cls[i] = (uint8_t)c;
+        atomicAdd(&hist[c], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < SIZE_ORDER_BINS; b += blockDim.x)
+        if (hist[b]) atomicAdd(&counters[b], hist[b]);
+}
+
+__global__ void size_place_kernel(const uint8_t* cls, uint32_t n, uint32_t* order,
+                                  uint32_t* counters) {
+    __shared__ uint32_t start[SIZE_ORDER_BINS];
+    __shared__ uint32_t local[SIZE_ORDER_BINS];
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (uint32_t b = 0; b < SIZE_ORDER_BINS; ++b) {
+            start[b] = acc;
+            acc += counters[b];
+        }
+    }
+    for (uint32_t b = threadIdx.x; b < SIZE_ORDER_BINS; b += blockDim.x) local[b] = 0;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t c = 0, rank = 0;
+    if (i < n) {
+        c = cls[i];
+        rank = atomicAdd(&local[c], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < SIZE_ORDER_BINS; b += blockDim.x)
+        if (local[b]) local[b] = atomicAdd(&counters[SIZE_ORDER_BINS + b], local[b]);
+    __syncthreads();
+    if (i < n) order[start[c] + local[c] + rank] = i;
+}
+
+cudaError_t launch_size_order(const uint32_t* point_offsets, uint32_t n, uint8_t* cls,
+                              uint32_t* order, uint32_t* counters, cudaStream_t s) {
+    cudaMemsetAsync(counters, 0, 2 * SIZE_ORDER_BINS * sizeof(uint32_t), s);
+    if (n == 0) return cudaGetLastError();
+    const uint32_t blocks = (n + 255) / 256;
+    size_count_kernel<<<blocks, 256, 0, s>>>(point_offsets, n, cls, counters);
+    note_launches(1);
+    size_place_kernel<<<blocks, 256, 0, s>>>(cls, n, order, counters);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_classify_paths(const uint8_t* verbs, const uint32_t* verb_offsets,
                                   const uint32_t* point_offsets, uint32_t n, uint32_t big_points,
                                   uint32_t short_points, uint8_t* path_class, uint32_t* order,

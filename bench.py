@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-polylines", action="store_true")
     ap.add_argument("--no-variable-width", action="store_true")
     ap.add_argument("--vw-paths", type=int, default=200_000)
+    ap.add_argument("--no-custom-attributes", action="store_true")
     ap.add_argument("--polyline-paths", type=int, default=2_000_000)
     ap.add_argument("--serve-seconds", type=float, default=0.1)
     ap.add_argument("--profile-fill", action="store_true",
@@ -355,6 +356,8 @@ def main():
             line["polylines_autotuned"] = run_polylines(ctx, args, T)
         if not args.no_variable_width:
             line["variable_width"] = run_variable_width(ctx, args, T)
+        if not args.no_custom_attributes:
+            line["custom_attributes"] = run_custom_attributes(ctx, args, T)
         if not args.no_serve and world == 1:
             del db, od
             ctx.close()
@@ -478,6 +481,61 @@ def run_variable_width(ctx, args, T):
                            "kind": "port",
                            "sample": f"first {n} paths, {cv} output vertices, "
                                      f"{dt:.2f} s wall on {threads} threads"}
+    return out
+
+
+def run_custom_attributes(ctx, args, T):
+    """Custom endpoint attributes (lyon_gpu_stroke_paths_custom): the variable-width workload's
+    paths with a fixed width and two f32 attributes per point; every vertex's source and its
+    interpolated attributes are written beside the positions. CPU baseline: the oracle strokes a
+    sample recording sources, then interpolates with numpy."""
+    import torch
+    from lyon_gb300 import workloads
+    from oracle import lyon_oracle as orc
+    batch, opts = workloads.batched_stroke(args.vw_paths, seed=2)
+    attrs = np.random.default_rng(22).uniform(0.0, 1.0, size=(len(batch.points), 2)).astype(
+        np.float32)
+    db = T.DeviceBatch.upload(batch, 0)
+    od = T.upload_options(opts, 0)
+    ad = torch.from_numpy(attrs).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    res = T.tessellate_paths("stroke", db, od, len(opts), 32, T.INDEX_GLOBAL, 0, ctx,
+                             custom_attributes=ad)
+    ctx.synchronize()
+    steps = max(1, args.steps)
+    launches0 = ctx.lib.lyon_gpu_kernel_launches()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        res = T.tessellate_paths("stroke", db, od, len(opts), 32, T.INDEX_GLOBAL, 0, ctx,
+                                 custom_attributes=ad)
+    end.record(stream)
+    end.synchronize()
+    ms = start.elapsed_time(end) / steps
+    out = {"workload": f"custom_attributes_{batch.num_paths}_paths",
+           "config": {"paths": batch.num_paths, "generator": "batched stroke, seed 2",
+                      "attributes": "2 f32 per point, U[0, 1], seed 22", "width": "fixed",
+                      "index_bits": 32, "index_mode": "global",
+                      "outputs": "positions, indices, vertex sources, interpolated attributes"},
+           "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
+           "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
+           "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
+    threads = os.cpu_count() or 1
+    n = min(20_000, batch.num_paths)
+    sub = batch.head(n)
+    # The oracle's output pass (stroke with sources into per-path buffers, copied to the
+    # offsets its count pass gave) and its C interpolation; the count pass is not timed.
+    r = orc.batch_stroke_sources(sub, opts[:n], 32, threads)
+    t0 = time.perf_counter()
+    orc.interpolate_attributes_threads(r["sources"], attrs, threads)
+    dt = r["output_pass_s"] + time.perf_counter() - t0
+    cv = int(r["vtx_counts"].sum())
+    out["cpu_baseline"] = {"value": cv / dt, "unit": "vertices/s", "cores": threads,
+                           "kind": "port",
+                           "sample": f"first {n} paths, {cv} output vertices, "
+                                     f"{dt:.2f} s wall on {threads} threads (output pass "
+                                     f"and interpolation)"}
     return out
 
 

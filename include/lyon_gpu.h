@@ -239,6 +239,66 @@ int lyon_gpu_stroke_paths_variable_width(lyon_gpu_context* ctx, const lyon_path_
                                          uint32_t vertex_offset, int vertex_attributes,
                                          lyon_gpu_batch_output* out);
 
+/* ---- Custom endpoint attributes: vertex sources and interpolated attributes ---------------- */
+
+/* VertexSource (crates/tessellation/src/lib.rs:282-291), what StrokeVertex::source returns
+ * (crates/tessellation/src/stroke.rs:2719-2722): the path endpoint a vertex was made for
+ * (`to` == LYON_NO_ENDPOINT: Endpoint { id: from }) or a point at parameter `t` of the curve
+ * between two endpoints (Edge { from, to, t }). Endpoint ids index the batch's point array (for a
+ * one-path call: the path's, which are lyon's EndpointId values for a Path built without
+ * attributes). 12 bytes. */
+#define LYON_NO_ENDPOINT 0xFFFFFFFFu
+typedef struct lyon_vertex_source {
+    uint32_t from;
+    uint32_t to;
+    float t;
+} lyon_vertex_source;
+
+/* The per-vertex outputs of lyon_gpu_stroke_paths_custom, in device memory owned by the context
+ * (valid until its next call). */
+typedef struct lyon_gpu_custom_output {
+    const lyon_vertex_source* sources; /* total_vertices records */
+    const float* attributes;           /* num_attributes floats per vertex, NULL when none */
+} lyon_gpu_custom_output;
+
+/* StrokeTessellator::tessellate_path for paths that carry custom endpoint attributes
+ * (crates/tessellation/src/stroke.rs:164-177 taking its `path.num_attributes() > 0` branch:
+ * tessellate_with_ids, :641-652), with a vertex constructor that reads StrokeVertex::source and
+ * StrokeVertex::interpolated_attributes (:2719-2747). `attributes` (device memory) holds
+ * `num_attributes` floats per point of the batch, indexed like `points` (entries of control points
+ * and of Close's repeated point are not read); `width_attribute` is
+ * StrokeOptions::variable_line_width: -1 for a fixed line width, else the index of the attribute
+ * that scales options.line_width. Writes positions, or lyon_stroke_vertex records when
+ * `vertex_attributes` is non-zero, to `out` as lyon_gpu_stroke_paths does, and each vertex's
+ * source and interpolated attributes to `custom`. Each path is stroked by one thread with lyon's
+ * sequential stepper (both passes). */
+int lyon_gpu_stroke_paths_custom(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                                 const float* attributes, uint32_t num_attributes,
+                                 int32_t width_attribute, const lyon_stroke_options* options,
+                                 uint32_t num_options, int index_bits, int index_mode,
+                                 uint32_t vertex_offset, int vertex_attributes,
+                                 lyon_gpu_batch_output* out, lyon_gpu_custom_output* custom);
+
+/* StrokeVertex::interpolated_attributes (crates/tessellation/src/stroke.rs:2728-2747) over many
+ * vertices (device memory, context's stream): out[v * num_attributes + i] is
+ * attributes[from * num_attributes + i] for an endpoint source and a * (1 - t) + b * t (f32, in
+ * that order) for an edge. A source whose ids are not below `num_endpoints` gives NaN. */
+int lyon_gpu_interpolate_attributes(lyon_gpu_context* ctx, const lyon_vertex_source* sources,
+                                    uint64_t num_vertices, const float* attributes,
+                                    uint32_t num_attributes, uint64_t num_endpoints, float* out);
+
+/* One path with custom attributes (host memory in and out): lyon_gpu_stroke_paths_custom on a
+ * one-path batch. `result` is as for lyon_gpu_stroke_path (records when `vertex_attributes`);
+ * `*sources` and `*vertex_attribute_values` (num_attributes floats per vertex) point at host
+ * memory valid until the next call on the context. */
+int lyon_gpu_stroke_path_custom(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                                const float* points, uint32_t num_points,
+                                const float* attributes, uint32_t num_attributes,
+                                int32_t width_attribute, const lyon_stroke_options* options,
+                                int index_bits, uint32_t index_base, int vertex_attributes,
+                                lyon_gpu_result* result, const lyon_vertex_source** sources,
+                                const float** vertex_attribute_values);
+
 /* Basic shapes: FillTessellator::tessellate_rectangle and tessellate_circle
  * (crates/tessellation/src/fill.rs:654-673 with crates/tessellation/src/basic_shapes.rs:12-124),
  * which fill without the sweep, over a batch of shapes. `params` (device memory) holds 4 floats

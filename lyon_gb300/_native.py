@@ -37,6 +37,14 @@ class CBatchOutput(ctypes.Structure):
                 ("total_vertices", u64), ("total_indices", u64), ("num_failed_paths", u32)]
 
 
+class CVertexSource(ctypes.Structure):
+    _fields_ = [("from_", u32), ("to", u32), ("t", ctypes.c_float)]
+
+
+class CCustomOutput(ctypes.Structure):
+    _fields_ = [("sources", c_p), ("attributes", c_p)]
+
+
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
                 ("device_budget_bytes", u64)]
@@ -167,6 +175,16 @@ def load(build_if_missing: bool = True):
         L.lyon_gpu_stroke_path_variable_width.restype = ctypes.c_int
         L.lyon_gpu_stroke_path_variable_width.argtypes = [c_p, c_p, u32, c_p, u32, c_p, c_p,
                                                           ctypes.c_int, u32, ctypes.c_int, c_p]
+        L.lyon_gpu_stroke_paths_custom.restype = ctypes.c_int
+        L.lyon_gpu_stroke_paths_custom.argtypes = [c_p, c_p, c_p, u32, i32, c_p, u32,
+                                                   ctypes.c_int, ctypes.c_int, u32, ctypes.c_int,
+                                                   c_p, c_p]
+        L.lyon_gpu_interpolate_attributes.restype = ctypes.c_int
+        L.lyon_gpu_interpolate_attributes.argtypes = [c_p, c_p, u64, c_p, u32, u64, c_p]
+        L.lyon_gpu_stroke_path_custom.restype = ctypes.c_int
+        L.lyon_gpu_stroke_path_custom.argtypes = [c_p, c_p, u32, c_p, u32, c_p, u32, i32, c_p,
+                                                  ctypes.c_int, u32, ctypes.c_int, c_p,
+                                                  ctypes.POINTER(c_p), ctypes.POINTER(c_p)]
         L.lyon_gpu_autotune_stroke.restype = ctypes.c_int
         L.lyon_gpu_autotune_stroke.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
                                                ctypes.POINTER(CStrokeTuning),
@@ -194,5 +212,6 @@ EXPORTED = [
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
     "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",
     "lyon_gpu_stroke_paths_variable_width", "lyon_gpu_stroke_path_variable_width",
-    "lyon_gpu_fill_shapes", "lyon_svg_parse_paths",
+    "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_stroke_paths_custom",
+    "lyon_gpu_interpolate_attributes", "lyon_gpu_stroke_path_custom",
 ]

@@ -52,6 +52,11 @@ struct lyon_gpu_context {
     uint32_t short_path_points = 32;   // line-only paths up to this size: one per thread
     bool vertex_attrs = false;  // during a *_attributes call: lyon_stroke_vertex records
     const float* vw_widths = nullptr;  // during a variable-width call: width factors (device)
+    uint32_t width_stride = 1;         // floats between consecutive points' width factors
+    bool want_sources = false;  // during a custom-attribute call: sequential stepper + sources
+    DevBuf out_sources, out_attrs;      // per-vertex sources and interpolated attributes
+    DevBuf in_attrs;                    // single-path custom attributes (staged)
+    HostBuf h_out_src, h_out_attrs;
     // outputs of device-buffer batched calls
     DevBuf out_vertices, out_indices;
     // host-buffer calls: inputs and double-buffered outputs
@@ -298,6 +303,9 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
     a.vertex_offset = (uint32_t)vertex_offset;
     a.vertex_attrs = ctx->vertex_attrs ? 1 : 0;
     a.widths = ctx->vw_widths;
+    a.width_stride = ctx->width_stride;
+    a.sequential = ctx->want_sources ? 1 : 0;
+    a.sources = ctx->want_sources ? as<lyon_vertex_source>(ctx->out_sources) : nullptr;
     a.request_first = ctx->request_first;
     if (ctx->split_valid) {
         a.item_split = as<uint32_t>(ctx->class_counters) + 2 * (3 + ctx->short_path_points);
@@ -330,8 +338,8 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     if (kind == KIND_STROKE) {
         // Long paths first, so that no single long path is left running at the end of a launch;
         // short line-only paths last, for the one-thread-per-path phase.
-        if (ctx->vw_widths) {
-            // The variable-width kernel takes paths in index order.
+        if (ctx->vw_widths || ctx->want_sources) {
+            // The sequential stepper takes paths in index order.
         } else if (n > 0 && ctx->short_path_points > 0) {
             if (ensure(ctx, ctx->order, (size_t)n * 4) && ensure(ctx, ctx->path_class, n) &&
                 ensure(ctx, ctx->class_counters, lg::CLASSIFY_COUNTER_WORDS * 4) &&
@@ -420,7 +428,9 @@ int batched_device(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     if (r != LYON_OK) return r;
     const size_t vbytes = ctx->vertex_attrs ? sizeof(lyon_stroke_vertex) : 8;
     if (!ensure(ctx, ctx->out_vertices, tv * vbytes + 16) ||
-        !ensure(ctx, ctx->out_indices, ti * (index_bits / 8) + 16))
+        !ensure(ctx, ctx->out_indices, ti * (index_bits / 8) + 16) ||
+        (ctx->want_sources &&
+         !ensure(ctx, ctx->out_sources, tv * sizeof(lyon_vertex_source) + 16)))
         return LYON_ERR_OUT_OF_MEMORY;
     r = pipeline_emit(ctx, kind, batch, options, num_options, index_bits, index_mode,
                       vertex_offset, as<float>(ctx->out_vertices), ctx->out_indices.ptr, tv);
@@ -565,9 +575,10 @@ int batched_host(lyon_gpu_context* ctx, int kind, const lyon_path_batch* hb, con
 bool stage_single_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
                        const float* points, uint32_t num_points, const void* options,
                        size_t options_size, lyon_path_batch* batch,
-                       const float* widths = nullptr) {
+                       const float* widths = nullptr, uint32_t floats_per_point = 1) {
     cudaStream_t s = ctx->stream;
-    size_t vb = num_verbs, pb = (size_t)num_points * 8, wb = widths ? (size_t)num_points * 4 : 0;
+    size_t vb = num_verbs, pb = (size_t)num_points * 8;
+    size_t wb = widths ? (size_t)num_points * floats_per_point * 4 : 0;
     if (!ensure(ctx, ctx->in_verbs, vb + 16) || !ensure(ctx, ctx->in_points, pb + 16) ||
         !ensure(ctx, ctx->in_offsets, 64) || !ensure(ctx, ctx->in_options, 64) ||
         (widths && !ensure(ctx, ctx->in_widths, wb + 16)) ||
@@ -605,7 +616,8 @@ bool stage_single_path(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num
 int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t num_verbs,
                 const float* points, uint32_t num_points, const void* options, size_t opt_size,
                 int index_bits, uint32_t index_base, lyon_gpu_result* result,
-                const float* widths = nullptr) {
+                const float* point_floats = nullptr, uint32_t floats_per_point = 1,
+                int32_t width_index = 0) {
     if (!ctx || !options || !result || (index_bits != 16 && index_bits != 32) ||
         (num_verbs && !verbs) || (num_points && !points)) {
         if (ctx) ctx->last_error = "invalid argument";
@@ -615,9 +627,12 @@ int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t 
     memset(result, 0, sizeof(*result));
     lyon_path_batch b;
     if (!stage_single_path(ctx, verbs, num_verbs, points, num_points, options, opt_size, &b,
-                           widths))
+                           point_floats, floats_per_point))
         return LYON_ERR_OUT_OF_MEMORY;
-    if (widths) ctx->vw_widths = as<float>(ctx->in_widths);
+    if (point_floats && width_index >= 0) {
+        ctx->vw_widths = as<float>(ctx->in_widths) + width_index;
+        ctx->width_stride = floats_per_point;
+    }
     lyon_gpu_batch_output bo;
     int r = batched_device(ctx, kind, &b, ctx->in_options.ptr, 1, index_bits,
                            LYON_INDEX_PER_PATH, index_base, &bo);
@@ -628,6 +643,26 @@ int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t 
     size_t ib = bo.total_indices * (index_bits / 8);
     if (!ensure_host(ctx, ctx->h_out_v, vb + 16) || !ensure_host(ctx, ctx->h_out_i, ib + 16))
         return LYON_ERR_OUT_OF_MEMORY;
+    if (ctx->want_sources) {
+        // Custom attributes: the vertices' sources and their interpolated attributes.
+        const size_t sb = bo.total_vertices * sizeof(lyon_vertex_source);
+        const size_t ab = point_floats ? bo.total_vertices * floats_per_point * 4 : 0;
+        if (!ensure_host(ctx, ctx->h_out_src, sb + 16) ||
+            !ensure_host(ctx, ctx->h_out_attrs, ab + 16) ||
+            (ab && !ensure(ctx, ctx->out_attrs, ab + 16)))
+            return LYON_ERR_OUT_OF_MEMORY;
+        if (ab &&
+            !set_err(ctx, "interpolate",
+                     lg::launch_interpolate(as<lyon_vertex_source>(ctx->out_sources),
+                                            bo.total_vertices, as<float>(ctx->in_widths),
+                                            floats_per_point, num_points,
+                                            as<float>(ctx->out_attrs), ctx->num_sms, s)))
+            return LYON_ERR_CUDA;
+        if (sb) cudaMemcpyAsync(ctx->h_out_src.ptr, ctx->out_sources.ptr, sb,
+                                cudaMemcpyDeviceToHost, s);
+        if (ab) cudaMemcpyAsync(ctx->h_out_attrs.ptr, ctx->out_attrs.ptr, ab,
+                                cudaMemcpyDeviceToHost, s);
+    }
     cudaMemcpyAsync(ctx->h_small.ptr, bo.status, 4, cudaMemcpyDeviceToHost, s);
     if (vb) cudaMemcpyAsync(ctx->h_out_v.ptr, bo.vertices, vb, cudaMemcpyDeviceToHost, s);
     if (ib) cudaMemcpyAsync(ctx->h_out_i.ptr, bo.indices, ib, cudaMemcpyDeviceToHost, s);
@@ -722,11 +757,12 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
                       &ctx->in_options, &ctx->order, &ctx->slot_status[0],
                       &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters,
-                      &ctx->in_widths};
+                      &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
-    HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v, &ctx->h_out_i, &ctx->h_small,
-                     &ctx->h_offs, &ctx->h_status};
+    HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v,  &ctx->h_out_i,
+                     &ctx->h_small, &ctx->h_offs,   &ctx->h_status, &ctx->h_out_src,
+                     &ctx->h_out_attrs};
     for (HostBuf* b : hb) free_host(*b);
     for (int i = 0; i < 4; ++i)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
@@ -1009,6 +1045,91 @@ int lyon_gpu_stroke_path_variable_width(lyon_gpu_context* ctx, const uint8_t* ve
                         num_points ? widths : &kNoPoints);
     ctx->vertex_attrs = false;
     ctx->vw_widths = nullptr;
+    ctx->width_stride = 1;
+    return r;
+}
+
+int lyon_gpu_stroke_paths_custom(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                                 const float* attributes, uint32_t num_attributes,
+                                 int32_t width_attribute, const lyon_stroke_options* options,
+                                 uint32_t num_options, int index_bits, int index_mode,
+                                 uint32_t vertex_offset, int vertex_attributes,
+                                 lyon_gpu_batch_output* out, lyon_gpu_custom_output* custom) {
+    if (!ctx || !custom || width_attribute < -1 ||
+        (width_attribute >= 0 && (uint32_t)width_attribute >= num_attributes) ||
+        (num_attributes > 0 && !attributes && batch && batch->num_paths > 0))
+        return LYON_ERR_INVALID_ARGUMENT;
+    memset(custom, 0, sizeof(*custom));
+    ctx->vertex_attrs = vertex_attributes != 0;
+    ctx->vw_widths = width_attribute >= 0 ? attributes + width_attribute : nullptr;
+    ctx->width_stride = num_attributes ? num_attributes : 1;
+    ctx->want_sources = true;
+    int r = batched_device(ctx, KIND_STROKE, batch, options, num_options, index_bits, index_mode,
+                           vertex_offset, out);
+    ctx->vertex_attrs = false;
+    ctx->vw_widths = nullptr;
+    ctx->width_stride = 1;
+    ctx->want_sources = false;
+    if (r != LYON_OK) return r;
+    custom->sources = as<lyon_vertex_source>(ctx->out_sources);
+    if (num_attributes > 0 && out->total_vertices > 0) {
+        if (!ensure(ctx, ctx->out_attrs, out->total_vertices * num_attributes * 4 + 16))
+            return LYON_ERR_OUT_OF_MEMORY;
+        // The sources come from the batch's own points: every id is in range.
+        if (!set_err(ctx, "interpolate",
+                     lg::launch_interpolate(custom->sources, out->total_vertices, attributes,
+                                            num_attributes, ~0ull, as<float>(ctx->out_attrs),
+                                            ctx->num_sms, ctx->stream)))
+            return LYON_ERR_CUDA;
+        custom->attributes = as<float>(ctx->out_attrs);
+    }
+    return LYON_OK;
+}
+
+int lyon_gpu_interpolate_attributes(lyon_gpu_context* ctx, const lyon_vertex_source* sources,
+                                    uint64_t num_vertices, const float* attributes,
+                                    uint32_t num_attributes, uint64_t num_endpoints, float* out) {
+    if (!ctx || (num_vertices && num_attributes && (!sources || !attributes || !out)))
+        return LYON_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (!set_err(ctx, "interpolate",
+                 lg::launch_interpolate(sources, num_vertices, attributes, num_attributes,
+                                        num_endpoints, out, ctx->num_sms, ctx->stream)))
+        return LYON_ERR_CUDA;
+    return LYON_OK;
+}
+
+int lyon_gpu_stroke_path_custom(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                                const float* points, uint32_t num_points,
+                                const float* attributes, uint32_t num_attributes,
+                                int32_t width_attribute, const lyon_stroke_options* options,
+                                int index_bits, uint32_t index_base, int vertex_attributes,
+                                lyon_gpu_result* result, const lyon_vertex_source** sources,
+                                const float** vertex_attribute_values) {
+    if (!ctx || width_attribute < -1 ||
+        (width_attribute >= 0 && (uint32_t)width_attribute >= num_attributes) ||
+        (num_attributes > 0 && num_points > 0 && !attributes))
+        return LYON_ERR_INVALID_ARGUMENT;
+    if (sources) *sources = nullptr;
+    if (vertex_attribute_values) *vertex_attribute_values = nullptr;
+    // A path without points still stages one (unread) float per attribute.
+    static const float kNoPoints[1] = {1.0f};
+    const float* pf = num_attributes == 0 ? nullptr : (num_points ? attributes : kNoPoints);
+    const uint32_t fpp = num_attributes == 0 ? 1 : (num_points ? num_attributes : 1);
+    ctx->vertex_attrs = vertex_attributes != 0;
+    ctx->want_sources = true;
+    int r = single_path(ctx, KIND_STROKE, verbs, num_verbs, points, num_points, options,
+                        sizeof(lyon_stroke_options), index_bits, index_base, result, pf, fpp,
+                        num_points ? width_attribute : (width_attribute >= 0 ? 0 : -1));
+    ctx->vertex_attrs = false;
+    ctx->want_sources = false;
+    ctx->vw_widths = nullptr;
+    ctx->width_stride = 1;
+    if (r == LYON_OK) {
+        if (sources) *sources = reinterpret_cast<const lyon_vertex_source*>(ctx->h_out_src.ptr);
+        if (vertex_attribute_values && num_attributes)
+            *vertex_attribute_values = reinterpret_cast<const float*>(ctx->h_out_attrs.ptr);
+    }
     return r;
 }
 

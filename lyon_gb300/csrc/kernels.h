@@ -48,6 +48,12 @@ struct StrokeArgs {
     // warp items left; `seq_counter` (zeroed before each launch) hands out those.
     const uint32_t* item_split;
     uint32_t* seq_counter;
+    // Non-zero: every path is stroked by lyon's sequential stepper, one path per thread, in both
+    // passes (set by the custom-attribute calls; `widths` implies it). With `sources` the emit
+    // pass writes each vertex's lyon_vertex_source next to it.
+    int sequential;
+    lyon_vertex_source* sources;
+    uint32_t width_stride;  // floats from one point's width factor to the next's (0 means 1)
 };
 
 // Basic shapes (shapes.cu): `params` holds 4 floats per rectangle (min x, min y, max x, max y)
@@ -73,6 +79,13 @@ cudaError_t launch_shapes(const ShapeArgs& args, bool emit, cudaStream_t stream)
 
 int stroke_blocks_per_sm();
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);
+// The sequential stepper (stroke_seq.cu): variable line width and the vertex-source output.
+cudaError_t launch_stroke_seq(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);
+// StrokeVertex::interpolated_attributes over `n` vertex sources (stroke_seq.cu).
+cudaError_t launch_interpolate(const lyon_vertex_source* sources, uint64_t n,
+                               const float* attributes, uint32_t num_attributes,
+                               uint64_t num_endpoints, float* out, int num_sms,
+                               cudaStream_t stream);
 
 // Exclusive scan of two u32 arrays into two u64 arrays (decoupled look-back), plus totals at
 // out_a[n] / out_b[n]. `tile_state` holds 2 * num_tiles(n) u64 and `counter` one u32; both are

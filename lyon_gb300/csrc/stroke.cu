@@ -29,6 +29,7 @@
 // test of flattened_step cannot fire instead of evaluating it, see below); a look-back scan turns
 // its per-path counts into offsets; the emit kernel repeats the walk and writes at those offsets.
 #include "stroke_core.cuh"
+#include "stroke_out.cuh"
 #include "kernels.h"
 
 namespace lg {
@@ -119,60 +120,6 @@ __device__ __forceinline__ bool same_bits(V2 a, V2 b) {
            __float_as_uint(a.y) == __float_as_uint(b.y);
 }
 
-struct PathOut {
-    uint32_t id_base;  // id of the path's first vertex
-    float2* vout;      // positions; null when counting or writing attribute records
-    lyon_stroke_vertex* rout;  // attribute records (the attribute output), else null
-    void* iout;
-    int bits;
-    uint32_t vmax, imax;  // the path's counts from the count pass (write bounds when emitting)
-};
-
-__device__ __forceinline__ uint32_t cap_left(uint32_t total, uint32_t used) {
-    return used < total ? total - used : 0u;
-}
-
-template <bool EMIT, bool ATTR>
-__device__ __forceinline__ PathOut path_out(const StrokeArgs& A, uint32_t path) {
-    PathOut po;
-    po.bits = A.index_bits;
-    if (EMIT) {
-        const uint64_t vo = A.vtx_offsets[path];
-        const uint64_t io = A.idx_offsets[path];
-        po.vout = ATTR ? nullptr : reinterpret_cast<float2*>(A.vertices) + vo;
-        po.rout = ATTR ? reinterpret_cast<lyon_stroke_vertex*>(A.vertices) + vo : nullptr;
-        po.iout = A.index_bits == 16 ? (void*)((uint16_t*)A.indices + io)
-                                     : (void*)((uint32_t*)A.indices + io);
-        const uint64_t rb = A.request_first ? A.vtx_offsets[A.request_first[path]] : 0ull;
-        po.id_base =
-            A.vertex_offset + (A.index_mode == LYON_INDEX_GLOBAL ? (uint32_t)(vo - rb) : 0u);
-        po.vmax = A.vtx_counts[path];
-        po.imax = A.idx_counts[path];
-    } else {
-        po.vout = nullptr;
-        po.rout = nullptr;
-        po.iout = nullptr;
-        po.id_base = 0;
-        po.vmax = 0xFFFFFFFFu;
-        po.imax = 0xFFFFFFFFu;
-    }
-    return po;
-}
-
-// Final per-path bookkeeping: the count pass records counts and status; the emit pass flags a
-// path whose walk disagreed with the count pass (its writes were bounded by the path's range).
-template <bool EMIT>
-__device__ __forceinline__ void finish_path(const StrokeArgs& A, uint32_t path, uint32_t vc,
-                                            uint32_t ic, int st, const PathOut& po) {
-    if (!EMIT) {
-        A.vtx_counts[path] = st == LYON_OK ? vc : 0u;
-        A.idx_counts[path] = st == LYON_OK ? ic : 0u;
-        A.status[path] = st;
-    } else if (st != LYON_OK || vc != po.vmax || ic != po.imax) {
-        A.status[path] = st != LYON_OK ? st : LYON_ERR_INTERNAL;
-    }
-}
-
 // t state carried across step chunks: the chunk's last step.
 struct TCarry {
     uint32_t verb;  // absolute verb index, or NO_VERB when the last step was not inside a curve
@@ -205,17 +152,6 @@ struct SubState {
     // Advancements (attribute output only): of the first point, of c1 and of c2.
     float adv0, adv1, adv2;
 };
-
-__device__ __forceinline__ uint32_t points_of_verb(int kind) {
-    switch (kind) {
-        case LYON_VERB_LINE_TO: return 1;
-        case LYON_VERB_QUADRATIC_TO: return 2;
-        case LYON_VERB_CUBIC_TO: return 3;
-        case LYON_VERB_BEGIN: return 1;
-        case LYON_VERB_CLOSE: return 1;
-        default: return 0;
-    }
-}
 
 // Flattening parameters of one verb of a window (lane = verb): lines and Begin give one step;
 // quadratics are split at a sharp turn (stroke.rs:2755-2779, 3178-3212) and each part gets lyon's
@@ -1249,140 +1185,6 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
     finish_path<EMIT>(A, path, s.nv, s.ni, status, po);
 }
 
-// A flattened run of a curve for the variable-width stepper: lyon's for_each_flattened_with_t
-// loop (quadratic_bezier.rs:891-938, cubic_bezier.rs:1318-1363: t advances by 1/n, the last
-// point is the end point at t = 1), with the curve parameter mapped to the width's t as
-// flatten_quad does for a split quadratic (stroke.rs:2755-2779: t = tadd + t_run * tmul) and the
-// half width interpolated linearly (stroke.rs:1022, 1060).
-template <class SK>
-__device__ __noinline__ void vw_flatten(VwState& W, const Poly& poly, V2 to, float n, float tmul,
-                                        float tadd, float sw, float ew, const StrokeParams& P,
-                                        SK& sink, int* status) {
-    const float step = 1.0f / n;
-    const uint32_t count = to_u32_or1(n) - 1;
-    float t0 = 0.0f;
-    for (uint32_t i = 0; i <= count; ++i) {
-        const bool last = i == count;
-        const float t1 = last ? 1.0f : t0 + step;
-        const V2 q = last ? to : poly_sample(poly, t1);
-        const float t = tadd + t1 * tmul;
-        DEP d;
-        dep_init(d, q, (sw * (1.0f - t) + ew * t) * 0.5f, P.line_join, t1 != 1.0f);
-        vw_step(W, d, P, sink, status);
-        t0 = t1;
-    }
-}
-
-// One thread strokes one path with a variable line width (tessellate_with_ids_vw,
-// stroke.rs:654-767): an endpoint's half width is line_width x its factor x 0.5. Verbs are
-// checked as they come (a Begin inside a sub-path, a sub-path without Begin, missing points or an
-// unknown verb fail the path with LYON_ERR_INVALID_ARGUMENT).
-template <bool EMIT, bool ATTR>
-__device__ __noinline__ void stroke_path_vw(const StrokeArgs& A, uint32_t path) {
-    const PathOut po = path_out<EMIT, ATTR>(A, path);
-    const uint32_t v_begin = A.verb_offsets[path], v_end = A.verb_offsets[path + 1];
-    const uint32_t p_end = A.point_offsets[path + 1];
-    const lyon_stroke_options opt = A.options[A.num_options > 1 ? path : 0];
-    const StrokeParams P = make_params(opt);
-    const float lw = opt.line_width;
-    SinkT<ATTR> s;
-    s.id_base = po.id_base;
-    s.nv = 0;
-    s.ni = 0;
-    s.vout = po.vout;
-    s.rout = po.rout;
-    s.iout = po.iout;
-    s.index_bits = po.bits;
-    s.vcap = po.vmax;
-    s.icap = po.imax;
-    s.overflow = false;
-    VwState W;
-    W.pb.start = W.pb.count = W.pb.n = 0;
-    W.nfirsts = 0;
-    W.mnec = false;
-    W.start_adv = 0.0f;
-    int status = LYON_OK;
-    bool open = false;
-    V2 cur = V2{0.0f, 0.0f};
-    float cur_w = 0.0f;
-    uint32_t pc = A.point_offsets[path];
-    for (uint32_t vi = v_begin; vi < v_end && status == LYON_OK; ++vi) {
-        const int k = A.verbs[vi];
-        if (k > LYON_VERB_END || pc + points_of_verb(k) > p_end ||
-            (k == LYON_VERB_BEGIN) == open) {
-            status = LYON_ERR_INVALID_ARGUMENT;
-            break;
-        }
-        if (k == LYON_VERB_BEGIN || k == LYON_VERB_LINE_TO) {
-            cur = load_pt(A.points, pc);
-            cur_w = A.widths[pc];
-            ++pc;
-            DEP d;
-            dep_init(d, cur, lw * cur_w * 0.5f, P.line_join, false);
-            if (k == LYON_VERB_BEGIN) {
-                open = true;
-                W.mnec = false;
-                d.adv = W.start_adv;
-            }
-            vw_step(W, d, P, s, &status);
-        } else if (k == LYON_VERB_QUADRATIC_TO) {
-            const V2 ctrl = load_pt(A.points, pc);
-            const V2 to = load_pt(A.points, pc + 1);
-            const float w1 = A.widths[pc + 1];
-            pc += 2;
-            const float sw = lw * cur_w, ew = lw * w1;
-            float ts;
-            if (find_sharp_turn(cur, ctrl, to, &ts)) {
-                const V2 sp = quad_sample(cur, ctrl, to, ts);
-                const V2 bc = lerp(cur, ctrl, ts);
-                const V2 ac = lerp(ctrl, to, ts);
-                vw_flatten(W, quad_poly(cur, bc, sp), sp, quad_wang(cur, bc, sp, P.tolerance), ts,
-                           0.0f, sw, ew, P, s, &status);
-                vw_flatten(W, quad_poly(sp, ac, to), to, quad_wang(sp, ac, to, P.tolerance),
-                           1.0f - ts, ts, sw, ew, P, s, &status);
-            } else {
-                vw_flatten(W, quad_poly(cur, ctrl, to), to, quad_wang(cur, ctrl, to, P.tolerance),
-                           1.0f, 0.0f, sw, ew, P, s, &status);
-            }
-            cur = to;
-            cur_w = w1;
-        } else if (k == LYON_VERB_CUBIC_TO) {
-            const V2 c1 = load_pt(A.points, pc);
-            const V2 c2 = load_pt(A.points, pc + 1);
-            const V2 to = load_pt(A.points, pc + 2);
-            const float w1 = A.widths[pc + 2];
-            pc += 3;
-            vw_flatten(W, cubic_poly(cur, c1, c2, to), to,
-                       cubic_wang(cur, c1, c2, to, P.tolerance), 1.0f, 0.0f, lw * cur_w, lw * w1,
-                       P, s, &status);
-            cur = to;
-            cur_w = w1;
-        } else {  // Close or End
-            if (k == LYON_VERB_CLOSE) ++pc;
-            vw_end(W, k == LYON_VERB_CLOSE, P, s, &status);
-            open = false;
-        }
-    }
-    if (s.overflow && status == LYON_OK) status = LYON_ERR_INTERNAL;
-    finish_path<EMIT>(A, path, s.nv, s.ni, status, po);
-}
-
-// Variable-width strokes: 32 paths per warp, one per lane.
-template <bool EMIT, bool ATTR>
-__global__ void __launch_bounds__(256) stroke_vw_kernel(StrokeArgs A) {
-    const int lane = threadIdx.x & 31;
-    for (;;) {
-        uint32_t first = 0;
-        if (lane == 0) first = atomicAdd(A.work_counter, 32u);
-        first = __shfl_sync(FULL, first, 0);
-        if (first >= A.num_paths) break;
-        const uint32_t path = first + (uint32_t)lane;
-        if (path < A.num_paths && (!EMIT || A.status[path] == LYON_OK))
-            stroke_path_vw<EMIT, ATTR>(A, path);
-        __syncwarp();
-    }
-}
-
 // The short line-only paths (items [split, num_paths) of the order): 32 per warp, one per lane.
 template <bool EMIT, bool ATTR>
 __device__ __noinline__ void stroke_short_paths(const StrokeArgs& A, uint32_t split, int lane) {
@@ -1459,18 +1261,10 @@ int stroke_blocks_per_sm() {
 }
 
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream) {
+    // Variable line width and the custom-attribute output use lyon's sequential stepper, one
+    // path per thread (stroke_seq.cu).
+    if (args.widths || args.sequential) return launch_stroke_seq(args, emit, grid, stream);
     configure_smem();
-    if (args.widths) {
-        if (emit && args.vertex_attrs) {
-            stroke_vw_kernel<true, true><<<grid, 256, 0, stream>>>(args);
-        } else if (emit) {
-            stroke_vw_kernel<true, false><<<grid, 256, 0, stream>>>(args);
-        } else {
-            stroke_vw_kernel<false, false><<<grid, 256, 0, stream>>>(args);
-        }
-        note_launches(1);
-        return cudaGetLastError();
-    }
     // The attribute output is its own instantiation, so the positions kernel carries none of
     // its work (the advancement chain, the record stores).
     if (emit && args.vertex_attrs) {

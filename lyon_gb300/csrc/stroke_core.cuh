@@ -63,6 +63,7 @@ __device__ __forceinline__ void dep_init(DEP& d, V2 pos, float hw, int join, boo
 template <bool REC>
 struct SinkT {
     static constexpr bool kRec = REC;
+    static constexpr bool kSrc = false;  // writes vertex sources (the sequential stepper's sink)
     uint32_t id_base;
     uint32_t nv, ni;
     float2* vout;
@@ -346,7 +347,7 @@ struct ArcPlan {
     bool cr;
 };
 
-__device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side, float tol,
+static __device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side, float tol,
                                                 int* status) {
     V2 center = join.pos;
     float radius = join.hw;
@@ -702,7 +703,7 @@ struct SlowJoin {
 
 // stroke.rs:1586-1608 for a join that is not a flattening step: side positions, folds and the
 // vertex layout. The join (without ids) is stored to *dep for the emission phase.
-__device__ __noinline__ void slow_join_geometry(DEP* dep, V2 prev, V2 cur, bool flat, V2 nxt,
+static __device__ __noinline__ void slow_join_geometry(DEP* dep, V2 prev, V2 cur, bool flat, V2 nxt,
                                                 const StrokeParams& P, SlowJoin* r,
                                                 int* status) {
     DEP J;
@@ -845,7 +846,7 @@ __device__ __forceinline__ void vw_side_attachment(DEP& p0, DEP& p1, float edge_
 }
 
 // stroke.rs:1808-1840
-__device__ __noinline__ void vw_edge_attachments(DEP& p0, DEP& p1) {
+static __device__ __noinline__ void vw_edge_attachments(DEP& p0, DEP& p1) {
     const V2 edge = p1.pos - p0.pos;
     const float d = vlength(edge);
     const float edge_angle = cr_atan2(edge.y, edge.x);
@@ -858,7 +859,7 @@ __device__ __noinline__ void vw_edge_attachments(DEP& p0, DEP& p1) {
 }
 
 // stroke.rs:2060-2128
-__device__ __noinline__ void vw_join_sides(const DEP& prev, DEP& join, const DEP& next,
+static __device__ __noinline__ void vw_join_sides(const DEP& prev, DEP& join, const DEP& next,
                                            float miter_limit, int side) {
     const float sign = side == SN ? -1.0f : 1.0f;
     const V2 v0 = normalize(join.s[side].prev - prev.s[side].next);
@@ -968,57 +969,6 @@ __device__ __noinline__ bool vw_step(VwState& W, DEP next, const StrokeParams& P
         pb.push(next);
     }
     return true;
-}
-
-// end (stroke.rs:1179-1193) with close (1206-1279), end_with_caps (1322-1378) and the empty
-// cap (1282-1316), on the stepper's own points.
-template <class SK>
-__device__ __noinline__ void vw_end(VwState& W, bool close, const StrokeParams& P, SK& sink,
-                                    int* status) {
-    SeqBuffer& pb = W.pb;
-    const uint32_t count = pb.count;
-    W.mnec |= close && count == 1;
-    if (close && count > 2) {
-        DEP p = W.firsts[0];
-        const float start_adv = p.adv;
-        p.adv = __int_as_float(0x7fc00000);
-        if (!vw_step(W, p, P, sink, status)) pb.last().pos = p.pos;
-        if (W.nfirsts >= 2) {
-            vw_step(W, W.firsts[1], P, sink, status);
-            DEP& p0 = pb.second_last();
-            DEP& p1 = pb.last();
-            sink.adv = start_adv;
-            for (int side = 0; side < 2; ++side) {
-                const V2 sp = p0.s[side].has_single ? p0.s[side].single : p0.s[side].next;
-                const V2 normal = (sp - p0.pos) / p0.hw;
-                p0.s[side].next_vertex = sink.vertex(p0.pos + normal * p0.hw, normal, side);
-            }
-            add_edge_triangles(p0, p1, sink);
-        }
-    } else if (W.mnec && count == 1) {
-        const DEP& point = pb.first();
-        sink.adv = point.adv;
-        if (P.start_cap == LYON_CAP_SQUARE) {
-            tessellate_empty_square_cap(point.pos, point.hw, sink);
-        } else if (P.start_cap == LYON_CAP_ROUND) {
-            tessellate_empty_round_cap(point.pos, point.hw, P, sink, status);
-        }
-    } else if (count >= 2) {
-        DEP p0 = pb.second_last();
-        DEP p1 = pb.last();
-        // tessellate_last_edge sets the last point's advancement (stroke.rs:2140), which the
-        // next sub-path starts from.
-        p1.adv = p0.adv + vlength(p1.pos - p0.pos);
-        tessellate_last_edge(p0, p1, count == 2, P, sink, status);
-        W.start_adv = p1.adv;
-        if (count > 2) {
-            p0 = W.firsts[0];
-            p1 = W.firsts[1];
-        }
-        tessellate_first_edge(p0, p1, P, sink, status);
-    }
-    pb.start = pb.count = pb.n = 0;
-    W.nfirsts = 0;
 }
 
 }  // namespace lg

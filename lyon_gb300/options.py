@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass, replace
+from typing import Optional
 
 import numpy as np
 
@@ -63,6 +64,10 @@ class StrokeOptions:
     line_width: float = 1.0
     miter_limit: float = 4.0
     tolerance: float = 0.1
+    # StrokeOptions::variable_line_width (lib.rs:340, 429-432): the index of the path's endpoint
+    # attribute that scales line_width, or None. Passed beside the C record, which has no field
+    # for it.
+    variable_line_width: Optional[int] = None
 
     MINIMUM_MITER_LIMIT = 1.0
 
@@ -91,6 +96,9 @@ class StrokeOptions:
 
     def with_line_width(self, width: float) -> "StrokeOptions":
         return replace(self, line_width=width)
+
+    def with_variable_line_width(self, index: int) -> "StrokeOptions":
+        return replace(self, variable_line_width=index)
 
     def with_miter_limit(self, limit: float) -> "StrokeOptions":
         # lib.rs:423-427 asserts limit >= MINIMUM_MITER_LIMIT.

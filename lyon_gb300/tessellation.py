@@ -158,6 +158,72 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
 
 
+def custom_vertex_dtype(num_attributes: int) -> np.dtype:
+    """What the vertex constructor receives for a path with custom attributes: the
+    lyon_stroke_vertex fields, the vertex's source (StrokeVertex::source: `src_to` is
+    NO_ENDPOINT for an endpoint) and its interpolated attributes
+    (StrokeVertex::interpolated_attributes)."""
+    fields = list(STROKE_VERTEX_DTYPE.descr) + [("src_from", "<u4"), ("src_to", "<u4"),
+                                                 ("src_t", "<f4")]
+    if num_attributes:
+        fields.append(("attributes", "<f4", (num_attributes,)))
+    return np.dtype(fields)
+
+
+NO_ENDPOINT = 0xFFFFFFFF
+
+
+def _single_custom(ctx: Context, path: Path, options, builder: BuffersBuilder,
+                   attributes) -> None:
+    """One path with custom endpoint attributes (lyon_gpu_stroke_path_custom)."""
+    bits = builder.buffers.index_bits
+    verbs = np.ascontiguousarray(path.verbs, dtype=np.uint8)
+    pts = np.ascontiguousarray(path.points, dtype=np.float32)
+    attrs = np.ascontiguousarray(attributes, dtype=np.float32)
+    attrs = attrs.reshape(len(pts), -1) if attrs.size else np.zeros((len(pts), 0), np.float32)
+    if attrs.shape[0] != len(pts):
+        raise ValueError("one attribute row per point")
+    na = attrs.shape[1]
+    wa = -1 if options.variable_line_width is None else int(options.variable_line_width)
+    opt = options.to_c()
+    res = _native.CResult()
+    src_p = ctypes.c_void_p()
+    att_p = ctypes.c_void_p()
+    records = builder.vertex_ctor is not None
+    r = ctx.lib.lyon_gpu_stroke_path_custom(
+        ctx.h, _ptr(verbs), len(verbs), _ptr(pts), len(pts), _ptr(attrs), na, wa,
+        ctypes.byref(opt), bits, builder.next_index(), 1 if records else 0, ctypes.byref(res),
+        ctypes.byref(src_p), ctypes.byref(att_p))
+    if r != LYON_OK:
+        raise TessellationError(r, ctx.last_error() if r >= 100 else "")
+    nv, ni = res.num_vertices, res.num_indices
+    ctype = ctypes.c_uint16 if bits == 16 else ctypes.c_uint32
+    i = np.ctypeslib.as_array(ctypes.cast(res.indices, ctypes.POINTER(ctype)),
+                              shape=(ni,)).copy() if ni else np.zeros(0, builder.buffers.indices.dtype)
+    if not records:
+        v = np.ctypeslib.as_array(ctypes.cast(res.vertices, ctypes.POINTER(ctypes.c_float)),
+                                  shape=(nv * 2,)).copy() if nv else np.zeros(0, np.float32)
+        builder.append(v.reshape(-1, 2), i)
+        return
+    out = np.zeros(nv, custom_vertex_dtype(na))
+    if nv:
+        raw = np.ctypeslib.as_array(ctypes.cast(res.vertices, ctypes.POINTER(ctypes.c_uint8)),
+                                    shape=(nv * STROKE_VERTEX_DTYPE.itemsize,)).copy()
+        rec = raw.view(STROKE_VERTEX_DTYPE)
+        for f in STROKE_VERTEX_DTYPE.names:
+            out[f] = rec[f]
+        src = np.ctypeslib.as_array(ctypes.cast(src_p, ctypes.POINTER(ctypes.c_uint32)),
+                                    shape=(nv * 3,)).copy().reshape(-1, 3)
+        out["src_from"] = src[:, 0]
+        out["src_to"] = src[:, 1]
+        out["src_t"] = src[:, 2].view(np.float32)
+        if na:
+            out["attributes"] = np.ctypeslib.as_array(
+                ctypes.cast(att_p, ctypes.POINTER(ctypes.c_float)), shape=(nv * na,)).copy(
+                ).reshape(-1, na)
+    builder.append(out, i)
+
+
 def _single(kind: str, ctx: Context, path: Path, options, builder: BuffersBuilder,
             widths=None) -> None:
     bits = builder.buffers.index_bits
@@ -246,9 +312,20 @@ class StrokeTessellator:
         self.ctx = ctx or Context.default()
 
     def tessellate_path(self, path: Path, options: StrokeOptions, builder: BuffersBuilder,
-                        widths=None) -> None:
-        """`widths`: one width factor per point for StrokeOptions::variable_line_width (lyon
-        reads it from the path's endpoint attribute); None strokes with the fixed width."""
+                        widths=None, attributes=None) -> None:
+        """`attributes`: the path's custom endpoint attributes, (num_points, A) f32 (rows of
+        control points and of Close's repeated point are not read), as lyon's Path built with
+        attributes carries them (stroke.rs:164-177 then takes tessellate_with_ids): the vertex
+        constructor then receives `custom_vertex_dtype(A)` records, and
+        `options.variable_line_width` names the attribute that scales the width.
+        `widths`: one width factor per point for a variable width without other attributes;
+        neither strokes with the fixed width."""
+        if attributes is not None:
+            _single_custom(self.ctx, path, options, builder, attributes)
+            return
+        if options.variable_line_width is not None and widths is None:
+            # stroke.rs:127-131: a variable width needs the attributes to read it from.
+            raise ValueError("variable line width requires custom attributes")
         _single("stroke", self.ctx, path, options, builder, widths)
 
     def tessellate_polygon(self, points, closed: bool, options: StrokeOptions,
@@ -375,6 +452,9 @@ class BatchResult:
     vertex_offsets_ptr: int = 0
     index_offsets_ptr: int = 0
     vertex_floats: int = 2  # 6 when the vertices are lyon_stroke_vertex records
+    sources_ptr: int = 0          # lyon_vertex_source records (custom-attribute calls)
+    custom_attributes_ptr: int = 0
+    num_attributes: int = 0
 
     def offsets(self):
         """(vertex_offsets, index_offsets) as int64 torch tensors of num_paths + 1 entries."""
@@ -400,6 +480,22 @@ class BatchResult:
         return torch.as_tensor(_CudaArray(self.vertices_ptr, (self.total_vertices, 6), "<f4"),
                                device="cuda")
 
+    def sources(self):
+        """Each vertex's lyon_vertex_source as a (V, 3) int32 tensor (from, to, t's f32 bits;
+        `to` == -1 for an endpoint)."""
+        import torch
+        assert self.sources_ptr, "not a custom-attribute output"
+        return torch.as_tensor(_CudaArray(self.sources_ptr, (self.total_vertices, 3), "<i4"),
+                               device="cuda")
+
+    def custom_attributes(self):
+        """Each vertex's interpolated custom attributes, (V, A) f32."""
+        import torch
+        assert self.custom_attributes_ptr, "no custom attributes"
+        return torch.as_tensor(_CudaArray(self.custom_attributes_ptr,
+                                          (self.total_vertices, self.num_attributes), "<f4"),
+                               device="cuda")
+
     def indices(self):
         import torch
         ts = "<u2" if self.index_bits == 16 else "<u4"
@@ -420,15 +516,35 @@ class BatchResult:
 def tessellate_paths(kind: str, dbatch: DeviceBatch, options_dev, num_options: int,
                      index_bits: int = 32, index_mode: int = INDEX_GLOBAL,
                      vertex_offset: int = 0, ctx: Optional[Context] = None,
-                     attributes: bool = False, widths=None) -> BatchResult:
+                     attributes: bool = False, widths=None, custom_attributes=None,
+                     width_attribute: int = -1) -> BatchResult:
     """Batched stroke or fill of every path of a DeviceBatch (results stay on the device,
     owned by the context until its next batched call). With `attributes` (strokes), the
-    vertices are lyon_stroke_vertex records (BatchResult.records)."""
+    vertices are lyon_stroke_vertex records (BatchResult.records). `custom_attributes`, a (P, A)
+    f32 device tensor of per-point endpoint attributes (A may be 0), selects
+    lyon_gpu_stroke_paths_custom: every vertex's source and interpolated attributes
+    (BatchResult.sources / custom_attributes); `width_attribute` >= 0 strokes with that
+    attribute as the variable line width."""
     ctx = ctx or Context.default()
     out = _native.CBatchOutput()
     cb = dbatch.c()
-    if (attributes or widths is not None) and kind != "stroke":
+    if (attributes or widths is not None or custom_attributes is not None) and kind != "stroke":
         raise ValueError("vertex attributes and variable widths are stroke options")
+    if custom_attributes is not None:
+        na = int(custom_attributes.shape[1]) if custom_attributes.dim() == 2 else 0
+        co = _native.CCustomOutput()
+        r = ctx.lib.lyon_gpu_stroke_paths_custom(
+            ctx.h, ctypes.byref(cb), custom_attributes.data_ptr() if na else None, na,
+            width_attribute, options_dev.data_ptr(), num_options, index_bits, index_mode,
+            vertex_offset, 1 if attributes else 0, ctypes.byref(out), ctypes.byref(co))
+        if r != LYON_OK:
+            raise TessellationError(r, ctx.last_error())
+        return BatchResult(r, int(out.total_vertices), int(out.total_indices),
+                           int(out.num_failed_paths), int(out.vertices or 0),
+                           int(out.indices or 0), int(out.status or 0), index_bits,
+                           dbatch.num_paths, int(out.vertex_offsets or 0),
+                           int(out.index_offsets or 0), 6 if attributes else 2,
+                           int(co.sources or 0), int(co.attributes or 0), na)
     if widths is not None:
         # Variable line width: `widths` is a device tensor of one f32 factor per point.
         r = ctx.lib.lyon_gpu_stroke_paths_variable_width(

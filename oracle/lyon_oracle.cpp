@@ -258,6 +258,9 @@ struct Evt {
     P from, ctrl1, ctrl2, to;  // Begin: to = at. End: from = last, to = first.
     bool close;
     float w_from = NAN, w_to = NAN;  // endpoint width factors (variable line width only)
+    // Endpoint ids (IdEvent, crates/path/src/events.rs): the index of the endpoint's point in the
+    // path's point array, as lyon's Path::id_iter gives them for a path without attributes.
+    uint32_t id_from = 0, id_to = 0;
 };
 
 struct PathIter {
@@ -271,6 +274,7 @@ struct PathIter {
     uint32_t vi = 0, pi = 0;
     P current{0, 0}, first{0, 0};
     float cur_w = NAN, first_w = NAN;
+    uint32_t cur_id = 0, first_id = 0;
     uint32_t last_idx = 0;
     bool bad = false;
     P take() {
@@ -292,9 +296,11 @@ struct PathIter {
             case LYON_VERB_BEGIN:
                 current = take();
                 cur_w = width_at(last_idx);
+                cur_id = first_id = last_idx;
                 first = current;
                 first_w = cur_w;
                 e->w_to = cur_w;
+                e->id_to = cur_id;
                 e->kind = EV_BEGIN;
                 e->to = current;
                 return true;
@@ -302,8 +308,10 @@ struct PathIter {
                 e->kind = EV_LINE;
                 e->from = current;
                 e->w_from = cur_w;
+                e->id_from = cur_id;
                 current = take();
                 cur_w = width_at(last_idx);
+                cur_id = e->id_to = last_idx;
                 e->w_to = cur_w;
                 e->to = current;
                 return true;
@@ -311,9 +319,11 @@ struct PathIter {
                 e->kind = EV_QUAD;
                 e->from = current;
                 e->w_from = cur_w;
+                e->id_from = cur_id;
                 e->ctrl1 = take();
                 current = take();
                 cur_w = width_at(last_idx);
+                cur_id = e->id_to = last_idx;
                 e->w_to = cur_w;
                 e->to = current;
                 return true;
@@ -321,10 +331,12 @@ struct PathIter {
                 e->kind = EV_CUBIC;
                 e->from = current;
                 e->w_from = cur_w;
+                e->id_from = cur_id;
                 e->ctrl1 = take();
                 e->ctrl2 = take();
                 current = take();
                 cur_w = width_at(last_idx);
+                cur_id = e->id_to = last_idx;
                 e->w_to = cur_w;
                 e->to = current;
                 return true;
@@ -345,6 +357,7 @@ struct PathIter {
                 e->w_from = cur_w;
                 e->w_to = first_w;
                 cur_w = first_w;
+                cur_id = first_id;
                 e->close = false;
                 return true;
             default:
@@ -358,6 +371,18 @@ struct PathIter {
 // Output: BuffersBuilder over VertexBuffers<Point, u16|u32> (geometry_builder.rs:300-351,451-508).
 // --------------------------------------------------------------------------------------------
 static const uint32_t INVALID_ID = 0xFFFFFFFFu;
+static const uint32_t NO_ENDPOINT = 0xFFFFFFFFu;
+
+struct Src {  // VertexSource (lib.rs:282-291)
+    uint32_t from = NO_ENDPOINT, to = NO_ENDPOINT;
+    float t = 0.0f;
+};
+static inline Src endpoint_src(uint32_t id) { return Src{id, NO_ENDPOINT, 0.0f}; }
+// The source of a point at parameter t of a curve between two endpoints: the end point itself
+// at t == 1 (stroke.rs:1007-1016, 1045-1053).
+static inline Src curve_src(uint32_t from, uint32_t to, float t) {
+    return t == 1.0f ? endpoint_src(to) : Src{from, to, t};
+}
 
 struct Output {
     std::vector<float> vertices;     // x, y
@@ -366,6 +391,10 @@ struct Output {
     // normal x, normal y, advancement (f32 bits) and side, four words per vertex.
     bool want_attributes = false;
     std::vector<uint32_t> attributes;
+    // With want_sources, each stroke vertex's VertexSource (lib.rs:282-291; StrokeVertex::source,
+    // stroke.rs:2719-2722): from, to, t (f32 bits); `to` is NO_ENDPOINT for Endpoint { id: from }.
+    bool want_sources = false;
+    std::vector<uint32_t> sources;
     uint64_t max_index = 0xFFFFFFFEull;
     uint64_t vertex_offset = 0;
     size_t first_vertex = 0, first_index = 0;
@@ -391,6 +420,7 @@ struct Output {
         vertices.resize(first_vertex * 2);
         indices.resize(first_index);
         if (want_attributes) attributes.resize(first_vertex * 4);
+        if (want_sources) sources.resize(first_vertex * 3);
     }
 };
 
@@ -419,6 +449,7 @@ struct EndpointData {  // stroke.rs:309-342
     SidePoints side[2];
     bool fold[2] = {false, false};
     bool is_flattening_step = false;
+    Src src;
     EndpointData() {
         for (int s = 0; s < 2; ++s) {
             side[s].prev = P{NAN, NAN};
@@ -461,6 +492,7 @@ struct StrokeVertexData {  // stroke.rs:2656-2665
     P normal{0, 0};
     float advancement = 0;
     int side = SIDE_NEGATIVE;
+    Src src;
 };
 
 // math_utils.rs:16-40
@@ -582,6 +614,13 @@ struct Stroker {
             std::memcpy(&w[2], &vertex.advancement, 4);
             out->attributes.insert(out->attributes.end(), w, w + 3);
             out->attributes.push_back((uint32_t)vertex.side);
+        }
+        if (out->want_sources) {
+            uint32_t tb;
+            std::memcpy(&tb, &vertex.src.t, 4);
+            out->sources.push_back(vertex.src.from);
+            out->sources.push_back(vertex.src.to);
+            out->sources.push_back(tb);
         }
         return id;
     }
@@ -823,6 +862,7 @@ struct Stroker {
             EndpointData& join = point_buffer.last();
             vertex.position_on_path = join.position;
             vertex.half_width = join.half_width;
+            vertex.src = join.src;
             bool fast_path = false;
             if (join.is_flattening_step) {
                 P v0 = sub(join.position, prev.position);
@@ -941,6 +981,7 @@ struct Stroker {
             vertex.position_on_path = join.position;
             vertex.half_width = join.half_width;
             vertex.advancement = join.advancement;
+            vertex.src = join.src;
             bool fast_path = false;
             if (join.is_flattening_step) {
                 P v0 = sub(join.position, prev.position);
@@ -994,47 +1035,59 @@ struct Stroker {
     // Events of tessellate_with_ids_vw (stroke.rs:654-767): the half width of an endpoint is
     // line_width x its factor x 0.5; along a curve the width is interpolated linearly in t
     // (stroke.rs:996-1067, with flatten_quad's t mapping, stroke.rs:2755-2779).
-    void begin_vw(P position, float w) {
+    void begin_vw(P position, float w, Src src) {
         may_need_empty_cap = false;
         EndpointData d = make_point(position);
         d.half_width = options.line_width * w * 0.5f;
         d.advancement = sub_path_start_advancement;
+        d.src = src;
         step(d);
     }
-    void line_to_vw(P to, float w) {
+    void line_to_vw(P to, float w, Src src) {
         EndpointData d = make_point(to);
         d.half_width = options.line_width * w * 0.5f;
+        d.src = src;
         step(d);
     }
     void curve_point_vw(P position, float t, bool is_flattening_step, float start_width,
-                        float end_width) {
+                        float end_width, Src src) {
         EndpointData d = make_point(position);
         d.half_width = (start_width * (1.0f - t) + end_width * t) * 0.5f;
         d.is_flattening_step = is_flattening_step;
+        d.src = src;
         step(d);
     }
-    void quadratic_bezier_to_vw(const Quad& curve, float w0, float w1) {
-        float sw = options.line_width * w0, ew = options.line_width * w1;
+    // flatten_quad (stroke.rs:2755-2779): `cb(position, t, is_flattening_step)` with t on the
+    // whole curve when it is split at a sharp turn.
+    template <class F>
+    static void flatten_quad(const Quad& curve, float tolerance, F&& cb) {
         float t_split;
         if (find_sharp_turn(curve, &t_split)) {
             Quad before, after;
             quad_split(curve, t_split, &before, &after);
-            quad_flatten_with_t(before, options.tolerance, [&](P, P to, float, float t1) {
-                curve_point_vw(to, t1 * t_split, t1 != 1.0f, sw, ew);
+            quad_flatten_with_t(before, tolerance, [&](P, P to, float, float t1) {
+                cb(to, t1 * t_split, t1 != 1.0f);
             });
-            quad_flatten_with_t(after, options.tolerance, [&](P, P to, float, float t1) {
-                curve_point_vw(to, t_split + t1 * (1.0f - t_split), t1 != 1.0f, sw, ew);
+            quad_flatten_with_t(after, tolerance, [&](P, P to, float, float t1) {
+                cb(to, t_split + t1 * (1.0f - t_split), t1 != 1.0f);
             });
         } else {
-            quad_flatten_with_t(curve, options.tolerance, [&](P, P to, float, float t1) {
-                curve_point_vw(to, t1, t1 != 1.0f, sw, ew);
-            });
+            quad_flatten_with_t(curve, tolerance,
+                                [&](P, P to, float, float t1) { cb(to, t1, t1 != 1.0f); });
         }
     }
-    void cubic_bezier_to_vw(const Cubic& curve, float w0, float w1) {
+    void quadratic_bezier_to_vw(const Quad& curve, float w0, float w1, uint32_t from_id,
+                                uint32_t to_id) {
+        float sw = options.line_width * w0, ew = options.line_width * w1;
+        flatten_quad(curve, options.tolerance, [&](P to, float t, bool flat) {
+            curve_point_vw(to, t, flat, sw, ew, curve_src(from_id, to_id, t));
+        });
+    }
+    void cubic_bezier_to_vw(const Cubic& curve, float w0, float w1, uint32_t from_id,
+                            uint32_t to_id) {
         float sw = options.line_width * w0, ew = options.line_width * w1;
         cubic_flatten_with_t(curve, options.tolerance, [&](P, P to, float, float t1) {
-            curve_point_vw(to, t1, t1 != 1.0f, sw, ew);
+            curve_point_vw(to, t1, t1 != 1.0f, sw, ew, curve_src(from_id, to_id, t1));
         });
     }
 
@@ -1046,14 +1099,19 @@ struct Stroker {
         return d;
     }
 
-    void begin_fw(P position) {  // stroke.rs:1069-1087
+    void begin_fw(P position, Src src) {  // stroke.rs:1069-1087
         may_need_empty_cap = false;
         EndpointData d = make_point(position);
         d.advancement = sub_path_start_advancement;
+        d.src = src;
         fixed_width_step(d);
     }
 
-    void line_to_fw(P to) { fixed_width_step(make_point(to)); }  // stroke.rs:1089-1106
+    void line_to_fw(P to, Src src) {  // stroke.rs:1089-1106
+        EndpointData d = make_point(to);
+        d.src = src;
+        fixed_width_step(d);
+    }
 
     // stroke.rs:3178-3212
     static bool find_sharp_turn(const Quad& curve, float* t_out) {
@@ -1082,35 +1140,24 @@ struct Stroker {
         return quad_local_x_extremum_t(rotated, t_out);
     }
 
-    void flattened_point(P position, bool is_flattening_step) {
+    void flattened_point(P position, bool is_flattening_step, Src src) {
         EndpointData d = make_point(position);
         d.is_flattening_step = is_flattening_step;
+        d.src = src;
         fixed_width_step(d);
     }
 
     // stroke.rs:1108-1143 and 2755-2779 (flatten_quad)
-    void quadratic_bezier_to_fw(const Quad& curve) {
-        float t_split;
-        if (find_sharp_turn(curve, &t_split)) {
-            Quad before, after;
-            quad_split(curve, t_split, &before, &after);
-            quad_flatten_with_t(before, options.tolerance, [&](P, P to, float, float t1) {
-                flattened_point(to, t1 != 1.0f);
-            });
-            quad_flatten_with_t(after, options.tolerance, [&](P, P to, float, float t1) {
-                flattened_point(to, t1 != 1.0f);
-            });
-        } else {
-            quad_flatten_with_t(curve, options.tolerance, [&](P, P to, float, float t1) {
-                flattened_point(to, t1 != 1.0f);
-            });
-        }
+    void quadratic_bezier_to_fw(const Quad& curve, uint32_t from_id, uint32_t to_id) {
+        flatten_quad(curve, options.tolerance, [&](P to, float t, bool flat) {
+            flattened_point(to, flat, curve_src(from_id, to_id, t));
+        });
     }
 
     // stroke.rs:1145-1177
-    void cubic_bezier_to_fw(const Cubic& curve) {
+    void cubic_bezier_to_fw(const Cubic& curve, uint32_t from_id, uint32_t to_id) {
         cubic_flatten_with_t(curve, options.tolerance, [&](P, P to, float, float t1) {
-            flattened_point(to, t1 != 1.0f);
+            flattened_point(to, t1 != 1.0f, curve_src(from_id, to_id, t1));
         });
     }
 
@@ -1187,6 +1234,7 @@ struct Stroker {
         EndpointData& point = point_buffer.get(0);
         vertex.advancement = point.advancement;
         vertex.half_width = point.half_width;
+        vertex.src = point.src;
         if (options.start_cap == LYON_CAP_SQUARE) {
             tessellate_empty_square_cap(point.position);
         } else if (options.start_cap == LYON_CAP_ROUND) {
@@ -1201,6 +1249,7 @@ struct Stroker {
         vertex.position_on_path = p1.position;
         vertex.advancement = p1.advancement;
         vertex.half_width = p1.half_width;
+        vertex.src = p1.src;
         for (int side = 0; side < 2; ++side) {
             P side_position = p1.side[side].prev;
             bool has_clip = options.end_cap == LYON_CAP_SQUARE || options.end_cap == LYON_CAP_BUTT;
@@ -1236,6 +1285,7 @@ struct Stroker {
         vertex.position_on_path = first.position;
         vertex.advancement = first.advancement;
         vertex.half_width = first.half_width;
+        vertex.src = first.src;
         for (int side = 0; side < 2; ++side) {
             P side_position = first.side[side].next;
             bool has_clip =
@@ -1313,6 +1363,7 @@ struct Stroker {
             vertex.position_on_path = p0.position;
             vertex.half_width = p0.half_width;
             vertex.advancement = advancement;
+            vertex.src = p0.src;
             for (int side = 0; side < 2; ++side) {
                 vertex.side = side;
                 if (p0.side[side].has_single) {
@@ -1348,20 +1399,27 @@ struct Stroker {
         while (it.next(&e)) {
             switch (e.kind) {
                 case EV_BEGIN:
-                    if (vw) begin_vw(e.to, e.w_to);
-                    else begin_fw(e.to);
+                    if (vw) begin_vw(e.to, e.w_to, endpoint_src(e.id_to));
+                    else begin_fw(e.to, endpoint_src(e.id_to));
                     break;
                 case EV_LINE:
-                    if (vw) line_to_vw(e.to, e.w_to);
-                    else line_to_fw(e.to);
+                    if (vw) line_to_vw(e.to, e.w_to, endpoint_src(e.id_to));
+                    else line_to_fw(e.to, endpoint_src(e.id_to));
                     break;
                 case EV_QUAD:
-                    if (vw) quadratic_bezier_to_vw(Quad{e.from, e.ctrl1, e.to}, e.w_from, e.w_to);
-                    else quadratic_bezier_to_fw(Quad{e.from, e.ctrl1, e.to});
+                    if (vw)
+                        quadratic_bezier_to_vw(Quad{e.from, e.ctrl1, e.to}, e.w_from, e.w_to,
+                                               e.id_from, e.id_to);
+                    else
+                        quadratic_bezier_to_fw(Quad{e.from, e.ctrl1, e.to}, e.id_from, e.id_to);
                     break;
                 case EV_CUBIC:
-                    if (vw) cubic_bezier_to_vw(Cubic{e.from, e.ctrl1, e.ctrl2, e.to}, e.w_from, e.w_to);
-                    else cubic_bezier_to_fw(Cubic{e.from, e.ctrl1, e.ctrl2, e.to});
+                    if (vw)
+                        cubic_bezier_to_vw(Cubic{e.from, e.ctrl1, e.ctrl2, e.to}, e.w_from,
+                                           e.w_to, e.id_from, e.id_to);
+                    else
+                        cubic_bezier_to_fw(Cubic{e.from, e.ctrl1, e.ctrl2, e.to}, e.id_from,
+                                           e.id_to);
                     break;
                 case EV_END:
                     end(e.close);
@@ -2754,6 +2812,7 @@ void lyon_oracle_out_clear(lyon_oracle_out* o) {
     o->out.vertices.clear();
     o->out.indices.clear();
     o->out.attributes.clear();
+    o->out.sources.clear();
     o->near_ties = 0;
 }
 // Stroke vertex attributes (four words per vertex: normal x, normal y, advancement, side),
@@ -2763,6 +2822,14 @@ void lyon_oracle_out_set_attributes(lyon_oracle_out* o, int enabled) {
 }
 const uint32_t* lyon_oracle_out_attributes(const lyon_oracle_out* o) {
     return o->out.attributes.data();
+}
+// Stroke vertex sources (three words per vertex: from, to, t bits; `to` = 0xFFFFFFFF for an
+// endpoint), recorded from the next call on. Ids index the path's point array.
+void lyon_oracle_out_set_sources(lyon_oracle_out* o, int enabled) {
+    o->out.want_sources = enabled != 0;
+}
+const uint32_t* lyon_oracle_out_sources(const lyon_oracle_out* o) {
+    return o->out.sources.data();
 }
 uint64_t lyon_oracle_out_num_vertices(const lyon_oracle_out* o) { return o->out.vertices.size() / 2; }
 uint64_t lyon_oracle_out_num_indices(const lyon_oracle_out* o) { return o->out.indices.size(); }
@@ -2855,7 +2922,7 @@ static int batch_impl(int kind, const lyon_path_batch* batch, const float* width
                       uint32_t* vtx_counts, uint32_t* idx_counts, int32_t* status,
                       uint32_t* near_ties, float* vertices, uint32_t* indices,
                       const uint64_t* vtx_offsets, const uint64_t* idx_offsets,
-                      uint32_t* attributes) {
+                      uint32_t* attributes, uint32_t* sources = nullptr) {
     uint32_t n = batch->num_paths;
     if (num_threads < 1) num_threads = 1;
     std::atomic<uint32_t> next{0};
@@ -2863,6 +2930,7 @@ static int batch_impl(int kind, const lyon_path_batch* batch, const float* width
         lyon_oracle_out o;
         o.out.max_index = index_bits == 16 ? 65535ull : 0xFFFFFFFEull;
         o.out.want_attributes = attributes != nullptr;
+        o.out.want_sources = sources != nullptr;
         for (;;) {
             uint32_t begin = next.fetch_add(64);
             if (begin >= n) break;
@@ -2871,6 +2939,7 @@ static int batch_impl(int kind, const lyon_path_batch* batch, const float* width
                 o.out.vertices.clear();
                 o.out.indices.clear();
                 o.out.attributes.clear();
+                o.out.sources.clear();
                 o.near_ties = 0;
                 uint32_t v0 = batch->verb_offsets[i], v1 = batch->verb_offsets[i + 1];
                 uint32_t p0 = batch->point_offsets[i], p1 = batch->point_offsets[i + 1];
@@ -2910,6 +2979,16 @@ static int batch_impl(int kind, const lyon_path_batch* batch, const float* width
                     std::memcpy(attributes + 4 * vtx_offsets[i], o.out.attributes.data(),
                                 o.out.attributes.size() * sizeof(uint32_t));
                 }
+                if (sources && vtx_offsets) {
+                    // Path-local endpoint ids made batch-global (indices into the batch's points).
+                    uint32_t* d = sources + 3 * vtx_offsets[i];
+                    for (size_t k = 0; k + 2 < o.out.sources.size(); k += 3) {
+                        d[k] = o.out.sources[k] + p0;
+                        d[k + 1] = o.out.sources[k + 1] == NO_ENDPOINT ? NO_ENDPOINT
+                                                                        : o.out.sources[k + 1] + p0;
+                        d[k + 2] = o.out.sources[k + 2];
+                    }
+                }
             }
         }
     };
@@ -2944,6 +3023,50 @@ int lyon_oracle_batch_stroke_vw(const lyon_path_batch* batch, const float* width
     return batch_impl(0, batch, widths, options, num_options, index_bits, num_threads,
                       vtx_counts, idx_counts, status, near_ties, vertices, indices, vtx_offsets,
                       idx_offsets, attributes);
+}
+
+// Batched stroke (fixed width when `widths` is NULL) recording every vertex's VertexSource
+// (three words per vertex, endpoint ids indexing the batch's points) and, when `attributes` is
+// set, the stroke vertex attributes.
+int lyon_oracle_batch_stroke_sources(const lyon_path_batch* batch, const float* widths,
+                                     const void* options, uint32_t num_options, int index_bits,
+                                     int num_threads, uint32_t* vtx_counts, uint32_t* idx_counts,
+                                     int32_t* status, float* vertices, uint32_t* indices,
+                                     const uint64_t* vtx_offsets, const uint64_t* idx_offsets,
+                                     uint32_t* attributes, uint32_t* sources) {
+    return batch_impl(0, batch, widths, options, num_options, index_bits, num_threads,
+                      vtx_counts, idx_counts, status, nullptr, vertices, indices, vtx_offsets,
+                      idx_offsets, attributes, sources);
+}
+
+// StrokeVertex::interpolated_attributes (stroke.rs:2728-2747) for `n` vertex sources (three
+// words each) over an attribute store of `na` floats per endpoint, on `num_threads` threads.
+void lyon_oracle_interpolate(const uint32_t* sources, uint64_t n, const float* attrs, uint32_t na,
+                             float* out, int num_threads) {
+    if (num_threads < 1) num_threads = 1;
+    auto work = [&](uint64_t v0, uint64_t v1) {
+        for (uint64_t v = v0; v < v1; ++v) {
+            const uint32_t* s = sources + 3 * v;
+            float t;
+            std::memcpy(&t, &s[2], 4);
+            const float* a = attrs + (uint64_t)s[0] * na;
+            float* o = out + v * na;
+            if (s[1] == NO_ENDPOINT) {
+                for (uint32_t i = 0; i < na; ++i) o[i] = a[i];
+            } else {
+                const float* b = attrs + (uint64_t)s[1] * na;
+                for (uint32_t i = 0; i < na; ++i) o[i] = a[i] * (1.0f - t) + b[i] * t;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    const uint64_t per = (n + num_threads - 1) / num_threads;
+    for (int k = 1; k < num_threads; ++k) {
+        const uint64_t v0 = std::min(n, per * k), v1 = std::min(n, per * (k + 1));
+        th.emplace_back(work, v0, v1);
+    }
+    work(0, std::min(n, per));
+    for (auto& t : th) t.join();
 }
 
 // The stroke vertex attributes of every path of a batch (four words per vertex, see

@@ -11,6 +11,7 @@ import ctypes
 import os
 import subprocess
 import threading
+import time
 
 import numpy as np
 
@@ -75,6 +76,15 @@ def lib():
             L.lyon_oracle_batch_stroke_vw.restype = ctypes.c_int
             L.lyon_oracle_batch_stroke_vw.argtypes = [c_p, c_p, c_p, ctypes.c_uint32,
                                                       ctypes.c_int, ctypes.c_int] + [c_p] * 9
+            L.lyon_oracle_out_set_sources.argtypes = [c_p, ctypes.c_int]
+            L.lyon_oracle_out_sources.restype = ctypes.POINTER(ctypes.c_uint32)
+            L.lyon_oracle_out_sources.argtypes = [c_p]
+            L.lyon_oracle_batch_stroke_sources.restype = ctypes.c_int
+            L.lyon_oracle_batch_stroke_sources.argtypes = [c_p, c_p, c_p, ctypes.c_uint32,
+                                                           ctypes.c_int, ctypes.c_int] + [c_p] * 9
+            L.lyon_oracle_interpolate.restype = None
+            L.lyon_oracle_interpolate.argtypes = [c_p, ctypes.c_uint64, c_p, ctypes.c_uint32, c_p,
+                                                  ctypes.c_int]
             L.lyon_oracle_batch.restype = ctypes.c_int
             L.lyon_oracle_batch.argtypes = [ctypes.c_int, c_p, c_p, ctypes.c_uint32, ctypes.c_int,
                                             ctypes.c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
@@ -89,9 +99,13 @@ def _ptr(a: np.ndarray):
 class Result:
     """Output of one oracle call: positions, indices (u32 VertexId values), status."""
 
-    def __init__(self, status, vertices, indices, near_ties, index_bits, attributes=None):
+    def __init__(self, status, vertices, indices, near_ties, index_bits, attributes=None,
+                 sources=None):
         self.status = status
         self.vertices = vertices
+        # Vertex sources when requested: (V, 3) u32 words (from, to, t as f32 bits; `to` is
+        # NO_ENDPOINT for VertexSource::Endpoint { id: from }).
+        self.sources = sources
         # Stroke vertex attributes when requested: (V, 4) u32 words (normal x, normal y,
         # advancement as f32 bits; side 0 positive / 1 negative).
         self.attributes = attributes
@@ -107,13 +121,17 @@ class Result:
 class Output:
     """A VertexBuffers + BuffersBuilder pair on the oracle side (append semantics)."""
 
-    def __init__(self, index_bits: int = 32, vertex_offset: int = 0, attributes: bool = False):
+    def __init__(self, index_bits: int = 32, vertex_offset: int = 0, attributes: bool = False,
+                 sources: bool = False):
         self.L = lib()
         self.h = self.L.lyon_oracle_out_new(index_bits, vertex_offset)
         self.index_bits = index_bits
         self.attributes = attributes
+        self.sources = sources
         if attributes:
             self.L.lyon_oracle_out_set_attributes(self.h, 1)
+        if sources:
+            self.L.lyon_oracle_out_set_sources(self.h, 1)
 
     def __del__(self):
         try:
@@ -136,8 +154,13 @@ class Output:
             a = np.ctypeslib.as_array(self.L.lyon_oracle_out_attributes(self.h),
                                       shape=(nv * 4,)).copy().reshape(-1, 4) \
                 if nv else np.zeros((0, 4), np.uint32)
+        src = None
+        if self.sources:
+            src = np.ctypeslib.as_array(self.L.lyon_oracle_out_sources(self.h),
+                                        shape=(nv * 3,)).copy().reshape(-1, 3) \
+                if nv else np.zeros((0, 3), np.uint32)
         return Result(status, v.reshape(-1, 2), i, self.L.lyon_oracle_out_near_ties(self.h),
-                      self.index_bits, a)
+                      self.index_bits, a, src)
 
     def stroke(self, path, options, widths=None):
         """`widths`: one variable-line-width factor per point (StrokeOptions::
@@ -162,10 +185,31 @@ class Output:
 
 
 def stroke(path, options, index_bits: int = 32, vertex_offset: int = 0,
-           attributes: bool = False, widths=None) -> Result:
-    out = Output(index_bits, vertex_offset, attributes)
+           attributes: bool = False, widths=None, sources: bool = False) -> Result:
+    out = Output(index_bits, vertex_offset, attributes, sources)
     st = out.stroke(path, options, widths)
     return out.snapshot(st)
+
+
+NO_ENDPOINT = 0xFFFFFFFF
+
+
+def interpolate_attributes(sources: np.ndarray, attributes: np.ndarray) -> np.ndarray:
+    """StrokeVertex::interpolated_attributes (crates/tessellation/src/stroke.rs:2728-2747) for
+    (V, 3) source words over an (endpoints, A) f32 attribute store: the endpoint's attributes,
+    or a * (1 - t) + b * t along an edge, in f32 operation by operation."""
+    src = np.asarray(sources, np.uint32).reshape(-1, 3)
+    attrs = np.asarray(attributes, np.float32)
+    attrs = attrs.reshape(len(attrs), -1)
+    frm = src[:, 0].astype(np.int64)
+    to = src[:, 1]
+    t = src[:, 2].copy().view(np.float32)[:, None]
+    edge = to != NO_ENDPOINT
+    a = attrs[frm]
+    b = attrs[np.where(edge, to, 0).astype(np.int64)]
+    one = np.float32(1.0)
+    lerp = (a * (one - t)).astype(np.float32) + (b * t).astype(np.float32)
+    return np.where(edge[:, None], lerp, a).astype(np.float32)
 
 
 def fill_rectangle(rect, index_bits: int = 32, vertex_offset: int = 0) -> Result:
@@ -214,6 +258,58 @@ class _CBatch(ctypes.Structure):
     _fields_ = [("verbs", ctypes.c_void_p), ("points", ctypes.c_void_p),
                 ("verb_offsets", ctypes.c_void_p), ("point_offsets", ctypes.c_void_p),
                 ("num_paths", ctypes.c_uint32)]
+
+
+def interpolate_attributes_threads(sources: np.ndarray, attributes: np.ndarray,
+                                   num_threads: int = 1) -> np.ndarray:
+    """interpolate_attributes in C on `num_threads` threads (the CPU baseline's version)."""
+    src = np.ascontiguousarray(sources, np.uint32).reshape(-1, 3)
+    attrs = np.ascontiguousarray(attributes, np.float32)
+    attrs = attrs.reshape(len(attrs), -1)
+    out = np.zeros((len(src), attrs.shape[1]), np.float32)
+    lib().lyon_oracle_interpolate(_ptr(src), len(src), _ptr(attrs), attrs.shape[1], _ptr(out),
+                                  num_threads)
+    return out
+
+
+def batch_stroke_sources(pb, options_records: np.ndarray, index_bits: int = 32,
+                         num_threads: int = 1, widths=None, want_attributes: bool = False):
+    """Strokes every path of a PathBatch with the oracle, recording each vertex's
+    VertexSource ((V, 3) words, endpoint ids indexing the batch's points) next to the outputs
+    `batch` returns."""
+    L = lib()
+    n = pb.num_paths
+    cb = _CBatch(_ptr(pb.verbs), _ptr(pb.points), _ptr(pb.verb_offsets),
+                 _ptr(pb.point_offsets), n)
+    opts = np.ascontiguousarray(options_records)
+    w = None
+    if widths is not None:
+        w = np.ascontiguousarray(widths, dtype=np.float32)
+        assert len(w) == len(pb.points)
+    vc = np.zeros(n, np.uint32)
+    ic = np.zeros(n, np.uint32)
+    st = np.zeros(n, np.int32)
+    L.lyon_oracle_batch_stroke_sources(ctypes.byref(cb), _ptr(w), _ptr(opts), len(opts),
+                                       index_bits, num_threads, _ptr(vc), _ptr(ic), _ptr(st),
+                                       None, None, None, None, None, None)
+    vo = np.zeros(n + 1, np.uint64)
+    io = np.zeros(n + 1, np.uint64)
+    vo[1:] = np.cumsum(vc, dtype=np.uint64)
+    io[1:] = np.cumsum(ic, dtype=np.uint64)
+    verts = np.zeros((int(vo[-1]), 2), np.float32)
+    idx = np.zeros(int(io[-1]), np.uint32)
+    attrs = np.zeros((int(vo[-1]), 4), np.uint32) if want_attributes else None
+    srcs = np.zeros((int(vo[-1]), 3), np.uint32)
+    t0 = time.perf_counter()
+    L.lyon_oracle_batch_stroke_sources(ctypes.byref(cb), _ptr(w), _ptr(opts), len(opts),
+                                       index_bits, num_threads, None, None, None, _ptr(verts),
+                                       _ptr(idx), _ptr(vo), _ptr(io), _ptr(attrs), _ptr(srcs))
+    res = {"vtx_counts": vc, "idx_counts": ic, "status": st, "vertices": verts, "indices": idx,
+           "vtx_offsets": vo, "idx_offsets": io, "sources": srcs,
+           "output_pass_s": time.perf_counter() - t0}
+    if want_attributes:
+        res["attributes"] = attrs
+    return res
 
 
 def batch(kind: str, pb, options_records: np.ndarray, index_bits: int = 32,

@@ -299,6 +299,54 @@ int lyon_gpu_stroke_path_custom(lyon_gpu_context* ctx, const uint8_t* verbs, uin
                                 lyon_gpu_result* result, const lyon_vertex_source** sources,
                                 const float** vertex_attribute_values);
 
+/* The per-vertex outputs of lyon_gpu_fill_paths_custom, in device memory owned by the context
+ * (valid until its next call). A fill vertex has one source per edge event at its position
+ * (FillVertex::sources, crates/tessellation/src/fill.rs:2172-2178, 2294-2337): vertex v's sources
+ * are sources[source_offsets[v] .. source_offsets[v + 1]). */
+typedef struct lyon_gpu_fill_custom_output {
+    const lyon_vertex_source* sources;  /* total_sources records, in vertex order */
+    const uint64_t* source_offsets;     /* total_vertices + 1 entries */
+    uint64_t total_sources;
+    const float* attributes;            /* num_attributes floats per vertex, NULL when none */
+} lyon_gpu_fill_custom_output;
+
+/* FillTessellator::tessellate_path for paths that carry custom endpoint attributes
+ * (crates/tessellation/src/fill.rs:628-641 taking its `path.num_attributes() > 0` branch:
+ * tessellate_with_ids, event_queue.rs:553-630), with a vertex constructor that reads
+ * FillVertex::sources and FillVertex::interpolated_attributes (fill.rs:2172-2286).
+ * `attributes` (device memory) holds `num_attributes` floats per point of the batch, indexed
+ * like `points` (may be NULL when num_attributes is 0). Writes positions and indices to `out` as
+ * lyon_gpu_fill_paths does, and every vertex's sources and interpolated attributes to `custom`.
+ * Note lyon's convention for a curve flattened downwards from its end: its sources' t runs from
+ * the curve's `to` end while from/to stay the curve's own endpoints. */
+int lyon_gpu_fill_paths_custom(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                               const float* attributes, uint32_t num_attributes,
+                               const lyon_fill_options* options, uint32_t num_options,
+                               int index_bits, int index_mode, uint32_t vertex_offset,
+                               lyon_gpu_batch_output* out, lyon_gpu_fill_custom_output* custom);
+
+/* FillVertex::interpolated_attributes (crates/tessellation/src/fill.rs:2208-2286) over many
+ * vertices (device memory, context's stream): the first source's attributes (the endpoint's, or
+ * a * (1 - t) + b * t), each further source's added in order, then a division by the number of
+ * sources when there are several. A vertex with an id not below `num_endpoints`, or without
+ * sources, gives NaN. */
+int lyon_gpu_interpolate_fill_attributes(lyon_gpu_context* ctx,
+                                         const lyon_vertex_source* sources,
+                                         const uint64_t* source_offsets, uint64_t num_vertices,
+                                         const float* attributes, uint32_t num_attributes,
+                                         uint64_t num_endpoints, float* out);
+
+/* One path with custom attributes (host memory in and out): lyon_gpu_fill_paths_custom on a
+ * one-path batch. `*sources`, `*source_offsets` (num_vertices + 1 entries) and
+ * `*vertex_attribute_values` point at host memory valid until the next call on the context. */
+int lyon_gpu_fill_path_custom(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                              const float* points, uint32_t num_points, const float* attributes,
+                              uint32_t num_attributes, const lyon_fill_options* options,
+                              int index_bits, uint32_t index_base, lyon_gpu_result* result,
+                              const lyon_vertex_source** sources,
+                              const uint64_t** source_offsets,
+                              const float** vertex_attribute_values);
+
 /* Basic shapes: FillTessellator::tessellate_rectangle and tessellate_circle
  * (crates/tessellation/src/fill.rs:654-673 with crates/tessellation/src/basic_shapes.rs:12-124),
  * which fill without the sweep, over a batch of shapes. `params` (device memory) holds 4 floats

@@ -45,6 +45,11 @@ class CCustomOutput(ctypes.Structure):
     _fields_ = [("sources", c_p), ("attributes", c_p)]
 
 
+class CFillCustomOutput(ctypes.Structure):
+    _fields_ = [("sources", c_p), ("source_offsets", c_p), ("total_sources", u64),
+                ("attributes", c_p)]
+
+
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
                 ("device_budget_bytes", u64)]
@@ -185,6 +190,16 @@ def load(build_if_missing: bool = True):
         L.lyon_gpu_stroke_path_custom.argtypes = [c_p, c_p, u32, c_p, u32, c_p, u32, i32, c_p,
                                                   ctypes.c_int, u32, ctypes.c_int, c_p,
                                                   ctypes.POINTER(c_p), ctypes.POINTER(c_p)]
+        L.lyon_gpu_fill_paths_custom.restype = ctypes.c_int
+        L.lyon_gpu_fill_paths_custom.argtypes = [c_p, c_p, c_p, u32, c_p, u32, ctypes.c_int,
+                                                 ctypes.c_int, u32, c_p, c_p]
+        L.lyon_gpu_interpolate_fill_attributes.restype = ctypes.c_int
+        L.lyon_gpu_interpolate_fill_attributes.argtypes = [c_p, c_p, c_p, u64, c_p, u32, u64,
+                                                           c_p]
+        L.lyon_gpu_fill_path_custom.restype = ctypes.c_int
+        L.lyon_gpu_fill_path_custom.argtypes = [c_p, c_p, u32, c_p, u32, c_p, u32, c_p,
+                                                ctypes.c_int, u32, c_p, ctypes.POINTER(c_p),
+                                                ctypes.POINTER(c_p), ctypes.POINTER(c_p)]
         L.lyon_gpu_autotune_stroke.restype = ctypes.c_int
         L.lyon_gpu_autotune_stroke.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
                                                ctypes.POINTER(CStrokeTuning),
@@ -214,4 +229,6 @@ EXPORTED = [
     "lyon_gpu_stroke_paths_variable_width", "lyon_gpu_stroke_path_variable_width",
     "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_stroke_paths_custom",
     "lyon_gpu_interpolate_attributes", "lyon_gpu_stroke_path_custom",
+    "lyon_gpu_fill_paths_custom", "lyon_gpu_interpolate_fill_attributes",
+    "lyon_gpu_fill_path_custom",
 ]

@@ -55,8 +55,11 @@ struct lyon_gpu_context {
     uint32_t width_stride = 1;         // floats between consecutive points' width factors
     bool want_sources = false;  // during a custom-attribute call: sequential stepper + sources
     DevBuf out_sources, out_attrs;      // per-vertex sources and interpolated attributes
+    // fill sources: per-path counts and offsets (+ scan scratch), per-vertex first source
+    DevBuf src_counts, src_offsets, src_scratch, out_source_offsets;
+    uint64_t total_sources = 0;
     DevBuf in_attrs;                    // single-path custom attributes (staged)
-    HostBuf h_out_src, h_out_attrs;
+    HostBuf h_out_src, h_out_attrs, h_out_soff;
     // outputs of device-buffer batched calls
     DevBuf out_vertices, out_indices;
     // host-buffer calls: inputs and double-buffered outputs
@@ -364,10 +367,16 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
                 return LYON_ERR_CUDA;
         }
     } else {
+        lg::FillSourceArgs fsa{};
+        if (ctx->want_sources) {
+            if (!ensure(ctx, ctx->src_counts, (size_t)n * 4 + 16)) return LYON_ERR_OUT_OF_MEMORY;
+            fsa.src_counts = as<uint32_t>(ctx->src_counts);
+        }
         int r = lg::fill_count(ctx->fill, batch, (const lyon_fill_options*)options, num_options,
                                ctx->num_sms, as<uint32_t>(ctx->vtx_counts),
                                as<uint32_t>(ctx->idx_counts), as<int32_t>(ctx->status),
-                               small_words(ctx), s, &ctx->last_error);
+                               small_words(ctx), s, &ctx->last_error,
+                               ctx->want_sources ? &fsa : nullptr);
         if (r != LYON_OK) return r;
     }
     mark(ctx, 1);
@@ -395,12 +404,20 @@ int pipeline_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
                 return LYON_ERR_CUDA;
         }
     } else {
+        lg::FillSourceArgs fsa{};
+        if (ctx->want_sources) {
+            fsa.src_offsets = as<uint64_t>(ctx->src_offsets);
+            fsa.point_offsets = batch->point_offsets;
+            fsa.sources = as<lyon_vertex_source>(ctx->out_sources);
+            fsa.source_offsets = as<uint64_t>(ctx->out_source_offsets);
+        }
         if (!set_err(ctx, "fill emit",
                      lg::fill_emit(ctx->fill, n, as<uint32_t>(ctx->vtx_counts),
                                    as<uint32_t>(ctx->idx_counts), as<int32_t>(ctx->status),
                                    as<uint64_t>(ctx->vtx_offsets),
                                    as<uint64_t>(ctx->idx_offsets), vout, iout, index_bits,
-                                   index_mode, (uint32_t)vertex_offset, ctx->request_first, s)))
+                                   index_mode, (uint32_t)vertex_offset, ctx->request_first, s,
+                                   ctx->want_sources ? &fsa : nullptr)))
             return LYON_ERR_CUDA;
     }
     mark(ctx, 3);
@@ -411,6 +428,49 @@ int pipeline_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
         cudaEventElapsedTime(&ctx->last_ms[2], ctx->ev[2], ctx->ev[3]);
         cudaEventElapsedTime(&ctx->last_ms[3], ctx->ev[0], ctx->ev[3]);
     }
+    return LYON_OK;
+}
+
+// Fill sources after the count phase: per-path source offsets (paths that failed count none),
+// the total, and room for every vertex's first source plus the closing total.
+int fill_source_offsets(lyon_gpu_context* ctx, uint32_t n, uint64_t tv) {
+    cudaStream_t s = ctx->stream;
+    ctx->total_sources = 0;
+    if (!ensure(ctx, ctx->src_offsets, ((size_t)n + 1) * 8 + 16) ||
+        !ensure(ctx, ctx->src_scratch, ((size_t)n + 1) * 8 + 16) ||
+        !ensure(ctx, ctx->out_source_offsets, (tv + 1) * 8 + 16) ||
+        !ensure(ctx, ctx->src_counts, (size_t)n * 4 + 16) ||
+        !ensure_host(ctx, ctx->h_small, 64))
+        return LYON_ERR_OUT_OF_MEMORY;
+    uint32_t* sw = small_words(ctx);
+    uint64_t* hs = reinterpret_cast<uint64_t*>(ctx->h_small.ptr);
+    if (n > 0) {
+        cudaMemsetAsync(sw + 2, 0, 4, s);
+        if (!set_err(ctx, "fill sources",
+                     lg::fill_zero_failed_source_counts(as<uint32_t>(ctx->src_counts),
+                                                        as<int32_t>(ctx->status), n, s)) ||
+            !set_err(ctx, "scan",
+                     lg::launch_scan_pairs(as<uint32_t>(ctx->src_counts),
+                                           as<uint32_t>(ctx->src_counts),
+                                           as<uint64_t>(ctx->src_offsets),
+                                           as<uint64_t>(ctx->src_scratch), n,
+                                           as<unsigned long long>(ctx->scan_state), sw + 1,
+                                           reinterpret_cast<int*>(sw + 2), s)))
+            return LYON_ERR_CUDA;
+        cudaMemcpyAsync(hs, as<uint64_t>(ctx->src_offsets) + n, 8, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hs + 1, sw + 2, 4, cudaMemcpyDeviceToHost, s);
+        if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return LYON_ERR_CUDA;
+        if (reinterpret_cast<uint32_t*>(hs + 1)[0] != 0) {
+            ctx->last_error = "scan look-back wait exceeded its bound";
+            return LYON_ERR_CUDA;
+        }
+        ctx->total_sources = hs[0];
+    }
+    // The closing entry: vertex v's sources are [offsets[v], offsets[v + 1]).
+    hs[2] = ctx->total_sources;
+    cudaMemcpyAsync(as<uint64_t>(ctx->out_source_offsets) + tv, hs + 2, 8,
+                    cudaMemcpyHostToDevice, s);
+    if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return LYON_ERR_CUDA;
     return LYON_OK;
 }
 
@@ -427,10 +487,15 @@ int batched_device(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
                            vertex_offset, &tv, &ti, &failed);
     if (r != LYON_OK) return r;
     const size_t vbytes = ctx->vertex_attrs ? sizeof(lyon_stroke_vertex) : 8;
+    if (kind == KIND_FILL && ctx->want_sources) {
+        r = fill_source_offsets(ctx, batch->num_paths, tv);
+        if (r != LYON_OK) return r;
+    }
+    const uint64_t nsrc = kind == KIND_FILL ? ctx->total_sources : tv;
     if (!ensure(ctx, ctx->out_vertices, tv * vbytes + 16) ||
         !ensure(ctx, ctx->out_indices, ti * (index_bits / 8) + 16) ||
         (ctx->want_sources &&
-         !ensure(ctx, ctx->out_sources, tv * sizeof(lyon_vertex_source) + 16)))
+         !ensure(ctx, ctx->out_sources, nsrc * sizeof(lyon_vertex_source) + 16)))
         return LYON_ERR_OUT_OF_MEMORY;
     r = pipeline_emit(ctx, kind, batch, options, num_options, index_bits, index_mode,
                       vertex_offset, as<float>(ctx->out_vertices), ctx->out_indices.ptr, tv);
@@ -644,21 +709,35 @@ int single_path(lyon_gpu_context* ctx, int kind, const uint8_t* verbs, uint32_t 
     if (!ensure_host(ctx, ctx->h_out_v, vb + 16) || !ensure_host(ctx, ctx->h_out_i, ib + 16))
         return LYON_ERR_OUT_OF_MEMORY;
     if (ctx->want_sources) {
-        // Custom attributes: the vertices' sources and their interpolated attributes.
-        const size_t sb = bo.total_vertices * sizeof(lyon_vertex_source);
+        // Custom attributes: the vertices' sources and their interpolated attributes (a fill
+        // vertex has any number of sources, located by per-vertex offsets).
+        const bool fill = kind == KIND_FILL;
+        const uint64_t ns = fill ? ctx->total_sources : bo.total_vertices;
+        const size_t sb = ns * sizeof(lyon_vertex_source);
+        const size_t ob = fill ? (bo.total_vertices + 1) * 8 : 0;
         const size_t ab = point_floats ? bo.total_vertices * floats_per_point * 4 : 0;
         if (!ensure_host(ctx, ctx->h_out_src, sb + 16) ||
+            !ensure_host(ctx, ctx->h_out_soff, ob + 16) ||
             !ensure_host(ctx, ctx->h_out_attrs, ab + 16) ||
             (ab && !ensure(ctx, ctx->out_attrs, ab + 16)))
             return LYON_ERR_OUT_OF_MEMORY;
-        if (ab &&
-            !set_err(ctx, "interpolate",
-                     lg::launch_interpolate(as<lyon_vertex_source>(ctx->out_sources),
+        cudaError_t e = cudaSuccess;
+        if (ab && fill) {
+            e = lg::launch_interpolate_fill(as<lyon_vertex_source>(ctx->out_sources),
+                                            as<uint64_t>(ctx->out_source_offsets),
                                             bo.total_vertices, as<float>(ctx->in_widths),
                                             floats_per_point, num_points,
-                                            as<float>(ctx->out_attrs), ctx->num_sms, s)))
-            return LYON_ERR_CUDA;
+                                            as<float>(ctx->out_attrs), ctx->num_sms, s);
+        } else if (ab) {
+            e = lg::launch_interpolate(as<lyon_vertex_source>(ctx->out_sources),
+                                       bo.total_vertices, as<float>(ctx->in_widths),
+                                       floats_per_point, num_points, as<float>(ctx->out_attrs),
+                                       ctx->num_sms, s);
+        }
+        if (!set_err(ctx, "interpolate", e)) return LYON_ERR_CUDA;
         if (sb) cudaMemcpyAsync(ctx->h_out_src.ptr, ctx->out_sources.ptr, sb,
+                                cudaMemcpyDeviceToHost, s);
+        if (ob) cudaMemcpyAsync(ctx->h_out_soff.ptr, ctx->out_source_offsets.ptr, ob,
                                 cudaMemcpyDeviceToHost, s);
         if (ab) cudaMemcpyAsync(ctx->h_out_attrs.ptr, ctx->out_attrs.ptr, ab,
                                 cudaMemcpyDeviceToHost, s);
@@ -757,12 +836,14 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
                       &ctx->in_options, &ctx->order, &ctx->slot_status[0],
                       &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters,
-                      &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs};
+                      &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs,
+                      &ctx->src_counts, &ctx->src_offsets, &ctx->src_scratch,
+                      &ctx->out_source_offsets};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
     HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v,  &ctx->h_out_i,
                      &ctx->h_small, &ctx->h_offs,   &ctx->h_status, &ctx->h_out_src,
-                     &ctx->h_out_attrs};
+                     &ctx->h_out_attrs, &ctx->h_out_soff};
     for (HostBuf* b : hb) free_host(*b);
     for (int i = 0; i < 4; ++i)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
@@ -1127,6 +1208,84 @@ int lyon_gpu_stroke_path_custom(lyon_gpu_context* ctx, const uint8_t* verbs, uin
     ctx->width_stride = 1;
     if (r == LYON_OK) {
         if (sources) *sources = reinterpret_cast<const lyon_vertex_source*>(ctx->h_out_src.ptr);
+        if (vertex_attribute_values && num_attributes)
+            *vertex_attribute_values = reinterpret_cast<const float*>(ctx->h_out_attrs.ptr);
+    }
+    return r;
+}
+
+int lyon_gpu_fill_paths_custom(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                               const float* attributes, uint32_t num_attributes,
+                               const lyon_fill_options* options, uint32_t num_options,
+                               int index_bits, int index_mode, uint32_t vertex_offset,
+                               lyon_gpu_batch_output* out, lyon_gpu_fill_custom_output* custom) {
+    if (!ctx || !custom || (num_attributes > 0 && !attributes && batch && batch->num_paths > 0))
+        return LYON_ERR_INVALID_ARGUMENT;
+    memset(custom, 0, sizeof(*custom));
+    ctx->want_sources = true;
+    int r = batched_device(ctx, KIND_FILL, batch, options, num_options, index_bits, index_mode,
+                           vertex_offset, out);
+    ctx->want_sources = false;
+    if (r != LYON_OK) return r;
+    custom->sources = as<lyon_vertex_source>(ctx->out_sources);
+    custom->source_offsets = as<uint64_t>(ctx->out_source_offsets);
+    custom->total_sources = ctx->total_sources;
+    if (num_attributes > 0 && out->total_vertices > 0) {
+        if (!ensure(ctx, ctx->out_attrs, out->total_vertices * num_attributes * 4 + 16))
+            return LYON_ERR_OUT_OF_MEMORY;
+        // The sources come from the batch's own points: every id is in range.
+        if (!set_err(ctx, "interpolate",
+                     lg::launch_interpolate_fill(custom->sources, custom->source_offsets,
+                                                 out->total_vertices, attributes,
+                                                 num_attributes, ~0ull,
+                                                 as<float>(ctx->out_attrs), ctx->num_sms,
+                                                 ctx->stream)))
+            return LYON_ERR_CUDA;
+        custom->attributes = as<float>(ctx->out_attrs);
+    }
+    return LYON_OK;
+}
+
+int lyon_gpu_interpolate_fill_attributes(lyon_gpu_context* ctx,
+                                         const lyon_vertex_source* sources,
+                                         const uint64_t* source_offsets, uint64_t num_vertices,
+                                         const float* attributes, uint32_t num_attributes,
+                                         uint64_t num_endpoints, float* out) {
+    if (!ctx || (num_vertices && num_attributes &&
+                 (!sources || !source_offsets || !attributes || !out)))
+        return LYON_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (!set_err(ctx, "interpolate",
+                 lg::launch_interpolate_fill(sources, source_offsets, num_vertices, attributes,
+                                             num_attributes, num_endpoints, out, ctx->num_sms,
+                                             ctx->stream)))
+        return LYON_ERR_CUDA;
+    return LYON_OK;
+}
+
+int lyon_gpu_fill_path_custom(lyon_gpu_context* ctx, const uint8_t* verbs, uint32_t num_verbs,
+                              const float* points, uint32_t num_points, const float* attributes,
+                              uint32_t num_attributes, const lyon_fill_options* options,
+                              int index_bits, uint32_t index_base, lyon_gpu_result* result,
+                              const lyon_vertex_source** sources,
+                              const uint64_t** source_offsets,
+                              const float** vertex_attribute_values) {
+    if (!ctx || (num_attributes > 0 && num_points > 0 && !attributes))
+        return LYON_ERR_INVALID_ARGUMENT;
+    if (sources) *sources = nullptr;
+    if (source_offsets) *source_offsets = nullptr;
+    if (vertex_attribute_values) *vertex_attribute_values = nullptr;
+    static const float kNoPoints[1] = {0.0f};
+    const float* pf = num_attributes == 0 ? nullptr : (num_points ? attributes : kNoPoints);
+    const uint32_t fpp = num_attributes == 0 ? 1 : (num_points ? num_attributes : 1);
+    ctx->want_sources = true;
+    int r = single_path(ctx, KIND_FILL, verbs, num_verbs, points, num_points, options,
+                        sizeof(lyon_fill_options), index_bits, index_base, result, pf, fpp, -1);
+    ctx->want_sources = false;
+    if (r == LYON_OK) {
+        if (sources) *sources = reinterpret_cast<const lyon_vertex_source*>(ctx->h_out_src.ptr);
+        if (source_offsets)
+            *source_offsets = reinterpret_cast<const uint64_t*>(ctx->h_out_soff.ptr);
         if (vertex_attribute_values && num_attributes)
             *vertex_attribute_values = reinterpret_cast<const float*>(ctx->h_out_attrs.ptr);
     }

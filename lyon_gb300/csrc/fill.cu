@@ -57,14 +57,21 @@ struct SweepArgs {
     int32_t* status;
     uint32_t* retry_list;
     int final_attempt;
+    // vertex sources (null src_counts: not requested)
+    uint32_t* src_counts;
+    uint32_t* stage_s;
+    uint32_t* stage_sfirst;
+    unsigned long long stage_s_cap;  // in sources
+    unsigned long long* stage_soff;
 };
 
+template <bool SRC>
 __global__ void __launch_bounds__(32, LG_FILL_MIN_BLOCKS) fill_sweep_kernel(SweepArgs A) {
     // One path per block of one warp, run by its first lane: the sweep's control flow depends on
     // the path, and 32 different paths in one warp would run one after the other anyway.
     if (threadIdx.x != 0) return;
     const uint32_t wid = blockIdx.x;
-    Filler f;
+    FillerT<SRC> f;
     f.h.w = A.heaps + (size_t)wid * A.heap_words;
     f.h.cap = A.heap_words;
     for (;;) {
@@ -77,15 +84,26 @@ __global__ void __launch_bounds__(32, LG_FILL_MIN_BLOCKS) fill_sweep_kernel(Swee
         f.h.reset();
         f.tessellate(A.verbs + v0, v1 - v0, A.points + 2 * (size_t)p0, p1 - p0, o);
         int32_t st = f.err;
-        uint32_t nv = 0, ni = 0;
+        uint32_t nv = 0, ni = 0, ns = 0;
         if (st == LYON_OK) {
             nv = f.out_v.n;
             ni = f.out_i.n;
+            ns = f.out_src.n / 3;
             const unsigned long long vb = atomicAdd(&A.stage_tops[0], (unsigned long long)nv);
             const unsigned long long ib = atomicAdd(&A.stage_tops[1], (unsigned long long)ni);
-            if (vb + nv > A.stage_v_cap || ib + ni > A.stage_i_cap) {
+            unsigned long long sb = 0;
+            if (SRC) sb = atomicAdd(&A.stage_tops[2], (unsigned long long)ns);
+            if (vb + nv > A.stage_v_cap || ib + ni > A.stage_i_cap ||
+                (SRC && sb + ns > A.stage_s_cap)) {
                 st = STATUS_RETRY;
             } else {
+                if (SRC) {
+                    const uint32_t* ss = f.out_src.p(f.h);
+                    for (uint32_t i = 0; i < 3 * ns; ++i) A.stage_s[3 * sb + i] = ss[i];
+                    const uint32_t* sf = f.out_sfirst.p(f.h);
+                    for (uint32_t i = 0; i < nv; ++i) A.stage_sfirst[vb + i] = sf[i];
+                    A.stage_soff[path] = sb;
+                }
                 const V2* sv = f.out_v.p(f.h);
                 for (uint32_t i = 0; i < nv; ++i) A.stage_v[vb + i] = make_float2(sv[i].x, sv[i].y);
                 const uint32_t* si = f.out_i.p(f.h);
@@ -107,7 +125,37 @@ __global__ void __launch_bounds__(32, LG_FILL_MIN_BLOCKS) fill_sweep_kernel(Swee
         }
         A.vtx_counts[path] = st == LYON_OK ? nv : 0u;
         A.idx_counts[path] = st == LYON_OK ? ni : 0u;
+        if (SRC) A.src_counts[path] = st == LYON_OK ? ns : 0u;
         A.status[path] = st;
+    }
+}
+
+// One warp per path: the staged sources of a successful path to their final offsets (ids made
+// batch-global) and every vertex's first source.
+__global__ void fill_emit_sources_kernel(uint32_t n, const uint32_t* vtx_counts,
+                                         const int32_t* status,
+                                         const unsigned long long* stage_off,
+                                         const unsigned long long* stage_soff,
+                                         const uint32_t* stage_s, const uint32_t* stage_sfirst,
+                                         const uint64_t* vtx_offsets, FillSourceArgs S) {
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; p < n; p += warps) {
+        if (status[p] != LYON_OK) continue;
+        const uint32_t nv = vtx_counts[p];
+        const uint64_t so = S.src_offsets[p];
+        const uint32_t ns = (uint32_t)(S.src_offsets[p + 1] - so);
+        const unsigned long long sb = stage_soff[p], vb = stage_off[2 * (size_t)p];
+        const uint32_t base = S.point_offsets[p];
+        for (uint32_t k = lane; k < ns; k += 32) {
+            const uint32_t* w = stage_s + 3 * (sb + k);
+            const uint32_t to = w[1];
+            S.sources[so + k] = lyon_vertex_source{w[0] + base,
+                                                   to == LYON_NO_ENDPOINT ? to : to + base,
+                                                   __uint_as_float(w[2])};
+        }
+        const uint64_t vo = vtx_offsets[p];
+        for (uint32_t i = lane; i < nv; i += 32) S.source_offsets[vo + i] = so + stage_sfirst[vb + i];
     }
 }
 
@@ -166,9 +214,11 @@ bool grow(void** p, size_t* cap, size_t bytes, size_t keep_bytes, cudaStream_t s
 
 int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_options* options,
                uint32_t num_options, int num_sms, uint32_t* vtx_counts, uint32_t* idx_counts,
-               int32_t* status, uint32_t* small_words, cudaStream_t stream, std::string* error) {
+               int32_t* status, uint32_t* small_words, cudaStream_t stream, std::string* error,
+               const FillSourceArgs* src) {
     const uint32_t n = batch->num_paths;
     if (n == 0) return LYON_OK;
+    const bool sources = src && src->src_counts;
     // Counters: [0] work, [1] retries, [2] heap overflows; two u64 staging tops; two retry
     // lists.
     // After them: the size-order scratch (counters, one byte per path).
@@ -199,7 +249,16 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
             return LYON_ERR_OUT_OF_MEMORY;
         }
     }
-    cudaMemsetAsync(tops, 0, 16, stream);
+    // Source staging: about one source per vertex, one first-source word per staged vertex.
+    if (sources &&
+        (!grow(&fb.stage_s, &fb.stage_s_cap, std::max<size_t>(fb.stage_v_cap / 8 * 12, 4096), 0,
+               stream) ||
+         !grow(&fb.stage_sfirst, &fb.stage_sfirst_cap, fb.stage_v_cap / 8 * 4 + 256, 0, stream) ||
+         !grow(&fb.stage_soff, &fb.stage_soff_cap, (size_t)n * 8, 0, stream))) {
+        if (error) *error = "cudaMalloc (fill source staging)";
+        return LYON_ERR_OUT_OF_MEMORY;
+    }
+    cudaMemsetAsync(tops, 0, 24, stream);
     // Big paths first, so that the last paths a sweeper takes are short ones and the launch
     // does not end on one long sweep. The order lives in the second retry list, which the first
     // attempt does not write.
@@ -247,7 +306,16 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         a.status = status;
         a.retry_list = lists[attempt & 1];
         a.final_attempt = attempt == MAX_ATTEMPTS - 1;
-        fillk::fill_sweep_kernel<<<nthreads, 32, 0, stream>>>(a);
+        a.src_counts = sources ? src->src_counts : nullptr;
+        a.stage_s = reinterpret_cast<uint32_t*>(fb.stage_s);
+        a.stage_sfirst = reinterpret_cast<uint32_t*>(fb.stage_sfirst);
+        a.stage_s_cap = fb.stage_s_cap / 12;
+        a.stage_soff = reinterpret_cast<unsigned long long*>(fb.stage_soff);
+        if (sources) {
+            fillk::fill_sweep_kernel<true><<<nthreads, 32, 0, stream>>>(a);
+        } else {
+            fillk::fill_sweep_kernel<false><<<nthreads, 32, 0, stream>>>(a);
+        }
         lg::note_launches(1);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
@@ -255,9 +323,9 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
             return LYON_ERR_CUDA;
         }
         uint32_t h_ctl[3];
-        unsigned long long h_tops[2];
+        unsigned long long h_tops[3];
         cudaMemcpyAsync(h_ctl, counters, 12, cudaMemcpyDeviceToHost, stream);
-        cudaMemcpyAsync(h_tops, tops, 16, cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(h_tops, tops, 24, cudaMemcpyDeviceToHost, stream);
         e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) {
             if (error) *error = std::string("fill sweep: ") + cudaGetErrorString(e);
@@ -268,13 +336,23 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         // The staging tops stay where they are (the failed reservations are abandoned).
         const bool staging_short =
             h_tops[0] > fb.stage_v_cap / 8 || h_tops[1] > fb.stage_i_cap / 4;
+        if (sources && h_tops[2] > fb.stage_s_cap / 12) {
+            const size_t used_s = std::min<size_t>(h_tops[2], fb.stage_s_cap / 12);
+            if (!grow(&fb.stage_s, &fb.stage_s_cap, (size_t)h_tops[2] * 2 * 12 + 4096,
+                      used_s * 12, stream)) {
+                if (error) *error = "cudaMalloc (fill source staging)";
+                return LYON_ERR_OUT_OF_MEMORY;
+            }
+        }
         if (staging_short) {
             const size_t used_v = std::min<size_t>(h_tops[0], fb.stage_v_cap / 8);
             const size_t used_i = std::min<size_t>(h_tops[1], fb.stage_i_cap / 4);
             if (!grow(&fb.stage_v, &fb.stage_v_cap, (size_t)h_tops[0] * 2 * 8 + 4096,
                       used_v * 8, stream) ||
                 !grow(&fb.stage_i, &fb.stage_i_cap, (size_t)h_tops[1] * 2 * 4 + 4096,
-                      used_i * 4, stream)) {
+                      used_i * 4, stream) ||
+                (sources && !grow(&fb.stage_sfirst, &fb.stage_sfirst_cap,
+                                  (size_t)h_tops[0] * 2 * 4 + 4096, used_v * 4, stream))) {
                 if (error) *error = "cudaMalloc (fill staging)";
                 return LYON_ERR_OUT_OF_MEMORY;
             }
@@ -291,8 +369,18 @@ cudaError_t fill_emit(FillBuffers& fb, uint32_t n, const uint32_t* vtx_counts,
                       const uint32_t* idx_counts, const int32_t* status,
                       const uint64_t* vtx_offsets, const uint64_t* idx_offsets, float* vertices,
                       void* indices, int index_bits, int index_mode, uint32_t vertex_offset,
-                      const uint32_t* request_first, cudaStream_t stream) {
+                      const uint32_t* request_first, cudaStream_t stream,
+                      const FillSourceArgs* src) {
     if (n == 0) return cudaSuccess;
+    if (src && src->sources) {
+        fillk::fill_emit_sources_kernel<<<std::min<uint32_t>((n + 7) / 8, 4096u), 256, 0,
+                                          stream>>>(
+            n, vtx_counts, status, reinterpret_cast<const unsigned long long*>(fb.stage_off),
+            reinterpret_cast<const unsigned long long*>(fb.stage_soff),
+            reinterpret_cast<const uint32_t*>(fb.stage_s),
+            reinterpret_cast<const uint32_t*>(fb.stage_sfirst), vtx_offsets, *src);
+        lg::note_launches(1);
+    }
     const uint32_t blocks = std::min<uint32_t>((n + 7) / 8, 4096u);
     fillk::fill_emit_kernel<<<blocks, 256, 0, stream>>>(
         n, vtx_counts, idx_counts, status,
@@ -304,8 +392,25 @@ cudaError_t fill_emit(FillBuffers& fb, uint32_t n, const uint32_t* vtx_counts,
     return cudaGetLastError();
 }
 
+namespace fillk {
+__global__ void zero_failed_counts_kernel(uint32_t* counts, const int32_t* status, uint32_t n) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        if (status[p] != LYON_OK) counts[p] = 0u;
+}
+}  // namespace fillk
+
+cudaError_t fill_zero_failed_source_counts(uint32_t* src_counts, const int32_t* status,
+                                           uint32_t n, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    fillk::zero_failed_counts_kernel<<<std::min<uint32_t>((n + 255) / 256, 1024u), 256, 0,
+                                       stream>>>(src_counts, status, n);
+    lg::note_launches(1);
+    return cudaGetLastError();
+}
+
 void fill_free(FillBuffers& fb) {
-    void* bufs[] = {fb.scratch, fb.stage_v, fb.stage_i, fb.stage_off, fb.work};
+    void* bufs[] = {fb.scratch, fb.stage_v,      fb.stage_i,   fb.stage_off,
+                    fb.work,    fb.stage_s, fb.stage_sfirst, fb.stage_soff};
     for (void* b : bufs)
         if (b) cudaFree(b);
     fb = FillBuffers();

@@ -16,15 +16,26 @@ namespace fillk {
 #define LG_FILL_SHARED_FN
 #endif
 
-struct Filler {
+// SRC: the fill also records every vertex's sources (an instantiation of its own, so that plain
+// fills carry none of that work).
+template <bool SRC>
+struct FillerT {
+    static constexpr bool want_sources = SRC;
     Heap h;
     int err;  // 0, a LYON_ERR_* code, or FILL_ERR_HEAP
     // output in the heap (path-relative ids)
     Vec<V2> out_v;
     Vec<uint32_t> out_i;
+    // With want_sources: every vertex's sources (FillVertex::sources), three words each with
+    // path-local endpoint ids, and each vertex's first source.
+    Vec<uint32_t> out_src;
+    Vec<uint32_t> out_sfirst;
     // event queue
     Vec<Event> events;
     Vec<EdgeData> edge_data;
+    // With want_sources: the endpoint ids (path-local) of each event's source edge, two words per
+    // event, beside edge_data so that plain fills carry none of it.
+    Vec<uint32_t> edge_ids;
     uint32_t first;
     // sweep
     V2 current_position;
@@ -69,12 +80,26 @@ struct Filler {
     }
 
     // ---- event queue (event_queue.rs) ----
-    __host__ __device__ void push_event(V2 pos, const EdgeData& d) {
+    __host__ __device__ void push_event(V2 pos, const EdgeData& d, uint32_t from_id,
+                                        uint32_t to_id) {
         events.push(h, Event{NONE, NONE, pos});
         edge_data.push(h, d);
+        if (SRC && edge_ids.reserve(h, edge_ids.n + 2)) {
+            uint32_t* w = edge_ids.p(h) + edge_ids.n;
+            w[0] = from_id;
+            w[1] = to_id;
+            edge_ids.n += 2;
+        }
     }
     __host__ __device__ __forceinline__ EdgeData no_edge(float t) {
         return EdgeData{V2{u2f(0x7fc00000u), u2f(0x7fc00000u)}, t, t, 0, 0u};
+    }
+    // The endpoint ids of event `e`'s source edge (want_sources only).
+    __host__ __device__ __forceinline__ uint32_t from_id_of(uint32_t e) {
+        return SRC ? edge_ids.at(h, 2 * e) : LYON_NO_ENDPOINT;
+    }
+    __host__ __device__ __forceinline__ uint32_t to_id_of(uint32_t e) {
+        return SRC ? edge_ids.at(h, 2 * e + 1) : LYON_NO_ENDPOINT;
     }
     // event_queue.rs:252-274
     __host__ __device__ void insert_into_sorted_list(uint32_t idx, V2 position, uint32_t after) {
@@ -97,26 +122,29 @@ struct Filler {
         ev[prev].next_event = idx;
     }
     // event_queue.rs:188-213
-    __host__ __device__ uint32_t insert_sorted(V2 position, const EdgeData& data, uint32_t after) {
+    __host__ __device__ uint32_t insert_sorted(V2 position, const EdgeData& data, uint32_t after,
+                                               uint32_t from_id, uint32_t to_id) {
         uint32_t idx = events.n;
-        push_event(position, data);
+        push_event(position, data, from_id, to_id);
         if (!ok()) return idx;
         insert_into_sorted_list(idx, position, after);
         return idx;
     }
     // event_queue.rs:215-230
-    __host__ __device__ void insert_sibling(uint32_t sibling, V2 position, const EdgeData& data) {
+    __host__ __device__ void insert_sibling(uint32_t sibling, V2 position, const EdgeData& data,
+                                            uint32_t from_id, uint32_t to_id) {
         uint32_t idx = events.n;
-        push_event(position, data);
+        push_event(position, data, from_id, to_id);
         if (!ok()) return;
         Event* ev = events.p(h);
         ev[idx].next_sibling = ev[sibling].next_sibling;
         ev[sibling].next_sibling = idx;
     }
     // event_queue.rs:232-250
-    __host__ __device__ void vertex_event_sorted(V2 position, uint32_t after) {
+    __host__ __device__ void vertex_event_sorted(V2 position, uint32_t endpoint_id,
+                                                 uint32_t after) {
         uint32_t idx = events.n;
-        push_event(position, no_edge(0.0f));
+        push_event(position, no_edge(0.0f), endpoint_id, endpoint_id);
         if (!ok()) return;
         insert_into_sorted_list(idx, position, after);
     }
@@ -653,7 +681,7 @@ struct Filler {
         const float t = dy == 0.0f ? 0.0f : (split_point.y - current_position.y) / dy;
         const float t_remapped = remap_t_in_range(t, src.range_start, edge.range_end);
         insert_sorted(split_point, EdgeData{edge.to, t_remapped, edge.range_end, edge.winding, 1u},
-                      current_event_id);
+                      current_event_id, from_id_of(edge.src_edge), to_id_of(edge.src_edge));
     }
     __host__ __device__ void handle_coincident_edges_below() {  // fill.rs:2016-2048
         if (edges_below.n < 2) return;
@@ -756,7 +784,10 @@ struct Filler {
         }
         const ActiveEdge ae0 = active.at(h, ai);
         const EdgeData a_src = edge_data.at(h, ae0.src_edge);
-        const EdgeData b_src = edge_data.at(h, edges_below.at(h, bi).src_edge);
+        const uint32_t b_src_edge = edges_below.at(h, bi).src_edge;
+        const EdgeData b_src = edge_data.at(h, b_src_edge);
+        const uint32_t a_from = from_id_of(ae0.src_edge), a_to = to_id_of(ae0.src_edge);
+        const uint32_t b_from = from_id_of(b_src_edge), b_to = to_id_of(b_src_edge);
         bool has_inserted = false;
         uint32_t inserted_evt = 0;
         bool flipped_active = false;
@@ -765,14 +796,14 @@ struct Filler {
             if (is_after(ae0.to, ip)) {
                 inserted_evt = insert_sorted(
                     ip, EdgeData{ae0.to, remapped_ta, ae0.range_end, ae0.winding, 1u},
-                    current_event_id);
+                    current_event_id, a_from, a_to);
                 has_inserted = true;
             } else {
                 flipped_active = true;
                 insert_sorted(ae0.to,
                               EdgeData{ip, ae0.range_end, remapped_ta, (int32_t)w16(-ae0.winding),
                                        1u},
-                              current_event_id);
+                              current_event_id, a_from, a_to);
             }
             if (!ok()) return;
             ActiveEdge& ae = active.at(h, ai);
@@ -785,15 +816,15 @@ struct Filler {
             if (is_after(eb.to, ip)) {
                 const EdgeData d{eb.to, remapped_tb, eb.range_end, eb.winding, 1u};
                 if (has_inserted) {
-                    insert_sibling(inserted_evt, ip, d);
+                    insert_sibling(inserted_evt, ip, d, b_from, b_to);
                 } else {
-                    insert_sorted(ip, d, current_event_id);
+                    insert_sorted(ip, d, current_event_id, b_from, b_to);
                 }
             } else {
                 insert_sorted(eb.to,
                               EdgeData{ip, eb.range_end, remapped_tb, (int32_t)w16(-eb.winding), 1u},
-                              current_event_id);
-                if (ok() && flipped_active) vertex_event_sorted(ip, current_event_id);
+                              current_event_id, b_from, b_to);
+                if (ok() && flipped_active) vertex_event_sorted(ip, b_to, current_event_id);
             }
             if (!ok()) return;
             PendingEdge& e = edges_below.at(h, bi);
@@ -1026,6 +1057,39 @@ struct Filler {
         }
     }
 
+    // VertexSourceIterator (fill.rs:2294-2337): every sibling event at the vertex gives its
+    // edge's endpoint (t = 0 or 1) or the point at t on it; a source equal to the previous one is
+    // skipped.
+    __host__ __device__ void record_sources(uint32_t ev) {
+        out_sfirst.push(h, out_src.n / 3);
+        uint32_t pf = 0, pt = 0;
+        float ptt = 0.0f;
+        bool have_prev = false;
+        for (uint32_t id = ev; id != NONE; id = events.at(h, id).next_sibling) {
+            const float t = edge_data.at(h, id).range_start;
+            const uint32_t e_from = edge_ids.at(h, 2 * id), e_to = edge_ids.at(h, 2 * id + 1);
+            uint32_t f = e_from, to = LYON_NO_ENDPOINT;
+            float tt = 0.0f;
+            if (t == 1.0f) {
+                f = e_to;
+            } else if (t != 0.0f) {
+                to = e_to;
+                tt = t;
+            }
+            if (have_prev && f == pf && to == pt && (to == LYON_NO_ENDPOINT || tt == ptt)) continue;
+            if (!out_src.reserve(h, out_src.n + 3)) return;
+            uint32_t* d = out_src.p(h) + out_src.n;
+            d[0] = f;
+            d[1] = to;
+            d[2] = f2u(tt);
+            out_src.n += 3;
+            pf = f;
+            pt = to;
+            ptt = tt;
+            have_prev = true;
+        }
+    }
+
     // ---- main loop (fill.rs:749-925) ----
     __host__ __device__ void initialize_events() {
         const uint32_t ce = current_event_id;
@@ -1038,6 +1102,7 @@ struct Filler {
                                 ? current_position
                                 : V2{current_position.y, -current_position.x};
         current_vertex = add_vertex(position);
+        if constexpr (SRC) record_sources(ce);
         uint32_t sib = ce;
         while (sib != NONE) {
             const EdgeData edge = edge_data.at(h, sib);
@@ -1074,11 +1139,18 @@ struct Filler {
     struct Builder {
         V2 current, prev, second;
         uint32_t nth;
+        uint32_t prev_id;  // prev_endpoint_id
         float tolerance;
     };
-    __host__ __device__ void eq_vertex_event(V2 at) { push_event(at, no_edge(0.0f)); }
-    __host__ __device__ void eq_vertex_event_on_curve(V2 at, float t) { push_event(at, no_edge(t)); }
-    __host__ __device__ void eq_add_edge(Builder& b, V2 from, V2 to, int16_t winding, float t0, float t1) {
+    __host__ __device__ void eq_vertex_event(V2 at, uint32_t id) {
+        push_event(at, no_edge(0.0f), id, id);
+    }
+    __host__ __device__ void eq_vertex_event_on_curve(V2 at, float t, uint32_t from_id,
+                                                      uint32_t to_id) {
+        push_event(at, no_edge(t), from_id, to_id);
+    }
+    __host__ __device__ void eq_add_edge(Builder& b, V2 from, V2 to, int16_t winding, float t0,
+                                         float t1, uint32_t from_id, uint32_t to_id) {
         if (peq(from, to)) return;
         V2 evt_pos = from, evt_to = to;
         if (is_after(evt_pos, to)) {
@@ -1089,28 +1161,35 @@ struct Filler {
             t1 = tt;
             winding = w16(-winding);
         }
-        push_event(evt_pos, EdgeData{evt_to, t0, t1, winding, 1u});
+        push_event(evt_pos, EdgeData{evt_to, t0, t1, winding, 1u}, from_id, to_id);
         b.nth += 1;
     }
-    __host__ __device__ void eq_line_segment(Builder& b, V2 to, float t0, float t1) {
+    __host__ __device__ void eq_line_segment(Builder& b, V2 to, uint32_t to_id, float t0,
+                                             float t1) {
         const V2 from = b.current;
         if (peq(from, to)) return;
-        if (is_after(from, to) && b.nth > 0 && is_after(from, b.prev)) eq_vertex_event(from);
+        if (is_after(from, to) && b.nth > 0 && is_after(from, b.prev))
+            eq_vertex_event(from, b.prev_id);
         if (b.nth == 0) b.second = to;
-        eq_add_edge(b, from, to, 1, t0, t1);
+        eq_add_edge(b, from, to, 1, t0, t1, b.prev_id, to_id);
         b.prev = b.current;
+        b.prev_id = to_id;
         b.current = to;
     }
-    __host__ __device__ void eq_end(Builder& b, V2 first_pt) {
+    __host__ __device__ void eq_end(Builder& b, V2 first_pt, uint32_t first_id) {
         if (b.nth == 0) return;
-        eq_line_segment(b, first_pt, 0.0f, 1.0f);
-        if (is_after(first_pt, b.prev) && is_after(first_pt, b.second)) eq_vertex_event(first_pt);
+        eq_line_segment(b, first_pt, first_id, 0.0f, 1.0f);
+        if (is_after(first_pt, b.prev) && is_after(first_pt, b.second))
+            eq_vertex_event(first_pt, first_id);
+        b.prev_id = first_id;
         b.nth = 0;
     }
     // Shared body of quadratic_bezier_segment / cubic_bezier_segment (event_queue.rs:758-900):
-    // the (possibly swapped) segment flattened with lyon's for_each_flattened_with_t.
-    __host__ __device__ void eq_curve(Builder& b, V2 original_from, V2 original_to, bool needs_swap,
-                             const Poly& poly, V2 seg_from, V2 seg_to, float n) {
+    // the (possibly swapped) segment flattened with lyon's for_each_flattened_with_t. A swapped
+    // curve's t values are those of the swapped segment while its ids stay the original ones.
+    __host__ __device__ void eq_curve(Builder& b, V2 original_from, V2 original_to, uint32_t to_id,
+                                      bool needs_swap, const Poly& poly, V2 seg_from, V2 seg_to,
+                                      float n) {
         const int16_t winding = needs_swap ? -1 : 1;
         V2 prev_pt = seg_from;
         bool have_first = false;
@@ -1136,9 +1215,9 @@ struct Filler {
                     have_first = true;
                     first_pt = to;
                 } else if (is_after(from, to) && is_after(from, prev_pt)) {
-                    eq_vertex_event_on_curve(from, t0);
+                    eq_vertex_event_on_curve(from, t0, b.prev_id, to_id);
                 }
-                eq_add_edge(b, from, to, winding, t0, t1);
+                eq_add_edge(b, from, to, winding, t0, t1, b.prev_id, to_id);
                 prev_pt = from;
             }
             from = to;
@@ -1157,13 +1236,14 @@ struct Filler {
             if (is_first_edge) {
                 b.second = second_pt;
             } else if (is_after(original_from, b.prev) && is_after(original_from, second_pt)) {
-                eq_vertex_event(original_from);
+                eq_vertex_event(original_from, b.prev_id);
             }
             b.prev = previous;
             b.current = original_to;
+            b.prev_id = to_id;
         }
     }
-    __host__ __device__ void eq_quad(Builder& b, V2 ctrl, V2 to) {
+    __host__ __device__ void eq_quad(Builder& b, V2 ctrl, V2 to, uint32_t to_id) {
         const V2 from = b.current;
         const bool needs_swap = is_after(from, to);
         V2 sf = from, st = to;
@@ -1173,9 +1253,9 @@ struct Filler {
         }
         const float n = quad_wang(sf, ctrl, st, b.tolerance);
         const Poly poly = quad_poly(sf, ctrl, st);
-        eq_curve(b, from, to, needs_swap, poly, sf, st, n);
+        eq_curve(b, from, to, to_id, needs_swap, poly, sf, st, n);
     }
-    __host__ __device__ void eq_cubic(Builder& b, V2 c1, V2 c2, V2 to) {
+    __host__ __device__ void eq_cubic(Builder& b, V2 c1, V2 c2, V2 to, uint32_t to_id) {
         const V2 from = b.current;
         const bool needs_swap = is_after(from, to);
         V2 sf = from, sc1 = c1, sc2 = c2, st = to;
@@ -1187,7 +1267,7 @@ struct Filler {
         }
         const float n = cubic_wang(sf, sc1, sc2, st, b.tolerance);
         const Poly poly = cubic_poly(sf, sc1, sc2, st);
-        eq_curve(b, from, to, needs_swap, poly, sf, st, n);
+        eq_curve(b, from, to, to_id, needs_swap, poly, sf, st, n);
     }
 
     // Number of edges the event queue builder will produce at most (lines, flattened curve
@@ -1227,10 +1307,12 @@ struct Filler {
         Builder b;
         b.current = b.prev = b.second = V2{u2f(0x7fc00000u), u2f(0x7fc00000u)};
         b.nth = 0;
+        b.prev_id = LYON_NO_ENDPOINT;
         b.tolerance = o.tolerance;
         const bool horizontal = o.sweep_orientation == LYON_ORIENTATION_HORIZONTAL;
         uint32_t pi = 0;
         V2 first_pt = V2{0.0f, 0.0f};
+        uint32_t first_id = LYON_NO_ENDPOINT;
         auto take = [&](bool* bad) -> V2 {
             if (pi >= npts) {
                 *bad = true;
@@ -1246,34 +1328,36 @@ struct Filler {
                 case LYON_VERB_BEGIN: {
                     V2 p = take(&bad);
                     first_pt = p;
+                    first_id = pi - 1;
                     b.nth = 0;
                     b.current = p;
+                    b.prev_id = first_id;
                     break;
                 }
                 case LYON_VERB_LINE_TO: {
                     V2 p = take(&bad);
-                    if (!bad) eq_line_segment(b, p, 0.0f, 1.0f);
+                    if (!bad) eq_line_segment(b, p, pi - 1, 0.0f, 1.0f);
                     break;
                 }
                 case LYON_VERB_QUADRATIC_TO: {
                     V2 c = take(&bad);
                     V2 p = take(&bad);
-                    if (!bad) eq_quad(b, c, p);
+                    if (!bad) eq_quad(b, c, p, pi - 1);
                     break;
                 }
                 case LYON_VERB_CUBIC_TO: {
                     V2 c1 = take(&bad);
                     V2 c2 = take(&bad);
                     V2 p = take(&bad);
-                    if (!bad) eq_cubic(b, c1, c2, p);
+                    if (!bad) eq_cubic(b, c1, c2, p, pi - 1);
                     break;
                 }
                 case LYON_VERB_CLOSE:
                     (void)take(&bad);
-                    if (!bad) eq_end(b, first_pt);
+                    if (!bad) eq_end(b, first_pt, first_id);
                     break;
                 case LYON_VERB_END:
-                    eq_end(b, first_pt);
+                    eq_end(b, first_pt, first_id);
                     break;
                 default:
                     bad = true;
@@ -1290,8 +1374,11 @@ struct Filler {
         err = 0;
         out_v.init();
         out_i.init();
+        out_src.init();
+        out_sfirst.init();
         events.init();
         edge_data.init();
+        edge_ids.init();
         active.init();
         edges_below.init();
         spans.init();
@@ -1308,6 +1395,7 @@ struct Filler {
             const uint32_t segs = count_segments(verbs, nverbs, pts, npts, o);
             events.reserve(h, segs + segs / 4 + 8);
             edge_data.reserve(h, segs + segs / 4 + 8);
+            if constexpr (SRC) edge_ids.reserve(h, 2 * (segs + segs / 4 + 8));
         }
         if (!build_events(verbs, nverbs, pts, npts, o)) {
             fail(LYON_ERR_INVALID_ARGUMENT);
@@ -1317,6 +1405,10 @@ struct Filler {
         sort_events();
         out_v.reserve(h, events.n + 8);
         out_i.reserve(h, 6 * events.n + 24);
+        if constexpr (SRC) {
+            out_sfirst.reserve(h, events.n + 8);
+            out_src.reserve(h, 3 * events.n + 24);
+        }
         if (o.tolerance != o.tolerance || o.tolerance <= 0.0f) {
             fail(LYON_ERR_TOLERANCE_IS_NAN);
             return;
@@ -1339,6 +1431,7 @@ struct Filler {
         ok();
     }
 };
+using Filler = FillerT<false>;
 
 }  // namespace fillk
 }  // namespace lg

@@ -81,11 +81,18 @@ int stroke_blocks_per_sm();
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);
 // The sequential stepper (stroke_seq.cu): variable line width and the vertex-source output.
 cudaError_t launch_stroke_seq(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);
-// StrokeVertex::interpolated_attributes over `n` vertex sources (stroke_seq.cu).
+// StrokeVertex::interpolated_attributes over `n` vertex sources (attributes.cu).
 cudaError_t launch_interpolate(const lyon_vertex_source* sources, uint64_t n,
                                const float* attributes, uint32_t num_attributes,
                                uint64_t num_endpoints, float* out, int num_sms,
                                cudaStream_t stream);
+// FillVertex::interpolated_attributes over `n` vertices whose sources are
+// sources[source_offsets[v] .. source_offsets[v + 1]) (attributes.cu).
+cudaError_t launch_interpolate_fill(const lyon_vertex_source* sources,
+                                    const uint64_t* source_offsets, uint64_t n,
+                                    const float* attributes, uint32_t num_attributes,
+                                    uint64_t num_endpoints, float* out, int num_sms,
+                                    cudaStream_t stream);
 
 // Exclusive scan of two u32 arrays into two u64 arrays (decoupled look-back), plus totals at
 // out_a[n] / out_b[n]. `tile_state` holds 2 * num_tiles(n) u64 and `counter` one u32; both are

@@ -1,5 +1,4 @@
-// stroke_seq.cu — lyon's sequential stroke stepper, one path per thread, and the interpolation of
-// custom endpoint attributes.
+// stroke_seq.cu — lyon's sequential stroke stepper, one path per thread.
 //
 // The warp-per-path kernel (stroke.cu) reproduces the fixed-width stroker's output without
 // running its state machine step by step. Two outputs need the state machine itself:
@@ -345,31 +344,6 @@ void launch_seq(const StrokeArgs& a, bool emit, int grid, cudaStream_t s) {
     }
 }
 
-// StrokeVertex::interpolated_attributes (stroke.rs:2728-2747), one thread per vertex.
-__global__ void __launch_bounds__(256)
-    interpolate_kernel(const lyon_vertex_source* __restrict__ src, uint64_t n,
-                       const float* __restrict__ attrs, uint32_t na, uint64_t ne,
-                       float* __restrict__ out) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-        const lyon_vertex_source s = src[v];
-        float* o = out + v * na;
-        const bool edge = s.to != LYON_NO_ENDPOINT;
-        if (s.from >= ne || (edge && s.to >= ne)) {
-            for (uint32_t i = 0; i < na; ++i) o[i] = __int_as_float(0x7fc00000);
-            continue;
-        }
-        const float* a = attrs + (uint64_t)s.from * na;
-        if (!edge) {
-            for (uint32_t i = 0; i < na; ++i) o[i] = a[i];
-        } else {
-            const float* b = attrs + (uint64_t)s.to * na;
-            const float u = 1.0f - s.t;
-            for (uint32_t i = 0; i < na; ++i) o[i] = a[i] * u + b[i] * s.t;
-        }
-    }
-}
-
 }  // namespace
 
 cudaError_t launch_stroke_seq(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream) {
@@ -378,20 +352,6 @@ cudaError_t launch_stroke_seq(const StrokeArgs& args, bool emit, int grid, cudaS
     } else {
         launch_seq<false>(args, emit, grid, stream);
     }
-    note_launches(1);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_interpolate(const lyon_vertex_source* sources, uint64_t n,
-                               const float* attributes, uint32_t num_attributes,
-                               uint64_t num_endpoints, float* out, int num_sms,
-                               cudaStream_t stream) {
-    if (n == 0 || num_attributes == 0) return cudaSuccess;
-    const uint64_t need = (n + 255) / 256;
-    const uint64_t cap = (uint64_t)(num_sms > 0 ? num_sms : 1) * 8;
-    const unsigned grid = (unsigned)(need < cap ? need : cap);
-    interpolate_kernel<<<grid, 256, 0, stream>>>(sources, n, attributes, num_attributes,
-                                                 num_endpoints, out);
     note_launches(1);
     return cudaGetLastError();
 }

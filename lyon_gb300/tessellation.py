@@ -94,6 +94,9 @@ class BuffersBuilder:
         self.buffers = buffers
         self.vertex_offset = vertex_offset
         self.vertex_ctor = vertex_ctor
+        # Fills with custom attributes: every vertex's sources, (S, 3) u32 words (from, to, t
+        # bits), which the fill vertex records index (src_first, src_count).
+        self.sources = np.zeros((0, 3), np.uint32)
 
     def with_vertex_offset(self, offset: int) -> "BuffersBuilder":
         self.vertex_offset = offset
@@ -221,6 +224,65 @@ def _single_custom(ctx: Context, path: Path, options, builder: BuffersBuilder,
             out["attributes"] = np.ctypeslib.as_array(
                 ctypes.cast(att_p, ctypes.POINTER(ctypes.c_float)), shape=(nv * na,)).copy(
                 ).reshape(-1, na)
+    builder.append(out, i)
+
+
+def fill_vertex_dtype(num_attributes: int) -> np.dtype:
+    """What the vertex constructor receives for a fill of a path with custom attributes: the
+    position, the vertex's sources (FillVertex::sources) as a range of BuffersBuilder.sources,
+    and its interpolated attributes (FillVertex::interpolated_attributes)."""
+    fields = [("x", "<f4"), ("y", "<f4"), ("src_first", "<u8"), ("src_count", "<u4")]
+    if num_attributes:
+        fields.append(("attributes", "<f4", (num_attributes,)))
+    return np.dtype(fields)
+
+
+def _single_fill_custom(ctx: Context, path: Path, options, builder: BuffersBuilder,
+                        attributes) -> None:
+    """One path with custom endpoint attributes (lyon_gpu_fill_path_custom)."""
+    bits = builder.buffers.index_bits
+    verbs = np.ascontiguousarray(path.verbs, dtype=np.uint8)
+    pts = np.ascontiguousarray(path.points, dtype=np.float32)
+    attrs = np.ascontiguousarray(attributes, dtype=np.float32)
+    attrs = attrs.reshape(len(pts), -1) if attrs.size else np.zeros((len(pts), 0), np.float32)
+    if attrs.shape[0] != len(pts):
+        raise ValueError("one attribute row per point")
+    na = attrs.shape[1]
+    opt = options.to_c()
+    res = _native.CResult()
+    src_p, off_p, att_p = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    r = ctx.lib.lyon_gpu_fill_path_custom(
+        ctx.h, _ptr(verbs), len(verbs), _ptr(pts), len(pts), _ptr(attrs), na, ctypes.byref(opt),
+        bits, builder.next_index(), ctypes.byref(res), ctypes.byref(src_p), ctypes.byref(off_p),
+        ctypes.byref(att_p))
+    if r != LYON_OK:
+        raise TessellationError(r, ctx.last_error() if r >= 100 else "")
+    nv, ni = res.num_vertices, res.num_indices
+    ctype = ctypes.c_uint16 if bits == 16 else ctypes.c_uint32
+    i = np.ctypeslib.as_array(ctypes.cast(res.indices, ctypes.POINTER(ctype)),
+                              shape=(ni,)).copy() if ni else np.zeros(0, builder.buffers.indices.dtype)
+    v = np.ctypeslib.as_array(ctypes.cast(res.vertices, ctypes.POINTER(ctypes.c_float)),
+                              shape=(nv * 2,)).copy().reshape(-1, 2) if nv else np.zeros((0, 2),
+                                                                                       np.float32)
+    if builder.vertex_ctor is None:
+        builder.append(v, i)
+        return
+    offs = np.ctypeslib.as_array(ctypes.cast(off_p, ctypes.POINTER(ctypes.c_uint64)),
+                                 shape=(nv + 1,)).copy() if nv else np.zeros(1, np.uint64)
+    ns = int(offs[-1])
+    src = np.ctypeslib.as_array(ctypes.cast(src_p, ctypes.POINTER(ctypes.c_uint32)),
+                                shape=(ns * 3,)).copy().reshape(-1, 3) if ns else np.zeros(
+        (0, 3), np.uint32)
+    out = np.zeros(nv, fill_vertex_dtype(na))
+    out["x"] = v[:, 0]
+    out["y"] = v[:, 1]
+    out["src_first"] = offs[:-1] + len(builder.sources)
+    out["src_count"] = np.diff(offs)
+    if na and nv:
+        out["attributes"] = np.ctypeslib.as_array(
+            ctypes.cast(att_p, ctypes.POINTER(ctypes.c_float)), shape=(nv * na,)).copy(
+            ).reshape(-1, na)
+    builder.sources = np.concatenate([builder.sources, src])
     builder.append(out, i)
 
 
@@ -382,7 +444,14 @@ class FillTessellator:
         """fill.rs:663-672 (basic_shapes.rs:40-124)."""
         self._shape(SHAPE_CIRCLE, [center[0], center[1], radius], options, builder)
 
-    def tessellate_path(self, path: Path, options: FillOptions, builder: BuffersBuilder) -> None:
+    def tessellate_path(self, path: Path, options: FillOptions, builder: BuffersBuilder,
+                        attributes=None) -> None:
+        """`attributes`: the path's custom endpoint attributes, (num_points, A) f32 (fill.rs:
+        636-640 then takes tessellate_with_ids): a vertex constructor receives
+        `fill_vertex_dtype(A)` records whose sources are ranges of `builder.sources`."""
+        if attributes is not None:
+            _single_fill_custom(self.ctx, path, options, builder, attributes)
+            return
         _single("fill", self.ctx, path, options, builder)
 
     tessellate = tessellate_path
@@ -455,6 +524,8 @@ class BatchResult:
     sources_ptr: int = 0          # lyon_vertex_source records (custom-attribute calls)
     custom_attributes_ptr: int = 0
     num_attributes: int = 0
+    source_offsets_ptr: int = 0   # fills: total_vertices + 1 u64 (vertex v's sources)
+    total_sources: int = 0
 
     def offsets(self):
         """(vertex_offsets, index_offsets) as int64 torch tensors of num_paths + 1 entries."""
@@ -485,8 +556,15 @@ class BatchResult:
         `to` == -1 for an endpoint)."""
         import torch
         assert self.sources_ptr, "not a custom-attribute output"
-        return torch.as_tensor(_CudaArray(self.sources_ptr, (self.total_vertices, 3), "<i4"),
-                               device="cuda")
+        n = self.total_sources if self.source_offsets_ptr else self.total_vertices
+        return torch.as_tensor(_CudaArray(self.sources_ptr, (n, 3), "<i4"), device="cuda")
+
+    def source_offsets(self):
+        """Fills: vertex v's sources are sources()[offsets[v]:offsets[v + 1]] (int64)."""
+        import torch
+        assert self.source_offsets_ptr, "not a fill custom-attribute output"
+        return torch.as_tensor(_CudaArray(self.source_offsets_ptr, (self.total_vertices + 1,),
+                                          "<i8"), device="cuda")
 
     def custom_attributes(self):
         """Each vertex's interpolated custom attributes, (V, A) f32."""
@@ -528,8 +606,24 @@ def tessellate_paths(kind: str, dbatch: DeviceBatch, options_dev, num_options: i
     ctx = ctx or Context.default()
     out = _native.CBatchOutput()
     cb = dbatch.c()
-    if (attributes or widths is not None or custom_attributes is not None) and kind != "stroke":
+    if (attributes or widths is not None) and kind != "stroke":
         raise ValueError("vertex attributes and variable widths are stroke options")
+    if custom_attributes is not None and kind == "fill":
+        na = int(custom_attributes.shape[1]) if custom_attributes.dim() == 2 else 0
+        co = _native.CFillCustomOutput()
+        r = ctx.lib.lyon_gpu_fill_paths_custom(
+            ctx.h, ctypes.byref(cb), custom_attributes.data_ptr() if na else None, na,
+            options_dev.data_ptr(), num_options, index_bits, index_mode, vertex_offset,
+            ctypes.byref(out), ctypes.byref(co))
+        if r != LYON_OK:
+            raise TessellationError(r, ctx.last_error())
+        return BatchResult(r, int(out.total_vertices), int(out.total_indices),
+                           int(out.num_failed_paths), int(out.vertices or 0),
+                           int(out.indices or 0), int(out.status or 0), index_bits,
+                           dbatch.num_paths, int(out.vertex_offsets or 0),
+                           int(out.index_offsets or 0), 2, int(co.sources or 0),
+                           int(co.attributes or 0), na, int(co.source_offsets or 0),
+                           int(co.total_sources))
     if custom_attributes is not None:
         na = int(custom_attributes.shape[1]) if custom_attributes.dim() == 2 else 0
         co = _native.CCustomOutput()

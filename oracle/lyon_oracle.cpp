@@ -343,6 +343,8 @@ struct PathIter {
             case LYON_VERB_CLOSE:
                 e->kind = EV_END;
                 e->from = current;
+                e->id_from = cur_id;
+                e->id_to = first_id;
                 (void)take();
                 e->to = first;
                 e->w_from = cur_w;
@@ -352,6 +354,8 @@ struct PathIter {
             case LYON_VERB_END:
                 e->kind = EV_END;
                 e->from = current;
+                e->id_from = cur_id;
+                e->id_to = first_id;
                 current = first;
                 e->to = first;
                 e->w_from = cur_w;
@@ -395,6 +399,11 @@ struct Output {
     // stroke.rs:2719-2722): from, to, t (f32 bits); `to` is NO_ENDPOINT for Endpoint { id: from }.
     bool want_sources = false;
     std::vector<uint32_t> sources;
+    // A fill with want_sources records each vertex's sources (FillVertex::sources,
+    // fill.rs:2172-2178, 2294-2337) instead: any number per vertex, three words each, with the
+    // number per vertex in fill_source_counts.
+    std::vector<uint32_t> fill_sources, fill_source_counts;
+    size_t first_fill_source = 0;
     uint64_t max_index = 0xFFFFFFFEull;
     uint64_t vertex_offset = 0;
     size_t first_vertex = 0, first_index = 0;
@@ -402,6 +411,7 @@ struct Output {
     void begin_geometry() {
         first_vertex = vertices.size() / 2;
         first_index = indices.size();
+        first_fill_source = fill_sources.size() / 3;
     }
     bool add_vertex(P p, uint32_t* id) {
         uint64_t i = vertices.size() / 2 + vertex_offset;
@@ -421,6 +431,10 @@ struct Output {
         indices.resize(first_index);
         if (want_attributes) attributes.resize(first_vertex * 4);
         if (want_sources) sources.resize(first_vertex * 3);
+        if (!fill_source_counts.empty() || !fill_sources.empty()) {
+            fill_sources.resize(first_fill_source * 3);
+            fill_source_counts.resize(first_vertex);
+        }
     }
 };
 
@@ -1463,6 +1477,7 @@ struct EdgeData {  // event_queue.rs:28-36
     float range_start, range_end;
     int16_t winding;
     bool is_edge;
+    uint32_t from_id = NO_ENDPOINT, to_id = NO_ENDPOINT;  // the source edge's endpoints
 };
 
 struct EventQueue {
@@ -1521,10 +1536,10 @@ struct EventQueue {
     }
 
     // event_queue.rs:232-250
-    void vertex_event_sorted(P position, uint32_t after) {
+    void vertex_event_sorted(P position, uint32_t endpoint_id, uint32_t after) {
         uint32_t idx = (uint32_t)events.size();
         push_unsorted(position);
-        edge_data.push_back(EdgeData{P{NAN, NAN}, 0.0f, 0.0f, 0, false});
+        edge_data.push_back(EdgeData{P{NAN, NAN}, 0.0f, 0.0f, 0, false, endpoint_id, endpoint_id});
         insert_into_sorted_list(idx, position, after);
     }
 
@@ -1599,31 +1614,36 @@ struct EventQueue {
 struct EventQueueBuilder {
     P current{NAN, NAN}, prev{NAN, NAN}, second{NAN, NAN};
     uint32_t nth = 0;
+    uint32_t prev_endpoint_id = NO_ENDPOINT;
     EventQueue* queue;
     float tolerance;
 
-    void vertex_event(P at) {  // event_queue.rs:637-647
+    void vertex_event(P at, uint32_t endpoint_id) {  // event_queue.rs:637-647
         queue->push_unsorted(at);
-        queue->edge_data.push_back(EdgeData{P{NAN, NAN}, 0.0f, 0.0f, 0, false});
+        queue->edge_data.push_back(
+            EdgeData{P{NAN, NAN}, 0.0f, 0.0f, 0, false, endpoint_id, endpoint_id});
     }
-    void vertex_event_on_curve(P at, float t) {  // event_queue.rs:649-659
+    void vertex_event_on_curve(P at, float t, uint32_t from_id, uint32_t to_id) {  // :649-659
         queue->push_unsorted(at);
-        queue->edge_data.push_back(EdgeData{P{NAN, NAN}, t, t, 0, false});
+        queue->edge_data.push_back(EdgeData{P{NAN, NAN}, t, t, 0, false, from_id, to_id});
     }
 
-    void end(P first) {  // event_queue.rs:661-682
+    void end(P first, uint32_t first_id) {  // event_queue.rs:661-682
         if (nth == 0) return;
-        line_segment(first, 0.0f, 1.0f);
-        if (is_after(first, prev) && is_after(first, second)) vertex_event(first);
+        line_segment(first, first_id, 0.0f, 1.0f);
+        if (is_after(first, prev) && is_after(first, second)) vertex_event(first, first_id);
+        prev_endpoint_id = first_id;
         nth = 0;
     }
 
-    void begin(P to) {  // event_queue.rs:684-691
+    void begin(P to, uint32_t to_id) {  // event_queue.rs:684-691
         nth = 0;
         current = to;
+        prev_endpoint_id = to_id;
     }
 
-    void add_edge(P from, P to, int16_t winding, float t0, float t1) {  // :693-726
+    void add_edge(P from, P to, int16_t winding, uint32_t from_id, uint32_t to_id, float t0,
+                  float t1) {  // :693-726
         if (peq(from, to)) return;
         P evt_pos = from, evt_to = to;
         if (is_after(evt_pos, to)) {
@@ -1633,22 +1653,27 @@ struct EventQueueBuilder {
             winding = (int16_t)(-winding);
         }
         queue->push_unsorted(evt_pos);
-        queue->edge_data.push_back(EdgeData{evt_to, t0, t1, winding, true});
+        queue->edge_data.push_back(EdgeData{evt_to, t0, t1, winding, true, from_id, to_id});
         nth += 1;
     }
 
-    void line_segment(P to, float t0, float t1) {  // :728-756
+    void line_segment(P to, uint32_t to_id, float t0, float t1) {  // :728-756
         P from = current;
         if (peq(from, to)) return;
-        if (is_after(from, to) && nth > 0 && is_after(from, prev)) vertex_event(from);
+        if (is_after(from, to) && nth > 0 && is_after(from, prev))
+            vertex_event(from, prev_endpoint_id);
         if (nth == 0) second = to;
-        add_edge(from, to, 1, t0, t1);
+        add_edge(from, to, 1, prev_endpoint_id, to_id, t0, t1);
         prev = current;
+        prev_endpoint_id = to_id;
         current = to;
     }
 
+    // The t values of a swapped curve are those of the swapped (downward) segment while the ids
+    // stay the original from and to, as in lyon.
     template <class FlattenFn>
-    void curve_segment(P original_from, P original_to, bool needs_swap, FlattenFn&& flatten) {
+    void curve_segment(P original_from, P original_to, uint32_t to_id, bool needs_swap,
+                       FlattenFn&& flatten) {
         // Shared body of quadratic_bezier_segment / cubic_bezier_segment (:758-900).
         int16_t winding = needs_swap ? -1 : 1;
         P seg_from = needs_swap ? original_to : original_from;
@@ -1662,9 +1687,9 @@ struct EventQueueBuilder {
                 have_first = true;
                 first = lt;
             } else if (is_after(lf, lt) && is_after(lf, prev_pt)) {
-                vertex_event_on_curve(lf, t0);
+                vertex_event_on_curve(lf, t0, prev_endpoint_id, to_id);
             }
-            add_edge(lf, lt, winding, t0, t1);
+            add_edge(lf, lt, winding, prev_endpoint_id, to_id, t0, t1);
             prev_pt = lf;
         });
         if (have_first) {
@@ -1679,24 +1704,25 @@ struct EventQueueBuilder {
             if (is_first_edge) {
                 second = second_pt;
             } else if (is_after(original_from, prev) && is_after(original_from, second_pt)) {
-                vertex_event(original_from);
+                vertex_event(original_from, prev_endpoint_id);
             }
             prev = previous;
             current = original_to;
+            prev_endpoint_id = to_id;
         }
     }
 
-    void quadratic_bezier_segment(P ctrl, P to) {  // :758-826
+    void quadratic_bezier_segment(P ctrl, P to, uint32_t to_id) {  // :758-826
         Quad original{current, ctrl, to};
         bool needs_swap = is_after(original.from, original.to);
         Quad segment = original;
         if (needs_swap) std::swap(segment.from, segment.to);
-        curve_segment(original.from, original.to, needs_swap, [&](auto&& cb) {
+        curve_segment(original.from, original.to, to_id, needs_swap, [&](auto&& cb) {
             quad_flatten_with_t(segment, tolerance, cb);
         });
     }
 
-    void cubic_bezier_segment(P ctrl1, P ctrl2, P to) {  // :828-900
+    void cubic_bezier_segment(P ctrl1, P ctrl2, P to, uint32_t to_id) {  // :828-900
         Cubic original{current, ctrl1, ctrl2, to};
         bool needs_swap = is_after(original.from, original.to);
         Cubic segment = original;
@@ -1704,7 +1730,7 @@ struct EventQueueBuilder {
             std::swap(segment.from, segment.to);
             std::swap(segment.ctrl1, segment.ctrl2);
         }
-        curve_segment(original.from, original.to, needs_swap, [&](auto&& cb) {
+        curve_segment(original.from, original.to, to_id, needs_swap, [&](auto&& cb) {
             cubic_flatten_with_t(segment, tolerance, cb);
         });
     }
@@ -2267,7 +2293,8 @@ struct Filler {
         float dy = edge.to.y - current_position.y;
         float t = dy == 0.0f ? 0.0f : (split_point.y - current_position.y) / dy;
         float t_remapped = remap_t_in_range(t, src.range_start, edge.range_end);
-        EdgeData data{edge.to, t_remapped, edge.range_end, edge.winding, true};
+        EdgeData data{edge.to, t_remapped, edge.range_end, edge.winding, true, src.from_id,
+                      src.to_id};
         events.insert_sorted(split_point, data, current_event_id);
     }
 
@@ -2369,13 +2396,14 @@ struct Filler {
         if (!peq(ae.to, intersection_position) && !peq(ae.from, intersection_position)) {
             float remapped_ta = remap_t_in_range((float)ta, a_src.range_start, ae.range_end);
             if (is_after(ae.to, intersection_position)) {
-                EdgeData d{ae.to, remapped_ta, ae.range_end, ae.winding, true};
+                EdgeData d{ae.to, remapped_ta, ae.range_end, ae.winding, true, a_src.from_id,
+                           a_src.to_id};
                 inserted_evt = events.insert_sorted(intersection_position, d, current_event_id);
                 has_inserted = true;
             } else {
                 flipped_active = true;
                 EdgeData d{intersection_position, ae.range_end, remapped_ta,
-                           (int16_t)(-ae.winding), true};
+                           (int16_t)(-ae.winding), true, a_src.from_id, a_src.to_id};
                 events.insert_sorted(ae.to, d, current_event_id);
             }
             ae.to = intersection_position;
@@ -2387,7 +2415,7 @@ struct Filler {
                 remap_t_in_range((float)tb, b_src.range_start, edge_below.range_end);
             if (is_after(edge_below.to, intersection_position)) {
                 EdgeData d{edge_below.to, remapped_tb, edge_below.range_end, edge_below.winding,
-                           true};
+                           true, b_src.from_id, b_src.to_id};
                 if (has_inserted) {
                     events.insert_sibling(inserted_evt, intersection_position, d);
                 } else {
@@ -2395,10 +2423,11 @@ struct Filler {
                 }
             } else {
                 EdgeData d{intersection_position, edge_below.range_end, remapped_tb,
-                           (int16_t)(-edge_below.winding), true};
+                           (int16_t)(-edge_below.winding), true, b_src.from_id, b_src.to_id};
                 events.insert_sorted(edge_below.to, d, current_event_id);
                 if (flipped_active) {
-                    events.vertex_event_sorted(intersection_position, current_event_id);
+                    events.vertex_event_sorted(intersection_position, b_src.to_id,
+                                               current_event_id);
                 }
             }
             edge_below.to = intersection_position;
@@ -2567,6 +2596,34 @@ struct Filler {
         }
     }
 
+    // VertexSourceIterator (fill.rs:2294-2337): every sibling event at the vertex gives its
+    // edge's endpoint (t = 0 or 1) or the point at t on it; a source equal to the previous one is
+    // skipped.
+    void record_sources(uint32_t evt) {
+        bool have_prev = false;
+        Src prev;
+        uint32_t count = 0;
+        for (uint32_t id = evt; id != INVALID_EVENT; id = events.events[id].next_sibling) {
+            const EdgeData& e = events.edge_data[id];
+            const float t = e.range_start;
+            const Src src = t == 0.0f   ? endpoint_src(e.from_id)
+                            : t == 1.0f ? endpoint_src(e.to_id)
+                                        : Src{e.from_id, e.to_id, t};
+            const bool same = have_prev && src.from == prev.from && src.to == prev.to &&
+                              (src.to == NO_ENDPOINT || src.t == prev.t);
+            if (same) continue;
+            uint32_t tb;
+            std::memcpy(&tb, &src.t, 4);
+            out->fill_sources.push_back(src.from);
+            out->fill_sources.push_back(src.to);
+            out->fill_sources.push_back(tb);
+            prev = src;
+            have_prev = true;
+            ++count;
+        }
+        out->fill_source_counts.push_back(count);
+    }
+
     // fill.rs:869-925
     void initialize_events() {
         uint32_t current_event = current_event_id;
@@ -2580,6 +2637,7 @@ struct Filler {
         uint32_t id;
         if (!out->add_vertex(position, &id)) throw TessError{LYON_ERR_TOO_MANY_VERTICES, 0};
         current_vertex = id;
+        if (out->want_sources) record_sources(current_event);
         uint32_t sib = current_event;
         while (sib != INVALID_EVENT) {
             const EdgeData& edge = events.edge_data[sib];
@@ -2646,19 +2704,19 @@ struct Filler {
         while (it.next(&e)) {
             switch (e.kind) {
                 case EV_BEGIN:
-                    b.begin(ro(e.to));
+                    b.begin(ro(e.to), e.id_to);
                     break;
                 case EV_LINE:
-                    b.line_segment(ro(e.to), 0.0f, 1.0f);
+                    b.line_segment(ro(e.to), e.id_to, 0.0f, 1.0f);
                     break;
                 case EV_QUAD:
-                    b.quadratic_bezier_segment(ro(e.ctrl1), ro(e.to));
+                    b.quadratic_bezier_segment(ro(e.ctrl1), ro(e.to), e.id_to);
                     break;
                 case EV_CUBIC:
-                    b.cubic_bezier_segment(ro(e.ctrl1), ro(e.ctrl2), ro(e.to));
+                    b.cubic_bezier_segment(ro(e.ctrl1), ro(e.ctrl2), ro(e.to), e.id_to);
                     break;
                 case EV_END:
-                    b.end(ro(e.to));
+                    b.end(ro(e.to), e.id_to);
                     break;
             }
         }
@@ -2813,6 +2871,8 @@ void lyon_oracle_out_clear(lyon_oracle_out* o) {
     o->out.indices.clear();
     o->out.attributes.clear();
     o->out.sources.clear();
+    o->out.fill_sources.clear();
+    o->out.fill_source_counts.clear();
     o->near_ties = 0;
 }
 // Stroke vertex attributes (four words per vertex: normal x, normal y, advancement, side),
@@ -2830,6 +2890,17 @@ void lyon_oracle_out_set_sources(lyon_oracle_out* o, int enabled) {
 }
 const uint32_t* lyon_oracle_out_sources(const lyon_oracle_out* o) {
     return o->out.sources.data();
+}
+// After a fill with sources on: every vertex's sources (three words each, path-local ids) and
+// the number of sources of each vertex.
+uint64_t lyon_oracle_out_num_fill_sources(const lyon_oracle_out* o) {
+    return o->out.fill_sources.size() / 3;
+}
+const uint32_t* lyon_oracle_out_fill_sources(const lyon_oracle_out* o) {
+    return o->out.fill_sources.data();
+}
+const uint32_t* lyon_oracle_out_fill_source_counts(const lyon_oracle_out* o) {
+    return o->out.fill_source_counts.data();
 }
 uint64_t lyon_oracle_out_num_vertices(const lyon_oracle_out* o) { return o->out.vertices.size() / 2; }
 uint64_t lyon_oracle_out_num_indices(const lyon_oracle_out* o) { return o->out.indices.size(); }
@@ -3037,6 +3108,96 @@ int lyon_oracle_batch_stroke_sources(const lyon_path_batch* batch, const float* 
     return batch_impl(0, batch, widths, options, num_options, index_bits, num_threads,
                       vtx_counts, idx_counts, status, nullptr, vertices, indices, vtx_offsets,
                       idx_offsets, attributes, sources);
+}
+
+// Batched fill recording every vertex's sources. Counting call (outputs NULL): per-path vertex,
+// index and source counts and statuses. Output call: vertices, indices (per-path ids), sources
+// (three words each, ids indexing the batch's points) at the offsets of a counting call, and the
+// number of sources of every vertex (at the vertex offsets).
+int lyon_oracle_batch_fill_sources(const lyon_path_batch* batch, const void* options,
+                                   uint32_t num_options, int index_bits, int num_threads,
+                                   uint32_t* vtx_counts, uint32_t* idx_counts,
+                                   uint32_t* src_counts, int32_t* status, float* vertices,
+                                   uint32_t* indices, uint32_t* sources, uint32_t* source_counts,
+                                   const uint64_t* vtx_offsets, const uint64_t* idx_offsets,
+                                   const uint64_t* src_offsets) {
+    uint32_t n = batch->num_paths;
+    if (num_threads < 1) num_threads = 1;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        lyon_oracle_out o;
+        o.out.max_index = index_bits == 16 ? 65535ull : 0xFFFFFFFEull;
+        o.out.want_sources = true;
+        for (;;) {
+            uint32_t begin = next.fetch_add(64);
+            if (begin >= n) break;
+            uint32_t end = std::min(n, begin + 64);
+            for (uint32_t i = begin; i < end; ++i) {
+                lyon_oracle_out_clear(&o);
+                uint32_t v0 = batch->verb_offsets[i], v1 = batch->verb_offsets[i + 1];
+                uint32_t p0 = batch->point_offsets[i], p1 = batch->point_offsets[i + 1];
+                const lyon_fill_options* fo =
+                    (const lyon_fill_options*)options + (num_options > 1 ? i : 0);
+                int r = lyon_oracle_fill_path(&o, batch->verbs + v0, v1 - v0,
+                                              batch->points + 2 * (size_t)p0, p1 - p0, fo);
+                const uint32_t nv = (uint32_t)(o.out.vertices.size() / 2);
+                const size_t ns = o.out.fill_sources.size() / 3;
+                if (vtx_counts) vtx_counts[i] = nv;
+                if (idx_counts) idx_counts[i] = (uint32_t)o.out.indices.size();
+                if (src_counts) src_counts[i] = (uint32_t)ns;
+                if (status) status[i] = r;
+                if (vertices && vtx_offsets)
+                    std::memcpy(vertices + 2 * vtx_offsets[i], o.out.vertices.data(),
+                                o.out.vertices.size() * sizeof(float));
+                if (indices && idx_offsets)
+                    std::memcpy(indices + idx_offsets[i], o.out.indices.data(),
+                                o.out.indices.size() * sizeof(uint32_t));
+                if (source_counts && vtx_offsets)
+                    std::memcpy(source_counts + vtx_offsets[i], o.out.fill_source_counts.data(),
+                                nv * sizeof(uint32_t));
+                if (sources && src_offsets) {
+                    uint32_t* d = sources + 3 * src_offsets[i];
+                    for (size_t k = 0; k < ns; ++k) {
+                        const uint32_t* w = o.out.fill_sources.data() + 3 * k;
+                        d[3 * k] = w[0] + p0;
+                        d[3 * k + 1] = w[1] == NO_ENDPOINT ? NO_ENDPOINT : w[1] + p0;
+                        d[3 * k + 2] = w[2];
+                    }
+                }
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < num_threads; ++t) th.emplace_back(worker);
+    worker();
+    for (auto& t : th) t.join();
+    return LYON_OK;
+}
+
+// FillVertex::interpolated_attributes (fill.rs:2208-2286) for `n` vertices whose sources are
+// sources[offsets[v] .. offsets[v + 1]) (three words each): the first source's attributes
+// (the endpoint's, or a * (1 - t) + b * t), the next ones added in order, then a division by
+// the number of sources when there are several.
+void lyon_oracle_interpolate_fill(const uint32_t* sources, const uint64_t* offsets, uint64_t n,
+                                  const float* attrs, uint32_t na, float* out) {
+    for (uint64_t v = 0; v < n; ++v) {
+        float* o = out + v * na;
+        float div = 1.0f;
+        for (uint64_t k = offsets[v]; k < offsets[v + 1]; ++k) {
+            const uint32_t* s = sources + 3 * k;
+            float t;
+            std::memcpy(&t, &s[2], 4);
+            const float* a = attrs + (uint64_t)s[0] * na;
+            const float* b = s[1] == NO_ENDPOINT ? nullptr : attrs + (uint64_t)s[1] * na;
+            for (uint32_t i = 0; i < na; ++i) {
+                const float x = b ? a[i] * (1.0f - t) + b[i] * t : a[i];
+                o[i] = k == offsets[v] ? x : o[i] + x;
+            }
+            if (k != offsets[v]) div += 1.0f;
+        }
+        if (div > 1.0f)
+            for (uint32_t i = 0; i < na; ++i) o[i] /= div;
+    }
 }
 
 // StrokeVertex::interpolated_attributes (stroke.rs:2728-2747) for `n` vertex sources (three

@@ -85,6 +85,18 @@ def lib():
             L.lyon_oracle_interpolate.restype = None
             L.lyon_oracle_interpolate.argtypes = [c_p, ctypes.c_uint64, c_p, ctypes.c_uint32, c_p,
                                                   ctypes.c_int]
+            L.lyon_oracle_out_num_fill_sources.restype = ctypes.c_uint64
+            L.lyon_oracle_out_num_fill_sources.argtypes = [c_p]
+            L.lyon_oracle_out_fill_sources.restype = ctypes.POINTER(ctypes.c_uint32)
+            L.lyon_oracle_out_fill_sources.argtypes = [c_p]
+            L.lyon_oracle_out_fill_source_counts.restype = ctypes.POINTER(ctypes.c_uint32)
+            L.lyon_oracle_out_fill_source_counts.argtypes = [c_p]
+            L.lyon_oracle_batch_fill_sources.restype = ctypes.c_int
+            L.lyon_oracle_batch_fill_sources.argtypes = [c_p, c_p, ctypes.c_uint32, ctypes.c_int,
+                                                         ctypes.c_int] + [c_p] * 11
+            L.lyon_oracle_interpolate_fill.restype = None
+            L.lyon_oracle_interpolate_fill.argtypes = [c_p, c_p, ctypes.c_uint64, c_p,
+                                                       ctypes.c_uint32, c_p]
             L.lyon_oracle_batch.restype = ctypes.c_int
             L.lyon_oracle_batch.argtypes = [ctypes.c_int, c_p, c_p, ctypes.c_uint32, ctypes.c_int,
                                             ctypes.c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
@@ -155,12 +167,26 @@ class Output:
                                       shape=(nv * 4,)).copy().reshape(-1, 4) \
                 if nv else np.zeros((0, 4), np.uint32)
         src = None
+        res_fill = None
         if self.sources:
-            src = np.ctypeslib.as_array(self.L.lyon_oracle_out_sources(self.h),
-                                        shape=(nv * 3,)).copy().reshape(-1, 3) \
-                if nv else np.zeros((0, 3), np.uint32)
-        return Result(status, v.reshape(-1, 2), i, self.L.lyon_oracle_out_near_ties(self.h),
-                      self.index_bits, a, src)
+            nfs = self.L.lyon_oracle_out_num_fill_sources(self.h)
+            if nfs or self._filled:
+                fs = np.ctypeslib.as_array(self.L.lyon_oracle_out_fill_sources(self.h),
+                                           shape=(nfs * 3,)).copy().reshape(-1, 3) \
+                    if nfs else np.zeros((0, 3), np.uint32)
+                fc = np.ctypeslib.as_array(self.L.lyon_oracle_out_fill_source_counts(self.h),
+                                           shape=(nv,)).copy() if nv else np.zeros(0, np.uint32)
+                res_fill = (fs, fc)
+            else:
+                src = np.ctypeslib.as_array(self.L.lyon_oracle_out_sources(self.h),
+                                            shape=(nv * 3,)).copy().reshape(-1, 3) \
+                    if nv else np.zeros((0, 3), np.uint32)
+        r = Result(status, v.reshape(-1, 2), i, self.L.lyon_oracle_out_near_ties(self.h),
+                   self.index_bits, a, src)
+        if res_fill is not None:
+            # Fill sources: (S, 3) words and the number of sources of each vertex.
+            r.sources, r.source_counts = res_fill
+        return r
 
     def stroke(self, path, options, widths=None):
         """`widths`: one variable-line-width factor per point (StrokeOptions::
@@ -176,7 +202,10 @@ class Output:
         return self.L.lyon_oracle_stroke_path(self.h, _ptr(v), len(v), _ptr(p), len(p),
                                               ctypes.byref(o))
 
+    _filled = False
+
     def fill(self, path, options):
+        self._filled = True
         o = options.to_c()
         v = np.ascontiguousarray(path.verbs, dtype=np.uint8)
         p = np.ascontiguousarray(path.points, dtype=np.float32)
@@ -229,10 +258,88 @@ def fill_circle(center, radius, tolerance, index_bits: int = 32,
     return out.snapshot(st)
 
 
-def fill(path, options, index_bits: int = 32, vertex_offset: int = 0) -> Result:
-    out = Output(index_bits, vertex_offset)
+def fill(path, options, index_bits: int = 32, vertex_offset: int = 0,
+         sources: bool = False) -> Result:
+    """With `sources`, Result.sources holds every vertex's sources ((S, 3) words, path-local
+    ids) and Result.source_counts the number per vertex."""
+    out = Output(index_bits, vertex_offset, sources=sources)
     st = out.fill(path, options)
     return out.snapshot(st)
+
+
+def interpolate_fill_attributes(sources: np.ndarray, counts: np.ndarray,
+                                attributes: np.ndarray) -> np.ndarray:
+    """FillVertex::interpolated_attributes (crates/tessellation/src/fill.rs:2208-2286): the
+    first source's attributes (the endpoint's, or a * (1 - t) + b * t), the next sources' added
+    in order, divided by the number of sources when there are several; f32 throughout."""
+    src = np.ascontiguousarray(sources, np.uint32).reshape(-1, 3)
+    cnt = np.asarray(counts, np.int64)
+    attrs = np.asarray(attributes, np.float32)
+    attrs = attrs.reshape(len(attrs), -1)
+    vals = interpolate_attributes(src, attrs) if len(src) else np.zeros((0, attrs.shape[1]),
+                                                                           np.float32)
+    out = np.zeros((len(cnt), attrs.shape[1]), np.float32)
+    starts = np.concatenate([[0], np.cumsum(cnt)[:-1]]) if len(cnt) else np.zeros(0, np.int64)
+    kmax = int(cnt.max()) if len(cnt) else 0
+    acc = np.zeros_like(out)
+    for k in range(kmax):
+        has = cnt > k
+        idx = starts[has] + k
+        acc[has] = vals[idx] if k == 0 else (acc[has] + vals[idx]).astype(np.float32)
+    div = np.maximum(cnt, 1).astype(np.float32)[:, None]
+    out = np.where(cnt[:, None] > 1, (acc / div).astype(np.float32), acc)
+    return out.astype(np.float32)
+
+
+def interpolate_fill_attributes_c(sources: np.ndarray, counts: np.ndarray,
+                                  attributes: np.ndarray) -> np.ndarray:
+    """interpolate_fill_attributes in C (the CPU baseline's version)."""
+    src = np.ascontiguousarray(sources, np.uint32).reshape(-1, 3)
+    cnt = np.asarray(counts, np.uint64)
+    offs = np.zeros(len(cnt) + 1, np.uint64)
+    offs[1:] = np.cumsum(cnt, dtype=np.uint64)
+    attrs = np.ascontiguousarray(attributes, np.float32)
+    attrs = attrs.reshape(len(attrs), -1)
+    out = np.zeros((len(cnt), attrs.shape[1]), np.float32)
+    lib().lyon_oracle_interpolate_fill(_ptr(src), _ptr(offs), len(cnt), _ptr(attrs),
+                                       attrs.shape[1], _ptr(out))
+    return out
+
+
+def batch_fill_sources(pb, options_records: np.ndarray, index_bits: int = 32,
+                       num_threads: int = 1):
+    """Fills every path of a PathBatch with the oracle, recording each vertex's sources
+    ((S, 3) words, ids indexing the batch's points) and the number per vertex."""
+    L = lib()
+    n = pb.num_paths
+    cb = _CBatch(_ptr(pb.verbs), _ptr(pb.points), _ptr(pb.verb_offsets),
+                 _ptr(pb.point_offsets), n)
+    opts = np.ascontiguousarray(options_records)
+    vc = np.zeros(n, np.uint32)
+    ic = np.zeros(n, np.uint32)
+    sc = np.zeros(n, np.uint32)
+    st = np.zeros(n, np.int32)
+    L.lyon_oracle_batch_fill_sources(ctypes.byref(cb), _ptr(opts), len(opts), index_bits,
+                                     num_threads, _ptr(vc), _ptr(ic), _ptr(sc), _ptr(st), None,
+                                     None, None, None, None, None, None)
+    offs = []
+    for c in (vc, ic, sc):
+        o = np.zeros(n + 1, np.uint64)
+        o[1:] = np.cumsum(c, dtype=np.uint64)
+        offs.append(o)
+    vo, io, so = offs
+    verts = np.zeros((int(vo[-1]), 2), np.float32)
+    idx = np.zeros(int(io[-1]), np.uint32)
+    srcs = np.zeros((int(so[-1]), 3), np.uint32)
+    counts = np.zeros(int(vo[-1]), np.uint32)
+    t0 = time.perf_counter()
+    L.lyon_oracle_batch_fill_sources(ctypes.byref(cb), _ptr(opts), len(opts), index_bits,
+                                     num_threads, None, None, None, None, _ptr(verts), _ptr(idx),
+                                     _ptr(srcs), _ptr(counts), _ptr(vo), _ptr(io), _ptr(so))
+    return {"vtx_counts": vc, "idx_counts": ic, "src_counts": sc, "status": st,
+            "vertices": verts, "indices": idx, "sources": srcs, "source_counts": counts,
+            "vtx_offsets": vo, "idx_offsets": io, "src_offsets": so,
+            "output_pass_s": time.perf_counter() - t0}
 
 
 def flatten(path, tolerance: float):

@@ -113,3 +113,119 @@ def test_threaded_interpolation_matches():
     a = orc.interpolate_attributes(res["sources"], attrs)
     b = orc.interpolate_attributes_threads(res["sources"], attrs, 4)
     assert np.array_equal(a, b)
+
+
+# ---- fill: FillVertex::sources / interpolated_attributes (crates/tessellation/src/fill.rs) ----
+
+from lyon_gb300.options import FillOptions  # noqa: E402
+
+FILL_01 = (Path.from_arrays([Verb.BEGIN, Verb.LINE_TO, Verb.LINE_TO, Verb.CLOSE],
+                            [[0, 0], [1, 1], [0, 2], [0, 0]]),
+           np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [9, 9, 9]], np.float32))
+# Two closed squares crossing each other; ids a..d = 0..3, e..h = 5..8 (4 and 9 are the Close
+# points).
+FILL_02 = (Path.from_arrays([Verb.BEGIN, Verb.LINE_TO, Verb.LINE_TO, Verb.LINE_TO, Verb.CLOSE] * 2,
+                            [[1, 0], [2, 0], [2, 4], [1, 4], [1, 0],
+                             [0, 1], [0, 3], [3, 3], [3, 1], [0, 1]]),
+           np.array([[1, 0, 1], [2, 0, 1], [3, 0, 1], [4, 0, 1], [9, 9, 9],
+                     [0, 1, 2], [0, 2, 2], [0, 3, 2], [0, 4, 2], [9, 9, 9]], np.float32))
+# Two triangles meeting at (1, 1): ids 0-2 and 4-6.
+FILL_03 = (Path.from_arrays([Verb.BEGIN, Verb.LINE_TO, Verb.LINE_TO, Verb.CLOSE] * 2,
+                            [[0, 0], [2, 0], [1, 1], [0, 0], [0, 2], [2, 2], [1, 1], [0, 2]]),
+           np.array([[0], [0], [1], [9], [0], [0], [2], [9]], np.float32))
+
+
+def _fill_sources(path, attrs):
+    r = orc.fill(path, FillOptions(), 32, sources=True)
+    assert r.status == 0
+    att = orc.interpolate_fill_attributes(r.sources, r.source_counts, attrs)
+    starts = np.concatenate([[0], np.cumsum(r.source_counts)]).astype(np.int64)
+    per_vertex = [r.sources[starts[v]:starts[v + 1]] for v in range(len(r.vertices))]
+    return r, per_vertex, att
+
+
+def _on_edge(s, frm, to, d):
+    t = _t(s[2])
+    return (int(s[0]), int(s[1])) == (frm, to) and (abs(d - t) < 1e-5 or abs(1 - d - t) <= 1e-5)
+
+
+def check_fill_vertex_source_01(vertices, per_vertex, att):
+    # fill.rs:2680-2748
+    expect = {(0.0, 0.0): 0, (1.0, 1.0): 1, (0.0, 2.0): 2}
+    for v, srcs, a in zip(vertices, per_vertex, att):
+        e = expect[(float(v[0]), float(v[1]))]
+        for s in srcs:
+            assert int(s[1]) == orc.NO_ENDPOINT and int(s[0]) == e
+        assert np.array_equal(a, np.eye(3, dtype=np.float32)[e])
+
+
+def check_fill_vertex_source_02(vertices, per_vertex, att):
+    # fill.rs:2750-2905
+    a, b, c, d, e, f, g, h = 0, 1, 2, 3, 5, 6, 7, 8
+    ends = {(1, 0): a, (2, 0): b, (2, 4): c, (1, 4): d, (0, 1): e, (0, 3): f, (3, 3): g,
+            (3, 1): h}
+    edges = {(1, 1): [(h, e, 2 / 3), (d, a, 3 / 4)], (2, 1): [(h, e, 1 / 3), (b, c, 1 / 4)],
+             (1, 3): [(f, g, 1 / 3), (d, a, 1 / 4)], (2, 3): [(f, g, 2 / 3), (b, c, 3 / 4)]}
+    attrs = {(1, 0): [1, 0, 1], (2, 0): [2, 0, 1], (2, 4): [3, 0, 1], (1, 4): [4, 0, 1],
+             (0, 1): [0, 1, 2], (0, 3): [0, 2, 2], (3, 3): [0, 3, 2], (3, 1): [0, 4, 2],
+             (1, 1): [0.875, 1.0, 1.5], (2, 1): [1.125, 1.5, 1.5],
+             (1, 3): [1.625, 1.16666, 1.5], (2, 3): [1.375, 1.33333, 1.5]}
+    for v, srcs, at in zip(vertices, per_vertex, att):
+        key = (int(round(float(v[0]))), int(round(float(v[1]))))
+        assert np.allclose(v, key, atol=1e-5)
+        for s in srcs:
+            if key in ends:
+                assert int(s[1]) == orc.NO_ENDPOINT and int(s[0]) == ends[key]
+            else:
+                assert any(_on_edge(s, *cand) for cand in edges[key]), (key, s)
+        assert np.all(np.abs(at - np.array(attrs[key], np.float32)) < 1e-3), (key, at)
+
+
+def check_fill_vertex_source_03(vertices, per_vertex, att):
+    # fill.rs:2907-2981
+    for v, srcs, a in zip(vertices, per_vertex, att):
+        if np.allclose(v, (1.0, 1.0)):
+            assert np.array_equal(a, [1.5]) and len(srcs) == 2
+        else:
+            assert np.array_equal(a, [0.0]) and len(srcs) == 1
+
+
+def test_fill_vertex_source_01():
+    path, attrs = FILL_01
+    r, per_vertex, att = _fill_sources(path, attrs)
+    check_fill_vertex_source_01(r.vertices, per_vertex, att)
+
+
+def test_fill_vertex_source_02():
+    path, attrs = FILL_02
+    r, per_vertex, att = _fill_sources(path, attrs)
+    assert len(r.vertices) == 12
+    check_fill_vertex_source_02(r.vertices, per_vertex, att)
+
+
+def test_fill_vertex_source_03():
+    path, attrs = FILL_03
+    r, per_vertex, att = _fill_sources(path, attrs)
+    check_fill_vertex_source_03(r.vertices, per_vertex, att)
+
+
+def test_fill_sources_batch_and_c_interpolation():
+    # The batched oracle equals per-path calls (ids shifted to the batch), and the C
+    # interpolation equals the numpy one bit for bit.
+    batch, opts = workloads.glyph_fill(300, seed=9)
+    res = orc.batch_fill_sources(batch, opts, 32, 4)
+    for p in range(0, batch.num_paths, 37):
+        r = orc.fill(batch.path(p), FillOptions(
+            tolerance=float(opts[p if len(opts) > 1 else 0]["tolerance"]),
+            fill_rule=int(opts[p if len(opts) > 1 else 0]["fill_rule"])), 32, sources=True)
+        s0, s1 = int(res["src_offsets"][p]), int(res["src_offsets"][p + 1])
+        got = res["sources"][s0:s1].copy()
+        base = int(batch.point_offsets[p])
+        got[:, 0] -= base
+        edge = got[:, 1] != orc.NO_ENDPOINT
+        got[edge, 1] -= base
+        assert np.array_equal(got, r.sources)
+    attrs = np.random.default_rng(10).normal(size=(len(batch.points), 2)).astype(np.float32)
+    a = orc.interpolate_fill_attributes(res["sources"], res["source_counts"], attrs)
+    b = orc.interpolate_fill_attributes_c(res["sources"], res["source_counts"], attrs)
+    assert np.array_equal(a, b)

@@ -415,6 +415,34 @@ int lyon_gpu_flatten_counts(lyon_gpu_context* ctx, const lyon_path_batch* batch,
 int lyon_gpu_flatten_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch, float tolerance,
                            float** out_points, uint32_t** out_offsets, uint64_t* total_points);
 
+/* lyon_geom::Arc (crates/geom/src/arc.rs:21-28): an elliptic arc, angles in radians. 28 bytes. */
+typedef struct lyon_arc {
+    float center_x, center_y;
+    float radius_x, radius_y;
+    float start_angle, sweep_angle, x_rotation;
+} lyon_arc;
+
+/* Arcs that need more segments than this fail with LYON_ERR_UNSUPPORTED. */
+#define LYON_MAX_ARC_SEGMENTS 4194304u
+
+/* Output of lyon_gpu_flatten_arcs: device memory owned by the context (valid until its next
+ * call). Arc i's points are points[offsets[i] .. offsets[i + 1]): its start point (t = 0), then
+ * the end point of every segment with that segment's t1. */
+typedef struct lyon_gpu_arc_output {
+    const float* points;      /* 2 floats per point */
+    const float* t;           /* one per point */
+    const uint64_t* offsets;  /* num_arcs + 1 entries */
+    const int32_t* status;    /* per arc: LYON_OK or LYON_ERR_UNSUPPORTED */
+    uint64_t total_points;
+} lyon_gpu_arc_output;
+
+/* Arc::for_each_flattened_with_t (crates/geom/src/arc.rs:339-367, flattening_step :369-389) for
+ * `num_arcs` arcs in device memory, one tolerance for all. cos, sin and acos are evaluated in f64
+ * and rounded once (lyon's f32 libm results may differ in the last bit). Synchronises once to
+ * size the output. */
+int lyon_gpu_flatten_arcs(lyon_gpu_context* ctx, const lyon_arc* arcs, uint32_t num_arcs,
+                          float tolerance, lyon_gpu_arc_output* out);
+
 /* Batched stroke with HOST buffers (the end-to-end form of lyon_gpu_stroke_paths): the batch
  * and options live in host memory, outputs are written to host memory. The call processes the
  * paths in chunks, overlapping each chunk's host->device copy, kernels and device->host copy with

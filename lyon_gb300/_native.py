@@ -50,6 +50,11 @@ class CFillCustomOutput(ctypes.Structure):
                 ("attributes", c_p)]
 
 
+class CArcOutput(ctypes.Structure):
+    _fields_ = [("points", c_p), ("t", c_p), ("offsets", c_p), ("status", c_p),
+                ("total_points", u64)]
+
+
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
                 ("device_budget_bytes", u64)]
@@ -200,6 +205,8 @@ def load(build_if_missing: bool = True):
         L.lyon_gpu_fill_path_custom.argtypes = [c_p, c_p, u32, c_p, u32, c_p, u32, c_p,
                                                 ctypes.c_int, u32, c_p, ctypes.POINTER(c_p),
                                                 ctypes.POINTER(c_p), ctypes.POINTER(c_p)]
+        L.lyon_gpu_flatten_arcs.restype = ctypes.c_int
+        L.lyon_gpu_flatten_arcs.argtypes = [c_p, c_p, u32, ctypes.c_float, c_p]
         L.lyon_gpu_autotune_stroke.restype = ctypes.c_int
         L.lyon_gpu_autotune_stroke.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
                                                ctypes.POINTER(CStrokeTuning),
@@ -230,5 +237,5 @@ EXPORTED = [
     "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_stroke_paths_custom",
     "lyon_gpu_interpolate_attributes", "lyon_gpu_stroke_path_custom",
     "lyon_gpu_fill_paths_custom", "lyon_gpu_interpolate_fill_attributes",
-    "lyon_gpu_fill_path_custom",
+    "lyon_gpu_fill_path_custom", "lyon_gpu_flatten_arcs",
 ]

@@ -58,6 +58,8 @@ struct lyon_gpu_context {
     // fill sources: per-path counts and offsets (+ scan scratch), per-vertex first source
     DevBuf src_counts, src_offsets, src_scratch, out_source_offsets;
     uint64_t total_sources = 0;
+    // arc flattening
+    DevBuf arc_counts, arc_status, arc_offsets, arc_points, arc_t;
     DevBuf in_attrs;                    // single-path custom attributes (staged)
     HostBuf h_out_src, h_out_attrs, h_out_soff;
     // outputs of device-buffer batched calls
@@ -838,7 +840,8 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters,
                       &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs,
                       &ctx->src_counts, &ctx->src_offsets, &ctx->src_scratch,
-                      &ctx->out_source_offsets};
+                      &ctx->out_source_offsets, &ctx->arc_counts, &ctx->arc_status,
+                      &ctx->arc_offsets, &ctx->arc_points, &ctx->arc_t};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
     HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v,  &ctx->h_out_i,
@@ -1317,6 +1320,64 @@ int lyon_gpu_flatten_counts(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                    lg::launch_flatten(a, false, ctx->num_sms * 8, ctx->stream))
                ? LYON_OK
                : LYON_ERR_CUDA;
+}
+
+int lyon_gpu_flatten_arcs(lyon_gpu_context* ctx, const lyon_arc* arcs, uint32_t num_arcs,
+                          float tolerance, lyon_gpu_arc_output* out) {
+    if (!ctx || !out || (num_arcs && !arcs)) return LYON_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = num_arcs;
+    if (!ensure(ctx, ctx->arc_counts, (size_t)n * 4 + 16) ||
+        !ensure(ctx, ctx->arc_status, (size_t)n * 4 + 16) ||
+        !ensure(ctx, ctx->arc_offsets, ((size_t)n + 1) * 8 * 2 + 16) ||
+        !ensure(ctx, ctx->scan_state, 2 * lg::scan_tile_count(n) * 8 + 16) ||
+        !ensure(ctx, ctx->small, 64) || !ensure_host(ctx, ctx->h_small, 64))
+        return LYON_ERR_OUT_OF_MEMORY;
+    uint64_t* offs = as<uint64_t>(ctx->arc_offsets);
+    uint64_t total = 0;
+    if (n > 0) {
+        if (!set_err(ctx, "arcs count",
+                     lg::launch_arcs(arcs, n, tolerance, as<uint32_t>(ctx->arc_counts),
+                                     as<int32_t>(ctx->arc_status), nullptr, nullptr, nullptr,
+                                     ctx->num_sms, s)))
+            return LYON_ERR_CUDA;
+        uint32_t* sw = small_words(ctx);
+        cudaMemsetAsync(sw + 2, 0, 4, s);
+        if (!set_err(ctx, "scan",
+                     lg::launch_scan_pairs(as<uint32_t>(ctx->arc_counts),
+                                           as<uint32_t>(ctx->arc_counts), offs, offs + n + 1, n,
+                                           as<unsigned long long>(ctx->scan_state), sw + 1,
+                                           reinterpret_cast<int*>(sw + 2), s)))
+            return LYON_ERR_CUDA;
+        uint64_t* hs = reinterpret_cast<uint64_t*>(ctx->h_small.ptr);
+        cudaMemcpyAsync(hs, offs + n, 8, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hs + 1, sw + 2, 4, cudaMemcpyDeviceToHost, s);
+        if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return LYON_ERR_CUDA;
+        if (reinterpret_cast<uint32_t*>(hs + 1)[0] != 0) {
+            ctx->last_error = "scan look-back wait exceeded its bound";
+            return LYON_ERR_CUDA;
+        }
+        total = hs[0];
+    } else {
+        cudaMemsetAsync(offs, 0, 8, s);
+    }
+    if (!ensure(ctx, ctx->arc_points, total * 8 + 16) ||
+        !ensure(ctx, ctx->arc_t, total * 4 + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    if (n > 0 && total > 0 &&
+        !set_err(ctx, "arcs emit",
+                 lg::launch_arcs(arcs, n, tolerance, nullptr, as<int32_t>(ctx->arc_status), offs,
+                                 as<float>(ctx->arc_points), as<float>(ctx->arc_t), ctx->num_sms,
+                                 s)))
+        return LYON_ERR_CUDA;
+    out->points = as<float>(ctx->arc_points);
+    out->t = as<float>(ctx->arc_t);
+    out->offsets = offs;
+    out->status = as<int32_t>(ctx->arc_status);
+    out->total_points = total;
+    return LYON_OK;
 }
 
 int lyon_gpu_flatten_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch, float tolerance,

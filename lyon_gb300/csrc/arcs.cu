@@ -1,0 +1,115 @@
+// arcs.cu — batched flattening of elliptic arcs: lyon_geom's Arc::for_each_flattened_with_t
+// (crates/geom/src/arc.rs:339-367) with its adaptive flattening_step (:369-389).
+//
+// One thread per arc: each step depends on the remaining arc (the step is taken from the
+// radius at the arc's current start), so an arc is a sequential walk. The count kernel walks
+// without writing; the library's scan turns the counts into offsets; the emit kernel walks again
+// and writes every point (the start point first) and its t. cos, sin and acos are evaluated in
+// f64 and rounded once, as the oracle does.
+#include "kernels.h"
+
+namespace lg {
+namespace {
+
+__device__ __forceinline__ float dcos(float x) { return (float)cos((double)x); }
+__device__ __forceinline__ float dsin(float x) { return (float)sin((double)x); }
+__device__ __forceinline__ float dacos(float x) { return (float)acos((double)x); }
+
+struct ArcState {
+    float cx, cy, rx, ry, start, sweep, rot;
+};
+
+// sample (arc.rs:194-197): center + Rotation2D(x_rotation) applied to (rx cos a, ry sin a).
+__device__ __forceinline__ float2 arc_sample(const ArcState& a, float t) {
+    const float angle = a.start + a.sweep * t;
+    const float ex = a.rx * dcos(angle), ey = a.ry * dsin(angle);
+    const float c = dcos(a.rot), s = dsin(a.rot);
+    return make_float2(a.cx + (ex * c - ey * s), a.cy + (ex * s + ey * c));
+}
+
+__device__ __forceinline__ float arc_step(const ArcState& a, float tolerance) {
+    const float2 from = arc_sample(a, 0.0f);
+    const float dx = from.x - a.cx, dy = from.y - a.cy;
+    const float r = sqrtf(dx * dx + dy * dy);
+    const float ang = 2.0f * dacos((r - tolerance) / r);
+    const float result = fminf(ang / fabsf(a.sweep), 1.0f);
+    return result < 1.1920929e-7f ? 1.0f : result;  // f32::EPSILON
+}
+
+// Walks one arc; with `pts` it writes the points and t values. Returns the point count, or
+// ARC_TOO_LONG past the segment bound (the arc then fails with LYON_ERR_UNSUPPORTED).
+constexpr uint32_t ARC_TOO_LONG = 0xFFFFFFFFu;
+__device__ uint32_t walk_arc(const lyon_arc& in, float tolerance, float2* pts, float* ts) {
+    const ArcState arc{in.center_x, in.center_y, in.radius_x, in.radius_y,
+                       in.start_angle, in.sweep_angle, in.x_rotation};
+    ArcState it = arc;
+    float t0 = 0.0f;
+    uint32_t k = 0;
+    if (pts) {
+        pts[0] = arc_sample(arc, 0.0f);
+        ts[0] = 0.0f;
+    }
+    k = 1;
+    for (;;) {
+        const float step = arc_step(it, tolerance);
+        if (step >= 1.0f) break;
+        if (k > LYON_MAX_ARC_SEGMENTS) return ARC_TOO_LONG;
+        const float split = it.sweep * step;  // after_split (arc.rs:286-296)
+        it.start = it.start + split;
+        it.sweep = it.sweep - split;
+        const float t1 = t0 + step * (1.0f - t0);
+        if (pts) {
+            pts[k] = arc_sample(it, 0.0f);
+            ts[k] = t1;
+        }
+        ++k;
+        t0 = t1;
+    }
+    if (pts) {
+        pts[k] = arc_sample(arc, 1.0f);
+        ts[k] = 1.0f;
+    }
+    return k + 1;
+}
+
+__global__ void __launch_bounds__(256) arcs_count_kernel(const lyon_arc* arcs, uint32_t n,
+                                                         float tolerance, uint32_t* counts,
+                                                         int32_t* status) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = walk_arc(arcs[i], tolerance, nullptr, nullptr);
+        counts[i] = k == ARC_TOO_LONG ? 0u : k;
+        status[i] = k == ARC_TOO_LONG ? LYON_ERR_UNSUPPORTED : LYON_OK;
+    }
+}
+
+__global__ void __launch_bounds__(256) arcs_emit_kernel(const lyon_arc* arcs, uint32_t n,
+                                                        float tolerance, const int32_t* status,
+                                                        const uint64_t* offsets, float2* pts,
+                                                        float* ts) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (status[i] != LYON_OK) continue;
+        const uint64_t o = offsets[i];
+        walk_arc(arcs[i], tolerance, pts + o, ts + o);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_arcs(const lyon_arc* arcs, uint32_t n, float tolerance, uint32_t* counts,
+                        int32_t* status, const uint64_t* offsets, float* pts, float* ts,
+                        int num_sms, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t need = (n + 255) / 256;
+    const uint32_t cap = (uint32_t)(num_sms > 0 ? num_sms : 1) * 8;
+    const uint32_t grid = need < cap ? need : cap;
+    if (pts) {
+        arcs_emit_kernel<<<grid, 256, 0, stream>>>(arcs, n, tolerance, status, offsets,
+                                                   reinterpret_cast<float2*>(pts), ts);
+    } else {
+        arcs_count_kernel<<<grid, 256, 0, stream>>>(arcs, n, tolerance, counts, status);
+    }
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+}  // namespace lg

@@ -94,6 +94,11 @@ cudaError_t launch_interpolate_fill(const lyon_vertex_source* sources,
                                     uint64_t num_endpoints, float* out, int num_sms,
                                     cudaStream_t stream);
 
+// Arc flattening (arcs.cu): count pass (pts null: counts and status) or emit pass.
+cudaError_t launch_arcs(const lyon_arc* arcs, uint32_t n, float tolerance, uint32_t* counts,
+                        int32_t* status, const uint64_t* offsets, float* pts, float* ts,
+                        int num_sms, cudaStream_t stream);
+
 // Exclusive scan of two u32 arrays into two u64 arrays (decoupled look-back), plus totals at
 // out_a[n] / out_b[n]. `tile_state` holds 2 * num_tiles(n) u64 and `counter` one u32; both are
 // reset by the call. `error` receives 1 if a look-back wait exceeded its bound.

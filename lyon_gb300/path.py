@@ -8,11 +8,69 @@ the input layout of the batched C ABI (`lyon_path_batch` in include/lyon_gpu.h).
 
 from __future__ import annotations
 
+import ctypes
+import ctypes.util
 import math
 from dataclasses import dataclass
 from typing import Iterable, List, Sequence, Tuple
 
 import numpy as np
+
+# lyon takes f32 cos/sin/tan from the platform's libm; the builder's ellipses do the same.
+_libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+for _name in ("cosf", "sinf", "tanf"):
+    getattr(_libm, _name).restype = ctypes.c_float
+    getattr(_libm, _name).argtypes = [ctypes.c_float]
+_F = np.float32
+
+
+def _cosf(x) -> np.float32:
+    return _F(_libm.cosf(float(x)))
+
+
+def _sinf(x) -> np.float32:
+    return _F(_libm.sinf(float(x)))
+
+
+def _rotate(angle, x, y):
+    """euclid's Rotation2D::transform_point / transform_vector, in f32."""
+    c, s = _cosf(angle), _sinf(angle)
+    return _F(x * c - y * s), _F(x * s + y * c)
+
+
+def arc_quadratic_beziers(center, radii, start_angle, sweep_angle, x_rotation):
+    """arc_to_quadratic_beziers_with_t (crates/geom/src/arc.rs:668-703), f32 arithmetic: the
+    arc split into ceil(|sweep| / (pi/4)) equal steps, each one quadratic whose control point is
+    on the tangent at its start (Maisonobe). Returns [(from, ctrl, to, t0, t1), ...]."""
+    cx, cy = _F(center[0]), _F(center[1])
+    rx, ry = _F(radii[0]), _F(radii[1])
+    start, sweep, rot = _F(start_angle), _F(sweep_angle), _F(x_rotation)
+    sign = _F(math.copysign(1.0, float(sweep))) if not math.isnan(float(sweep)) else _F(np.nan)
+    two_pi = _F(np.pi) * _F(2.0)
+    sw = min(_F(abs(sweep)), two_pi)
+    n_steps = _F(np.ceil(sw / _F(np.pi / 4)))
+    step = _F(sw / n_steps * sign)
+    dt = _F(_F(1.0) / n_steps)
+    alpha = _F(_libm.tanf(float(step * _F(0.5))))
+    n = int(n_steps)
+    out = []
+    t0 = _F(0.0)
+
+    def sample(a):
+        ex, ey = _F(rx * _cosf(a)), _F(ry * _sinf(a))
+        vx, vy = _rotate(rot, ex, ey)
+        return _F(cx + vx), _F(cy + vy)
+    for i in range(n):
+        a1 = _F(start + _F(step * _F(i)))
+        a2 = _F(start + _F(step * _F(i + 1)))
+        frm = sample(a1)
+        to = sample(a2)
+        tx, ty = _rotate(rot, _F(-rx * _sinf(a1)), _F(ry * _cosf(a1)))
+        ctrl = (_F(frm[0] + _F(tx * alpha)), _F(frm[1] + _F(ty * alpha)))
+        t1 = _F(1.0) if i + 1 == n else _F(t0 + dt)
+        out.append((frm, ctrl, to, t0, t1))
+        t0 = t1
+    return out
 
 
 class Verb:
@@ -189,6 +247,20 @@ class PathBuilder:
         self.cubic_bezier_to(at(r, d * d_dir), at(d, r * d_dir), at(f(0.0), r * d_dir))
         self.cubic_bezier_to(at(-d, r * d_dir), at(-r, d * d_dir), at(-r, f(0.0)))
         self.close()
+
+    def add_ellipse(self, center, radii, x_rotation: float = 0.0, winding: int = 1) -> None:
+        """builder.rs:606-636: the full arc (start 0, sweep 2 pi in the winding's direction)
+        as quadratic béziers, closed."""
+        sweep = _F(_F(2.0) * _F(np.pi)) * (_F(1.0) if winding >= 0 else _F(-1.0))
+        quads = arc_quadratic_beziers(center, radii, 0.0, sweep, x_rotation)
+        # Arc::sample(0.0): the start angle is 0.
+        cx, cy = _F(center[0]), _F(center[1])
+        ex, ey = _F(_F(radii[0]) * _cosf(_F(0.0))), _F(_F(radii[1]) * _sinf(_F(0.0)))
+        vx, vy = _rotate(_F(x_rotation), ex, ey)
+        self.begin((_F(cx + vx), _F(cy + vy)))
+        for _frm, ctrl, to, _t0, _t1 in quads:
+            self.quadratic_bezier_to(ctrl, to)
+        self.end(True)
 
     def add_rounded_rectangle(self, rect, radii, winding: int = 1) -> None:
         """builder.rs:1551-1660; radii = (top_left, top_right, bottom_left, bottom_right)."""

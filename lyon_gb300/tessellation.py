@@ -366,6 +366,42 @@ def fill_shapes(kind: int, params_dev, num_shapes: int, options_dev=None, num_op
 SHAPE_RECTANGLE = 0
 SHAPE_CIRCLE = 1
 
+# lyon_arc (lyon_geom::Arc, crates/geom/src/arc.rs:21-28), angles in radians.
+ARC_DTYPE = np.dtype([("center_x", "<f4"), ("center_y", "<f4"), ("radius_x", "<f4"),
+                      ("radius_y", "<f4"), ("start_angle", "<f4"), ("sweep_angle", "<f4"),
+                      ("x_rotation", "<f4")])
+
+
+@dataclass
+class ArcFlattening:
+    """Device tensors of lyon_gpu_flatten_arcs (owned by the context until its next call):
+    arc i's points are points[offsets[i]:offsets[i + 1]] (its start point first)."""
+    points: object   # (P, 2) f32
+    t: object        # (P,) f32
+    offsets: object  # (n + 1,) int64
+    status: object   # (n,) int32
+    total_points: int
+
+
+def flatten_arcs(arcs_dev, num_arcs: int, tolerance: float,
+                 ctx: Optional[Context] = None) -> ArcFlattening:
+    """Arc::for_each_flattened_with_t (crates/geom/src/arc.rs:339-367) for `num_arcs` arcs in
+    a device tensor of ARC_DTYPE records (7 f32 each)."""
+    import torch
+    ctx = ctx or Context.default()
+    out = _native.CArcOutput()
+    r = ctx.lib.lyon_gpu_flatten_arcs(ctx.h, arcs_dev.data_ptr() if num_arcs else None,
+                                      num_arcs, tolerance, ctypes.byref(out))
+    if r != LYON_OK:
+        raise TessellationError(r, ctx.last_error())
+    tp = int(out.total_points)
+
+    def dev(ptr, shape, ts):
+        return torch.as_tensor(_CudaArray(int(ptr or 0), shape, ts), device="cuda")
+    return ArcFlattening(dev(out.points, (tp, 2), "<f4"), dev(out.t, (tp,), "<f4"),
+                         dev(out.offsets, (num_arcs + 1,), "<i8"),
+                         dev(out.status, (num_arcs,), "<i4"), tp)
+
 
 class StrokeTessellator:
     """lyon's StrokeTessellator (fixed line width, `Positions` vertices)."""
@@ -389,6 +425,13 @@ class StrokeTessellator:
             # stroke.rs:127-131: a variable width needs the attributes to read it from.
             raise ValueError("variable line width requires custom attributes")
         _single("stroke", self.ctx, path, options, builder, widths)
+
+    def tessellate_ellipse(self, center, radii, x_rotation: float, winding: int,
+                           options: StrokeOptions, builder: BuffersBuilder) -> None:
+        """stroke.rs:294-307: the path builder's ellipse (quadratic arcs), stroked."""
+        b = PathBuilder()
+        b.add_ellipse(center, radii, x_rotation, winding)
+        self.tessellate_path(b.build(), options, builder)
 
     def tessellate_polygon(self, points, closed: bool, options: StrokeOptions,
                            builder: BuffersBuilder) -> None:
@@ -418,6 +461,13 @@ class FillTessellator:
 
     def __init__(self, ctx: Optional[Context] = None):
         self.ctx = ctx or Context.default()
+
+    def tessellate_ellipse(self, center, radii, x_rotation: float, winding: int,
+                           options: FillOptions, builder: BuffersBuilder) -> None:
+        """fill.rs:675-690: the path builder's ellipse, filled without intersection handling."""
+        b = PathBuilder()
+        b.add_ellipse(center, radii, x_rotation, winding)
+        self.tessellate_path(b.build(), options.with_intersections(False), builder)
 
     def tessellate_polygon(self, points, closed: bool, options: FillOptions,
                            builder: BuffersBuilder) -> None:

@@ -2842,6 +2842,70 @@ static int fill_circle(Output* out, P center, float radius, float tolerance) {
     return LYON_OK;
 }
 
+// --------------------------------------------------------------------------------------------
+// Elliptic arcs (crates/geom/src/arc.rs). cos/sin/acos are evaluated in f64 and rounded once, as
+// on the GPU; lyon takes them from the platform's f32 libm, which may differ in the last bit.
+// --------------------------------------------------------------------------------------------
+struct ArcF {  // arc.rs:21-28
+    P center, radii;
+    float start_angle, sweep_angle, x_rotation;
+};
+
+// sample (arc.rs:194-197) = center + sample_ellipse(radii, x_rotation, get_angle(t))
+// (arc.rs:217-219, 741-746; euclid's Rotation2D::transform_point).
+static P arc_sample(const ArcF& a, float t) {
+    const float angle = a.start_angle + a.sweep_angle * t;
+    const float ex = a.radii.x * cr_cos(angle), ey = a.radii.y * cr_sin(angle);
+    const float c = cr_cos(a.x_rotation), s = cr_sin(a.x_rotation);
+    return P{a.center.x + (ex * c - ey * s), a.center.y + (ex * s + ey * c)};
+}
+
+// flattening_step (arc.rs:369-389).
+static float arc_flattening_step(const ArcF& a, float tolerance) {
+    const P from = arc_sample(a, 0.0f);
+    const float r = length(sub(from, a.center));
+    const float ang = 2.0f * cr_acos((r - tolerance) / r);
+    const float result = fminf(ang / fabsf(a.sweep_angle), 1.0f);
+    if (result < 1.1920929e-7f) return 1.0f;  // f32::EPSILON
+    return result;
+}
+
+// Arcs with more segments than this fail with LYON_ERR_UNSUPPORTED (the GPU's bound).
+static const uint64_t MAX_ARC_SEGMENTS = 1ull << 22;
+
+// for_each_flattened_with_t (arc.rs:339-367): the start point (t = 0), then every segment's end
+// point and t1. `pts`/`ts` may be NULL (counting). Returns the number of points or
+// UINT64_MAX when the arc needs more than MAX_ARC_SEGMENTS segments.
+static uint64_t arc_flatten(const ArcF& arc, float tolerance, float* pts, float* ts) {
+    ArcF iter = arc;
+    float t0 = 0.0f;
+    P from = arc_sample(arc, 0.0f);
+    uint64_t k = 0;
+    auto put = [&](P p, float t) {
+        if (pts) {
+            pts[2 * k] = p.x;
+            pts[2 * k + 1] = p.y;
+        }
+        if (ts) ts[k] = t;
+        ++k;
+    };
+    put(from, 0.0f);
+    for (;;) {
+        const float step = arc_flattening_step(iter, tolerance);
+        if (step >= 1.0f) break;
+        if (k > MAX_ARC_SEGMENTS) return UINT64_MAX;
+        // after_split (arc.rs:286-296)
+        const float split_angle = iter.sweep_angle * step;
+        iter.start_angle = iter.start_angle + split_angle;
+        iter.sweep_angle = iter.sweep_angle - split_angle;
+        const float t1 = t0 + step * (1.0f - t0);
+        put(arc_sample(iter, 0.0f), t1);
+        t0 = t1;
+    }
+    put(arc_sample(arc, 1.0f), 1.0f);
+    return k;
+}
+
 }  // namespace lo
 
 // ============================================================================================
@@ -2933,6 +2997,25 @@ int lyon_oracle_stroke_path_vw(lyon_oracle_out* o, const uint8_t* verbs, uint32_
     int r = s.tessellate(it);
     o->near_ties += g_near_ties;
     return r;
+}
+
+// Arc::for_each_flattened_with_t for `n` arcs of 7 floats (center x, y, radii x, y, start angle,
+// sweep angle, x rotation). Counting call (pts NULL): counts[i] = points of arc i (start point
+// included) and status. Output call: points and t at `offsets`.
+void lyon_oracle_flatten_arcs(const float* arcs, uint32_t n, float tolerance, uint32_t* counts,
+                              int32_t* status, const uint64_t* offsets, float* pts, float* ts) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* a = arcs + 7 * (size_t)i;
+        ArcF arc{P{a[0], a[1]}, P{a[2], a[3]}, a[4], a[5], a[6]};
+        uint64_t k;
+        if (pts && offsets) {
+            k = arc_flatten(arc, tolerance, pts + 2 * offsets[i], ts ? ts + offsets[i] : nullptr);
+        } else {
+            k = arc_flatten(arc, tolerance, nullptr, nullptr);
+        }
+        if (counts) counts[i] = k == UINT64_MAX ? 0u : (uint32_t)k;
+        if (status) status[i] = k == UINT64_MAX ? LYON_ERR_UNSUPPORTED : LYON_OK;
+    }
 }
 
 // FillTessellator::tessellate_rectangle / tessellate_circle appending to the output.

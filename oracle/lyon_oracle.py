@@ -97,6 +97,9 @@ def lib():
             L.lyon_oracle_interpolate_fill.restype = None
             L.lyon_oracle_interpolate_fill.argtypes = [c_p, c_p, ctypes.c_uint64, c_p,
                                                        ctypes.c_uint32, c_p]
+            L.lyon_oracle_flatten_arcs.restype = None
+            L.lyon_oracle_flatten_arcs.argtypes = [c_p, ctypes.c_uint32, ctypes.c_float, c_p,
+                                                   c_p, c_p, c_p, c_p]
             L.lyon_oracle_batch.restype = ctypes.c_int
             L.lyon_oracle_batch.argtypes = [ctypes.c_int, c_p, c_p, ctypes.c_uint32, ctypes.c_int,
                                             ctypes.c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
@@ -480,3 +483,27 @@ def batch(kind: str, pb, options_records: np.ndarray, index_bits: int = 32,
                                                   num_threads, _ptr(vo), _ptr(attrs))
             res["attributes"] = attrs
     return res
+
+
+ARC_DTYPE = np.dtype([("center_x", "<f4"), ("center_y", "<f4"), ("radius_x", "<f4"),
+                      ("radius_y", "<f4"), ("start_angle", "<f4"), ("sweep_angle", "<f4"),
+                      ("x_rotation", "<f4")])
+
+
+def flatten_arcs(arcs: np.ndarray, tolerance: float):
+    """Arc::for_each_flattened_with_t (crates/geom/src/arc.rs:339-367) for every arc (an
+    ARC_DTYPE array): (points (P, 2), t (P,), offsets (n + 1,), status (n,)); each arc's points
+    start with its start point."""
+    L = lib()
+    a = np.ascontiguousarray(arcs).view(np.float32).reshape(-1, 7)
+    n = len(a)
+    counts = np.zeros(n, np.uint32)
+    st = np.zeros(n, np.int32)
+    L.lyon_oracle_flatten_arcs(_ptr(a), n, tolerance, _ptr(counts), _ptr(st), None, None, None)
+    offs = np.zeros(n + 1, np.uint64)
+    offs[1:] = np.cumsum(counts, dtype=np.uint64)
+    pts = np.zeros((int(offs[-1]), 2), np.float32)
+    ts = np.zeros(int(offs[-1]), np.float32)
+    L.lyon_oracle_flatten_arcs(_ptr(a), n, tolerance, None, None, _ptr(offs), _ptr(pts),
+                               _ptr(ts))
+    return pts, ts, offs, st

@@ -443,6 +443,60 @@ typedef struct lyon_gpu_arc_output {
 int lyon_gpu_flatten_arcs(lyon_gpu_context* ctx, const lyon_arc* arcs, uint32_t num_arcs,
                           float tolerance, lyon_gpu_arc_output* out);
 
+/* ---- Hatching and dots (lyon_algorithms::hatching, crates/algorithms/src/hatching.rs) ------- */
+
+/* HatchingOptions / DotOptions (hatching.rs:44-179) with the regular patterns' intervals
+ * (RegularHatchingPattern::interval, RegularDotPattern::row_interval / column_interval,
+ * hatching.rs:640-675). */
+typedef struct lyon_hatching_options {
+    float tolerance;
+    float angle;             /* radians */
+    float uv_origin_x, uv_origin_y;
+    float interval;          /* distance between rows (hatches), row_interval (dots) */
+    float column_interval;   /* dots: distance between dots in a row */
+    int32_t compute_tangents;  /* hatches only */
+} lyon_hatching_options;
+
+/* HatchSegment (hatching.rs:181-205): endpoints a (left) and b (right) with the outline's
+ * tangent there (NaN when tangents are not computed) and their u; row index and v. 48 bytes. */
+typedef struct lyon_hatch_segment {
+    float a_x, a_y, a_tangent_x, a_tangent_y, a_u;
+    float b_x, b_y, b_tangent_x, b_tangent_y, b_u;
+    uint32_t row;
+    float v;
+} lyon_hatch_segment;
+
+/* Dot (hatching.rs:216-227). 24 bytes. */
+typedef struct lyon_dot {
+    float x, y, u, v;
+    uint32_t column, row;
+} lyon_dot;
+
+/* A path needing more rows than this, or more dots, fails with LYON_ERR_UNSUPPORTED (lyon keeps
+ * looping, e.g. when the interval is too small to move the scan line). */
+#define LYON_MAX_HATCH_ROWS 16777216u
+#define LYON_MAX_HATCH_DOTS 67108864u
+
+/* Output of lyon_gpu_hatch_paths / lyon_gpu_dot_paths, device memory owned by the context
+ * (valid until its next call). Path i's records are [offsets[i], offsets[i + 1]). */
+typedef struct lyon_gpu_hatch_output {
+    const lyon_hatch_segment* segments;  /* hatches */
+    const lyon_dot* dots;                /* dots */
+    const uint64_t* offsets;             /* num_paths + 1 */
+    const int32_t* status;               /* per path */
+    uint64_t total;
+} lyon_gpu_hatch_output;
+
+/* Hatcher::hatch_path with a RegularHatchingPattern (hatching.rs:276-347, 374-428, 464-577)
+ * for every path of `batch` (device memory), `options` in host memory. A path without edges
+ * produces nothing (lyon panics on it). */
+int lyon_gpu_hatch_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                         const lyon_hatching_options* options, lyon_gpu_hatch_output* out);
+
+/* Hatcher::dot_path with a RegularDotPattern (hatching.rs:286-298, 349-372, 671-722). */
+int lyon_gpu_dot_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                       const lyon_hatching_options* options, lyon_gpu_hatch_output* out);
+
 /* Batched stroke with HOST buffers (the end-to-end form of lyon_gpu_stroke_paths): the batch
  * and options live in host memory, outputs are written to host memory. The call processes the
  * paths in chunks, overlapping each chunk's host->device copy, kernels and device->host copy with

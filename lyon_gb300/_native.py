@@ -55,6 +55,18 @@ class CArcOutput(ctypes.Structure):
                 ("total_points", u64)]
 
 
+class CHatchingOptions(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_float), ("angle", ctypes.c_float),
+                ("uv_origin_x", ctypes.c_float), ("uv_origin_y", ctypes.c_float),
+                ("interval", ctypes.c_float), ("column_interval", ctypes.c_float),
+                ("compute_tangents", i32)]
+
+
+class CHatchOutput(ctypes.Structure):
+    _fields_ = [("segments", c_p), ("dots", c_p), ("offsets", c_p), ("status", c_p),
+                ("total", u64)]
+
+
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
                 ("device_budget_bytes", u64)]
@@ -207,6 +219,9 @@ def load(build_if_missing: bool = True):
                                                 ctypes.POINTER(c_p), ctypes.POINTER(c_p)]
         L.lyon_gpu_flatten_arcs.restype = ctypes.c_int
         L.lyon_gpu_flatten_arcs.argtypes = [c_p, c_p, u32, ctypes.c_float, c_p]
+        for _fn in ("lyon_gpu_hatch_paths", "lyon_gpu_dot_paths"):
+            getattr(L, _fn).restype = ctypes.c_int
+            getattr(L, _fn).argtypes = [c_p, c_p, c_p, c_p]
         L.lyon_gpu_autotune_stroke.restype = ctypes.c_int
         L.lyon_gpu_autotune_stroke.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
                                                ctypes.POINTER(CStrokeTuning),
@@ -237,5 +252,6 @@ EXPORTED = [
     "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_stroke_paths_custom",
     "lyon_gpu_interpolate_attributes", "lyon_gpu_stroke_path_custom",
     "lyon_gpu_fill_paths_custom", "lyon_gpu_interpolate_fill_attributes",
-    "lyon_gpu_fill_path_custom", "lyon_gpu_flatten_arcs",
+    "lyon_gpu_fill_path_custom", "lyon_gpu_flatten_arcs", "lyon_gpu_hatch_paths",
+    "lyon_gpu_dot_paths",
 ]

@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "liblyon_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
-SOURCES = ["stroke.cu", "stroke_seq.cu", "attributes.cu", "arcs.cu", "scan.cu", "flatten.cu", "fill.cu", "api.cu", "noalloc.cu", "serve.cu",
+SOURCES = ["stroke.cu", "stroke_seq.cu", "attributes.cu", "arcs.cu", "hatch.cu", "scan.cu", "flatten.cu", "fill.cu", "api.cu", "noalloc.cu", "serve.cu",
            "shapes.cu", "svg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-prec-div=true",

@@ -60,6 +60,9 @@ struct lyon_gpu_context {
     uint64_t total_sources = 0;
     // arc flattening
     DevBuf arc_counts, arc_status, arc_offsets, arc_points, arc_t;
+    // hatching
+    DevBuf hatch_bound, hatch_edge_count, hatch_counts, hatch_status, hatch_offsets,
+        hatch_scratch, hatch_out;
     DevBuf in_attrs;                    // single-path custom attributes (staged)
     HostBuf h_out_src, h_out_attrs, h_out_soff;
     // outputs of device-buffer batched calls
@@ -841,7 +844,9 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs,
                       &ctx->src_counts, &ctx->src_offsets, &ctx->src_scratch,
                       &ctx->out_source_offsets, &ctx->arc_counts, &ctx->arc_status,
-                      &ctx->arc_offsets, &ctx->arc_points, &ctx->arc_t};
+                      &ctx->arc_offsets, &ctx->arc_points, &ctx->arc_t, &ctx->hatch_bound,
+                      &ctx->hatch_edge_count, &ctx->hatch_counts, &ctx->hatch_status,
+                      &ctx->hatch_offsets, &ctx->hatch_scratch, &ctx->hatch_out};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
     HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v,  &ctx->h_out_i,
@@ -1320,6 +1325,119 @@ int lyon_gpu_flatten_counts(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                    lg::launch_flatten(a, false, ctx->num_sms * 8, ctx->stream))
                ? LYON_OK
                : LYON_ERR_CUDA;
+}
+
+namespace {
+
+// Exclusive scan of n u32 counts into n + 1 u64 offsets (the second scan output is scratch);
+// returns the total through *total (one synchronisation).
+int scan_counts(lyon_gpu_context* ctx, const uint32_t* counts, uint64_t* offsets,
+                uint64_t* scratch, uint32_t n, uint64_t* total) {
+    cudaStream_t s = ctx->stream;
+    *total = 0;
+    if (!ensure(ctx, ctx->scan_state, 2 * lg::scan_tile_count(n) * 8 + 16) ||
+        !ensure(ctx, ctx->small, 64) || !ensure_host(ctx, ctx->h_small, 64))
+        return LYON_ERR_OUT_OF_MEMORY;
+    if (n == 0) {
+        cudaMemsetAsync(offsets, 0, 8, s);
+        return LYON_OK;
+    }
+    uint32_t* sw = small_words(ctx);
+    cudaMemsetAsync(sw + 2, 0, 4, s);
+    if (!set_err(ctx, "scan",
+                 lg::launch_scan_pairs(counts, counts, offsets, scratch, n,
+                                       as<unsigned long long>(ctx->scan_state), sw + 1,
+                                       reinterpret_cast<int*>(sw + 2), s)))
+        return LYON_ERR_CUDA;
+    uint64_t* hs = reinterpret_cast<uint64_t*>(ctx->h_small.ptr);
+    cudaMemcpyAsync(hs, offsets + n, 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hs + 1, sw + 2, 4, cudaMemcpyDeviceToHost, s);
+    if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return LYON_ERR_CUDA;
+    if (reinterpret_cast<uint32_t*>(hs + 1)[0] != 0) {
+        ctx->last_error = "scan look-back wait exceeded its bound";
+        return LYON_ERR_CUDA;
+    }
+    *total = hs[0];
+    return LYON_OK;
+}
+
+int hatch_impl(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+               const lyon_hatching_options* o, bool dots, lyon_gpu_hatch_output* out) {
+    if (!ctx || !batch || !o || !out) return LYON_ERR_INVALID_ARGUMENT;
+    memset(out, 0, sizeof(*out));
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = batch->num_paths;
+    lg::HatchArgs a;
+    memset(&a, 0, sizeof a);
+    a.verbs = batch->verbs;
+    a.points = batch->points;
+    a.verb_offsets = batch->verb_offsets;
+    a.point_offsets = batch->point_offsets;
+    a.num_paths = n;
+    a.tolerance = o->tolerance;
+    // Rotation::new(angle) and Rotation::new(-angle) (euclid: f32 cos and sin).
+    a.c = cosf(o->angle);
+    a.s = sinf(o->angle);
+    a.ci = cosf(-o->angle);
+    a.si = sinf(-o->angle);
+    a.uv_x = o->uv_origin_x;
+    a.uv_y = o->uv_origin_y;
+    a.interval = o->interval;
+    a.column_interval = o->column_interval;
+    a.compute_tangents = dots ? 0 : (o->compute_tangents != 0);
+    a.dots = dots ? 1 : 0;
+    if (!ensure(ctx, ctx->hatch_bound, (size_t)n * 4 + 16) ||
+        !ensure(ctx, ctx->hatch_edge_count, (size_t)n * 4 + 16) ||
+        !ensure(ctx, ctx->hatch_counts, (size_t)n * 4 + 16) ||
+        !ensure(ctx, ctx->hatch_status, (size_t)n * 4 + 16) ||
+        !ensure(ctx, ctx->hatch_offsets, ((size_t)n + 1) * 8 * 3 + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    a.edge_bound = as<uint32_t>(ctx->hatch_bound);
+    a.edge_count = as<uint32_t>(ctx->hatch_edge_count);
+    a.counts = as<uint32_t>(ctx->hatch_counts);
+    a.status = as<int32_t>(ctx->hatch_status);
+    uint64_t* scr_off = as<uint64_t>(ctx->hatch_offsets);
+    uint64_t* out_off = scr_off + n + 1;
+    uint64_t* tmp_off = out_off + n + 1;
+    if (!set_err(ctx, "hatch bound", lg::launch_hatch(a, 0, ctx->num_sms, s)))
+        return LYON_ERR_CUDA;
+    uint64_t edges = 0, total = 0;
+    int r = scan_counts(ctx, a.edge_bound, scr_off, tmp_off, n, &edges);
+    if (r != LYON_OK) return r;
+    if (!ensure(ctx, ctx->hatch_scratch, edges * 16 * 3 + 16)) return LYON_ERR_OUT_OF_MEMORY;
+    a.scratch_offsets = scr_off;
+    a.scratch_total = edges;
+    a.scratch = ctx->hatch_scratch.ptr;
+    if (!set_err(ctx, "hatch count", lg::launch_hatch(a, 1, ctx->num_sms, s)))
+        return LYON_ERR_CUDA;
+    r = scan_counts(ctx, a.counts, out_off, tmp_off, n, &total);
+    if (r != LYON_OK) return r;
+    const size_t rec = dots ? sizeof(lyon_dot) : sizeof(lyon_hatch_segment);
+    if (!ensure(ctx, ctx->hatch_out, total * rec + 16)) return LYON_ERR_OUT_OF_MEMORY;
+    a.out_offsets = out_off;
+    a.segments = reinterpret_cast<lyon_hatch_segment*>(ctx->hatch_out.ptr);
+    a.dot_out = reinterpret_cast<lyon_dot*>(ctx->hatch_out.ptr);
+    if (total > 0 && !set_err(ctx, "hatch emit", lg::launch_hatch(a, 2, ctx->num_sms, s)))
+        return LYON_ERR_CUDA;
+    out->segments = dots ? nullptr : a.segments;
+    out->dots = dots ? a.dot_out : nullptr;
+    out->offsets = out_off;
+    out->status = a.status;
+    out->total = total;
+    return LYON_OK;
+}
+
+}  // namespace
+
+int lyon_gpu_hatch_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                         const lyon_hatching_options* options, lyon_gpu_hatch_output* out) {
+    return hatch_impl(ctx, batch, options, false, out);
+}
+
+int lyon_gpu_dot_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                       const lyon_hatching_options* options, lyon_gpu_hatch_output* out) {
+    return hatch_impl(ctx, batch, options, true, out);
 }
 
 int lyon_gpu_flatten_arcs(lyon_gpu_context* ctx, const lyon_arc* arcs, uint32_t num_arcs,

@@ -94,6 +94,34 @@ cudaError_t launch_interpolate_fill(const lyon_vertex_source* sources,
                                     uint64_t num_endpoints, float* out, int num_sms,
                                     cudaStream_t stream);
 
+// Hatching and dots (hatch.cu).
+struct HatchArgs {
+    const uint8_t* verbs;
+    const float* points;
+    const uint32_t* verb_offsets;
+    const uint32_t* point_offsets;
+    uint32_t num_paths;
+    float tolerance;
+    float c, s;    // cos / sin of the pattern angle
+    float ci, si;  // cos / sin of its negation
+    float uv_x, uv_y;
+    float interval, column_interval;
+    int compute_tangents;
+    int dots;
+    uint32_t* edge_bound;            // phase 0 output
+    const uint64_t* scratch_offsets; // per path, in edges (num_paths + 1)
+    uint64_t scratch_total;          // edges per scratch region (three regions)
+    void* scratch;
+    uint32_t* edge_count;            // phase 1 output
+    uint32_t* counts;                // phase 1 output
+    int32_t* status;                 // phase 1 output
+    const uint64_t* out_offsets;     // phase 2 input
+    lyon_hatch_segment* segments;    // phase 2 output (hatches)
+    lyon_dot* dot_out;               // phase 2 output (dots)
+};
+// phase 0: edge bounds, 1: build, sort and count, 2: emit.
+cudaError_t launch_hatch(const HatchArgs& args, int phase, int num_sms, cudaStream_t stream);
+
 // Arc flattening (arcs.cu): count pass (pts null: counts and status) or emit pass.
 cudaError_t launch_arcs(const lyon_arc* arcs, uint32_t n, float tolerance, uint32_t* counts,
                         int32_t* status, const uint64_t* offsets, float* pts, float* ts,

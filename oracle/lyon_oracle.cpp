@@ -2906,6 +2906,201 @@ static uint64_t arc_flatten(const ArcF& arc, float tolerance, float* pts, float*
     return k;
 }
 
+// --------------------------------------------------------------------------------------------
+// Hatching and dots (crates/algorithms/src/hatching.rs). The rotation of the pattern is given as
+// cos/sin pairs computed once by the caller (lyon's Rotation2D takes them from f32 libm).
+// --------------------------------------------------------------------------------------------
+struct HatchParams {
+    float tolerance;
+    float c, s;    // Rotation::new(angle)
+    float ci, si;  // Rotation::new(-angle)
+    float uv_x, uv_y;  // options.uv_origin
+    float interval;    // RegularHatchingPattern::interval, or the dots' row interval
+    bool compute_tangents;
+    bool dots;
+    float column_interval;  // RegularDotPattern::column_interval
+};
+struct HatchSeg {  // HatchSegment (hatching.rs:181-205)
+    P a, a_tan;
+    float a_u;
+    P b, b_tan;
+    float b_u;
+    uint32_t row;
+    float v;
+};
+struct DotOut {  // Dot (hatching.rs:216-227)
+    P position;
+    float u, v;
+    uint32_t column, row;
+};
+struct Edge2 {
+    P from, to;
+};
+
+// Rows and dots beyond these bounds fail the path (lyon loops on, e.g. when the interval is too
+// small to move y): LYON_ERR_UNSUPPORTED.
+static const uint64_t MAX_HATCH_ROWS = 1u << 24;
+static const uint64_t MAX_DOTS = 1u << 26;
+
+static int cmp_pos(P a, P b) {  // hatching.rs:617-632
+    if (a.y > b.y) return 1;
+    if (a.y < b.y) return -1;
+    if (a.x > b.x) return 1;
+    if (a.x < b.x) return -1;
+    return 0;
+}
+
+struct Hatcher {
+    HatchParams hp;
+    std::vector<Edge2> edges, active;
+    P first{0, 0}, current{0, 0};
+    std::vector<HatchSeg>* segs = nullptr;
+    std::vector<DotOut>* dots = nullptr;
+    uint64_t rows = 0, ndots = 0;
+    uint32_t column = 0;
+    bool too_many = false;
+    P uv{0, 0};  // the rotated uv origin (hatching.rs:307)
+
+    P rot(P p, float c, float s) const { return P{p.x * c - p.y * s, p.x * s + p.y * c}; }
+
+    void add_edge(P from, P to) {  // hatching.rs:471-482
+        if (peq(from, to)) return;
+        P f = rot(from, hp.c, hp.s), t = rot(to, hp.c, hp.s);
+        if (cmp_pos(f, t) > 0) std::swap(f, t);
+        edges.push_back(Edge2{f, t});
+    }
+    // EventsBuilder (hatching.rs:500-577) over the path's events.
+    bool build(PathIter it) {
+        Evt e;
+        while (it.next(&e)) {
+            switch (e.kind) {
+                case EV_BEGIN:
+                    first = current = e.to;
+                    break;
+                case EV_LINE:
+                    add_edge(current, e.to);
+                    current = e.to;
+                    break;
+                case EV_QUAD:
+                    quad_flatten_with_t(Quad{current, e.ctrl1, e.to}, hp.tolerance,
+                                        [&](P, P to, float, float) {
+                                            add_edge(current, to);
+                                            current = to;
+                                        });
+                    break;
+                case EV_CUBIC:
+                    cubic_flatten_with_t(Cubic{current, e.ctrl1, e.ctrl2, e.to}, hp.tolerance,
+                                         [&](P, P to, float, float) {
+                                             add_edge(current, to);
+                                             current = to;
+                                         });
+                    break;
+                case EV_END:
+                    add_edge(current, first);
+                    break;
+            }
+        }
+        if (it.bad) return false;
+        std::stable_sort(edges.begin(), edges.end(),
+                         [](const Edge2& a, const Edge2& b) { return cmp_pos(a.from, b.from) < 0; });
+        return true;
+    }
+    static float x_for_y(const Edge2& e, float y) {  // geom line.rs:56-71
+        const float dy = e.to.y - e.from.y;
+        const float t = dy == 0.0f ? 0.0f : (y - e.from.y) / dy;
+        return e.from.x * (1.0f - t) + e.to.x * t;
+    }
+    // HatchesToDots::add_segment (hatching.rs:677-714) with RegularDotPattern.
+    void seg_to_dots(const HatchSeg& g) {
+        float u = 0.0f;
+        const float u_start = g.a_u;
+        const float d = hp.column_interval;
+        const float m = u_start >= 0.0f ? fmodf(u_start, d) : d + fmodf(u_start, d);
+        if (m != 0.0f) u += d - m;
+        const P a = g.a;
+        const P ab = normalize(sub(g.b, a));
+        while (u_start + u < g.b_u) {
+            if (++ndots > MAX_DOTS) {
+                too_many = true;
+                return;
+            }
+            if (dots) dots->push_back(DotOut{add(a, mul(ab, u)), g.a_u + u, g.v, column, g.row});
+            column += 1;
+            const float du = hp.column_interval;
+            if (du <= 0.0f) return;
+            u += du;
+        }
+    }
+    // hatch_line (hatching.rs:381-428).
+    void hatch_line(float y, uint32_t row) {
+        std::stable_sort(active.begin(), active.end(), [&](const Edge2& a, const Edge2& b) {
+            return x_for_y(a, y) < x_for_y(b, y);
+        });
+        bool inside = false;
+        float prev_x = NAN;
+        P prev_tan{NAN, NAN}, tan{NAN, NAN};
+        const float v = y - uv.y;
+        for (const Edge2& e : active) {
+            if (e.to.y <= y) continue;
+            const float x = x_for_y(e, y);
+            if (hp.compute_tangents) tan = normalize(rot(sub(e.to, e.from), hp.ci, hp.si));
+            if (inside) {
+                HatchSeg g;
+                g.a = rot(P{prev_x, y}, hp.ci, hp.si);
+                g.b = rot(P{x, y}, hp.ci, hp.si);
+                g.a_u = prev_x - uv.x;
+                g.b_u = x - uv.x;
+                g.a_tan = hp.compute_tangents ? prev_tan : P{NAN, NAN};
+                g.b_tan = hp.compute_tangents ? tan : P{NAN, NAN};
+                g.row = row;
+                g.v = v;
+                if (hp.dots) {
+                    seg_to_dots(g);
+                    if (too_many) return;
+                } else if (segs) {
+                    segs->push_back(g);
+                }
+            }
+            inside = !inside;
+            prev_x = x;
+            prev_tan = tan;
+        }
+    }
+    // hatch (hatching.rs:300-347). Returns LYON_OK, or LYON_ERR_UNSUPPORTED past the bounds.
+    int hatch() {
+        if (edges.empty()) return LYON_OK;
+        uv = rot(P{hp.uv_x, hp.uv_y}, hp.c, hp.s);
+        uint32_t row = 0;
+        float y = edges[0].from.y + hp.interval;
+        float y_max = y;
+        auto line = [&]() -> bool {  // hatch_line, then next_offset (column reset for dots)
+            if (++rows > MAX_HATCH_ROWS) {
+                too_many = true;
+                return false;
+            }
+            hatch_line(y, row);
+            if (too_many) return false;
+            row += 1;
+            column = 0;
+            y += hp.interval;
+            return hp.interval > 0.0f;
+        };
+        for (const Edge2& e : edges) {
+            while (y < e.from.y)
+                if (!line()) return too_many ? LYON_ERR_UNSUPPORTED : LYON_OK;
+            y_max = fmaxf(y_max, e.to.y);
+            // update_sweep_line (hatching.rs:374-379)
+            active.erase(std::remove_if(active.begin(), active.end(),
+                                        [&](const Edge2& a) { return cmp_pos(a.to, e.from) < 0; }),
+                         active.end());
+            active.push_back(e);
+        }
+        while (y < y_max)
+            if (!line()) return too_many ? LYON_ERR_UNSUPPORTED : LYON_OK;
+        return LYON_OK;
+    }
+};
+
 }  // namespace lo
 
 // ============================================================================================
@@ -3015,6 +3210,64 @@ void lyon_oracle_flatten_arcs(const float* arcs, uint32_t n, float tolerance, ui
         }
         if (counts) counts[i] = k == UINT64_MAX ? 0u : (uint32_t)k;
         if (status) status[i] = k == UINT64_MAX ? LYON_ERR_UNSUPPORTED : LYON_OK;
+    }
+}
+
+// Hatcher::hatch_path / dot_path (hatching.rs:276-298) with a regular pattern for every path of a
+// batch. params: tolerance, cos(angle), sin(angle), cos(-angle), sin(-angle), uv origin x, y,
+// interval (hatches) or row interval (dots), compute_tangents (0/1), dots (0/1), column
+// interval. Counting call (outputs NULL): counts and statuses. Output call: 12 words per hatch
+// segment (a: x, y, tangent x, y, u; b: the same; row; v) or 6 per dot (x, y, u, v, column,
+// row) at `offsets`.
+void lyon_oracle_hatch(const lyon_path_batch* batch, const float* params, uint32_t* counts,
+                       int32_t* status, const uint64_t* offsets, uint32_t* out) {
+    HatchParams hp{params[0], params[1], params[2], params[3], params[4], params[5], params[6],
+                   params[7], params[8] != 0.0f, params[9] != 0.0f, params[10]};
+    for (uint32_t i = 0; i < batch->num_paths; ++i) {
+        uint32_t v0 = batch->verb_offsets[i], v1 = batch->verb_offsets[i + 1];
+        uint32_t p0 = batch->point_offsets[i], p1 = batch->point_offsets[i + 1];
+        Hatcher h;
+        h.hp = hp;
+        std::vector<HatchSeg> segs;
+        std::vector<DotOut> dots;
+        const bool write = out && offsets;
+        if (write) {
+            if (hp.dots) h.dots = &dots;
+            else h.segs = &segs;
+        } else if (!hp.dots) {
+            h.segs = &segs;
+        }
+        int st = LYON_OK;
+        if (!h.build(PathIter{batch->verbs + v0, v1 - v0, batch->points + 2 * (size_t)p0,
+                              p1 - p0}))
+            st = LYON_ERR_INVALID_ARGUMENT;
+        else
+            st = h.hatch();
+        const uint64_t n = st != LYON_OK ? 0 : (hp.dots ? h.ndots : segs.size());
+        if (counts) counts[i] = (uint32_t)n;
+        if (status) status[i] = st;
+        if (!write || st != LYON_OK) continue;
+        if (hp.dots) {
+            uint32_t* d = out + 6 * offsets[i];
+            for (size_t k = 0; k < dots.size(); ++k) {
+                const DotOut& o = dots[k];
+                std::memcpy(d + 6 * k, &o.position.x, 4);
+                std::memcpy(d + 6 * k + 1, &o.position.y, 4);
+                std::memcpy(d + 6 * k + 2, &o.u, 4);
+                std::memcpy(d + 6 * k + 3, &o.v, 4);
+                d[6 * k + 4] = o.column;
+                d[6 * k + 5] = o.row;
+            }
+        } else {
+            uint32_t* d = out + 12 * offsets[i];
+            for (size_t k = 0; k < segs.size(); ++k) {
+                const HatchSeg& g = segs[k];
+                const float f[12] = {g.a.x, g.a.y, g.a_tan.x, g.a_tan.y, g.a_u,
+                                     g.b.x, g.b.y, g.b_tan.x, g.b_tan.y, g.b_u, 0.0f, g.v};
+                std::memcpy(d + 12 * k, f, sizeof f);
+                d[12 * k + 10] = g.row;
+            }
+        }
     }
 }
 

@@ -100,6 +100,8 @@ def lib():
             L.lyon_oracle_flatten_arcs.restype = None
             L.lyon_oracle_flatten_arcs.argtypes = [c_p, ctypes.c_uint32, ctypes.c_float, c_p,
                                                    c_p, c_p, c_p, c_p]
+            L.lyon_oracle_hatch.restype = None
+            L.lyon_oracle_hatch.argtypes = [c_p, c_p, c_p, c_p, c_p, c_p]
             L.lyon_oracle_batch.restype = ctypes.c_int
             L.lyon_oracle_batch.argtypes = [ctypes.c_int, c_p, c_p, ctypes.c_uint32, ctypes.c_int,
                                             ctypes.c_int, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
@@ -507,3 +509,31 @@ def flatten_arcs(arcs: np.ndarray, tolerance: float):
     L.lyon_oracle_flatten_arcs(_ptr(a), n, tolerance, None, None, _ptr(offs), _ptr(pts),
                                _ptr(ts))
     return pts, ts, offs, st
+
+
+HATCH_SEGMENT_DTYPE = np.dtype([("a_x", "<f4"), ("a_y", "<f4"), ("a_tangent_x", "<f4"),
+                                ("a_tangent_y", "<f4"), ("a_u", "<f4"), ("b_x", "<f4"),
+                                ("b_y", "<f4"), ("b_tangent_x", "<f4"), ("b_tangent_y", "<f4"),
+                                ("b_u", "<f4"), ("row", "<u4"), ("v", "<f4")])
+DOT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("u", "<f4"), ("v", "<f4"), ("column", "<u4"),
+                      ("row", "<u4")])
+
+
+def hatch(pb, params):
+    """Hatcher::hatch_path / dot_path (crates/algorithms/src/hatching.rs) over a PathBatch.
+    `params`: 11 floats (see lyon_oracle_hatch). Returns (records, offsets, status)."""
+    L = lib()
+    n = pb.num_paths
+    cb = _CBatch(_ptr(pb.verbs), _ptr(pb.points), _ptr(pb.verb_offsets),
+                 _ptr(pb.point_offsets), n)
+    prm = np.ascontiguousarray(params, np.float32)
+    counts = np.zeros(n, np.uint32)
+    st = np.zeros(n, np.int32)
+    L.lyon_oracle_hatch(ctypes.byref(cb), _ptr(prm), _ptr(counts), _ptr(st), None, None)
+    offs = np.zeros(n + 1, np.uint64)
+    offs[1:] = np.cumsum(counts, dtype=np.uint64)
+    dt = DOT_DTYPE if prm[9] != 0 else HATCH_SEGMENT_DTYPE
+    out = np.zeros(int(offs[-1]), dt)
+    L.lyon_oracle_hatch(ctypes.byref(cb), _ptr(prm), None, None, _ptr(offs),
+                        out.ctypes.data_as(ctypes.c_void_p) if len(out) else None)
+    return out, offs, st

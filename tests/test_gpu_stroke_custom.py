@@ -234,3 +234,27 @@ def test_interpolate_attributes_standalone(gpu):
     assert np.all(np.isnan(out[bad]))
     want = orc.interpolate_attributes(src[~bad], attrs)
     assert np.array_equal(out[~bad], want)
+
+
+def test_path_buffer_with_attributes_feeds_the_custom_stroke(gpu):
+    # PathBuffer (crates/path/src/path_buffer.rs) as the batched container: its batch and its
+    # attribute table go to lyon_gpu_stroke_paths_custom unchanged.
+    from lyon_gb300.path_buffer import PathBuffer
+    buf = PathBuffer()
+    rng = np.random.default_rng(141)
+    for i in range(200):
+        b = buf.builder().with_attributes(2)
+        b.begin(rng.uniform(0, 100, 2), rng.uniform(0.5, 2, 2))
+        for _ in range(int(rng.integers(1, 6))):
+            if rng.random() < 0.5:
+                b.line_to(rng.uniform(0, 100, 2), rng.uniform(0.5, 2, 2))
+            else:
+                b.quadratic_bezier_to(rng.uniform(0, 100, 2), rng.uniform(0, 100, 2),
+                                      rng.uniform(0.5, 2, 2))
+        b.end(bool(i % 2))
+        b.build()
+    batch = buf.as_batch()
+    attrs = buf.attribute_table()
+    opts = _options(batch.num_paths, 142)
+    bad, exact, _ = compare_custom(gpu, batch, opts, attrs, width_attribute=1)
+    assert len(bad) <= 1, bad

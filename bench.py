@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-variable-width", action="store_true")
     ap.add_argument("--vw-paths", type=int, default=200_000)
     ap.add_argument("--no-custom-attributes", action="store_true")
+    ap.add_argument("--no-producers", action="store_true",
+                    help="skip the arc flattening and hatching lines")
     ap.add_argument("--polyline-paths", type=int, default=2_000_000)
     ap.add_argument("--serve-seconds", type=float, default=0.1)
     ap.add_argument("--profile-fill", action="store_true",
@@ -358,6 +360,10 @@ def main():
             line["variable_width"] = run_variable_width(ctx, args, T)
         if not args.no_custom_attributes:
             line["custom_attributes"] = run_custom_attributes(ctx, args, T)
+            line["fill_custom_attributes"] = run_fill_custom(ctx, args, T)
+        if not args.no_producers:
+            line["arcs"] = run_arcs(ctx, args, T)
+            line["hatching"] = run_hatching(ctx, args, T)
         if not args.no_serve and world == 1:
             del db, od
             ctx.close()
@@ -536,6 +542,127 @@ def run_custom_attributes(ctx, args, T):
                            "sample": f"first {n} paths, {cv} output vertices, "
                                      f"{dt:.2f} s wall on {threads} threads (output pass "
                                      f"and interpolation)"}
+    return out
+
+
+def _time_calls(ctx, steps, fn):
+    """Device time per call of `fn` on the library's stream (after one untimed call), and the
+    library's kernel launches during the timed calls."""
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", 0))
+    res = fn()
+    ctx.synchronize()
+    launches0 = ctx.lib.lyon_gpu_kernel_launches()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        res = fn()
+    end.record(stream)
+    end.synchronize()
+    return res, start.elapsed_time(end) / steps, ctx.lib.lyon_gpu_kernel_launches() - launches0
+
+
+def run_fill_custom(ctx, args, T):
+    """Fills with custom attributes (lyon_gpu_fill_paths_custom): 50,000 glyph paths (seed 3),
+    non-zero, two attributes per point; sources and interpolated attributes written beside the
+    fill. CPU baseline: the oracle's output pass with sources and its interpolation."""
+    import torch
+    from lyon_gb300 import workloads
+    from lyon_gb300.options import FILL_OPTIONS_DTYPE, FillRule
+    from oracle import lyon_oracle as orc
+    batch, _ = workloads.glyph_fill(50_000, seed=3)
+    opts = np.zeros(1, FILL_OPTIONS_DTYPE)
+    opts[0] = (0.1, FillRule.NonZero, 0, 1)
+    attrs = np.random.default_rng(23).uniform(size=(len(batch.points), 2)).astype(np.float32)
+    db = T.DeviceBatch.upload(batch, 0)
+    od = T.upload_options(opts, 0)
+    ad = torch.from_numpy(attrs).cuda()
+    res, ms, launches = _time_calls(ctx, max(1, args.steps), lambda: T.tessellate_paths(
+        "fill", db, od, 1, 32, T.INDEX_GLOBAL, 0, ctx, custom_attributes=ad))
+    out = {"workload": f"fill_custom_attributes_{batch.num_paths}_paths",
+           "config": {"paths": batch.num_paths, "generator": "glyph fill, seed 3",
+                      "fill_rule": "non-zero", "attributes": "2 f32 per point, seed 23",
+                      "outputs": "positions, indices, vertex sources, interpolated attributes"},
+           "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
+           "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
+           "sources_per_step": res.total_sources, "gpu_launches": launches}
+    threads = os.cpu_count() or 1
+    sub = batch.head(5_000)
+    r = orc.batch_fill_sources(sub, opts, 32, threads)
+    t0 = time.perf_counter()
+    orc.interpolate_fill_attributes_c(r["sources"], r["source_counts"], attrs)
+    dt = r["output_pass_s"] + time.perf_counter() - t0
+    cv = int(r["vtx_counts"].sum())
+    out["cpu_baseline"] = {"value": cv / dt, "unit": "vertices/s", "cores": threads,
+                           "kind": "port", "sample": f"first 5000 paths, {cv} output vertices, "
+                                                     f"{dt:.2f} s wall on {threads} threads"}
+    return out
+
+
+def run_arcs(ctx, args, T):
+    """Arc flattening (lyon_gpu_flatten_arcs): 1,000,000 elliptic arcs (centres in
+    [-1000, 1000]^2, radii e^U[-3, 7], sweeps U[-20, 20] rad, seed 24), tolerance 0.1. CPU
+    baseline: the oracle, one thread, on 20,000 arcs."""
+    import torch
+    from oracle import lyon_oracle as orc
+    n = 1_000_000
+    rng = np.random.default_rng(24)
+    a = np.zeros(n, T.ARC_DTYPE)
+    a["center_x"] = rng.uniform(-1000, 1000, n)
+    a["center_y"] = rng.uniform(-1000, 1000, n)
+    a["radius_x"] = np.exp(rng.uniform(-3, 7, n))
+    a["radius_y"] = np.exp(rng.uniform(-3, 7, n))
+    a["start_angle"] = rng.uniform(-10, 10, n)
+    a["sweep_angle"] = rng.uniform(-20, 20, n)
+    a["x_rotation"] = rng.uniform(-4, 4, n)
+    d = torch.from_numpy(a.view(np.uint8).copy()).cuda()
+    res, ms, launches = _time_calls(ctx, max(1, args.steps),
+                                    lambda: T.flatten_arcs(d, n, 0.1, ctx))
+    out = {"workload": f"arcs_{n}", "config": {"arcs": n, "tolerance": 0.1, "seed": 24},
+           "metric": "flattened points/s", "value": res.total_points / (ms / 1e3),
+           "unit": "points/s", "ms_per_step": ms, "points_per_step": res.total_points,
+           "gpu_launches": launches}
+    k = 20_000
+    t0 = time.perf_counter()
+    pts, _, _, _ = orc.flatten_arcs(a[:k].view(orc.ARC_DTYPE), 0.1)
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": len(pts) / dt, "unit": "points/s", "cores": 1,
+                           "kind": "port", "sample": f"first {k} arcs, {len(pts)} points, "
+                                                     f"{dt:.2f} s wall, one thread, counting and output passes"}
+    return out
+
+
+def run_hatching(ctx, args, T):
+    """Hatching (lyon_gpu_hatch_paths): the fill workload's 200,000 glyph paths hatched every
+    2.0 at 0.7 rad with tangents. CPU baseline: the oracle, one thread, on 10,000 paths."""
+    import ctypes
+    import ctypes.util
+    from lyon_gb300 import hatching as H, workloads
+    from oracle import lyon_oracle as orc
+    batch, _ = workloads.glyph_fill(args.fill_paths, seed=3)
+    db = T.DeviceBatch.upload(batch, 0)
+    opts = H.HatchingOptions(0.1, 0.7, True)
+    res, ms, launches = _time_calls(ctx, max(1, args.steps),
+                                    lambda: H.hatch_paths(db, opts, 2.0, ctx))
+    out = {"workload": f"hatching_glyph_{batch.num_paths}_paths",
+           "config": {"paths": batch.num_paths, "interval": 2.0, "angle": 0.7,
+                      "tolerance": 0.1, "tangents": True},
+           "metric": "hatch segments/s", "value": res.total / (ms / 1e3), "unit": "segments/s",
+           "ms_per_step": ms, "segments_per_step": res.total, "gpu_launches": launches}
+    libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+    for f in ("cosf", "sinf"):
+        getattr(libm, f).restype = ctypes.c_float
+        getattr(libm, f).argtypes = [ctypes.c_float]
+    prm = [0.1, libm.cosf(0.7), libm.sinf(0.7), libm.cosf(-0.7), libm.sinf(-0.7), 0.0, 0.0,
+           2.0, 1.0, 0.0, 0.0]
+    k = 10_000
+    t0 = time.perf_counter()
+    segs, _, _ = orc.hatch(batch.head(k), prm)
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": len(segs) / dt, "unit": "segments/s", "cores": 1,
+                           "kind": "port", "sample": f"first {k} paths, {len(segs)} segments, "
+                                                     f"{dt:.2f} s wall, one thread, counting and output passes"}
     return out
 
 

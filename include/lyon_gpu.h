@@ -360,6 +360,28 @@ int lyon_gpu_fill_shapes(lyon_gpu_context* ctx, int shape_kind, const float* par
                          uint32_t num_options, int index_bits, int index_mode,
                          uint32_t vertex_offset, lyon_gpu_batch_output* out);
 
+/* ---- Sizing and emitting separately (caller-allocated outputs) ---------------------------- */
+
+/* The sizing half of lyon_gpu_stroke_paths / lyon_gpu_fill_paths (`kind`: LYON_KIND_STROKE or
+ * LYON_KIND_FILL, declared with the serving loop below): the count pass and
+ * the scan, then one synchronisation. `*total_vertices`, `*total_indices` and
+ * `*num_failed_paths` receive the batch's totals so that the caller can allocate the outputs;
+ * per-path counts, offsets and statuses stay in the context for lyon_gpu_emit_into. */
+int lyon_gpu_query_sizes(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
+                         const void* options, uint32_t num_options, int index_bits,
+                         int index_mode, uint32_t vertex_offset, uint64_t* total_vertices,
+                         uint64_t* total_indices, uint32_t* num_failed_paths);
+
+/* The emitting half, after lyon_gpu_query_sizes with the same batch and arguments and no other
+ * batched call on the context in between: writes the vertices (2 floats each) and indices into
+ * the caller's device buffers, which hold at least the queried totals. `out` receives the
+ * caller's buffers with the context's per-path offsets and statuses and the totals. Returns
+ * LYON_ERR_INVALID_ARGUMENT when no matching query precedes it. */
+int lyon_gpu_emit_into(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
+                       const void* options, uint32_t num_options, int index_bits, int index_mode,
+                       uint32_t vertex_offset, float* vertices, void* indices,
+                       lyon_gpu_batch_output* out);
+
 /* Largest batch lyon_gpu_stroke_paths_noalloc accepts (its fixed scratch holds this many paths). */
 #define LYON_NOALLOC_MAX_PATHS 262144u
 

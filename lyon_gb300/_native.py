@@ -222,6 +222,13 @@ def load(build_if_missing: bool = True):
         for _fn in ("lyon_gpu_hatch_paths", "lyon_gpu_dot_paths"):
             getattr(L, _fn).restype = ctypes.c_int
             getattr(L, _fn).argtypes = [c_p, c_p, c_p, c_p]
+        L.lyon_gpu_query_sizes.restype = ctypes.c_int
+        L.lyon_gpu_query_sizes.argtypes = [c_p, ctypes.c_int, c_p, c_p, u32, ctypes.c_int,
+                                           ctypes.c_int, u32, ctypes.POINTER(u64),
+                                           ctypes.POINTER(u64), ctypes.POINTER(u32)]
+        L.lyon_gpu_emit_into.restype = ctypes.c_int
+        L.lyon_gpu_emit_into.argtypes = [c_p, ctypes.c_int, c_p, c_p, u32, ctypes.c_int,
+                                         ctypes.c_int, u32, c_p, c_p, c_p]
         L.lyon_gpu_autotune_stroke.restype = ctypes.c_int
         L.lyon_gpu_autotune_stroke.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
                                                ctypes.POINTER(CStrokeTuning),
@@ -253,5 +260,5 @@ EXPORTED = [
     "lyon_gpu_interpolate_attributes", "lyon_gpu_stroke_path_custom",
     "lyon_gpu_fill_paths_custom", "lyon_gpu_interpolate_fill_attributes",
     "lyon_gpu_fill_path_custom", "lyon_gpu_flatten_arcs", "lyon_gpu_hatch_paths",
-    "lyon_gpu_dot_paths",
+    "lyon_gpu_dot_paths", "lyon_gpu_query_sizes", "lyon_gpu_emit_into",
 ]

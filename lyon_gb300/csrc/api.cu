@@ -60,6 +60,15 @@ struct lyon_gpu_context {
     uint64_t total_sources = 0;
     // arc flattening
     DevBuf arc_counts, arc_status, arc_offsets, arc_points, arc_t;
+    // the last lyon_gpu_query_sizes (for lyon_gpu_emit_into)
+    struct {
+        bool valid = false;
+        int kind = 0, index_bits = 0, index_mode = 0;
+        const void* verbs = nullptr;
+        uint32_t num_paths = 0, vertex_offset = 0;
+        uint64_t tv = 0, ti = 0;
+        uint32_t failed = 0;
+    } query;
     // hatching
     DevBuf hatch_bound, hatch_edge_count, hatch_counts, hatch_status, hatch_offsets,
         hatch_scratch, hatch_out;
@@ -965,6 +974,65 @@ void lyon_gpu_set_timing(lyon_gpu_context* ctx, int enabled) {
 int lyon_gpu_last_timings(lyon_gpu_context* ctx, float* ms4) {
     if (!ctx || !ms4) return LYON_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < 4; ++i) ms4[i] = ctx->last_ms[i];
+    return LYON_OK;
+}
+
+int lyon_gpu_query_sizes(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
+                         const void* options, uint32_t num_options, int index_bits,
+                         int index_mode, uint32_t vertex_offset, uint64_t* total_vertices,
+                         uint64_t* total_indices, uint32_t* num_failed_paths) {
+    if (!ctx || (kind != KIND_STROKE && kind != KIND_FILL) || !total_vertices ||
+        !total_indices || !valid_args(ctx, batch, options, num_options, index_bits, index_mode))
+        return LYON_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    ctx->query.valid = false;
+    uint64_t tv = 0, ti = 0;
+    uint32_t failed = 0;
+    int r = pipeline_count(ctx, kind, batch, options, num_options, index_bits, index_mode,
+                           vertex_offset, &tv, &ti, &failed);
+    if (r != LYON_OK) return r;
+    *total_vertices = tv;
+    *total_indices = ti;
+    if (num_failed_paths) *num_failed_paths = failed;
+    ctx->query.valid = true;
+    ctx->query.kind = kind;
+    ctx->query.index_bits = index_bits;
+    ctx->query.index_mode = index_mode;
+    ctx->query.verbs = batch->verbs;
+    ctx->query.num_paths = batch->num_paths;
+    ctx->query.vertex_offset = vertex_offset;
+    ctx->query.tv = tv;
+    ctx->query.ti = ti;
+    ctx->query.failed = failed;
+    return LYON_OK;
+}
+
+int lyon_gpu_emit_into(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
+                       const void* options, uint32_t num_options, int index_bits, int index_mode,
+                       uint32_t vertex_offset, float* vertices, void* indices,
+                       lyon_gpu_batch_output* out) {
+    if (!ctx || !out || !batch || !ctx->query.valid || ctx->query.kind != kind ||
+        ctx->query.index_bits != index_bits || ctx->query.index_mode != index_mode ||
+        ctx->query.verbs != batch->verbs || ctx->query.num_paths != batch->num_paths ||
+        ctx->query.vertex_offset != vertex_offset ||
+        (ctx->query.tv > 0 && !vertices) || (ctx->query.ti > 0 && !indices)) {
+        if (ctx) ctx->last_error = "lyon_gpu_emit_into without a matching lyon_gpu_query_sizes";
+        return LYON_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(ctx->device);
+    ctx->query.valid = false;
+    memset(out, 0, sizeof(*out));
+    int r = pipeline_emit(ctx, kind, batch, options, num_options, index_bits, index_mode,
+                          vertex_offset, vertices, indices, ctx->query.tv);
+    if (r != LYON_OK) return r;
+    out->vertices = vertices;
+    out->indices = indices;
+    out->vertex_offsets = as<uint64_t>(ctx->vtx_offsets);
+    out->index_offsets = as<uint64_t>(ctx->idx_offsets);
+    out->status = as<int32_t>(ctx->status);
+    out->total_vertices = ctx->query.tv;
+    out->total_indices = ctx->query.ti;
+    out->num_failed_paths = ctx->query.failed;
     return LYON_OK;
 }
 

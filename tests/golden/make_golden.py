@@ -13,6 +13,8 @@ Outputs:
                           their asserted triangle counts / properties
   lyon_flatten_cases.json curves and asserted counts from crates/geom/src/quadratic_bezier.rs and
                           crates/geom/src/cubic_bezier.rs
+  lyon_fuzz_cases.json    the polygons of crates/tessellation/src/fuzz_tests.rs (lyon's own
+                          regression cases: the fill must succeed with both fill rules)
   rust_logo.json          the rust logo path of crates/extra/src/rust_logo.rs (lyon's own test
                           data), converted from its SVG-builder calls to absolute verbs/points
                           with f32 arithmetic (crates/path/src/builder.rs:1193-1480 semantics)
@@ -426,6 +428,23 @@ def rust_logo(ref):
     return {"src": "crates/extra/src/rust_logo.rs:5", "verbs": pb.verbs, "points": pb.points}
 
 
+def fuzz_cases(ref):
+    """crates/tessellation/src/fuzz_tests.rs: every test builds a polygon path with builder calls
+    and asserts that filling it (after flattening at 0.05) succeeds with both fill rules."""
+    path = os.path.join(ref, "crates/tessellation/src/fuzz_tests.rs")
+    src = open(path).read()
+    out = []
+    for name, line, body in split_tests(src):
+        if "test_path(" not in body:
+            continue
+        pb = parse_builder_calls(body)
+        if pb is None or not pb.verbs or pb.open:
+            continue
+        out.append({"name": name, "src": f"crates/tessellation/src/fuzz_tests.rs:{line}",
+                    "verbs": pb.verbs, "points": pb.points})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -434,6 +453,7 @@ def main():
         "lyon_fill_cases.json": fill_cases(a.reference),
         "lyon_stroke_cases.json": stroke_cases(a.reference),
         "lyon_flatten_cases.json": flatten_cases(a.reference),
+        "lyon_fuzz_cases.json": fuzz_cases(a.reference),
         "rust_logo.json": rust_logo(a.reference),
     }
     for fname, data in outputs.items():

@@ -5,6 +5,9 @@ Fill output is compared exactly: vertex and index counts, index topology and ver
 is also checked against the oracle's within 1e-4 relative.
 """
 
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -14,7 +17,7 @@ from lyon_gb300.options import FillOptions, FillRule, fill_options_array
 from lyon_gb300.path import Path, PathBatch
 from oracle import lyon_oracle as orc
 
-from lyon_cases import case_path, flatten_to_lines, load, rotation_angles, rust_logo
+from lyon_cases import GOLDEN, case_path, flatten_to_lines, load, rotation_angles, rust_logo
 
 pytestmark = pytest.mark.gpu
 
@@ -103,6 +106,20 @@ def test_lyon_fill_fixtures(gpu):
         assert g["status"][i] == 0
         if e is not None:
             assert (g["idx_offsets"][i + 1] - g["idx_offsets"][i]) // 3 == e
+
+
+def test_lyon_fuzz_fixtures(gpu):
+    # crates/tessellation/src/fuzz_tests.rs polygons (lyon's regression cases), both fill rules,
+    # tolerance 0.05, u16: every path succeeds, with the oracle's triangles.
+    with open(os.path.join(GOLDEN, "lyon_fuzz_cases.json")) as f:
+        cases = json.load(f)
+    flat = _lyon_fill_paths([case_path(c) for c in cases])
+    batch = PathBatch.from_paths(flat + flat)
+    recs = ([FillOptions(tolerance=0.05, fill_rule=FillRule.EvenOdd).to_record()[0]] * len(flat)
+            + [FillOptions(tolerance=0.05, fill_rule=FillRule.NonZero).to_record()[0]]
+            * len(flat))
+    s = _check(gpu, batch, fill_options_array(recs), index_bits=16)
+    assert np.all(s["gpu"]["status"] == 0)
 
 
 def test_rust_logo_variants(gpu):

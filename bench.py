@@ -62,6 +62,9 @@ def parse():
                     help="only run the fill warm-up and timed steps (for profilers)")
     ap.add_argument("--profile", action="store_true",
                     help="only run the warm-up and timed device steps (for profilers)")
+    ap.add_argument("--profile-producers", action="store_true",
+                    help="only run the stroke/fill custom-attribute, arc and hatching lines "
+                         "(one timed step each, no CPU baselines; for profilers)")
     ap.add_argument("--profile-polylines", action="store_true",
                     help="only run the map-polyline stroke (tolerance 0.1, default launch "
                          "settings, --polyline-paths paths) for --warmup + --steps calls "
@@ -258,6 +261,18 @@ def main():
         end.synchronize()
         print(json.dumps({"profile_polylines_ms_per_step": start.elapsed_time(end) / args.steps,
                           "paths": pb.num_paths, "vertices": res.total_vertices}))
+        ctx.close()
+        return 0
+    if args.profile_producers:
+        ctx = T.Context(dev)
+        args.steps = 1
+        out = {}
+        for name, fn in (("custom_attributes", run_custom_attributes),
+                         ("fill_custom_attributes", run_fill_custom), ("arcs", run_arcs),
+                         ("hatching", run_hatching)):
+            r = fn(ctx, args, T, baseline=False)
+            out[name] = {"value": r["value"], "ms_per_step": r["ms_per_step"]}
+        print(json.dumps(out))
         ctx.close()
         return 0
     if args.profile_fill:
@@ -490,7 +505,7 @@ def run_variable_width(ctx, args, T):
     return out
 
 
-def run_custom_attributes(ctx, args, T):
+def run_custom_attributes(ctx, args, T, baseline=True):
     """Custom endpoint attributes (lyon_gpu_stroke_paths_custom): the variable-width workload's
     paths with a fixed width and two f32 attributes per point; every vertex's source and its
     interpolated attributes are written beside the positions. CPU baseline: the oracle strokes a
@@ -527,6 +542,8 @@ def run_custom_attributes(ctx, args, T):
            "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
            "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
            "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
+    if not baseline:
+        return out
     threads = os.cpu_count() or 1
     n = min(20_000, batch.num_paths)
     sub = batch.head(n)
@@ -563,7 +580,7 @@ def _time_calls(ctx, steps, fn):
     return res, start.elapsed_time(end) / steps, ctx.lib.lyon_gpu_kernel_launches() - launches0
 
 
-def run_fill_custom(ctx, args, T):
+def run_fill_custom(ctx, args, T, baseline=True):
     """Fills with custom attributes (lyon_gpu_fill_paths_custom): 50,000 glyph paths (seed 3),
     non-zero, two attributes per point; sources and interpolated attributes written beside the
     fill. CPU baseline: the oracle's output pass with sources and its interpolation."""
@@ -587,6 +604,8 @@ def run_fill_custom(ctx, args, T):
            "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
            "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
            "sources_per_step": res.total_sources, "gpu_launches": launches}
+    if not baseline:
+        return out
     threads = os.cpu_count() or 1
     sub = batch.head(5_000)
     r = orc.batch_fill_sources(sub, opts, 32, threads)
@@ -600,7 +619,7 @@ def run_fill_custom(ctx, args, T):
     return out
 
 
-def run_arcs(ctx, args, T):
+def run_arcs(ctx, args, T, baseline=True):
     """Arc flattening (lyon_gpu_flatten_arcs): 1,000,000 elliptic arcs (centres in
     [-1000, 1000]^2, radii e^U[-3, 7], sweeps U[-20, 20] rad, seed 24), tolerance 0.1. CPU
     baseline: the oracle, one thread, on 20,000 arcs."""
@@ -623,6 +642,8 @@ def run_arcs(ctx, args, T):
            "metric": "flattened points/s", "value": res.total_points / (ms / 1e3),
            "unit": "points/s", "ms_per_step": ms, "points_per_step": res.total_points,
            "gpu_launches": launches}
+    if not baseline:
+        return out
     k = 20_000
     t0 = time.perf_counter()
     pts, _, _, _ = orc.flatten_arcs(a[:k].view(orc.ARC_DTYPE), 0.1)
@@ -633,7 +654,7 @@ def run_arcs(ctx, args, T):
     return out
 
 
-def run_hatching(ctx, args, T):
+def run_hatching(ctx, args, T, baseline=True):
     """Hatching (lyon_gpu_hatch_paths): the fill workload's 200,000 glyph paths hatched every
     2.0 at 0.7 rad with tangents. CPU baseline: the oracle, one thread, on 10,000 paths."""
     import ctypes
@@ -650,6 +671,8 @@ def run_hatching(ctx, args, T):
                       "tolerance": 0.1, "tangents": True},
            "metric": "hatch segments/s", "value": res.total / (ms / 1e3), "unit": "segments/s",
            "ms_per_step": ms, "segments_per_step": res.total, "gpu_launches": launches}
+    if not baseline:
+        return out
     libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
     for f in ("cosf", "sinf"):
         getattr(libm, f).restype = ctypes.c_float

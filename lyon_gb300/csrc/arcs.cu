@@ -16,19 +16,20 @@ __device__ __forceinline__ float dsin(float x) { return (float)sin((double)x); }
 __device__ __forceinline__ float dacos(float x) { return (float)acos((double)x); }
 
 struct ArcState {
-    float cx, cy, rx, ry, start, sweep, rot;
+    float cx, cy, rx, ry, start, sweep;
+    float rc, rs;  // cos and sin of x_rotation (the same for every sample of the arc)
 };
 
 // sample (arc.rs:194-197): center + Rotation2D(x_rotation) applied to (rx cos a, ry sin a).
 __device__ __forceinline__ float2 arc_sample(const ArcState& a, float t) {
     const float angle = a.start + a.sweep * t;
     const float ex = a.rx * dcos(angle), ey = a.ry * dsin(angle);
-    const float c = dcos(a.rot), s = dsin(a.rot);
-    return make_float2(a.cx + (ex * c - ey * s), a.cy + (ex * s + ey * c));
+    return make_float2(a.cx + (ex * a.rc - ey * a.rs), a.cy + (ex * a.rs + ey * a.rc));
 }
 
-__device__ __forceinline__ float arc_step(const ArcState& a, float tolerance) {
-    const float2 from = arc_sample(a, 0.0f);
+// flattening_step (arc.rs:369-389) of an arc whose start point, sample(0), is `from` (the
+// point the walk emitted last: the same value lyon recomputes).
+__device__ __forceinline__ float arc_step(const ArcState& a, float2 from, float tolerance) {
     const float dx = from.x - a.cx, dy = from.y - a.cy;
     const float r = sqrtf(dx * dx + dy * dy);
     const float ang = 2.0f * dacos((r - tolerance) / r);
@@ -40,26 +41,27 @@ __device__ __forceinline__ float arc_step(const ArcState& a, float tolerance) {
 // ARC_TOO_LONG past the segment bound (the arc then fails with LYON_ERR_UNSUPPORTED).
 constexpr uint32_t ARC_TOO_LONG = 0xFFFFFFFFu;
 __device__ uint32_t walk_arc(const lyon_arc& in, float tolerance, float2* pts, float* ts) {
-    const ArcState arc{in.center_x, in.center_y, in.radius_x, in.radius_y,
-                       in.start_angle, in.sweep_angle, in.x_rotation};
+    const ArcState arc{in.center_x, in.center_y, in.radius_x, in.radius_y, in.start_angle,
+                       in.sweep_angle, dcos(in.x_rotation), dsin(in.x_rotation)};
     ArcState it = arc;
     float t0 = 0.0f;
-    uint32_t k = 0;
+    float2 from = arc_sample(arc, 0.0f);
     if (pts) {
-        pts[0] = arc_sample(arc, 0.0f);
+        pts[0] = from;
         ts[0] = 0.0f;
     }
-    k = 1;
+    uint32_t k = 1;
     for (;;) {
-        const float step = arc_step(it, tolerance);
+        const float step = arc_step(it, from, tolerance);
         if (step >= 1.0f) break;
         if (k > LYON_MAX_ARC_SEGMENTS) return ARC_TOO_LONG;
         const float split = it.sweep * step;  // after_split (arc.rs:286-296)
         it.start = it.start + split;
         it.sweep = it.sweep - split;
         const float t1 = t0 + step * (1.0f - t0);
+        from = arc_sample(it, 0.0f);
         if (pts) {
-            pts[k] = arc_sample(it, 0.0f);
+            pts[k] = from;
             ts[k] = t1;
         }
         ++k;

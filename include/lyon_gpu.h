@@ -270,8 +270,8 @@ typedef struct lyon_gpu_custom_output {
  * StrokeOptions::variable_line_width: -1 for a fixed line width, else the index of the attribute
  * that scales options.line_width. Writes positions, or lyon_stroke_vertex records when
  * `vertex_attributes` is non-zero, to `out` as lyon_gpu_stroke_paths does, and each vertex's
- * source and interpolated attributes to `custom`. Each path is stroked by one thread with lyon's
- * sequential stepper (both passes). */
+ * source and interpolated attributes to `custom`. The output pass strokes each path on one
+ * thread with lyon's sequential stepper (with a variable width, the count pass too). */
 int lyon_gpu_stroke_paths_custom(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                                  const float* attributes, uint32_t num_attributes,
                                  int32_t width_attribute, const lyon_stroke_options* options,

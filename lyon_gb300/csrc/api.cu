@@ -355,8 +355,8 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
     if (kind == KIND_STROKE) {
         // Long paths first, so that no single long path is left running at the end of a launch;
         // short line-only paths last, for the one-thread-per-path phase.
-        if (ctx->vw_widths || ctx->want_sources) {
-            // The sequential stepper takes paths in index order.
+        if (ctx->vw_widths) {
+            // The variable-width stepper takes paths in index order (both passes).
         } else if (n > 0 && ctx->short_path_points > 0) {
             if (ensure(ctx, ctx->order, (size_t)n * 4) && ensure(ctx, ctx->path_class, n) &&
                 ensure(ctx, ctx->class_counters, lg::CLASSIFY_COUNTER_WORDS * 4) &&

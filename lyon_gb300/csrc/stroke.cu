@@ -1262,8 +1262,11 @@ int stroke_blocks_per_sm() {
 
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream) {
     // Variable line width and the custom-attribute output use lyon's sequential stepper, one
-    // path per thread (stroke_seq.cu).
-    if (args.widths || args.sequential) return launch_stroke_seq(args, emit, grid, stream);
+    // path per thread (stroke_seq.cu). A fixed-width custom-attribute call counts with this
+    // file's warp kernel: both restate the same stroker, so the counts agree (and an emit pass
+    // that disagreed would flag its path LYON_ERR_INTERNAL, its writes bounded by the counts).
+    if (args.widths || (args.sequential && emit))
+        return launch_stroke_seq(args, emit, grid, stream);
     configure_smem();
     // The attribute output is its own instantiation, so the positions kernel carries none of
     // its work (the advancement chain, the record stores).

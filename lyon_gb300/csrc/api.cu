@@ -59,7 +59,7 @@ struct lyon_gpu_context {
     DevBuf src_counts, src_offsets, src_scratch, out_source_offsets;
     uint64_t total_sources = 0;
     // arc flattening
-    DevBuf arc_counts, arc_status, arc_offsets, arc_points, arc_t;
+    DevBuf arc_counts, arc_status, arc_offsets, arc_points, arc_t, arc_order;
     // the last lyon_gpu_query_sizes (for lyon_gpu_emit_into)
     struct {
         bool valid = false;
@@ -71,7 +71,7 @@ struct lyon_gpu_context {
     } query;
     // hatching
     DevBuf hatch_bound, hatch_edge_count, hatch_counts, hatch_status, hatch_offsets,
-        hatch_scratch, hatch_out;
+        hatch_scratch, hatch_out, hatch_order;
     DevBuf in_attrs;                    // single-path custom attributes (staged)
     HostBuf h_out_src, h_out_attrs, h_out_soff;
     // outputs of device-buffer batched calls
@@ -853,9 +853,11 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs,
                       &ctx->src_counts, &ctx->src_offsets, &ctx->src_scratch,
                       &ctx->out_source_offsets, &ctx->arc_counts, &ctx->arc_status,
-                      &ctx->arc_offsets, &ctx->arc_points, &ctx->arc_t, &ctx->hatch_bound,
+                      &ctx->arc_offsets, &ctx->arc_points, &ctx->arc_t, &ctx->arc_order,
+                      &ctx->hatch_bound,
                       &ctx->hatch_edge_count, &ctx->hatch_counts, &ctx->hatch_status,
-                      &ctx->hatch_offsets, &ctx->hatch_scratch, &ctx->hatch_out};
+                      &ctx->hatch_offsets, &ctx->hatch_scratch, &ctx->hatch_out,
+                      &ctx->hatch_order};
     for (DevBuf* b : bufs) free_buf(*b);
     lg::fill_free(ctx->fill);
     HostBuf* hb[] = {&ctx->h_verbs, &ctx->h_points, &ctx->h_out_v,  &ctx->h_out_i,
@@ -1473,17 +1475,31 @@ int hatch_impl(lyon_gpu_context* ctx, const lyon_path_batch* batch,
     uint64_t edges = 0, total = 0;
     int r = scan_counts(ctx, a.edge_bound, scr_off, tmp_off, n, &edges);
     if (r != LYON_OK) return r;
-    if (!ensure(ctx, ctx->hatch_scratch, edges * 16 * 3 + 16)) return LYON_ERR_OUT_OF_MEMORY;
+    if (!ensure(ctx, ctx->hatch_scratch, edges * 16 * 3 + 16) ||
+        !ensure(ctx, ctx->hatch_order, (size_t)n * 5 + lg::SIZE_ORDER_BINS * 8 + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
     a.scratch_offsets = scr_off;
     a.scratch_total = edges;
     a.scratch = ctx->hatch_scratch.ptr;
-    if (!set_err(ctx, "hatch count", lg::launch_hatch(a, 1, ctx->num_sms, s)))
+    // One thread per path: both passes take the paths largest first (by edge count, then by
+    // output count), so that the 32 paths of a warp take similar times.
+    uint32_t* order = as<uint32_t>(ctx->hatch_order);
+    uint32_t* counters = order + n;
+    uint8_t* cls = reinterpret_cast<uint8_t*>(counters + 2 * lg::SIZE_ORDER_BINS);
+    a.order = order;
+    if (!set_err(ctx, "hatch order",
+                 lg::launch_size_order(nullptr, n, cls, order, counters, s, a.edge_bound)) ||
+        !set_err(ctx, "hatch count", lg::launch_hatch(a, 1, ctx->num_sms, s)))
         return LYON_ERR_CUDA;
     r = scan_counts(ctx, a.counts, out_off, tmp_off, n, &total);
     if (r != LYON_OK) return r;
     const size_t rec = dots ? sizeof(lyon_dot) : sizeof(lyon_hatch_segment);
     if (!ensure(ctx, ctx->hatch_out, total * rec + 16)) return LYON_ERR_OUT_OF_MEMORY;
     a.out_offsets = out_off;
+    if (total > 0 &&
+        !set_err(ctx, "hatch order",
+                 lg::launch_size_order(nullptr, n, cls, order, counters, s, a.counts)))
+        return LYON_ERR_CUDA;
     a.segments = reinterpret_cast<lyon_hatch_segment*>(ctx->hatch_out.ptr);
     a.dot_out = reinterpret_cast<lyon_dot*>(ctx->hatch_out.ptr);
     if (total > 0 && !set_err(ctx, "hatch emit", lg::launch_hatch(a, 2, ctx->num_sms, s)))
@@ -1523,11 +1539,24 @@ int lyon_gpu_flatten_arcs(lyon_gpu_context* ctx, const lyon_arc* arcs, uint32_t 
         return LYON_ERR_OUT_OF_MEMORY;
     uint64_t* offs = as<uint64_t>(ctx->arc_offsets);
     uint64_t total = 0;
+    if (!ensure(ctx, ctx->arc_order, (size_t)n * 5 + lg::SIZE_ORDER_BINS * 8 + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    // Both passes take the arcs largest first (the count pass by an estimate, the emit pass by
+    // the counts), so that the 32 arcs of a warp take similar numbers of steps.
+    uint32_t* order = as<uint32_t>(ctx->arc_order);
+    uint32_t* counters = order + n;
+    uint8_t* cls = reinterpret_cast<uint8_t*>(counters + 2 * lg::SIZE_ORDER_BINS);
     if (n > 0) {
-        if (!set_err(ctx, "arcs count",
+        if (!set_err(ctx, "arcs estimate",
+                     lg::launch_arcs_estimate(arcs, n, tolerance, as<uint32_t>(ctx->arc_counts),
+                                              ctx->num_sms, s)) ||
+            !set_err(ctx, "arcs order",
+                     lg::launch_size_order(nullptr, n, cls, order, counters, s,
+                                           as<uint32_t>(ctx->arc_counts))) ||
+            !set_err(ctx, "arcs count",
                      lg::launch_arcs(arcs, n, tolerance, as<uint32_t>(ctx->arc_counts),
                                      as<int32_t>(ctx->arc_status), nullptr, nullptr, nullptr,
-                                     ctx->num_sms, s)))
+                                     ctx->num_sms, s, order)))
             return LYON_ERR_CUDA;
         uint32_t* sw = small_words(ctx);
         cudaMemsetAsync(sw + 2, 0, 4, s);
@@ -1553,10 +1582,13 @@ int lyon_gpu_flatten_arcs(lyon_gpu_context* ctx, const lyon_arc* arcs, uint32_t 
         !ensure(ctx, ctx->arc_t, total * 4 + 16))
         return LYON_ERR_OUT_OF_MEMORY;
     if (n > 0 && total > 0 &&
-        !set_err(ctx, "arcs emit",
-                 lg::launch_arcs(arcs, n, tolerance, nullptr, as<int32_t>(ctx->arc_status), offs,
-                                 as<float>(ctx->arc_points), as<float>(ctx->arc_t), ctx->num_sms,
-                                 s)))
+        (!set_err(ctx, "arcs order",
+                  lg::launch_size_order(nullptr, n, cls, order, counters, s,
+                                        as<uint32_t>(ctx->arc_counts))) ||
+         !set_err(ctx, "arcs emit",
+                  lg::launch_arcs(arcs, n, tolerance, nullptr, as<int32_t>(ctx->arc_status),
+                                  offs, as<float>(ctx->arc_points), as<float>(ctx->arc_t),
+                                  ctx->num_sms, s, order))))
         return LYON_ERR_CUDA;
     out->points = as<float>(ctx->arc_points);
     out->t = as<float>(ctx->arc_t);

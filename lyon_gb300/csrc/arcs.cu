@@ -23,7 +23,10 @@ struct ArcState {
 // sample (arc.rs:194-197): center + Rotation2D(x_rotation) applied to (rx cos a, ry sin a).
 __device__ __forceinline__ float2 arc_sample(const ArcState& a, float t) {
     const float angle = a.start + a.sweep * t;
-    const float ex = a.rx * dcos(angle), ey = a.ry * dsin(angle);
+    // cos and sin of the angle in f64 from one shared argument reduction, each rounded once.
+    double sd, cd;
+    sincos((double)angle, &sd, &cd);
+    const float ex = a.rx * (float)cd, ey = a.ry * (float)sd;
     return make_float2(a.cx + (ex * a.rc - ey * a.rs), a.cy + (ex * a.rs + ey * a.rc));
 }
 
@@ -74,21 +77,38 @@ __device__ uint32_t walk_arc(const lyon_arc& in, float tolerance, float2* pts, f
     return k + 1;
 }
 
+// A rough step count (f32, mean radius) that only orders the count pass.
+__global__ void __launch_bounds__(256) arcs_estimate_kernel(const lyon_arc* arcs, uint32_t n,
+                                                            float tolerance, uint32_t* est) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const lyon_arc a = arcs[i];
+        const float r = 0.5f * (fabsf(a.radius_x) + fabsf(a.radius_y));
+        const float c = fminf(fmaxf((r - tolerance) / r, -1.0f), 1.0f);
+        const float step = 2.0f * acosf(c);
+        const float k = fabsf(a.sweep_angle) / fmaxf(step, 1e-7f);
+        est[i] = k == k ? (uint32_t)fminf(k + 1.0f, 4.0e6f) : 1u;
+    }
+}
+
 __global__ void __launch_bounds__(256) arcs_count_kernel(const lyon_arc* arcs, uint32_t n,
                                                          float tolerance, uint32_t* counts,
-                                                         int32_t* status) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+                                                         int32_t* status, const uint32_t* order) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t i = order ? order[j] : j;
         const uint32_t k = walk_arc(arcs[i], tolerance, nullptr, nullptr);
         counts[i] = k == ARC_TOO_LONG ? 0u : k;
         status[i] = k == ARC_TOO_LONG ? LYON_ERR_UNSUPPORTED : LYON_OK;
     }
 }
 
+// Arcs in decreasing size class (`order`), so that the 32 arcs of a warp take similar numbers of
+// steps.
 __global__ void __launch_bounds__(256) arcs_emit_kernel(const lyon_arc* arcs, uint32_t n,
                                                         float tolerance, const int32_t* status,
                                                         const uint64_t* offsets, float2* pts,
-                                                        float* ts) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+                                                        float* ts, const uint32_t* order) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t i = order ? order[k] : k;
         if (status[i] != LYON_OK) continue;
         const uint64_t o = offsets[i];
         walk_arc(arcs[i], tolerance, pts + o, ts + o);
@@ -99,17 +119,27 @@ __global__ void __launch_bounds__(256) arcs_emit_kernel(const lyon_arc* arcs, ui
 
 cudaError_t launch_arcs(const lyon_arc* arcs, uint32_t n, float tolerance, uint32_t* counts,
                         int32_t* status, const uint64_t* offsets, float* pts, float* ts,
-                        int num_sms, cudaStream_t stream) {
+                        int num_sms, cudaStream_t stream, const uint32_t* order) {
     if (n == 0) return cudaSuccess;
     const uint32_t need = (n + 255) / 256;
     const uint32_t cap = (uint32_t)(num_sms > 0 ? num_sms : 1) * 8;
     const uint32_t grid = need < cap ? need : cap;
     if (pts) {
         arcs_emit_kernel<<<grid, 256, 0, stream>>>(arcs, n, tolerance, status, offsets,
-                                                   reinterpret_cast<float2*>(pts), ts);
+                                                   reinterpret_cast<float2*>(pts), ts, order);
     } else {
-        arcs_count_kernel<<<grid, 256, 0, stream>>>(arcs, n, tolerance, counts, status);
+        arcs_count_kernel<<<grid, 256, 0, stream>>>(arcs, n, tolerance, counts, status, order);
     }
+    note_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_arcs_estimate(const lyon_arc* arcs, uint32_t n, float tolerance,
+                                 uint32_t* est, int num_sms, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t need = (n + 255) / 256;
+    const uint32_t cap = (uint32_t)(num_sms > 0 ? num_sms : 1) * 8;
+    arcs_estimate_kernel<<<need < cap ? need : cap, 256, 0, stream>>>(arcs, n, tolerance, est);
     note_launches(1);
     return cudaGetLastError();
 }

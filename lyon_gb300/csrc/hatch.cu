@@ -248,8 +248,9 @@ struct Sweep {
 
 // Step 2: edges built and sorted in the path's scratch; outputs counted.
 __global__ void hatch_count_kernel(HatchArgs A) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < A.num_paths;
-         p += gridDim.x * blockDim.x) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < A.num_paths;
+         j += gridDim.x * blockDim.x) {
+        const uint32_t p = A.order ? A.order[j] : j;
         const uint64_t so = A.scratch_offsets[p];
         const uint32_t cap = (uint32_t)(A.scratch_offsets[p + 1] - so);
         HEdge* edges = reinterpret_cast<HEdge*>(A.scratch) + so;
@@ -311,8 +312,9 @@ __global__ void hatch_count_kernel(HatchArgs A) {
 
 // Step 3: the sweep over the sorted edges again, writing.
 __global__ void hatch_emit_kernel(HatchArgs A) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < A.num_paths;
-         p += gridDim.x * blockDim.x) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < A.num_paths;
+         j += gridDim.x * blockDim.x) {
+        const uint32_t p = A.order ? A.order[j] : j;
         if (A.status[p] != LYON_OK || A.counts[p] == 0) continue;
         const uint64_t so = A.scratch_offsets[p];
         HEdge* edges = reinterpret_cast<HEdge*>(A.scratch) + so;

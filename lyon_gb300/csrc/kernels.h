@@ -116,6 +116,7 @@ struct HatchArgs {
     uint32_t* counts;                // phase 1 output
     int32_t* status;                 // phase 1 output
     const uint64_t* out_offsets;     // phase 2 input
+    const uint32_t* order;           // phases 1 and 2: paths largest first (null: index order)
     lyon_hatch_segment* segments;    // phase 2 output (hatches)
     lyon_dot* dot_out;               // phase 2 output (dots)
 };
@@ -123,9 +124,13 @@ struct HatchArgs {
 cudaError_t launch_hatch(const HatchArgs& args, int phase, int num_sms, cudaStream_t stream);
 
 // Arc flattening (arcs.cu): count pass (pts null: counts and status) or emit pass.
+// Both passes take the arcs in `order` (null: index order).
 cudaError_t launch_arcs(const lyon_arc* arcs, uint32_t n, float tolerance, uint32_t* counts,
                         int32_t* status, const uint64_t* offsets, float* pts, float* ts,
-                        int num_sms, cudaStream_t stream);
+                        int num_sms, cudaStream_t stream, const uint32_t* order = nullptr);
+// A rough per-arc step count, to order the count pass.
+cudaError_t launch_arcs_estimate(const lyon_arc* arcs, uint32_t n, float tolerance,
+                                 uint32_t* est, int num_sms, cudaStream_t stream);
 
 // Exclusive scan of two u32 arrays into two u64 arrays (decoupled look-back), plus totals at
 // out_a[n] / out_b[n]. `tile_state` holds 2 * num_tiles(n) u64 and `counter` one u32; both are
@@ -166,8 +171,10 @@ cudaError_t launch_classify_paths(const uint8_t* verbs, const uint32_t* verb_off
 // work queues whose last items should be the cheap ones. `cls` holds one byte per path,
 // `counters` 2 * SIZE_ORDER_BINS words; both are scratch.
 constexpr uint32_t SIZE_ORDER_BINS = 33;
+// With `sizes`, the items' sizes are read from it instead of point_offsets differences.
 cudaError_t launch_size_order(const uint32_t* point_offsets, uint32_t n, uint8_t* cls,
-                              uint32_t* order, uint32_t* counters, cudaStream_t s);
+                              uint32_t* order, uint32_t* counters, cudaStream_t s,
+                              const uint32_t* sizes = nullptr);
 
 // Processing order for a batch: paths with more than `big_points` points first (their work can
 // exceed the rest of a launch), then the others. `counters` holds two u32 and is reset here.

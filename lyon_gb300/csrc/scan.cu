@@ -277,14 +277,14 @@ __global__ void classify_place_kernel(const uint8_t* path_class, uint32_t n,
 }
 
 // Order by size: bin 31 - floor(log2(points)) (0 points: bin 32), so bigger paths come first.
-__global__ void size_count_kernel(const uint32_t* point_offsets, uint32_t n, uint8_t* cls,
-                                  uint32_t* counters) {
+__global__ void size_count_kernel(const uint32_t* point_offsets, const uint32_t* sizes,
+                                  uint32_t n, uint8_t* cls, uint32_t* counters) {
     __shared__ uint32_t hist[SIZE_ORDER_BINS];
     for (uint32_t b = threadIdx.x; b < SIZE_ORDER_BINS; b += blockDim.x) hist[b] = 0;
     __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        const uint32_t pts = point_offsets[i + 1] - point_offsets[i];
+        const uint32_t pts = sizes ? sizes[i] : point_offsets[i + 1] - point_offsets[i];
         const uint32_t c = pts == 0 ? 32u : (uint32_t)__clz(pts);
         cls[i] = (uint8_t)c;
         atomicAdd(&hist[c], 1u);
@@ -321,11 +321,12 @@ __global__ void size_place_kernel(const uint8_t* cls, uint32_t n, uint32_t* orde
 }
 
 cudaError_t launch_size_order(const uint32_t* point_offsets, uint32_t n, uint8_t* cls,
-                              uint32_t* order, uint32_t* counters, cudaStream_t s) {
+                              uint32_t* order, uint32_t* counters, cudaStream_t s,
+                              const uint32_t* sizes) {
     cudaMemsetAsync(counters, 0, 2 * SIZE_ORDER_BINS * sizeof(uint32_t), s);
     if (n == 0) return cudaGetLastError();
     const uint32_t blocks = (n + 255) / 256;
-    size_count_kernel<<<blocks, 256, 0, s>>>(point_offsets, n, cls, counters);
+    size_count_kernel<<<blocks, 256, 0, s>>>(point_offsets, sizes, n, cls, counters);
     note_launches(1);
     size_place_kernel<<<blocks, 256, 0, s>>>(cls, n, order, counters);
     note_launches(1);

@@ -417,6 +417,9 @@ def run_fill(ctx, args, T, world, batch=None):
         ctx.synchronize()
         steps = max(1, args.steps)
         sweep_ms, phases = [], []
+        # Phase events on: the end-to-end leg switches them off, and without them the
+        # context's last timings would still be another call's.
+        ctx.lib.lyon_gpu_set_timing(ctx.h, 1)
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
         launches0 = ctx.lib.lyon_gpu_kernel_launches()

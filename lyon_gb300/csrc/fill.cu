@@ -1,11 +1,12 @@
-// fill.cu — batched fill tessellation: lyon's sweep-line FillTessellator, one thread per path.
+// fill.cu — batched fill tessellation: lyon's sweep-line FillTessellator, one thread per path
+// (several per warp).
 //
 // Pipeline (per batched call):
-//   1. fill_sweep_kernel: a persistent grid of threads takes paths from an atomic counter. Each
-//      thread builds the path's event queue (event_queue.rs:441-905: downward-oriented edges,
-//      curves flattened with their t ranges, vertex events at local maxima), sorts it with lyon's
-//      linked-list merge sort (event_queue.rs:301-384, same recursion so equal positions form the
-//      same sibling chains), runs the sweep (fill.rs:749-2151) and the monotone tessellators
+//   1. fill_sweep_kernel: a persistent grid of sweeper threads (several per warp) takes paths
+//      from an atomic counter. Each sweeper builds the path's event queue (event_queue.rs:
+//      441-905: downward-oriented edges, curves flattened with their t ranges, vertex events
+//      at local maxima), sorts it with lyon's linked-list merge sort (event_queue.rs:301-384,
+//      same recursion so equal positions form the same sibling chains), runs the sweep (fill.rs:749-2151) and the monotone tessellators
 //      (monotone.rs), writing vertices and triangles (path-relative ids) into its private heap;
 //      at the end it reserves room in a staging pool with one atomic add and copies them there.
 //   2. the caller's index-range check and look-back scan turn the per-path counts into offsets;
@@ -14,6 +15,7 @@
 // A path whose heap or staging room ran out is re-run, alone with the other such paths, with
 // more room; after the last attempt it fails with LYON_ERR_CAPACITY.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -32,8 +34,16 @@ constexpr int32_t STATUS_RETRY = -1;
 #ifndef LG_FILL_MIN_BLOCKS
 #define LG_FILL_MIN_BLOCKS 32
 #endif
-// One sweeper per 32-thread block (its first lane runs the path).
+#ifndef LG_FILL_LANES
+#define LG_FILL_LANES 8
+#endif
+// 32-thread blocks per SM; the first `lanes` threads of each block are sweepers, each with its
+// own path and heap (LYON_GB300_FILL_LANES overrides the default lane count, 1 to 32). On
+// 200,000 glyph paths the non-zero sweep took 1800 / 1717 / 1551 / 1643 / 2400 ms with 1 / 4 /
+// 8 / 16 / 32 lanes: diverged lanes run one after another, so more than 8 loses again.
 constexpr uint32_t FILL_SWEEPERS_PER_SM = LG_FILL_SWEEPERS_PER_SM;
+// Heaps of all sweepers together stay under this many bytes (fewer blocks when larger).
+constexpr size_t FILL_HEAP_POOL_BYTES = 16ull << 30;
 
 struct SweepArgs {
     const uint8_t* verbs;
@@ -44,6 +54,7 @@ struct SweepArgs {
     uint32_t num_options;
     const uint32_t* order;  // null: item = path
     uint32_t num_items;
+    uint32_t lanes;         // sweepers per block (its first threads)
     uint32_t* counters;     // [0] work, [1] retry count, [2] paths whose heap ran out
     unsigned long long* stage_tops;  // [0] vertices, [1] indices
     uint32_t* heaps;
@@ -67,10 +78,11 @@ struct SweepArgs {
 
 template <bool SRC>
 __global__ void __launch_bounds__(32, LG_FILL_MIN_BLOCKS) fill_sweep_kernel(SweepArgs A) {
-    // One path per block of one warp, run by its first lane: the sweep's control flow depends on
-    // the path, and 32 different paths in one warp would run one after the other anyway.
-    if (threadIdx.x != 0) return;
-    const uint32_t wid = blockIdx.x;
+    // Each of the block's first `lanes` threads sweeps its own paths with its own heap. The
+    // sweep's control flow depends on the path, so lanes diverge; where they run the same code
+    // (the event loop's common steps) one instruction fetch serves several paths.
+    if (threadIdx.x >= A.lanes) return;
+    const uint32_t wid = blockIdx.x * A.lanes + threadIdx.x;
     FillerT<SRC> f;
     f.h.w = A.heaps + (size_t)wid * A.heap_words;
     f.h.cap = A.heap_words;
@@ -269,12 +281,17 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         cudaSuccess)
         order = lists[1];
     uint32_t items = n;
+    uint32_t lanes = LG_FILL_LANES;
+    if (const char* env = getenv("LYON_GB300_FILL_LANES")) {
+        const long v = strtol(env, nullptr, 10);
+        if (v >= 1 && v <= 32) lanes = (uint32_t)v;
+    }
     const int MAX_ATTEMPTS = 4;
     for (int attempt = 0; attempt < MAX_ATTEMPTS; ++attempt) {
         uint32_t nthreads = threads;
-        size_t heap_bytes = (size_t)fb.heap_words * 4 * nthreads;
-        // Keep the heaps under 8 GB: fewer threads when each heap is large.
-        while (heap_bytes > (8ull << 30) && nthreads > 4) {
+        size_t heap_bytes = (size_t)fb.heap_words * 4 * nthreads * lanes;
+        // Keep the heaps under the pool size: fewer blocks when each heap is large.
+        while (heap_bytes > fillk::FILL_HEAP_POOL_BYTES && nthreads > 4) {
             nthreads /= 2;
             heap_bytes /= 2;
         }
@@ -292,6 +309,7 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         a.num_options = num_options;
         a.order = order;
         a.num_items = items;
+        a.lanes = lanes;
         a.counters = counters;
         a.stage_tops = tops;
         a.heaps = reinterpret_cast<uint32_t*>(fb.scratch);

@@ -6,9 +6,10 @@
 //      from an atomic counter. Each sweeper builds the path's event queue (event_queue.rs:
 //      441-905: downward-oriented edges, curves flattened with their t ranges, vertex events
 //      at local maxima), sorts it with lyon's linked-list merge sort (event_queue.rs:301-384,
-//      same recursion so equal positions form the same sibling chains), runs the sweep (fill.rs:749-2151) and the monotone tessellators
-//      (monotone.rs), writing vertices and triangles (path-relative ids) into its private heap;
-//      at the end it reserves room in a staging pool with one atomic add and copies them there.
+//      same recursion so equal positions form the same sibling chains), runs the sweep
+//      (fill.rs:749-2151) and the monotone tessellators (monotone.rs), writing vertices and
+//      triangles (path-relative ids) into its private heap; at the end it reserves room in a
+//      staging pool with one atomic add and copies them there.
 //   2. the caller's index-range check and look-back scan turn the per-path counts into offsets;
 //   3. fill_emit_kernel: one warp per path copies the staged vertices to their final place and
 //      the indices with the path's id base added (u16 or u32).

@@ -30,10 +30,10 @@ namespace fillk {
 constexpr int32_t STATUS_RETRY = -1;
 
 #ifndef LG_FILL_SWEEPERS_PER_SM
-#define LG_FILL_SWEEPERS_PER_SM 32
+#define LG_FILL_SWEEPERS_PER_SM 20
 #endif
 #ifndef LG_FILL_MIN_BLOCKS
-#define LG_FILL_MIN_BLOCKS 32
+#define LG_FILL_MIN_BLOCKS 20
 #endif
 #ifndef LG_FILL_LANES
 #define LG_FILL_LANES 8
@@ -41,7 +41,9 @@ constexpr int32_t STATUS_RETRY = -1;
 // 32-thread blocks per SM; the first `lanes` threads of each block are sweepers, each with its
 // own path and heap (LYON_GB300_FILL_LANES overrides the default lane count, 1 to 32). On
 // 200,000 glyph paths the non-zero sweep took 1800 / 1717 / 1551 / 1643 / 2400 ms with 1 / 4 /
-// 8 / 16 / 32 lanes: diverged lanes run one after another, so more than 8 loses again.
+// 8 / 16 / 32 lanes at 32 blocks per SM (64 registers, small spills): diverged lanes run one
+// after another, so more than 8 loses again. 20 blocks per SM (96 registers, no spills) took
+// 1462 / 1491 / 1443 ms with 8 / 12 / 16 lanes; 8 lanes keep the heaps at 6.2 GB.
 constexpr uint32_t FILL_SWEEPERS_PER_SM = LG_FILL_SWEEPERS_PER_SM;
 // Heaps of all sweepers together stay under this many bytes (fewer blocks when larger).
 constexpr size_t FILL_HEAP_POOL_BYTES = 16ull << 30;

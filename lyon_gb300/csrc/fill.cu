@@ -39,7 +39,8 @@ constexpr int32_t STATUS_RETRY = -1;
 #define LG_FILL_LANES 8
 #endif
 // 32-thread blocks per SM; the first `lanes` threads of each block are sweepers, each with its
-// own path and heap (LYON_GB300_FILL_LANES overrides the default lane count, 1 to 32). On
+// own path and heap: up to LG_FILL_LANES when a launch has more paths than blocks, one lane
+// otherwise (LYON_GB300_FILL_LANES forces a lane count, 1 to 32, for every launch). On
 // 200,000 glyph paths the non-zero sweep took 1800 / 1717 / 1551 / 1643 / 2400 ms with 1 / 4 /
 // 8 / 16 / 32 lanes at 32 blocks per SM (64 registers, small spills): diverged lanes run one
 // after another, so more than 8 loses again. 20 blocks per SM (96 registers, no spills) took
@@ -284,14 +285,22 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         cudaSuccess)
         order = lists[1];
     uint32_t items = n;
-    uint32_t lanes = LG_FILL_LANES;
+    uint32_t max_lanes = LG_FILL_LANES;
+    bool forced = false;
     if (const char* env = getenv("LYON_GB300_FILL_LANES")) {
         const long v = strtol(env, nullptr, 10);
-        if (v >= 1 && v <= 32) lanes = (uint32_t)v;
+        if (v >= 1 && v <= 32) max_lanes = (uint32_t)v, forced = true;
     }
     const int MAX_ATTEMPTS = 4;
     for (int attempt = 0; attempt < MAX_ATTEMPTS; ++attempt) {
         uint32_t nthreads = threads;
+        // A lane shares its warp's issue slots with the other lanes, so a path on a shared warp
+        // takes longer than alone: lanes are added only when there are more paths than blocks
+        // (large batches, for throughput), never for a small launch (a served request, the
+        // retry of a few paths), whose latency is one path's sweep.
+        uint32_t lanes = forced ? max_lanes
+                                : std::max<uint32_t>(1u, std::min<uint32_t>(max_lanes,
+                                                                            items / nthreads));
         size_t heap_bytes = (size_t)fb.heap_words * 4 * nthreads * lanes;
         // Keep the heaps under the pool size: fewer blocks when each heap is large.
         while (heap_bytes > fillk::FILL_HEAP_POOL_BYTES && nthreads > 4) {

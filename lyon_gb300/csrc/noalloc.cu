@@ -30,7 +30,7 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = OFF_SCAN + 2 * SCAN_TILES_MAX * 8 + 256
 
 // The scratch array. In host code `noalloc_scratch` only names the symbol; its device address
 // comes from cudaGetSymbolAddress (once per device, below).
-__device__ __align__(256) unsigned char noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+static __device__ __align__(256) unsigned char noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
 constexpr int MAX_DEVICES = 64;
 

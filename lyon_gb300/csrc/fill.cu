@@ -30,21 +30,22 @@ namespace fillk {
 constexpr int32_t STATUS_RETRY = -1;
 
 #ifndef LG_FILL_SWEEPERS_PER_SM
-#define LG_FILL_SWEEPERS_PER_SM 20
+#define LG_FILL_SWEEPERS_PER_SM 16
 #endif
 #ifndef LG_FILL_MIN_BLOCKS
-#define LG_FILL_MIN_BLOCKS 20
+#define LG_FILL_MIN_BLOCKS 16
 #endif
 #ifndef LG_FILL_LANES
-#define LG_FILL_LANES 8
+#define LG_FILL_LANES 12
 #endif
 // 32-thread blocks per SM; the first `lanes` threads of each block are sweepers, each with its
-// own path and heap: up to LG_FILL_LANES when a launch has more paths than blocks, one lane
-// otherwise (LYON_GB300_FILL_LANES forces a lane count, 1 to 32, for every launch). On
+// own path and heap: as many lanes as the launch has paths per block (rounded down), between 1
+// and LG_FILL_LANES (LYON_GB300_FILL_LANES forces a lane count, 1 to 32, for every launch). On
 // 200,000 glyph paths the non-zero sweep took 1800 / 1717 / 1551 / 1643 / 2400 ms with 1 / 4 /
 // 8 / 16 / 32 lanes at 32 blocks per SM (64 registers, small spills): diverged lanes run one
-// after another, so more than 8 loses again. 20 blocks per SM (96 registers, no spills) took
-// 1462 / 1491 / 1443 ms with 8 / 12 / 16 lanes; 8 lanes keep the heaps at 6.2 GB.
+// after another, so more than 8 loses again. With 96 registers and no spills, 20 blocks per SM
+// took 1462 / 1491 / 1443 ms with 8 / 12 / 16 lanes, 24 blocks (80 registers) 1442 ms with 8,
+// and 16 blocks 1487 / 1310 ms with 8 / 12 lanes (192 sweepers per SM, 7.5 GB of heaps).
 constexpr uint32_t FILL_SWEEPERS_PER_SM = LG_FILL_SWEEPERS_PER_SM;
 // Heaps of all sweepers together stay under this many bytes (fewer blocks when larger).
 constexpr size_t FILL_HEAP_POOL_BYTES = 16ull << 30;
@@ -295,8 +296,8 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
     for (int attempt = 0; attempt < MAX_ATTEMPTS; ++attempt) {
         uint32_t nthreads = threads;
         // A lane shares its warp's issue slots with the other lanes, so a path on a shared warp
-        // takes longer than alone: lanes are added only when there are more paths than blocks
-        // (large batches, for throughput), never for a small launch (a served request, the
+        // takes longer than alone: lanes are added only when there are two or more paths per
+        // block (large batches, for throughput), never for a small launch (a served request, the
         // retry of a few paths), whose latency is one path's sweep.
         uint32_t lanes = forced ? max_lanes
                                 : std::max<uint32_t>(1u, std::min<uint32_t>(max_lanes,

@@ -2,8 +2,10 @@
 //
 // Every routine evaluates in f32 with the same operation order as lyon (the translation unit is
 // compiled with --fmad=false, so no multiply-add is fused), so positions computed here are
-// bit-identical to lyon's wherever only + - * / sqrt are involved. Transcendentals (atan2f,
-// cosf, sinf, acosf, log2f) use CUDA's accurate f32 functions.
+// bit-identical to lyon's wherever only + - * / sqrt are involved. Angles from vectors use
+// euclid's fast_atan2 polynomial, exactly as lyon does (pure f32 arithmetic); cosf, sinf,
+// acosf and log2f use CUDA's accurate f32 functions, and the few places where their last bit
+// could change a count are evaluated correctly rounded (see the call sites).
 #pragma once
 
 #include <cstdint>
@@ -38,14 +40,33 @@ __host__ __device__ __forceinline__ V2 lerp(V2 a, V2 b, float t) {
     float one_t = 1.0f - t;
     return V2{one_t * a.x + t * b.x, one_t * a.y + t * b.y};
 }
-__device__ __forceinline__ float angle_from_x_axis(V2 v) { return atan2f(v.y, v.x); }
 #define LG_PI_F 3.14159265358979323846f
-__device__ __forceinline__ float angle_to(float from, float to) {
-    const float two_pi = 2.0f * LG_PI_F;
-    float d = fmodf(to - from, two_pi);
-    if (d > LG_PI_F) d -= two_pi;
-    if (d < -LG_PI_F) d += two_pi;
-    return d;
+#define LG_FRAC_PI_2_F 1.57079632679489661923f
+// euclid 0.22.9 `Vector2D::angle_from_x_axis` = `Trig::fast_atan2(y, x)` (euclid src/trig.rs),
+// which lyon calls for join, cap and sharp-turn angles (stroke.rs:1812,1986-1987,2482-2483,3204).
+// Published method: the polynomial approximation of atan on [0, 1] from math.stackexchange.com
+// question 1098487 (answer 1105038), atan(a) ~ ((-0.0464964749 s + 0.15931422) s - 0.327622764)
+// s a + a with s = a^2 and a = min(|x|,|y|) / max(|x|,|y|), reflected into the octant of (x, y).
+// Only f32 + - * / and compares (no fused multiply-add in this build), so it rounds as lyon's.
+// (0, 0) gives NaN (0 / 0), as euclid's does.
+__host__ __device__ __forceinline__ float fast_atan2(float y, float x) {
+    const float x_abs = fabsf(x);
+    const float y_abs = fabsf(y);
+    const float a = fminf(x_abs, y_abs) / fmaxf(x_abs, y_abs);
+    const float s = a * a;
+    float r = ((-0.0464964749f * s + 0.15931422f) * s - 0.327622764f) * s * a + a;
+    if (y_abs > x_abs) r = LG_FRAC_PI_2_F - r;
+    if (x < 0.0f) r = LG_PI_F - r;
+    if (y < 0.0f) r = -r;
+    return r;
+}
+__host__ __device__ __forceinline__ float angle_from_x_axis(V2 v) { return fast_atan2(v.y, v.x); }
+// euclid 0.22.9 `Angle::angle_to` (euclid src/angle.rs): d = (to - from) % max, then
+// (2 d) % max - d with max = PI * 2 and the exact float remainder (fmodf).
+__host__ __device__ __forceinline__ float angle_to(float from, float to) {
+    const float max = LG_PI_F * 2.0f;
+    const float d = fmodf(to - from, max);
+    return fmodf(2.0f * d, max) - d;
 }
 __host__ __device__ __forceinline__ bool isnan_f(float v) { return v != v; }
 
@@ -159,9 +180,10 @@ static __device__ __noinline__ bool find_sharp_turn(V2 from, V2 ctrl, V2 to, flo
     } else {
         long_axis = baseline;
     }
-    // Correctly rounded f32 angle, sine and cosine (evaluated in f64, rounded once), as the
-    // oracle does: the split point feeds later integer decisions and must be bit-identical.
-    float angle = -(float)atan2((double)long_axis.y, (double)long_axis.x);
+    // Rotation2D::new(-long_axis.angle_from_x_axis()): euclid's fast_atan2, then the correctly
+    // rounded f32 sine and cosine (evaluated in f64, rounded once), as the oracle does: the split
+    // point feeds later integer decisions and must be bit-identical.
+    float angle = -angle_from_x_axis(long_axis);
     float s = (float)sin((double)angle), c = (float)cos((double)angle);
     float cx = v.x * c - v.y * s;
     float tx = baseline.x * c - baseline.y * s;

@@ -183,19 +183,23 @@ __device__ __forceinline__ void get_clip_intersections(V2 prev_n, V2 next_n, V2 
 }
 
 // Correctly rounded f32 transcendentals (f64 evaluation, one rounding).
-__device__ __forceinline__ float cr_atan2(float y, float x) { return (float)atan2((double)y, (double)x); }
 __device__ __forceinline__ float cr_acos(float x) { return (float)acos((double)x); }
 __device__ __forceinline__ float cr_cos(float x) { return (float)cos((double)x); }
 __device__ __forceinline__ float cr_sin(float x) { return (float)sin((double)x); }
 __device__ __forceinline__ float cr_asin(float x) { return (float)asin((double)x); }
 
-// An arc's subdivision count is ceil(|diff| / step) with diff from two atan2 values and step from
-// acos (stroke.rs:1986-2004, 2482-2490, 2749-2753). f32 libms differ by an ulp between
-// platforms, which can move the quotient across an integer; within this margin of an integer the
-// angles, step and quotient are re-evaluated correctly rounded, identically in the oracle.
-__device__ __forceinline__ bool arc_near_tie(float x, float step) {
-    float margin = 1e-3f + 4e-6f / step;
-    return fabsf(x - rintf(x)) < margin;
+// An arc's subdivision count is ceil(|diff| / step) (stroke.rs:1986-2004, 2482-2490, 2749-2753).
+// diff comes from fast_atan2 and angle_to, identical on every platform; step = 2 acos(..) from
+// an f32 libm whose last bit differs between platforms, which moves the quotient by an ulp or
+// two. Within 2e-6 (relative) of an integer, step is re-evaluated correctly rounded, as the
+// oracle does, so both take the same ceil (the oracle counts the quotients within 1e-6 of an
+// integer as near ties: lyon on another libm may round those the other way).
+__device__ __forceinline__ float arc_quotient(float adiff, float radius, float tol) {
+    const float t = fminf(tol, radius);
+    const float arg = (radius - t) / radius;
+    const float x = adiff / (2.0f * acosf(arg));
+    if (!(fabsf(x - rintf(x)) <= 2e-6f * fmaxf(1.0f, x))) return x;
+    return adiff / (2.0f * cr_acos(arg));
 }
 
 // round(log2(ceil(x))) as u32 (stroke.rs:2003-2004).
@@ -344,7 +348,6 @@ __device__ __forceinline__ uint32_t join_interior_tris(const DEP& j) {
 struct ArcPlan {
     float a0, a1;
     uint32_t depth;
-    bool cr;
 };
 
 static __device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side, float tol,
@@ -354,20 +357,10 @@ static __device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side
     V2 sn = join.s[side].prev - center;
     V2 en = join.s[side].next - center;
     float angle_sign = side == SN ? 1.0f : -1.0f;
-    bool cr = false;
-    float start_angle, diff, step;
-    for (;;) {
-        start_angle = cr ? cr_atan2(sn.y, sn.x) : angle_from_x_axis(sn);
-        float end_a = cr ? cr_atan2(en.y, en.x) : angle_from_x_axis(en);
-        diff = angle_to(start_angle, end_a);
-        if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * LG_PI_F - fabsf(diff));
-        float t = fminf(tol, radius);
-        float arg = (radius - t) / radius;
-        step = 2.0f * (cr ? cr_acos(arg) : acosf(arg));
-        if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
-        cr = true;
-    }
-    float end_angle = start_angle + diff;
+    const float start_angle = angle_from_x_axis(sn);
+    float diff = angle_to(start_angle, angle_from_x_axis(en));
+    if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * LG_PI_F - fabsf(diff));
+    const float end_angle = start_angle + diff;
     ArcPlan p;
     if (side == SN) {
         p.a0 = end_angle;
@@ -376,8 +369,7 @@ static __device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side
         p.a0 = start_angle;
         p.a1 = end_angle;
     }
-    p.cr = cr;
-    p.depth = depth_of(fabsf(diff) / step, status);
+    p.depth = depth_of(arc_quotient(fabsf(diff), radius, tol), status);
     return p;
 }
 
@@ -388,8 +380,7 @@ __device__ __forceinline__ uint32_t arc_vertex_count(uint32_t depth) {
 // stroke.rs:2612-2653 (pre-order recursion, made iterative with an explicit stack).
 template <class SK>
 __device__ __noinline__ void tessellate_arc(V2 center, float radius, float a0, float a1, uint32_t va,
-                                            uint32_t vb, uint32_t depth, bool cr, int side,
-                                            SK& sink) {
+                                            uint32_t vb, uint32_t depth, int side, SK& sink) {
     if (depth == 0) return;
     struct Frame {
         float a0, a1;
@@ -402,7 +393,7 @@ __device__ __noinline__ void tessellate_arc(V2 center, float radius, float a0, f
         Frame f = st[--sp];
         if (f.n == 0) continue;
         float mid = (f.a0 + f.a1) * 0.5f;
-        V2 normal = cr ? V2{cr_cos(mid), cr_sin(mid)} : V2{cosf(mid), sinf(mid)};
+        V2 normal = V2{cosf(mid), sinf(mid)};
         uint32_t vid = sink.vertex(center + normal * radius, normal, side);
         sink.tri(f.va, vid, f.vb);
         st[sp++] = Frame{mid, f.a1, vid, f.vb, f.n - 1};
@@ -514,7 +505,7 @@ __device__ __forceinline__ void tessellate_join(const DEP& j, const StrokeParams
             ArcPlan a = round_join_plan(j, side, P.tolerance, status);
             uint32_t va = side == SN ? j.s[side].next_vertex : j.s[side].prev_vertex;
             uint32_t vb = side == SN ? j.s[side].prev_vertex : j.s[side].next_vertex;
-            tessellate_arc(j.pos, j.hw, a.a0, a.a1, va, vb, a.depth, a.cr, side, sink);
+            tessellate_arc(j.pos, j.hw, a.a0, a.a1, va, vb, a.depth, side, sink);
         }
     }
 }
@@ -543,28 +534,17 @@ __device__ __noinline__ void tessellate_round_cap(V2 center, float radius, V2 st
                                                   int* status) {
     if (radius < P.tolerance) return;
     const int first_side = (is_start ^ (cross(edge_normal, start_normal) >= 0.0f)) ? SP : SN;
-    bool cr = false;
-    float start_angle, diff, step;
-    for (;;) {
-        start_angle = cr ? cr_atan2(start_normal.y, start_normal.x)
-                         : angle_from_x_axis(start_normal);
-        float edge_a = cr ? cr_atan2(edge_normal.y, edge_normal.x) : angle_from_x_axis(edge_normal);
-        diff = angle_to(start_angle, edge_a);
-        float t = fminf(P.tolerance, radius);
-        float arg = (radius - t) / radius;
-        step = 2.0f * (cr ? cr_acos(arg) : acosf(arg));
-        if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
-        cr = true;
-    }
-    float mid_angle = start_angle + diff;
-    float end_angle = mid_angle + diff;
-    uint32_t depth = depth_of(fabsf(diff) / step, status);
+    const float start_angle = angle_from_x_axis(start_normal);
+    const float diff = angle_to(start_angle, angle_from_x_axis(edge_normal));
+    const float mid_angle = start_angle + diff;
+    const float end_angle = mid_angle + diff;
+    const uint32_t depth = depth_of(arc_quotient(fabsf(diff), radius, P.tolerance), status);
     const V2 mid_normal = normalize(edge_normal);
     uint32_t mid_vertex = sink.vertex(center + mid_normal * radius, mid_normal, first_side);
     sink.tri(start_vertex, mid_vertex, end_vertex);
-    tessellate_arc(center, radius, start_angle, mid_angle, start_vertex, mid_vertex, depth, cr,
+    tessellate_arc(center, radius, start_angle, mid_angle, start_vertex, mid_vertex, depth,
                    first_side, sink);
-    tessellate_arc(center, radius, mid_angle, end_angle, mid_vertex, end_vertex, depth, cr,
+    tessellate_arc(center, radius, mid_angle, end_angle, mid_vertex, end_vertex, depth,
                    1 - first_side, sink);
 }
 
@@ -823,9 +803,9 @@ __device__ __noinline__ bool seq_step(SeqBuffer& pb, DEP next, const StrokeParam
 
 
 // ---- variable line width (StrokeOptions::variable_line_width) -------------------------------
-// One thread strokes a whole path with lyon's sequential variable-width stepper. The edge
-// attachment angles are evaluated in f64 with one rounding (cr_*), as in the oracle; lyon takes
-// them from the platform's f32 libm.
+// One thread strokes a whole path with lyon's sequential variable-width stepper. The edge angle
+// is euclid's fast_atan2, as lyon's; the attachment angles' asin/cos/sin are evaluated in f64
+// with one rounding (cr_*), as in the oracle (lyon takes them from the platform's f32 libm).
 
 struct VwState {
     SeqBuffer pb;
@@ -849,7 +829,7 @@ __device__ __forceinline__ void vw_side_attachment(DEP& p0, DEP& p1, float edge_
 static __device__ __noinline__ void vw_edge_attachments(DEP& p0, DEP& p1) {
     const V2 edge = p1.pos - p0.pos;
     const float d = vlength(edge);
-    const float edge_angle = cr_atan2(edge.y, edge.x);
+    const float edge_angle = angle_from_x_axis(edge);  // stroke.rs:1812
     const float sin_vwidth_angle = (p1.hw - p0.hw) / d;
     float vwidth_angle = cr_asin(sin_vwidth_angle);
     if (isnan(vwidth_angle)) vwidth_angle = 0.0f;

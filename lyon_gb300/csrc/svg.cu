@@ -5,10 +5,10 @@
 //
 // Strings are parsed on all host threads in two passes (sizes, then output at scanned offsets).
 // Arcs become quadratic béziers as lyon's SvgArc / Arc do (crates/geom/src/arc.rs:58-138,
-// 668-703), in f32 with the platform's libm. Two details differ from lyon and are stated where
-// they apply: `angle_from_x_axis` is atan2 (lyon takes it from euclid 0.22.9), and only ASCII
-// digits count as numeric (lyon accepts any Unicode numeric character into a number, which then
-// fails to parse).
+// 668-703), in f32 with the platform's libm; `angle_from_x_axis` is euclid 0.22.9's fast_atan2,
+// as lyon's. One detail differs from lyon and is stated where it applies: only ASCII digits count
+// as numeric (lyon accepts any Unicode numeric character into a number, which then fails to
+// parse).
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -141,7 +141,19 @@ Pt rotate(float angle, Pt v) {
     return Pt{v.x * c - v.y * s, v.x * s + v.y * c};
 }
 
-float angle_from_x_axis(Pt v) { return atan2f(v.y, v.x); }
+// euclid 0.22.9 `Vector2D::angle_from_x_axis` = `Trig::fast_atan2(y, x)` (euclid src/trig.rs):
+// the published polynomial approximation of atan on [0, 1] (math.stackexchange.com question
+// 1098487, answer 1105038), reflected into the octant of (x, y); f32, evaluated left to right.
+float angle_from_x_axis(Pt v) {
+    const float x_abs = fabsf(v.x), y_abs = fabsf(v.y);
+    const float a = fminf(x_abs, y_abs) / fmaxf(x_abs, y_abs);
+    const float s = a * a;
+    float r = ((-0.0464964749f * s + 0.15931422f) * s - 0.327622764f) * s * a + a;
+    if (y_abs > x_abs) r = 1.57079632679489661923f - r;
+    if (v.x < 0.0f) r = PI_F - r;
+    if (v.y < 0.0f) r = -r;
+    return r;
+}
 
 struct Arc {
     Pt center, radii;

@@ -11,12 +11,16 @@
 //   * f32 wherever lyon uses f32, f64 exactly where lyon converts to f64
 //     (stroke.rs:2169-2173,2243-2247,2285-2312; fill.rs:1634-1676);
 //   * f32 math functions (acosf, cosf, sinf, atan2f, log2f) from the platform libm, as Rust's std;
-//   * helpers that live in the third-party crate euclid 0.22.9 (not part of the lyon sources) are
-//     restated from their documented meaning: `normalize` = v / |v|, `lerp(a, b, t)` =
-//     a * (1 - t) + b * t, `angle_from_x_axis` = atan2(y, x), `angle_to` = shortest signed
-//     difference wrapped to [-pi, pi], `Rotation2D::transform_vector` = the usual rotation
-//     matrix. Their rounding relative to lyon is therefore not pinned; see the parity notes in
-//     the repository's design document.
+//   * helpers that live in the third-party crate euclid 0.22.9 (Cargo.lock:603-605; not part of
+//     the lyon sources) are restated from euclid's published source: `normalize` = v / |v|,
+//     `lerp(a, b, t)` = a * (1 - t) + b * t, `angle_from_x_axis` = euclid's `Trig::fast_atan2`
+//     (a degree-7 polynomial for atan on [0, 1], folded into the quadrants; see fast_atan2
+//     below), `Angle::angle_to` = `(2d) % 2pi - d` with `d = (to - from) % 2pi`,
+//     `Rotation2D::transform_vector` = (x cos - y sin, y cos + x sin). These use only + - * /
+//     and fmod, so they round exactly as lyon's calls do;
+//   * cos/sin/acos/asin with a count or a split point depending on their last bit are
+//     evaluated in f64 and rounded once (the correctly rounded f32 value, which the GPU
+//     reproduces), documented at each site.
 //
 // Where lyon would panic (an `assert!`, an `unwrap` of a NaN comparison) the oracle reports
 // LYON_ERR_INTERNAL for that path instead.
@@ -59,14 +63,35 @@ static inline P lerp(P a, P b, float t) {
     return P{one_t * a.x + t * b.x, one_t * a.y + t * b.y};
 }
 static inline P tangent(P v) { return P{-v.y, v.x}; }  // geom/src/utils.rs:15-17
-static inline float angle_from_x_axis(P v) { return atan2f(v.y, v.x); }
 static const float PI_F = 3.14159265358979323846f;
+static const float FRAC_PI_2_F = 1.57079632679489661923f;
+// euclid 0.22.9 `impl Trig for f32 { fn fast_atan2 }` (euclid src/trig.rs), which lyon reaches
+// through `Vector2D::angle_from_x_axis` (stroke.rs:1812,1986-1987,2482-2483,3204; arc.rs:129-131).
+// Published method: the polynomial approximation of atan(a) on [0, 1] given at
+// math.stackexchange.com/questions/1098487 (answer 1105038),
+//   atan(a) ~ ((-0.0464964749 s + 0.15931422) s - 0.327622764) s a + a,  s = a^2,
+// with a = min(|x|, |y|) / max(|x|, |y|), then reflected into the octant of (x, y). Evaluated
+// left to right in f32 without fused multiply-adds, as Rust evaluates it. (0, 0) gives NaN
+// (0 / 0), as euclid's does.
+static inline float fast_atan2(float y, float x) {
+    const float x_abs = fabsf(x);
+    const float y_abs = fabsf(y);
+    const float a = fminf(x_abs, y_abs) / fmaxf(x_abs, y_abs);
+    const float s = a * a;
+    float r = ((-0.0464964749f * s + 0.15931422f) * s - 0.327622764f) * s * a + a;
+    if (y_abs > x_abs) r = FRAC_PI_2_F - r;
+    if (x < 0.0f) r = PI_F - r;
+    if (y < 0.0f) r = -r;
+    return r;
+}
+static inline float angle_from_x_axis(P v) { return fast_atan2(v.y, v.x); }
+// euclid 0.22.9 `Angle::angle_to` (euclid src/angle.rs): the shortest signed angle, computed as
+// `d = (to - from) % max; (2 * d) % max - d` with `max = PI * 2` and Rust's float remainder
+// (C's fmodf: exact).
 static inline float angle_to(float from, float to) {
-    const float two_pi = 2.0f * PI_F;
-    float d = fmodf(to - from, two_pi);
-    if (d > PI_F) d -= two_pi;
-    if (d < -PI_F) d += two_pi;
-    return d;
+    const float max = PI_F * 2.0f;
+    const float d = fmodf(to - from, max);
+    return fmodf(2.0f * d, max) - d;
 }
 static inline bool is_nan_f(float v) { return v != v; }
 
@@ -575,17 +600,27 @@ static uint32_t depth_of(float x) {
     return d;
 }
 
-// The arc's subdivision count is ceil(|diff| / step), where diff comes from two atan2 values and
-// step from acos. Platform f32 libms differ by an ulp, which can move the quotient across an
-// integer. When the quotient lies within `arc_tie_margin` of an integer, the angles, the step and
-// the quotient are re-evaluated with correctly rounded f32 functions (f64 evaluation, one
-// rounding), so every platform — and the GPU — takes the same decision.
-static inline bool arc_near_tie(float x, float step) {
-    float margin = 1e-3f + 4e-6f / step;
-    return fabsf(x - rintf(x)) < margin;
-}
-static inline float cr_atan2(float y, float x) { return (float)atan2((double)y, (double)x); }
 static inline float cr_acos(float x) { return (float)acos((double)x); }
+
+// The arc's subdivision count is ceil(|diff| / step) (stroke.rs:2001-2004, 2487-2490). diff comes
+// from fast_atan2 and angle_to, which round identically everywhere; step = 2 acos(..) comes from
+// the platform's f32 libm, whose last bit varies between platforms, so the quotient can move by
+// an ulp or two. Where it lies within 2e-6 (relative) of an integer, step is re-evaluated
+// correctly rounded (f64 acos, one rounding; the GPU does the same), so both sides take the same
+// ceil. A quotient within 1e-6 (relative) of an integer is a near tie: lyon itself may round it
+// either way depending on its libm, so it is counted in `g_near_ties` (reported per path).
+static inline float arc_step(float radius, float tol) {  // stroke.rs:2749-2753
+    float t = fminf(tol, radius);
+    return 2.0f * acosf((radius - t) / radius);
+}
+static inline float arc_quotient(float adiff, float radius, float tol, float step) {
+    float x = adiff / step;
+    if (!(fabsf(x - rintf(x)) <= 2e-6f * fmaxf(1.0f, x))) return x;
+    float t = fminf(tol, radius);
+    float xc = adiff / (2.0f * cr_acos((radius - t) / radius));
+    if (rintf(xc) >= 1.0f && fabsf(xc - rintf(xc)) <= 1e-6f * fmaxf(1.0f, xc)) ++g_near_ties;
+    return xc;
+}
 static inline float cr_cos(float x) { return (float)cos((double)x); }
 static inline float cr_sin(float x) { return (float)sin((double)x); }
 static inline float cr_asin(float x) { return (float)asin((double)x); }
@@ -658,16 +693,15 @@ struct Stroker {
         if (p0_neg != p1_neg && p1_pos != p1_neg) out->add_triangle(p0_neg, p1_pos, p1_neg);
     }
 
-    // stroke.rs:2612-2653. `cr` selects correctly rounded cos/sin (arcs decided on a near tie).
-    void tessellate_arc(float a0, float a1, uint32_t va, uint32_t vb, uint32_t n, bool cr) {
+    // stroke.rs:2612-2653
+    void tessellate_arc(float a0, float a1, uint32_t va, uint32_t vb, uint32_t n) {
         if (n == 0) return;
         float mid_angle = (a0 + a1) * 0.5f;
-        vertex.normal = cr ? P{cr_cos(mid_angle), cr_sin(mid_angle)}
-                           : P{cosf(mid_angle), sinf(mid_angle)};
+        vertex.normal = P{cosf(mid_angle), sinf(mid_angle)};
         uint32_t vid = add_stroke_vertex();
         out->add_triangle(va, vid, vb);
-        tessellate_arc(a0, mid_angle, va, vid, n - 1, cr);
-        tessellate_arc(mid_angle, a1, vid, vb, n - 1, cr);
+        tessellate_arc(a0, mid_angle, va, vid, n - 1);
+        tessellate_arc(mid_angle, a1, vid, vb, n - 1);
     }
 
     // stroke.rs:1968-2021
@@ -679,27 +713,19 @@ struct Stroker {
         uint32_t start_vertex = join.side[side].prev_vertex;
         uint32_t end_vertex = join.side[side].next_vertex;
         float angle_sign = side == SIDE_NEGATIVE ? 1.0f : -1.0f;
-        bool cr = false;
-        float start_angle, diff, step;
-        for (;;) {
-            start_angle = cr ? cr_atan2(start_normal.y, start_normal.x)
-                             : angle_from_x_axis(start_normal);
-            float end_a = cr ? cr_atan2(end_normal.y, end_normal.x) : angle_from_x_axis(end_normal);
-            diff = angle_to(start_angle, end_a);
-            if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * PI_F - fabsf(diff));
-            float tol = fminf(options.tolerance, radius);
-            step = 2.0f * (cr ? cr_acos((radius - tol) / radius) : acosf((radius - tol) / radius));
-            if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
-            cr = true;
-        }
+        float start_angle = angle_from_x_axis(start_normal);
+        float diff = angle_to(start_angle, angle_from_x_axis(end_normal));
+        if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * PI_F - fabsf(diff));
         float end_angle = start_angle + diff;
         if (side == SIDE_NEGATIVE) {
             std::swap(start_angle, end_angle);
             std::swap(start_vertex, end_vertex);
         }
-        uint32_t num_subdivisions = depth_of(fabsf(diff) / step);
+        float step = arc_step(radius, options.tolerance);
+        uint32_t num_subdivisions =
+            depth_of(arc_quotient(fabsf(diff), radius, options.tolerance, step));
         vertex.side = side;
-        tessellate_arc(start_angle, end_angle, start_vertex, end_vertex, num_subdivisions, cr);
+        tessellate_arc(start_angle, end_angle, start_vertex, end_vertex, num_subdivisions);
     }
 
     // stroke.rs:1907-1965
@@ -911,9 +937,10 @@ struct Stroker {
     }
 
     // ---- Variable line width (StrokeOptions::variable_line_width) --------------------------
-    // The edge's attachment angles use atan2/asin/cos/sin; lyon takes them from the platform's
-    // f32 libm, whose last bit varies between platforms. Here (and on the GPU) they are
-    // evaluated in f64 and rounded once, so both sides agree bit for bit.
+    // The edge's angle is euclid's fast_atan2 (exact f32 arithmetic); the attachment angles'
+    // asin/cos/sin come from the platform's f32 libm in lyon, whose last bit varies between
+    // platforms. Here (and on the GPU) those are evaluated in f64 and rounded once, so both sides
+    // agree bit for bit.
 
     // stroke.rs:1842-1866
     static void compute_side_attachment_positions(EndpointData& p0, EndpointData& p1,
@@ -930,7 +957,7 @@ struct Stroker {
     static void compute_edge_attachment_positions(EndpointData& p0, EndpointData& p1) {
         P edge = sub(p1.position, p0.position);
         float d = length(edge);
-        float edge_angle = cr_atan2(edge.y, edge.x);
+        float edge_angle = angle_from_x_axis(edge);  // stroke.rs:1812
         float sin_vwidth_angle = (p1.half_width - p0.half_width) / d;
         float vwidth_angle = cr_asin(sin_vwidth_angle);
         if (is_nan_f(vwidth_angle)) vwidth_angle = 0.0f;
@@ -1142,11 +1169,13 @@ struct Stroker {
         } else {
             long_axis = baseline;
         }
-        // atan2/sin/cos evaluated in f64 and rounded once: the correctly rounded f32 values
-        // (lyon's libm/euclid results agree with them to within an ulp). The GPU does the same,
-        // so the split point, which feeds later integer decisions, is bit-identical.
-        float angle = -(float)atan2((double)long_axis.y, (double)long_axis.x);
-        float s = (float)sin((double)angle), c = (float)cos((double)angle);
+        // Rotation2D::new(-long_axis.angle_from_x_axis()): the angle is euclid's fast_atan2
+        // (exact f32 arithmetic); its sin/cos are evaluated in f64 and rounded once, the
+        // correctly rounded f32 values, which the GPU reproduces (lyon takes them from the
+        // platform's f32 libm, within an ulp of these). The split point feeds segment counts,
+        // whose near ties are counted.
+        float angle = -angle_from_x_axis(long_axis);
+        float s = cr_sin(angle), c = cr_cos(angle);
         Quad rotated;
         rotated.from = P{0.0f, 0.0f};
         rotated.ctrl = P{v.x * c - v.y * s, v.x * s + v.y * c};
@@ -1181,31 +1210,22 @@ struct Stroker {
         if (radius < options.tolerance) return;
         int first_side = (is_start ^ (cross(edge_normal, start_normal) >= 0.0f)) ? SIDE_POSITIVE
                                                                                 : SIDE_NEGATIVE;
-        bool cr = false;
-        float start_angle, diff, step;
-        for (;;) {
-            start_angle = cr ? cr_atan2(start_normal.y, start_normal.x)
-                             : angle_from_x_axis(start_normal);
-            float edge_a = cr ? cr_atan2(edge_normal.y, edge_normal.x)
-                              : angle_from_x_axis(edge_normal);
-            diff = angle_to(start_angle, edge_a);
-            float tol = fminf(options.tolerance, radius);
-            step = 2.0f * (cr ? cr_acos((radius - tol) / radius) : acosf((radius - tol) / radius));
-            if (cr || !arc_near_tie(fabsf(diff) / step, step)) break;
-            cr = true;
-        }
+        float start_angle = angle_from_x_axis(start_normal);
+        float diff = angle_to(start_angle, angle_from_x_axis(edge_normal));
         float mid_angle = start_angle + diff;
         float end_angle = mid_angle + diff;
-        uint32_t num_subdivisions = depth_of(fabsf(diff) / step);
+        float step = arc_step(radius, options.tolerance);
+        uint32_t num_subdivisions =
+            depth_of(arc_quotient(fabsf(diff), radius, options.tolerance, step));
         vertex.position_on_path = center;
         vertex.half_width = radius;
         vertex.side = first_side;
         vertex.normal = normalize(edge_normal);
         uint32_t mid_vertex = add_stroke_vertex();
         out->add_triangle(start_vertex, mid_vertex, end_vertex);
-        tessellate_arc(start_angle, mid_angle, start_vertex, mid_vertex, num_subdivisions, cr);
+        tessellate_arc(start_angle, mid_angle, start_vertex, mid_vertex, num_subdivisions);
         vertex.side = 1 - first_side;
-        tessellate_arc(mid_angle, end_angle, mid_vertex, end_vertex, num_subdivisions, cr);
+        tessellate_arc(mid_angle, end_angle, mid_vertex, end_vertex, num_subdivisions);
     }
 
     // stroke.rs:2526-2560
@@ -3166,6 +3186,10 @@ uint64_t lyon_oracle_out_num_indices(const lyon_oracle_out* o) { return o->out.i
 const float* lyon_oracle_out_vertices(const lyon_oracle_out* o) { return o->out.vertices.data(); }
 const uint32_t* lyon_oracle_out_indices32(const lyon_oracle_out* o) { return o->out.indices.data(); }
 uint32_t lyon_oracle_out_near_ties(const lyon_oracle_out* o) { return o->near_ties; }
+
+// euclid's angle helpers as the oracle restates them (for the known-answer tests).
+float lyon_oracle_fast_atan2(float y, float x) { return lo::fast_atan2(y, x); }
+float lyon_oracle_angle_to(float from, float to) { return lo::angle_to(from, to); }
 
 // StrokeTessellator::tessellate_path appending to the output (BuffersBuilder semantics).
 int lyon_oracle_stroke_path(lyon_oracle_out* o, const uint8_t* verbs, uint32_t num_verbs,

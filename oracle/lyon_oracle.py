@@ -51,6 +51,10 @@ def lib():
             L.lyon_oracle_out_indices32.argtypes = [c_p]
             L.lyon_oracle_out_near_ties.restype = ctypes.c_uint32
             L.lyon_oracle_out_near_ties.argtypes = [c_p]
+            for n in ("fast_atan2", "angle_to"):
+                f = getattr(L, "lyon_oracle_" + n)
+                f.restype = ctypes.c_float
+                f.argtypes = [ctypes.c_float, ctypes.c_float]
             for n in ("stroke", "fill"):
                 f = getattr(L, f"lyon_oracle_{n}_path")
                 f.restype = ctypes.c_int

@@ -1,8 +1,9 @@
 """A Python restatement of lyon_extra's PathParser (crates/extra/src/parser.rs:138-490) and of
 the arc conversion it uses (crates/geom/src/arc.rs:58-138, 668-703) — TEST INFRASTRUCTURE ONLY,
 the checker of the library's SVG parser. f32 arithmetic through numpy; the f32 math functions
-(cosf, sinf, tanf, atan2f, sqrtf, fmodf) are the C library's, as lyon takes them from the
-platform's libm; `angle_from_x_axis` is atan2.
+(cosf, sinf, tanf, sqrtf, fmodf) are the C library's, as lyon takes them from the
+platform's libm; `angle_from_x_axis` is euclid 0.22.9's `fast_atan2` (the published polynomial
+of math.stackexchange question 1098487, answer 1105038), in f32 as lyon evaluates it.
 
 parse(src, num_attributes, stop_at) -> (verbs, points, widths, error) with error None or
 (kind, line, column), kind one of "number", "flag", "command", "missing_move_to".
@@ -20,7 +21,7 @@ _libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
 for _name in ("cosf", "sinf", "tanf", "sqrtf"):
     getattr(_libm, _name).restype = ctypes.c_float
     getattr(_libm, _name).argtypes = [ctypes.c_float]
-for _name in ("atan2f", "fmodf"):
+for _name in ("fmodf",):
     getattr(_libm, _name).restype = ctypes.c_float
     getattr(_libm, _name).argtypes = [ctypes.c_float, ctypes.c_float]
 
@@ -114,7 +115,20 @@ def _fn(f, x):
 
 
 def _atan2(y, x):
-    return f32(_libm.atan2f(float(y), float(x)))
+    # euclid's Trig::fast_atan2 for f32: numpy float32 scalars round every operation to f32.
+    y, x = f32(y), f32(x)
+    xa, ya = abs(x), abs(y)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        a = f32(min(xa, ya) / max(xa, ya))
+    s = a * a
+    r = ((f32(-0.0464964749) * s + f32(0.15931422)) * s - f32(0.327622764)) * s * a + a
+    if ya > xa:
+        r = f32(math.pi / 2) - r
+    if x < 0:
+        r = PI - r
+    if y < 0:
+        r = -r
+    return f32(r)
 
 
 def _fmod(a, b):

@@ -13,11 +13,13 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long CPU test")
 
 
-REFERENCE = os.environ.get("LYON_REFERENCE_DIR", "/root/reference")
+# A checkout of lyon's sources, for the tests that parse its third-party fixtures in place
+# (they are never copied into this repository). Unset: those tests are skipped.
+REFERENCE = os.environ.get("LYON_REFERENCE_DIR")
 
 
 @pytest.fixture(scope="session")
 def reference_dir():
-    if not os.path.isdir(REFERENCE):
-        pytest.skip("lyon sources not available on this machine")
+    if not REFERENCE or not os.path.isdir(REFERENCE):
+        pytest.skip("set LYON_REFERENCE_DIR to a checkout of lyon's sources")
     return REFERENCE

@@ -1,6 +1,6 @@
 """Generates the golden fixtures under tests/golden/ from lyon's own test sources.
 
-Run in a container where the lyon repository is available (default location given by
+Run where a checkout of the lyon repository is available (its location given by
 ``--reference``). The script reads lyon's Rust test files as text, extracts the paths they build
 with `Path::builder()` calls together with the results those tests assert (triangle counts, "must
 not fail"), and writes them as JSON. Nothing of lyon is executed: the expectations are the ones
@@ -19,7 +19,7 @@ Outputs:
                           data), converted from its SVG-builder calls to absolute verbs/points
                           with f32 arithmetic (crates/path/src/builder.rs:1193-1480 semantics)
 
-Usage: python tests/golden/make_golden.py [--reference PATH]
+Usage: python tests/golden/make_golden.py --reference PATH  (a checkout of lyon's sources)
 """
 
 import argparse
@@ -447,7 +447,7 @@ def fuzz_cases(ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="a checkout of lyon's sources")
     a = ap.parse_args()
     outputs = {
         "lyon_fill_cases.json": fill_cases(a.reference),

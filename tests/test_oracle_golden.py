@@ -326,3 +326,104 @@ def test_wang_lut_matches_ceil_fourth_root():
             assert n == max(1, math.ceil(r - 1e-9)) or abs(r - round(r)) < 1e-4
         else:
             assert abs(n - r) <= 1e-3 * r
+
+
+# ---- euclid's angle helpers (euclid 0.22.9, the version lyon's Cargo.lock pins) -------------
+
+def _fast_atan2_f32(y, x):
+    """euclid's Trig::fast_atan2 for f32, evaluated with numpy float32 scalars: the published
+    polynomial of math.stackexchange question 1098487 (answer 1105038)."""
+    f = np.float32
+    y, x = f(y), f(x)
+    xa, ya = abs(x), abs(y)
+    a = f(min(xa, ya) / max(xa, ya))
+    s = a * a
+    r = ((f(-0.0464964749) * s + f(0.15931422)) * s - f(0.327622764)) * s * a + a
+    if ya > xa:
+        r = f(math.pi / 2) - r
+    if x < 0:
+        r = f(math.pi) - r
+    if y < 0:
+        r = -r
+    return f(r)
+
+
+def test_fast_atan2_is_euclids_polynomial():
+    # lyon's join, cap and sharp-turn angles come from Vector2D::angle_from_x_axis, which is
+    # euclid's fast_atan2 (stroke.rs:1986-1987, 2482-2483, 3204). The oracle must return that
+    # polynomial's f32 value bit for bit, not the libm arctangent.
+    L = orc.lib()
+    rng = np.random.default_rng(12)
+    v = rng.normal(size=(4000, 2)).astype(np.float32) * np.float32(100.0)
+    worst = 0.0
+    for x, y in v:
+        got = np.float32(L.lyon_oracle_fast_atan2(float(y), float(x)))
+        assert got == _fast_atan2_f32(y, x)
+        worst = max(worst, abs(float(got) - math.atan2(float(y), float(x))))
+    # The published method's error (about 2e-4 rad at a = 1); a libm atan2 would be ~1e-7.
+    assert 1e-4 < worst < 2.1e-4
+    # Axis directions are exact.
+    f = lambda y, x: np.float32(L.lyon_oracle_fast_atan2(y, x))
+    assert f(0.0, 1.0) == 0.0
+    assert f(1.0, 0.0) == np.float32(math.pi / 2)
+    assert f(0.0, -1.0) == np.float32(math.pi)
+    assert f(-1.0, 0.0) == -np.float32(math.pi / 2)
+    assert math.isnan(f(0.0, 0.0))  # 0 / 0, as euclid's
+
+
+def test_angle_to_is_euclids_remainder_form():
+    # Angle::angle_to: d = (to - from) % 2pi; (2 d) % 2pi - d, with exact float remainders.
+    L = orc.lib()
+    f32 = np.float32
+    pi = f32(math.pi)
+    two_pi = pi * f32(2)
+    cases = [(0.0, 3.0), (0.0, 4.0), (3.0, -3.0), (0.0, float(pi)), (1.0, -2.5), (-3.1, 3.1)]
+    for a, b in cases:
+        d = f32(math.fmod(f32(f32(b) - f32(a)), two_pi))
+        want = f32(f32(math.fmod(f32(2) * d, two_pi)) - d)
+        assert np.float32(L.lyon_oracle_angle_to(a, b)) == want
+    # Hand-derived values: 4 - 2pi for a turn of 4 rad, and -pi (not +pi) at exactly pi.
+    assert np.float32(L.lyon_oracle_angle_to(0.0, 4.0)) == f32(f32(8.0) - two_pi) - f32(4.0)
+    assert np.float32(L.lyon_oracle_angle_to(0.0, float(pi))) == -pi
+
+
+@pytest.mark.parametrize("vw,expect", [(False, (200, 204)), (True, (104, 108))])
+def test_square_round_joins_and_caps_counts(vw, expect):
+    # stroke.rs test_square, Round joins and Round caps at tolerance 0.001 (lyon asserts only the
+    # TestBuilder's per-triangle checks there). Counts derived by hand from stroke.rs:
+    # circle_flattening_step(r, 0.001) = 2 acos((r - 0.001) / r); every turn and cap half is a
+    # quarter turn (the normals are axis aligned, so fast_atan2 is exact there).
+    #   fixed width, r = 0.5: pi/2 / 0.12652 = 12.4 -> 13 segments -> depth round(log2 13) = 4,
+    #     15 arc vertices per arc. Per sub-path: 3 edges x 2 triangles; 2 joins x (1 interior
+    #     triangle + 15); 2 caps x (1 + 2 x 15) = 6 + 32 + 62 = 100 triangles; 2 sub-paths.
+    #     Vertices: 4 end vertices + 2 joins x (3 + 15) + 2 caps x (1 + 30) = 102 per sub-path.
+    #   variable width 0.3 (r = 0.15): pi/2 / 0.23112 = 6.8 -> 7 -> depth 3, 7 per arc:
+    #     6 + 2 x 8 + 2 x 15 = 52 triangles and 4 + 2 x 10 + 2 x 15 = 54 vertices per sub-path.
+    case = next(c for c in STROKE_CASES if c["name"] == "test_square"
+                and c["options"].get("line_join") == "Round"
+                and bool(c["options"].get("variable_line_width")) == vw)
+    opts = stroke_options_from_case(case["options"])
+    widths = case.get("widths") if vw else None
+    r = orc.stroke(case_path(case), opts, index_bits=16, attributes=True, widths=widths)
+    assert r.status == 0
+    assert (r.num_triangles, len(r.vertices)) == expect
+    assert r.near_ties == 0
+    check_stroke_builder_asserts(r)
+
+
+@pytest.mark.parametrize("vw", [False, True])
+def test_empty_round_caps_counts(vw):
+    # stroke.rs test_empty_caps with Round caps (default tolerance 0.1, radius 0.5): a quarter
+    # turn is pi/2 / (2 acos(0.8)) = 1.22 -> 2 segments -> depth 1, one vertex per arc. Each
+    # empty cap: 2 vertices + 2 half caps x (1 mid vertex + 2 arc vertices) = 8 vertices and
+    # 2 x (1 + 2) = 6 triangles; the test path has 4 empty sub-paths.
+    case = next(c for c in STROKE_CASES if c["name"] == "test_empty_caps"
+                and c["options"].get("line_cap") == "Round"
+                and bool(c["options"].get("variable_line_width")) == vw)
+    opts = stroke_options_from_case(case["options"])
+    widths = case.get("widths") if vw else None
+    r = orc.stroke(case_path(case), opts, index_bits=16, attributes=True, widths=widths)
+    assert r.status == 0
+    assert (r.num_triangles, len(r.vertices)) == (24, 32)
+    check_stroke_builder_asserts(r)
+

@@ -217,6 +217,18 @@ int lyon_gpu_stroke_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                           int index_bits, int index_mode, uint32_t vertex_offset,
                           lyon_gpu_batch_output* out);
 
+/* The plain per-path GPU method, the baseline the batched call is measured against: paths
+ * [first, first + count) of `batch` (device memory) each run through their own batched call of
+ * one path (count kernel, look-back scan, one host wait for the totals, emit kernel), one after
+ * the other, into the context's output buffers (per-path indices). `*total_vertices` receives
+ * the sum of their vertex counts. No lyon counterpart: lyon strokes one path per
+ * `tessellate_path` call (crates/tessellation/src/stroke.rs:164-177), and this is that call
+ * pattern on the GPU. */
+int lyon_gpu_stroke_paths_each(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                               const lyon_stroke_options* options, uint32_t num_options,
+                               int index_bits, uint32_t first, uint32_t count,
+                               uint64_t* total_vertices);
+
 /* lyon_gpu_stroke_paths with lyon_stroke_vertex records (position, normal, advancement, side):
  * `out->vertices` points at `total_vertices` records in device memory (cast the pointer); the
  * rest of `out` is as for lyon_gpu_stroke_paths. */
@@ -561,9 +573,19 @@ typedef struct lyon_srv lyon_srv;
 
 typedef struct lyon_srv_config {
     int device;
-    uint32_t num_workers;          /* batches in flight at once, each on its own stream; 0 -> 2 */
+    uint32_t num_workers;          /* batches in flight at once, each on its own stream; 0 -> 2.
+                                      With stroke workers, these take fill requests only. */
     uint32_t max_batch_paths;      /* most paths coalesced into one launch; 0 -> 65536 */
     uint64_t device_budget_bytes;  /* device memory for batches and resident outputs; 0 -> 40 GB */
+    uint32_t num_stroke_workers;   /* workers reserved for stroke requests, on streams of the
+                                      device's highest priority and with one stroke block per SM,
+                                      so that their launches start beside running fill sweeps
+                                      instead of queueing behind them; 0 -> none (every worker
+                                      takes both kinds, oldest request first) */
+    uint32_t fill_blocks_per_sm;   /* fill sweep blocks per SM in this loop; 0 -> 8 with stroke
+                                      workers (room for one stroke block per SM), else the
+                                      library's default */
+    uint32_t max_stroke_batch_paths; /* most paths per stroke launch; 0 -> max_batch_paths */
 } lyon_srv_config;
 
 /* A finished request. Its output stays on the device until lyon_srv_release. */
@@ -624,6 +646,26 @@ typedef struct lyon_srv_load_stats {
 int lyon_srv_run_load(lyon_srv* srv, const lyon_srv_load_item* items, uint32_t num_items,
                       double rate_per_s, double duration_s, uint64_t seed,
                       lyon_srv_load_stats* stats, double* latencies_ms, uint32_t latencies_cap);
+
+/* ---- Coverage check (no lyon counterpart) -------------------------------------------------- */
+
+/* Per-sample coverage of two tessellations of the same paths, for checking fill output: for each
+ * of `num_paths` paths a `grid` x `grid` (at most 4096) grid of sample points spans the path's box
+ * (`boxes`: x0, y0, x1, y1 per path; samples at x0 + (i + 0.5)(x1 - x0) / grid, likewise y). A
+ * triangle covers a sample strictly inside it or on an edge that the tie rule gives it (edges
+ * are evaluated from their lexicographically smaller end point; a counter-clockwise edge keeps
+ * ties when it points down, or right when horizontal), so triangles sharing an edge cover each
+ * sample on it once. Each tessellation is given as device arrays in the per-path layout:
+ * vertices (2 floats each), u32 indices relative to the path's first vertex, and num_paths + 1
+ * vertex and index offsets. `counts` (device, 3 u64 per path) receives the samples covered by A,
+ * the samples covered by B and the samples whose coverage counts differ. Asynchronous on
+ * `stream`. */
+int lyon_gpu_coverage_compare(const float* boxes, uint32_t num_paths, uint32_t grid,
+                              const float* vertices_a, const uint32_t* indices_a,
+                              const uint64_t* vertex_offsets_a, const uint64_t* index_offsets_a,
+                              const float* vertices_b, const uint32_t* indices_b,
+                              const uint64_t* vertex_offsets_b, const uint64_t* index_offsets_b,
+                              uint64_t* counts, void* stream);
 
 /* ---- Stroke launch settings and autotuner (no lyon counterpart) ---------------------------- */
 

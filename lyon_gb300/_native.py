@@ -69,7 +69,8 @@ class CHatchOutput(ctypes.Structure):
 
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
-                ("device_budget_bytes", u64)]
+                ("device_budget_bytes", u64), ("num_stroke_workers", u32),
+                ("fill_blocks_per_sm", u32), ("max_stroke_batch_paths", u32)]
 
 
 class CSrvResult(ctypes.Structure):
@@ -150,6 +151,9 @@ def load(build_if_missing: bool = True):
             f.restype = ctypes.c_int
             f.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, ctypes.c_int, ctypes.c_int,
                           u32, ctypes.POINTER(CBatchOutput)]
+        L.lyon_gpu_stroke_paths_each.restype = ctypes.c_int
+        L.lyon_gpu_stroke_paths_each.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32,
+                                                 ctypes.c_int, u32, u32, ctypes.POINTER(u64)]
         for name in ("lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host"):
             f = getattr(L, name)
             f.restype = ctypes.c_int
@@ -248,6 +252,7 @@ def load(build_if_missing: bool = True):
 EXPORTED = [
     "lyon_gpu_create", "lyon_gpu_destroy", "lyon_gpu_stream", "lyon_gpu_last_error",
     "lyon_gpu_stroke_path", "lyon_gpu_fill_path", "lyon_gpu_stroke_paths", "lyon_gpu_fill_paths",
+    "lyon_gpu_stroke_paths_each", "lyon_gpu_coverage_compare",
     "lyon_gpu_flatten_counts", "lyon_gpu_flatten_paths", "lyon_gpu_synchronize",
     "lyon_gpu_version", "lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host",
     "lyon_gpu_set_timing", "lyon_gpu_last_timings", "lyon_gpu_stroke_paths_noalloc",

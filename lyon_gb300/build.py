@@ -21,7 +21,7 @@ LIB_NAME = "liblyon_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
 SOURCES = ["stroke.cu", "stroke_seq.cu", "attributes.cu", "arcs.cu", "hatch.cu", "scan.cu", "flatten.cu", "fill.cu", "api.cu", "noalloc.cu", "serve.cu",
-           "shapes.cu", "svg.cu"]
+           "shapes.cu", "svg.cu", "coverage.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math",

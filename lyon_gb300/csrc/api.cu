@@ -829,6 +829,29 @@ const uint64_t* srv_idx_offsets(lyon_gpu_context* ctx) { return as<uint64_t>(ctx
 const int32_t* srv_status(lyon_gpu_context* ctx) { return as<int32_t>(ctx->status); }
 cudaStream_t srv_stream(lyon_gpu_context* ctx) { return ctx->stream; }
 
+// Settings of a serving worker's context. A stroke lane gets a stream of the device's highest
+// priority (its blocks are dispatched before queued blocks of other streams) and one stroke block
+// per SM; `fill_blocks_per_sm` (0: default) bounds the fill sweep's residency.
+int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm) {
+    ctx->fill.blocks_per_sm_cap = fill_blocks_per_sm;
+    if (!stroke_lane) return LYON_OK;
+    ctx->blocks_per_sm = 1;
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+        cudaGetLastError();
+        return LYON_OK;  // priorities unsupported: keep the default stream
+    }
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+        cudaGetLastError();
+        return LYON_OK;
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    ctx->stream = s;
+    return LYON_OK;
+}
+
 }  // namespace lg
 
 extern "C" {
@@ -1071,6 +1094,31 @@ int lyon_gpu_stroke_paths(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                           lyon_gpu_batch_output* out) {
     return batched_device(ctx, KIND_STROKE, batch, options, num_options, index_bits, index_mode,
                           vertex_offset, out);
+}
+
+int lyon_gpu_stroke_paths_each(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                               const lyon_stroke_options* options, uint32_t num_options,
+                               int index_bits, uint32_t first, uint32_t count,
+                               uint64_t* total_vertices) {
+    if (!ctx || !batch || !options || !total_vertices || num_options == 0 ||
+        (num_options != 1 && num_options != batch->num_paths) || first > batch->num_paths ||
+        count > batch->num_paths - first)
+        return LYON_ERR_INVALID_ARGUMENT;
+    uint64_t tv = 0;
+    for (uint32_t p = first; p < first + count; ++p) {
+        // A one-path view of the batch (offsets stay absolute).
+        lyon_path_batch one = *batch;
+        one.verb_offsets = batch->verb_offsets + p;
+        one.point_offsets = batch->point_offsets + p;
+        one.num_paths = 1;
+        lyon_gpu_batch_output out;
+        const int r = batched_device(ctx, KIND_STROKE, &one, options + (num_options > 1 ? p : 0),
+                                     1, index_bits, LYON_INDEX_PER_PATH, 0, &out);
+        if (r != LYON_OK) return r;
+        tv += out.total_vertices;
+    }
+    *total_vertices = tv;
+    return LYON_OK;
 }
 
 int lyon_gpu_stroke_paths_attributes(lyon_gpu_context* ctx, const lyon_path_batch* batch,

@@ -252,7 +252,11 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
                           reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(fb.work) + 64) + n};
     // Sweepers (one per warp) and heaps; heaps start at 64 K words (256 KB), which covers nearly
     // every glyph-sized path.
-    const uint32_t threads = (uint32_t)(num_sms > 0 ? num_sms : 1) * fillk::FILL_SWEEPERS_PER_SM;
+    const uint32_t per_sm =
+        fb.blocks_per_sm_cap > 0 && fb.blocks_per_sm_cap < (uint32_t)fillk::FILL_SWEEPERS_PER_SM
+            ? fb.blocks_per_sm_cap
+            : (uint32_t)fillk::FILL_SWEEPERS_PER_SM;
+    const uint32_t threads = (uint32_t)(num_sms > 0 ? num_sms : 1) * per_sm;
     if (fb.heap_words == 0) fb.heap_words = 65536;
     // Staging: start from a guess of 4 vertices and 12 indices per input point.
     if (fb.stage_v_cap == 0) {

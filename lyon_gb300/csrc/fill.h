@@ -22,6 +22,9 @@ struct FillBuffers {
     void* work = nullptr;           // counters, staging tops and retry lists
     size_t work_cap = 0;
     uint32_t heap_words = 0;        // per-thread sweep heap size (grows when a path needs more)
+    // Most sweep blocks per SM (0: the default, FILL_SWEEPERS_PER_SM). The serving loop lowers
+    // it so that stroke kernels launched meanwhile find room on every SM.
+    uint32_t blocks_per_sm_cap = 0;
     // Vertex sources (FillVertex::sources), when a call asks for them:
     void* stage_s = nullptr;        // staged sources, three u32 words each, path-local ids
     size_t stage_s_cap = 0;

@@ -7,6 +7,13 @@
 // per request. While one worker's batch runs, the next worker gathers the requests that arrived
 // meanwhile, so their work overlaps on the device. Outputs stay resident in device slabs until
 // the caller releases the request; slabs are pooled per worker and reused.
+//
+// Stroke requests take microseconds to milliseconds of GPU time, fill requests tens of
+// milliseconds (one path's sweep runs on one thread). With stroke workers configured, the kinds
+// get separate workers: stroke workers run on streams of the device's highest priority with one
+// stroke block per SM, and fill sweeps keep at most `fill_blocks_per_sm` blocks per SM, so that
+// a stroke launch finds room on every SM and starts while fill sweeps are running instead of
+// waiting for them to end.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -25,6 +32,7 @@ namespace lg {
 int srv_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
               uint32_t num_options, const uint32_t* request_first, uint64_t* tv, uint64_t* ti,
               uint32_t* failed);
+int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm);
 int srv_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
              uint32_t num_options, const uint32_t* request_first, float* vout, void* iout,
              uint64_t tv);
@@ -104,8 +112,11 @@ bool host_grow(T** p, size_t* cap, size_t n) {
     return true;
 }
 
+enum Role { ROLE_ANY = 0, ROLE_STROKE = 1, ROLE_FILL = 2 };
+
 struct Worker {
     lyon_gpu_context* ctx = nullptr;
+    int role = ROLE_ANY;
     std::thread th;
     // pinned staging and device copies of the batch inputs
     uint8_t* h_verbs = nullptr;
@@ -330,7 +341,8 @@ void worker_main(lyon_srv* s, Worker* w) {
             std::unique_lock<std::mutex> lk(s->mu);
             for (;;) {
                 if (s->stop) return;
-                const bool have0 = !s->queue[0].empty(), have1 = !s->queue[1].empty();
+                const bool have0 = w->role != ROLE_FILL && !s->queue[0].empty();
+                const bool have1 = w->role != ROLE_STROKE && !s->queue[1].empty();
                 if (!have0 && !have1) {
                     s->cv_work.wait(lk);
                     continue;
@@ -341,11 +353,13 @@ void worker_main(lyon_srv* s, Worker* w) {
                            ? 0
                            : 1;
                 std::deque<Request*>& q = s->queue[kind];
+                const uint32_t max_paths =
+                    kind == LYON_KIND_STROKE ? s->cfg.max_stroke_batch_paths : s->cfg.max_batch_paths;
                 uint32_t paths = 0;
                 while (!q.empty()) {
                     Request* r = q.front();
                     const bool first = batch.empty();
-                    if (!first && paths + r->batch.num_paths > s->cfg.max_batch_paths) break;
+                    if (!first && paths + r->batch.num_paths > max_paths) break;
                     if (s->held_bytes + reserved + r->est_bytes > s->cfg.device_budget_bytes &&
                         !(first && s->held_bytes == 0))
                         break;
@@ -408,18 +422,24 @@ extern "C" {
 
 lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
     lyon_srv* s = new lyon_srv();
-    lyon_srv_config c = config ? *config : lyon_srv_config{0, 0, 0, 0};
+    lyon_srv_config c = config ? *config : lyon_srv_config{0, 0, 0, 0, 0, 0, 0};
     if (c.num_workers == 0) c.num_workers = 2;
     if (c.max_batch_paths == 0) c.max_batch_paths = 65536;
     if (c.device_budget_bytes == 0) c.device_budget_bytes = 40ull << 30;
+    if (c.max_stroke_batch_paths == 0) c.max_stroke_batch_paths = c.max_batch_paths;
+    if (c.num_stroke_workers > 0 && c.fill_blocks_per_sm == 0) c.fill_blocks_per_sm = 8;
     s->cfg = c;
-    for (uint32_t i = 0; i < c.num_workers; ++i) {
+    const uint32_t total = c.num_workers + c.num_stroke_workers;
+    for (uint32_t i = 0; i < total; ++i) {
         std::unique_ptr<Worker> w(new Worker());
         w->ctx = lyon_gpu_create(c.device);
         if (!w->ctx) {
             lyon_srv_destroy(s);
             return nullptr;
         }
+        const bool stroke_lane = i >= c.num_workers;
+        w->role = c.num_stroke_workers == 0 ? ROLE_ANY : (stroke_lane ? ROLE_STROKE : ROLE_FILL);
+        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm);
         s->workers.push_back(std::move(w));
     }
     for (auto& w : s->workers) w->th = std::thread(worker_main, s, w.get());

@@ -85,10 +85,15 @@ def _result(r: _native.CSrvResult) -> Result:
 
 
 class Server:
+    """lyon_srv_*: `num_workers` workers take any request (fill requests only when
+    `num_stroke_workers` > 0, whose workers take the strokes on high-priority streams)."""
+
     def __init__(self, device: int = 0, num_workers: int = 2, max_batch_paths: int = 65536,
-                 device_budget_bytes: int = 40 << 30):
+                 device_budget_bytes: int = 40 << 30, num_stroke_workers: int = 0,
+                 fill_blocks_per_sm: int = 0, max_stroke_batch_paths: int = 0):
         self.lib = _native.load()
-        cfg = _native.CSrvConfig(device, num_workers, max_batch_paths, device_budget_bytes)
+        cfg = _native.CSrvConfig(device, num_workers, max_batch_paths, device_budget_bytes,
+                                 num_stroke_workers, fill_blocks_per_sm, max_stroke_batch_paths)
         self.h = self.lib.lyon_srv_create(ctypes.byref(cfg))
         if not self.h:
             raise RuntimeError("lyon_srv_create failed")

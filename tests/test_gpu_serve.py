@@ -36,7 +36,10 @@ def _alone(ctx, req):
     return v, i, st
 
 
-def test_mixed_requests_equal_alone(pools):
+@pytest.mark.parametrize("stroke_workers", [0, 2])
+def test_mixed_requests_equal_alone(pools, stroke_workers):
+    # With stroke workers, strokes run on their own high-priority streams with one stroke block
+    # per SM while fill sweeps keep at most 8 blocks per SM: the results must not change.
     sb, so, sb2, so2, fb, fo = pools
     rng = np.random.default_rng(7)
     reqs = []
@@ -49,7 +52,8 @@ def test_mixed_requests_equal_alone(pools):
         start = int(rng.integers(0, pool.num_paths - n + 1))
         o = opts if len(opts) == 1 else opts[start:start + n]
         reqs.append(serving.Request(kind, pool, start, n, o))
-    srv = serving.Server(0, num_workers=2, max_batch_paths=1500)
+    srv = serving.Server(0, num_workers=2, max_batch_paths=1500,
+                         num_stroke_workers=stroke_workers, max_stroke_batch_paths=1500)
     try:
         tickets = [srv.submit(r) for r in reqs]  # all queued at once: coalesced into batches
         ctx = T.Context(0)

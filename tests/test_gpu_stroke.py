@@ -279,3 +279,23 @@ def test_autotuner_picks_a_setting_and_keeps_outputs(gpu):
         assert np.array_equal(after["vertices"], before["vertices"])
     finally:
         c.lib.lyon_gpu_set_stroke_tuning(c.h, ctypes.byref(saved))
+
+
+def test_plain_per_path_entry_point_counts(gpu):
+    # lyon_gpu_stroke_paths_each (the per-path pipeline the batched call is measured against)
+    # strokes each path by itself: its vertex total equals the batched call's for those paths.
+    import ctypes
+    batch, opts = workloads.batched_stroke(300, seed=9)
+    g = gpu.gpu_batch("stroke", batch, opts, index_bits=32)
+    c = gpu.ctx()
+    db = T.DeviceBatch.upload(batch, 0)
+    od = T.upload_options(opts, 0)
+    cb = db.c()
+    tv = ctypes.c_uint64(0)
+    r = c.lib.lyon_gpu_stroke_paths_each(c.h, ctypes.byref(cb), od.data_ptr(), len(opts), 32,
+                                         100, 150, ctypes.byref(tv))
+    assert r == 0
+    assert tv.value == int(g["vtx_offsets"][250] - g["vtx_offsets"][100])
+    bad = c.lib.lyon_gpu_stroke_paths_each(c.h, ctypes.byref(cb), od.data_ptr(), len(opts), 32,
+                                           200, 101, ctypes.byref(tv))
+    assert bad == T.LYON_ERR_INVALID_ARGUMENT

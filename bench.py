@@ -159,6 +159,28 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def roofline_entry(alg_bytes, kernel_s, kernel, traffic=None):
+    """The roofline object of a bench entry: algorithmic bytes over the kernel's event time,
+    against the measured HBM copy bandwidth."""
+    peak, kind = measured_peak_hbm()
+    achieved = alg_bytes / max(kernel_s, 1e-12) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": kind, "traffic": traffic, "kernel": kernel,
+            "algorithmic_bytes": alg_bytes, "kernel_ms": kernel_s * 1e3}
+
+
+def profiled_figure(name, key):
+    """A figure (`key: value` line) from a committed ncu summary under profiles/, if any."""
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(p):
+            if line.startswith(key + ":"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
 def profiled_traffic_per_vertex():
     """DRAM bytes per output vertex of the emit kernel from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "stroke_emit_batched_stroke.md")
@@ -171,44 +193,60 @@ def profiled_traffic_per_vertex():
     return None
 
 
-def cpu_baseline(batch, opts, sample_paths: int):
-    """The oracle on a bounded sample, all host threads."""
+def _oracle_rate(kind, batch, opts, n, threads):
+    """The oracle over the first n paths: each path tessellated into one reused VertexBuffers per
+    thread (lyon's tessellate_path into a cleared buffer), nothing copied into batch arrays.
+    Returns (vertices/s, vertices, seconds)."""
     from oracle import lyon_oracle as orc
-    n = min(sample_paths, batch.num_paths)
     sub = batch.head(n)
     sub_opts = opts[:n] if len(opts) > 1 else opts
-    threads = os.cpu_count() or 1
-    orc.batch("stroke", sub.head(min(n, 2000)),
-              sub_opts[:min(n, 2000)] if len(sub_opts) > 1 else sub_opts, 32, threads, False)
+    w = min(n, 2000)
+    orc.batch(kind, sub.head(w), sub_opts[:w] if len(sub_opts) > 1 else sub_opts, 32, threads,
+              want_output=False)
     t0 = time.perf_counter()
-    r = orc.batch("stroke", sub, sub_opts, 32, threads, want_output=False)
+    r = orc.batch(kind, sub, sub_opts, 32, threads, want_output=False)
     dt = time.perf_counter() - t0
     verts = int(r["vtx_counts"].sum())
-    return {"value": verts / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {n} paths of the workload, {verts} output vertices, "
-                      f"{dt:.2f} s wall on {threads} threads"}
+    return verts / dt, verts, dt
+
+
+def cpu_baseline(batch, opts, sample_paths: int, kind: str = "stroke",
+                 single_paths: int = 10_000):
+    """The oracle (lyon's algorithm restated) on the host cores: all threads on a bounded sample,
+    and one thread on a smaller one (lyon itself is single-threaded per tessellator)."""
+    threads = os.cpu_count() or 1
+    n = min(sample_paths, batch.num_paths)
+    v, verts, dt = _oracle_rate(kind, batch, opts, n, threads)
+    n1 = min(single_paths, batch.num_paths)
+    v1, verts1, dt1 = _oracle_rate(kind, batch, opts, n1, 1)
+    return {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {n} paths of the workload, {verts} output vertices, {dt:.2f} s "
+                      f"wall on {threads} threads; every path tessellated into a reused "
+                      f"per-thread VertexBuffers, outputs not copied into batch arrays",
+            "single_thread": {"value": v1, "unit": UNIT, "cores": 1, "kind": "port",
+                              "sample": f"first {n1} paths, {verts1} output vertices, "
+                                        f"{dt1:.2f} s wall on 1 thread"}}
 
 
 def run_reference(args):
     """The reference arm: lyon's algorithm on the host cores (the oracle port: lyon itself is
-    Rust and has no toolchain on this machine), each step a bounded sample of the workload."""
+    Rust and has no toolchain on this machine), every step the whole workload on all threads,
+    each path tessellated into a reused per-thread VertexBuffers (outputs not copied into batch
+    arrays); warm-up steps run on a tenth of it."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
     from lyon_gb300 import workloads
     from oracle import lyon_oracle as orc
-    sample = min(args.paths, 100_000)
     batch, opts = workloads.batched_stroke(args.paths, seed=2)
-    sub = batch.head(sample)
-    sub_opts = opts[:sample]
     threads = os.cpu_count() or 1
+    warm = max(1, batch.num_paths // 10)
     for _ in range(args.warmup):
-        orc.batch("stroke", sub.head(min(sample, 5000)), sub_opts[:min(sample, 5000)],
-                  32, threads, want_output=False)
+        orc.batch("stroke", batch.head(warm), opts[:warm], 32, threads, want_output=False)
     verts = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r = orc.batch("stroke", sub, sub_opts, 32, threads, want_output=False)
+        r = orc.batch("stroke", batch, opts, 32, threads, want_output=False)
         verts += int(r["vtx_counts"].sum())
     dt = time.perf_counter() - t0
     value = verts / dt
@@ -219,7 +257,9 @@ def run_reference(args):
         "data": "synthetic (seeded)", "config": workload_config(args.paths),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"first {sample} paths of the workload per step"},
+                         "sample": f"all {batch.num_paths} paths of the workload per step, "
+                                   f"each tessellated into a reused per-thread VertexBuffers "
+                                   f"(outputs not copied into batch arrays)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -366,7 +406,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(batch, opts, args.cpu_sample)
     if rank == 0:
-        line["plain_per_path"] = plain_per_path(ctx, batch, opts, T)
+        line["plain_per_path"] = plain_per_path(ctx, db, od, len(opts), value, T)
         if not args.no_fill:
             line["fill"] = run_fill(ctx, args, T, world)
         if not args.no_polylines:
@@ -444,17 +484,27 @@ def run_fill(ctx, args, T, world, batch=None):
         if args.profile_fill:
             out[name] = entry
             continue
+        # Roofline of the sweep kernel (the dominant one): the call's algorithmic bytes (inputs,
+        # output vertices and indices, per-path descriptors) over the sweep's event time.
+        alg = (batch.input_bytes(options_bytes_per_path=0) + 16 + v * 8 +
+               res.total_indices * 4 + 16 * batch.num_paths)
+        tpp = profiled_figure("fill_sweep_glyph_fill.md", "dram_bytes_per_path")
+        entry["roofline"] = roofline_entry(
+            alg, statistics.median(sweep_ms) / 1e3, "fill_sweep_kernel",
+            tpp * batch.num_paths if tpp is not None else None)
         n = min(20_000, batch.num_paths)
-        sub = batch.head(n)
-        orc.batch("fill", sub.head(min(n, 1000)), opts, 32, threads, want_output=False)
-        t0 = time.perf_counter()
-        r = orc.batch("fill", sub, opts, 32, threads, want_output=False)
-        dt = time.perf_counter() - t0
-        cv = int(r["vtx_counts"].sum())
-        entry["cpu_baseline"] = {"value": cv / dt, "unit": "vertices/s", "cores": threads,
+        rate, cv, dt = _oracle_rate("fill", batch, opts, n, threads)
+        n1 = min(2_000, batch.num_paths)
+        rate1, cv1, dt1 = _oracle_rate("fill", batch, opts, n1, 1)
+        entry["cpu_baseline"] = {"value": rate, "unit": "vertices/s", "cores": threads,
                                  "kind": "port",
                                  "sample": f"first {n} paths, {cv} output vertices, "
-                                           f"{dt:.2f} s wall on {threads} threads"}
+                                           f"{dt:.2f} s wall on {threads} threads",
+                                 "single_thread": {"value": rate1, "unit": "vertices/s",
+                                                   "cores": 1, "kind": "port",
+                                                   "sample": f"first {n1} paths, {cv1} output "
+                                                             f"vertices, {dt1:.2f} s wall on "
+                                                             f"1 thread"}}
         out[name] = entry
     return out
 
@@ -721,13 +771,18 @@ def run_polylines(ctx, args, T):
                                          ctypes.byref(best), times, ctypes.byref(nc))
         res = T.tessellate_paths("stroke", db, od, len(o), 32, T.INDEX_GLOBAL, 0, ctx)
         ctx.synchronize()
+        ctx.lib.lyon_gpu_set_timing(ctx.h, 1)
         steps = max(1, args.steps)
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
         launches0 = ctx.lib.lyon_gpu_kernel_launches()
+        emit_ms = []
         start.record(stream)
         for _ in range(steps):
             res = T.tessellate_paths("stroke", db, od, len(o), 32, T.INDEX_GLOBAL, 0, ctx)
+            ms4 = (ctypes.c_float * 4)()
+            ctx.lib.lyon_gpu_last_timings(ctx.h, ms4)
+            emit_ms.append(ms4[2])
         end.record(stream)
         end.synchronize()
         ms = start.elapsed_time(end) / steps
@@ -738,6 +793,12 @@ def run_polylines(ctx, args, T):
                             "short_path_points": best.short_path_points},
                  "candidate_ms": [round(float(t), 3) for t in times[:nc.value]],
                  "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
+        alg = (batch.input_bytes(options_bytes_per_path=24) + res.total_vertices * 8 +
+               res.total_indices * 4 + 16 * batch.num_paths)
+        tpv = profiled_figure("stroke_emit_map_polylines_300k.md", "dram_bytes_per_output_vertex")
+        entry["roofline"] = roofline_entry(
+            alg, statistics.median(emit_ms) / 1e3, "stroke emit (walk + run kernel)",
+            tpv * res.total_vertices if tpv is not None else None)
         if tol == 0.1:
             n = batch.num_paths  # the whole batch: well under a second on the host cores
             sub = batch.head(n)
@@ -754,59 +815,122 @@ def run_polylines(ctx, args, T):
     return out
 
 
+def _latency_groups(stats, reqs):
+    """p50/p99/p99.9 of a load's request latencies per kind and size class (the latencies come
+    in arrival order; arrival k submitted request k % len(reqs))."""
+    lat = np.asarray(stats.get("latencies_ms", []), np.float64)
+    out = {}
+    if len(lat) == 0:
+        return out
+    kinds = np.array([reqs[k % len(reqs)].kind for k in range(len(lat))])
+    sizes = np.array([reqs[k % len(reqs)].count for k in range(len(lat))])
+    for kname, kv in (("stroke", 0), ("fill", 1)):
+        for sname, sel in (("le_1000_paths", sizes <= 1000), ("gt_1000_paths", sizes > 1000),
+                           ("all", sizes > 0)):
+            m = (kinds == kv) & sel
+            if m.sum() == 0:
+                continue
+            x = lat[m]
+            out[f"{kname}_{sname}"] = {"requests": int(m.sum()),
+                                       "p50_ms": float(np.percentile(x, 50)),
+                                       "p99_ms": float(np.percentile(x, 99)),
+                                       "p999_ms": float(np.percentile(x, 99.9)),
+                                       "max_ms": float(x.max())}
+    return out
+
+
 def run_serving(args):
     """Serving loop: Poisson arrivals of scenes of 1-5,000 paths (log-uniform), 70 % strokes from
     the plain-stroke generator, 30 % fills from the glyph generator; outputs stay resident; each
-    request released on completion. Offered load 50,000 requests/s, plus a load below
-    saturation; p50/p99/p99.9 latency from the scheduled arrival to the output on the device."""
+    request released on completion. Two stroke workers on high-priority streams, two fill
+    workers. Reported: the offered 50,000 requests/s (saturated), the saturation throughput of
+    each kind alone, and loads below saturation with p50/p99/p99.9 latency (from the scheduled
+    arrival to the output on the device) per kind and size class."""
     from lyon_gb300 import serving, workloads
     sp, so = workloads.plain_stroke(20_000, seed=1)
     fp, fo = workloads.glyph_fill(5_000, seed=3)
     reqs = serving.mixed_requests(sp, so, fp, fo, 4096, seed=5, max_paths=5000)
     small = [r for r in reqs if r.count <= 1000]
-    srv = serving.Server(0, num_workers=3)
+    strokes = [r for r in reqs if r.kind == serving.KIND_STROKE]
+    fills = [r for r in reqs if r.kind == serving.KIND_FILL]
+    srv = serving.Server(0, num_workers=2, num_stroke_workers=2, max_stroke_batch_paths=16384)
     try:
-        srv.run_load(reqs[:64], rate_per_s=2000.0, duration_s=0.2, seed=1)  # warm-up
-        offered = srv.run_load(reqs, rate_per_s=50_000.0, duration_s=args.serve_seconds, seed=2)
+        # Warm-up: the largest request of each kind first (buffers grow to their final sizes),
+        # then a short mixed load.
+        for group in (strokes, fills):
+            big = max(group, key=lambda r: r.count)
+            t = srv.submit(big)
+            srv.wait(t)
+            srv.release(t)
+        srv.run_load(reqs[:64], rate_per_s=2000.0, duration_s=0.2, seed=1)
+        offered = srv.run_load(reqs, rate_per_s=50_000.0, duration_s=args.serve_seconds, seed=2,
+                               want_latencies=True)
+        sat_stroke = srv.run_load(strokes, rate_per_s=50_000.0, duration_s=0.2, seed=6)
+        sat_fill = srv.run_load(fills, rate_per_s=50_000.0, duration_s=0.02, seed=7)
         cap_paths = offered["paths"] / max(offered["elapsed_s"], 1e-9)
         mean_paths = float(np.mean([r.count for r in reqs]))
         moderate_rate = max(50.0, 0.3 * cap_paths / mean_paths)
-        moderate = srv.run_load(reqs, rate_per_s=moderate_rate, duration_s=1.0, seed=3)
-        small_load = srv.run_load(small, rate_per_s=moderate_rate, duration_s=1.0, seed=4)
+        moderate = srv.run_load(reqs, rate_per_s=moderate_rate, duration_s=2.0, seed=3,
+                                want_latencies=True)
+        small_load = srv.run_load(small, rate_per_s=moderate_rate, duration_s=2.0, seed=4,
+                                  want_latencies=True)
     finally:
         srv.close()
 
-    def brief(st):
-        return {k: st[k] for k in ("offered_rate", "submitted", "completed", "failed",
-                                   "achieved_rate", "elapsed_s", "p50_ms", "p99_ms", "p999_ms",
-                                   "max_ms", "batches", "mean_batch_paths")} | {
+    in_per_path = ((sp.input_bytes(options_bytes_per_path=24) / sp.num_paths) * 0.7 +
+                   (fp.input_bytes(options_bytes_per_path=16) / fp.num_paths) * 0.3)
+
+    def brief(st, pool=None):
+        out = {k: st[k] for k in ("offered_rate", "submitted", "completed", "failed",
+                                  "achieved_rate", "elapsed_s", "p50_ms", "p99_ms", "p999_ms",
+                                  "max_ms", "batches", "mean_batch_paths")} | {
             "vertices_per_s": st["vertices"] / max(st["elapsed_s"], 1e-9),
             "paths_per_s": st["paths"] / max(st["elapsed_s"], 1e-9)}
+        # The whole loop against HBM: the requests' algorithmic bytes (inputs estimated from
+        # the pools' mean bytes per path, outputs exact) over the load's wall time.
+        alg = st["paths"] * in_per_path + st["vertices"] * 8 + st["indices"] * 4
+        out["roofline"] = roofline_entry(alg, st["elapsed_s"], "serving loop (wall clock)")
+        if pool is not None:
+            out["by_kind_and_size"] = _latency_groups(st, pool)
+        return out
 
     return {"workload": "Poisson scenes of 1-5000 paths, 70% plain-stroke / 30% glyph-fill, "
                         "u32, device-resident outputs",
+            "workers": {"stroke": 2, "fill": 2, "fill_blocks_per_sm": 8,
+                        "max_stroke_batch_paths": 16384},
             "requests_in_pool": len(reqs), "mean_paths_per_request": mean_paths,
-            "offered_50k_per_s": brief(offered),
-            "below_saturation": brief(moderate),
-            "below_saturation_requests_le_1000_paths": brief(small_load)}
+            "offered_50k_per_s": brief(offered, reqs),
+            "saturation_stroke_only": brief(sat_stroke),
+            "saturation_fill_only": brief(sat_fill),
+            "below_saturation": brief(moderate, reqs),
+            "below_saturation_requests_le_1000_paths": brief(small_load, small)}
 
 
-def plain_per_path(ctx, batch, opts, T, count: int = 300):
-    """The plain per-path GPU launch: lyon_gpu_stroke_path per path (host in, host out)."""
-    from lyon_gb300.options import StrokeOptions
-    st = T.StrokeTessellator(ctx)
-    verts = 0
-    buf = T.VertexBuffers(32)
+def plain_per_path(ctx, db, opts_dev, num_options, batched_vps, T, count: int = 2000):
+    """The plain per-path GPU method of the benchmark spec: the count -> scan -> emit pipeline
+    launched once per path from C (lyon_gpu_stroke_paths_each) on the device-resident batch,
+    one host wait per path; no Python loop and no host staging. Its rate beside the batched
+    call's gives the batched / plain ratio."""
+    import torch
+    lib = ctx.lib
+    cb = db.c()
+    tv = ctypes.c_uint64(0)
+    r = lib.lyon_gpu_stroke_paths_each(ctx.h, ctypes.byref(cb), opts_dev.data_ptr(),
+                                       num_options, 32, 0, 64, ctypes.byref(tv))  # warm-up
+    assert r == 0, r
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for p in range(count):
-        o = opts[p]
-        so = StrokeOptions(int(o["start_cap"]), int(o["end_cap"]), int(o["line_join"]),
-                           float(o["line_width"]), float(o["miter_limit"]), float(o["tolerance"]))
-        buf.clear()
-        st.tessellate_path(batch.path(p), so, T.BuffersBuilder(buf))
-        verts += len(buf.vertices)
+    r = lib.lyon_gpu_stroke_paths_each(ctx.h, ctypes.byref(cb), opts_dev.data_ptr(),
+                                       num_options, 32, 0, count, ctypes.byref(tv))
+    torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    return {"value": verts / dt, "unit": UNIT, "paths": count, "us_per_path": dt / count * 1e6}
+    assert r == 0, r
+    value = tv.value / dt
+    return {"value": value, "unit": UNIT, "paths": count, "vertices": tv.value,
+            "us_per_path": dt / count * 1e6,
+            "method": "lyon_gpu_stroke_paths_each: one count/scan/emit pipeline per path, "
+                      "device-resident inputs, first paths of the workload",
+            "batched_over_plain": batched_vps / value}
 
 
 def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
@@ -843,7 +967,7 @@ def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
 
     lib.lyon_gpu_set_timing(ctx.h, 0)
     call()
-    steps = max(1, min(args.steps, 3))
+    steps = max(1, args.steps)
     launches0 = lib.lyon_gpu_kernel_launches()
     t0 = time.perf_counter()
     for _ in range(steps):

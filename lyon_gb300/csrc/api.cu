@@ -43,10 +43,6 @@ struct lyon_gpu_context {
     DevBuf small;  // [0] work counter, [1] scan counter, [2] error flag, [3] failed paths,
                    // [4..5] processing-order counters
     DevBuf order;  // processing order of the current stroke batch (long paths first)
-    // Interior runs of the last stroke count pass (small word 8 counts them) and the records
-    // the emit pass writes for stroke_run_kernel.
-    uint32_t run_count = 0;
-    DevBuf runs;
     bool order_valid = false;
     DevBuf path_class, class_counters;  // classification for the one-thread-per-path phase
     bool split_valid = false;           // class_counters holds the first short item
@@ -256,22 +252,18 @@ bool finish_counts(lyon_gpu_context* ctx, uint32_t n, int index_bits, int index_
         if (!ensure_host(ctx, ctx->h_small, 64)) return false;
         uint64_t* hs = reinterpret_cast<uint64_t*>(ctx->h_small.ptr);
         uint64_t* hs_dev = direct_host_pointer<uint64_t>(hs);
-        hs[3] = 0;
         if (hs_dev) {
             lg::launch_read_totals(as<uint64_t>(ctx->vtx_offsets) + n,
-                                   as<uint64_t>(ctx->idx_offsets) + n, sw + 2, hs_dev, s,
-                                   sw + 8);
+                                   as<uint64_t>(ctx->idx_offsets) + n, sw + 2, hs_dev, s);
         } else {
             cudaMemcpyAsync(hs, as<uint64_t>(ctx->vtx_offsets) + n, 8, cudaMemcpyDeviceToHost, s);
             cudaMemcpyAsync(hs + 1, as<uint64_t>(ctx->idx_offsets) + n, 8, cudaMemcpyDeviceToHost,
                             s);
             cudaMemcpyAsync(hs + 2, sw + 2, 8, cudaMemcpyDeviceToHost, s);
-            cudaMemcpyAsync(hs + 3, sw + 8, 4, cudaMemcpyDeviceToHost, s);
         }
         if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return false;
         *tv = hs[0];
         *ti = hs[1];
-        ctx->run_count = (uint32_t)hs[3];
         uint32_t* hw = reinterpret_cast<uint32_t*>(hs + 2);
         if (hw[0] != 0) {
             ctx->last_error = "scan look-back wait exceeded its bound";
@@ -336,10 +328,6 @@ lg::StrokeArgs stroke_args(lyon_gpu_context* ctx, const lyon_path_batch* batch,
         a.item_split = as<uint32_t>(ctx->class_counters) + 2 * (3 + ctx->short_path_points);
         a.seq_counter = small_words(ctx) + 6;
     }
-    // Interior runs: the fixed-width walk with positions output (not the attribute records, the
-    // sequential stepper or variable width).
-    a.use_runs = (!ctx->vertex_attrs && !ctx->want_sources && !ctx->vw_widths) ? 1 : 0;
-    a.run_counter = small_words(ctx) + 8;
     a.vtx_offsets = as<uint64_t>(ctx->vtx_offsets);
     a.idx_offsets = as<uint64_t>(ctx->idx_offsets);
     return a;
@@ -386,8 +374,6 @@ int pipeline_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch
         }
         lg::StrokeArgs a = stroke_args(ctx, batch, (const lyon_stroke_options*)options,
                                        num_options, index_bits, index_mode, vertex_offset);
-        ctx->run_count = 0;
-        cudaMemsetAsync(a.run_counter, 0, 4, s);
         if (n > 0) {
             cudaMemsetAsync(small_words(ctx), 0, 4, s);
             if (a.seq_counter) cudaMemsetAsync(a.seq_counter, 0, 4, s);
@@ -425,23 +411,10 @@ int pipeline_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch,
                                        num_options, index_bits, index_mode, vertex_offset);
         a.vertices = vout;
         a.indices = iout;
-        // The runs the count pass found are recorded by the emit walk and written by the run
-        // kernel (without room for the records the walk takes every step itself, identically).
-        const uint32_t nruns = a.use_runs ? ctx->run_count : 0u;
-        if (nruns > 0 && ensure(ctx, ctx->runs, (size_t)nruns * sizeof(lg::RunRec))) {
-            a.runs = as<lg::RunRec>(ctx->runs);
-            a.runs_cap = nruns;
-        }
         if (n > 0 && tv > 0) {
             cudaMemsetAsync(small_words(ctx), 0, 4, s);
             if (a.seq_counter) cudaMemsetAsync(a.seq_counter, 0, 4, s);
-            cudaMemsetAsync(a.run_counter, 0, 4, s);
             if (!set_err(ctx, "stroke emit", lg::launch_stroke(a, true, stroke_grid(ctx, n), s)))
-                return LYON_ERR_CUDA;
-            if (a.runs &&
-                !set_err(ctx, "stroke runs",
-                         lg::launch_stroke_runs(a.runs, nruns, vout, iout, index_bits,
-                                                ctx->num_sms, s)))
                 return LYON_ERR_CUDA;
         }
     } else {
@@ -898,7 +871,7 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->h_in_poff,  &ctx->h_in_opts,   &ctx->slot_v[0],   &ctx->slot_v[1],
                       &ctx->slot_i[0],  &ctx->slot_i[1],   &ctx->flat_counts, &ctx->flat_offsets,
                       &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
-                      &ctx->in_options, &ctx->order, &ctx->runs, &ctx->slot_status[0],
+                      &ctx->in_options, &ctx->order, &ctx->slot_status[0],
                       &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters,
                       &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs,
                       &ctx->src_counts, &ctx->src_offsets, &ctx->src_scratch,

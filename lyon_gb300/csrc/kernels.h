@@ -13,21 +13,6 @@ namespace lg {
 void note_launches(uint32_t k);
 uint64_t launches_total();
 
-// An interior run of a curve, found by the walk of the emit pass and written by the run kernel:
-// `len` flattening-step joins at the unit's flattened points 2 .. len + 1, each two vertices
-// (+ then -) and the two triangles of the edge before it (stroke.rs:1743-1806, 1869-1904).
-struct RunRec {
-    float a0x, a0y, a1x, a1y, a2x, a2y, a3x, a3y;  // the unit's polynomial (a3 = 0: quadratic)
-    float s;        // flattening step 1 / n
-    float t2;       // lyon's accumulated t at the unit's second point
-    float hw;       // half line width
-    uint32_t cubic;
-    uint32_t len;   // joins in the run
-    uint32_t base;  // vertex id of the first join's + vertex
-    uint64_t vo;    // its offset in the vertex output
-    uint64_t io;    // offset of its first index
-};
-
 struct StrokeArgs {
     const uint8_t* verbs;
     const float* points;
@@ -69,19 +54,7 @@ struct StrokeArgs {
     int sequential;
     lyon_vertex_source* sources;
     uint32_t width_stride;  // floats from one point's width factor to the next's (0 means 1)
-    // Interior runs (fixed width, positions output): with `use_runs`, the count pass takes a
-    // curve's flattening steps in runs (stroke.cu) and counts the runs in `*run_counter`; with
-    // `runs` (capacity `runs_cap`), the emit pass takes the same runs and appends one RunRec per
-    // run there (through `*run_counter`, zeroed before the launch) for launch_stroke_runs.
-    // Runs change no output: an emit pass without `runs` walks every step.
-    int use_runs;
-    uint32_t* run_counter;
-    RunRec* runs;
-    uint32_t runs_cap;
 };
-// Writes the output of `n` interior runs (after the emit pass that recorded them).
-cudaError_t launch_stroke_runs(const RunRec* runs, uint32_t n, float* vertices, void* indices,
-                               int index_bits, int num_sms, cudaStream_t stream);
 
 // Basic shapes (shapes.cu): `params` holds 4 floats per rectangle (min x, min y, max x, max y)
 // or 3 per circle (center x, center y, radius).
@@ -178,10 +151,8 @@ cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cud
 // Writes out_a[n], out_b[n] (the scan totals) and the two u32 words at `words` into `host_dst`
 // (mapped pinned host memory) with a kernel, so that the read-back does not queue behind large
 // device->host copies on the copy engines.
-// With `extra` (optional), host_dst[3] receives *extra.
 cudaError_t launch_read_totals(const uint64_t* a_total, const uint64_t* b_total,
-                               const uint32_t* words, uint64_t* host_dst, cudaStream_t s,
-                               const uint32_t* extra = nullptr);
+                               const uint32_t* words, uint64_t* host_dst, cudaStream_t s);
 
 // Processing order by class: paths with more than `big_points` points (0: none) first, then the
 // other paths, then line-only paths of at most `short_points` points (0: none; at most

@@ -192,18 +192,15 @@ __global__ void narrow_u64_kernel(const uint64_t* in, uint32_t* out, uint32_t n)
 }
 
 __global__ void read_totals_kernel(const uint64_t* a_total, const uint64_t* b_total,
-                                   const uint32_t* words, uint64_t* host_dst,
-                                   const uint32_t* extra) {
+                                   const uint32_t* words, uint64_t* host_dst) {
     host_dst[0] = *a_total;
     host_dst[1] = *b_total;
     host_dst[2] = (uint64_t)words[0] | ((uint64_t)words[1] << 32);
-    if (extra) host_dst[3] = *extra;
 }
 
 cudaError_t launch_read_totals(const uint64_t* a_total, const uint64_t* b_total,
-                               const uint32_t* words, uint64_t* host_dst, cudaStream_t s,
-                               const uint32_t* extra) {
-    read_totals_kernel<<<1, 1, 0, s>>>(a_total, b_total, words, host_dst, extra);
+                               const uint32_t* words, uint64_t* host_dst, cudaStream_t s) {
+    read_totals_kernel<<<1, 1, 0, s>>>(a_total, b_total, words, host_dst);
     note_launches(1);
     return cudaGetLastError();
 }

@@ -489,16 +489,16 @@ __device__ __noinline__ void flush_tails(WarpSmem& sm, int lane, uint32_t count,
     __syncwarp();
 }
 
-// Steps [cb, min(ce, cb + 32)) of the current verb window (lane = step): flattened points, merge filter,
+// Steps [cb, cb + 32) of the current verb window (lane = step): flattened points, merge filter,
 // joins, output. See the file comment. `ejn` counts the joins queued for emission.
 template <bool EMIT, bool ATTR>
 __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, const uint32_t vi,
                                               const uint32_t nv, const uint32_t sincl,
                                               const uint32_t S_w, const uint32_t cb,
-                                              const uint32_t ce, const StrokeParams& P,
-                                              const PathOut& po, SubState& S, uint32_t& vcur,
-                                              uint32_t& icur, uint32_t& ejn, int& status) {
-    const uint32_t nsteps = min(32u, ce - cb);
+                                              const StrokeParams& P, const PathOut& po,
+                                              SubState& S, uint32_t& vcur, uint32_t& icur,
+                                              uint32_t& ejn, int& status) {
+    const uint32_t nsteps = min(32u, S_w - cb);
     const bool active = (uint32_t)lane < nsteps;
 
     // ---- 1. the flattened point of step cb + lane ----
@@ -927,311 +927,6 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
     __syncwarp();
 }
 
-// ---- interior runs ------------------------------------------------------------------------------
-// Inside a curve, lyon's steps are flattening steps (stroke.rs:1743-1806): two vertices at
-// join +- normal * hw and the two triangles of the edge before it, nothing else, as long as no
-// point is merged into its predecessor (stroke.rs:1530-1536), every join's turn is below 90
-// degrees (the fast-path test) and the skip test cannot fire. Once the walk has taken a unit's
-// first two steps, it checks the unit's later steps 30 at a time (lane = step) with only that
-// arithmetic: each lane evaluates the walk's own conditions for its step (merge test, fast-path
-// test, the count pass's skip bound) on the same f32 values, and the run ends at the first step
-// that fails one of them or at the unit's end point. The count pass adds the run's counts; the
-// emit pass records the run (RunRec) and stroke_run_kernel writes its output, so the walk's large
-// code and a run's small loop do not share the instruction cache. The walk then resumes at the
-// step that ended the run with the state it would have had, so both passes take identical
-// decisions and the output is the walk's, bit for bit.
-constexpr uint32_t RUN_MIN_STEPS = 8;  // units with fewer flattened points are walked
-constexpr uint32_t NO_RUN = 0xFFFFFFFFu;
-
-struct RunAt {
-    uint32_t step;  // window step of the unit's third point (NO_RUN: none)
-    uint32_t slot;  // verb slot
-    uint32_t unit;  // 0: part A, 1: part B of a split quadratic
-};
-
-// The first unit whose third step lies in [from, window end), among the window's curves.
-__device__ __forceinline__ RunAt next_run(const WarpSmem& sm, int lane, uint32_t nv,
-                                          uint32_t from) {
-    uint32_t best = NO_RUN;
-    if ((uint32_t)lane < nv) {
-        const VerbSlot& sl = sm.verbs[lane];
-        if (sl.kind == LYON_VERB_QUADRATIC_TO || sl.kind == LYON_VERB_CUBIC_TO) {
-            const uint32_t a = sl.excl + 2u;
-            const uint32_t b = sl.excl + sl.mA + 2u;
-            if (sl.mA >= RUN_MIN_STEPS && a >= from) {
-                best = a;
-            } else if (sl.mB >= RUN_MIN_STEPS && b >= from) {
-                best = b;
-            }
-        }
-    }
-    RunAt r;
-    r.step = __reduce_min_sync(FULL, best);
-    r.slot = 0;
-    r.unit = 0;
-    if (r.step != NO_RUN) {
-        const uint32_t owner = __ffs(__ballot_sync(FULL, best == r.step)) - 1;
-        r.slot = owner;
-        r.unit = sm.verbs[owner].excl + 2u == r.step ? 0u : 1u;
-    }
-    return r;
-}
-
-// What the run needs of the walk's state (passed by value, so that the walk's state stays in
-// registers) and what it gives back.
-struct RunIn {
-    V2 c1, c2;
-    uint32_t n, tc_verb, tc_unit, tc_k, jbase, jfpos, jfneg, first_id;
-    float tc_t;
-    bool f1, jfast, jskip, jsym;
-};
-struct RunOut {
-    uint32_t taken;  // steps taken (0: none, the walk goes on unchanged)
-    V2 c1, c2, c3;   // the new last three kept points
-    float t1;        // t of the new last kept point
-};
-
-// Checks the unit's steps from its third on (its join at the second point) while they are plain
-// flattening steps; returns how many the run takes.
-__device__ __noinline__ RunOut run_check(const WarpSmem& sm, const int lane, const RunAt r,
-                                         const uint32_t abs_verb, const StrokeParams P,
-                                         const RunIn S) {
-    RunOut out;
-    out.taken = 0;
-    const VerbSlot& sl = sm.verbs[r.slot];
-    const Poly pp = r.unit == 0 ? sl.pA : sl.pB;
-    const float s = r.unit == 0 ? sl.sA : sl.sB;
-    const uint32_t m = r.unit == 0 ? sl.mA : sl.mB;
-    // The walk has taken steps 1 and 2 of this unit, both kept, and the join at step 1 was a
-    // flattening step right before this one (its two vertices end the output so far).
-    if (S.n < 3 || S.tc_verb != abs_verb || S.tc_unit != r.unit || S.tc_k != 2 || !S.f1 ||
-        !S.jfast || S.jskip || !S.jsym || S.jfpos != S.jbase || S.jfneg != S.jbase + 1 ||
-        S.jbase + 2u != S.first_id)
-        return out;
-    uint32_t a = 3;          // first step of this iteration
-    uint32_t kc = 2;         // carried t: t_kc
-    float tcv = S.tc_t;
-    uint32_t taken = 0;
-    V2 l_c1 = S.c1, l_c2 = S.c2, l_c3 = S.c2;
-    float l_t1 = tcv;
-    for (;;) {
-        // Lane L holds the point of step kp = a - 2 + L, the join there for L = 1..30.
-        const uint32_t kp = min(a - 2u + (uint32_t)lane, m - 1u);
-        const float t = kp <= kc ? (kp == kc ? tcv : accumulate_t(s, 0, 0.0f, kp))
-                                 : accumulate_t_from(s, kc, tcv, kp);
-        const V2 cur = poly_sample(pp, t);
-        const V2 prv = shfl_up_v2(cur, 1);
-        const V2 nxt = V2{__shfl_down_sync(FULL, cur.x, 1), __shfl_down_sync(FULL, cur.y, 1)};
-        if (a == 3) {
-            // Steps 1 and 2 as the walk kept them.
-            const bool same = same_bits(shfl_v2(cur, 0), S.c2) && same_bits(shfl_v2(cur, 1), S.c1);
-            if (!same) return out;
-        }
-        const V2 pe = cur - prv;
-        const V2 ne = nxt - cur;
-        const bool valid = lane >= 1 && lane <= 30 && a - 2u + (uint32_t)lane <= m - 2u;
-        bool ok = valid && t != 1.0f && !too_close(cur, nxt, P.merge_threshold) &&
-                  dot(pe, ne) > 0.0f;
-        if (ok) {
-            const float mm = fmaxf(fmaxf(fabsf(cur.x), fabsf(cur.y)),
-                                   fmaxf(fabsf(prv.x), fabsf(prv.y))) + 3.0f * P.hw;
-            const float bnd = mm * 7.62939453125e-06f;  // 2^-17, as the walk's skip bound
-            ok = sqlen(pe) > bnd * bnd;
-        }
-        const uint32_t fail = __ballot_sync(FULL, valid && !ok);
-        const uint32_t vmask = __ballot_sync(FULL, valid);
-        // Taken: lanes 1 .. F - 1, F the first failing lane (or every valid lane).
-        const uint32_t lim = fail ? (uint32_t)(__ffs(fail) - 1) : 32u;
-        const uint32_t tmask = vmask & ((lim >= 32u) ? FULL : ((1u << lim) - 1u));
-        const uint32_t nt = __popc(tmask);
-        if (nt > 0) {
-            // The last taken join is at lane nt (its point is step a - 2 + nt).
-            const int lj = (int)nt;
-            l_c1 = shfl_v2(cur, lj + 1);
-            l_c2 = shfl_v2(cur, lj);
-            l_c3 = shfl_v2(cur, lj - 1);
-            l_t1 = __shfl_sync(FULL, t, lj + 1);
-            taken += nt;
-        }
-        const uint32_t nvalid = __popc(vmask);
-        if (nt < nvalid || nvalid < 30u) break;
-        // Carry t of lane 30 (step a + 28) into the next iteration.
-        kc = a + 28u;
-        tcv = __shfl_sync(FULL, t, 30);
-        a += 30u;
-    }
-    out.taken = taken;
-    out.c1 = l_c1;
-    out.c2 = l_c2;
-    out.c3 = l_c3;
-    out.t1 = l_t1;
-    return out;
-}
-
-// The walk's state after `o.taken` steps of a run (the unit's steps 3 .. 2 + taken), as the
-// walk itself would have left it. The side points of the last join are left to the walk
-// (fast_join_sides recomputes them from the last three points when it needs them); the emit
-// pass's tangent of the last edge is computed here as the walk computes it.
-template <bool EMIT>
-__device__ __forceinline__ void apply_run(const RunOut& o, const RunAt r, uint32_t abs_verb,
-                                          const PathOut& po, SubState& S, uint32_t& vcur,
-                                          uint32_t& icur) {
-    vcur += 2u * o.taken;
-    icur += 6u * o.taken;
-    S.n += o.taken;
-    S.c1 = o.c1;
-    S.c2 = o.c2;
-    S.c3 = o.c3;
-    S.f1 = o.t1 != 1.0f;
-    S.f2 = true;
-    S.s1 = NO_SLOT;
-    S.tc.verb = abs_verb;
-    S.tc.unit = r.unit;
-    S.tc.k = 2u + o.taken;
-    S.tc.t = o.t1;
-    S.jbase = po.id_base + vcur - 2u;
-    S.jfpos = S.jbase;
-    S.jfneg = S.jbase + 1u;
-    S.jfrom_f = 0;
-    S.jsym = true;
-    S.jfast = true;
-    S.jskip = false;
-    S.jside_valid = false;
-    if (EMIT) {
-        const V2 e = S.c1 - S.c2;
-        S.jtan = e / vlength(e);
-    }
-}
-
-// One run's output (a RunRec): 30 joins per iteration, lane L (1..30) performing the join at
-// the unit's point kp = a - 2 + L as the walk's flattening-step join does (process_chunk): the
-// tangents of its two edges, compute_normal (math_utils.rs:16-40), the vertices
-// join +- normal * hw, then the edge's two triangles.
-__device__ __forceinline__ void emit_run(const RunRec& R, const int lane, float2* vertices,
-                                         void* indices, int index_bits) {
-    Poly pp;
-    pp.a0 = V2{R.a0x, R.a0y};
-    pp.a1 = V2{R.a1x, R.a1y};
-    pp.a2 = V2{R.a2x, R.a2y};
-    pp.a3 = V2{R.a3x, R.a3y};
-    pp.cubic = R.cubic != 0;
-    const float s = R.s;
-    const uint32_t last = R.len + 1u;  // the run's last join point
-    uint32_t kc = 2;
-    float tcv = R.t2;
-    for (uint32_t a = 3;; a += 30u) {
-        const uint32_t kp = min(a - 2u + (uint32_t)lane, last + 1u);
-        const float t = kp <= kc ? (kp == kc ? tcv : accumulate_t(s, 0, 0.0f, kp))
-                                 : accumulate_t_from(s, kc, tcv, kp);
-        const V2 cur = poly_sample(pp, t);
-        const V2 nxt = V2{__shfl_down_sync(FULL, cur.x, 1), __shfl_down_sync(FULL, cur.y, 1)};
-        const V2 ne = nxt - cur;
-        const V2 tan_out = ne / vlength(ne);
-        const V2 tan_in = shfl_up_v2(tan_out, 1);
-        const uint32_t k = a - 2u + (uint32_t)lane;
-        if (lane >= 1 && lane <= 30 && k <= last) {
-            const V2 nrm = compute_normal(tan_in, tan_out);
-            const V2 pn = cur + nrm * R.hw;
-            const V2 nn = cur - nrm * R.hw;
-            const uint32_t rel = k - 2u;
-            const uint64_t vo = R.vo + 2ull * rel;
-            const uint64_t io = R.io + 6ull * rel;
-            const uint32_t b = R.base + 2u * rel;
-            float2* dst = vertices + vo;
-            if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
-                *reinterpret_cast<float4*>(dst) = make_float4(pn.x, pn.y, nn.x, nn.y);
-            } else {
-                dst[0] = make_float2(pn.x, pn.y);
-                dst[1] = make_float2(nn.x, nn.y);
-            }
-            // add_edge_triangles (stroke.rs:1869-1904) after a flattening step:
-            // (prev -, prev +, +) and (prev -, +, -).
-            if (index_bits == 32) {
-                uint32_t* di = reinterpret_cast<uint32_t*>(indices) + io;
-                if ((reinterpret_cast<uintptr_t>(di) & 7u) == 0) {
-                    uint2* d2 = reinterpret_cast<uint2*>(di);
-                    d2[0] = make_uint2(b - 1u, b - 2u);
-                    d2[1] = make_uint2(b, b - 1u);
-                    d2[2] = make_uint2(b, b + 1u);
-                } else {
-                    di[0] = b - 1u;
-                    di[1] = b - 2u;
-                    di[2] = b;
-                    di[3] = b - 1u;
-                    di[4] = b;
-                    di[5] = b + 1u;
-                }
-            } else {
-                uint16_t* di = reinterpret_cast<uint16_t*>(indices) + io;
-                di[0] = (uint16_t)(b - 1u);
-                di[1] = (uint16_t)(b - 2u);
-                di[2] = (uint16_t)b;
-                di[3] = (uint16_t)(b - 1u);
-                di[4] = (uint16_t)b;
-                di[5] = (uint16_t)(b + 1u);
-            }
-        }
-        if (a + 28u >= last) break;
-        kc = a + 28u;
-        tcv = __shfl_sync(FULL, t, 30);
-    }
-}
-
-constexpr int RUN_WARPS = 8;
-
-// Writes every recorded run, one warp per run.
-__global__ void __launch_bounds__(RUN_WARPS * 32)
-    stroke_run_kernel(const RunRec* __restrict__ runs, uint32_t n, float2* vertices,
-                      void* indices, int index_bits) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * RUN_WARPS;
-    for (uint32_t w = blockIdx.x * RUN_WARPS + (threadIdx.x >> 5); w < n; w += warps) {
-        const RunRec R = runs[w];
-        emit_run(R, lane, vertices, indices, index_bits);
-    }
-}
-
-// Appends the run that starts at the unit's third step (the walk's output position vcur/icur)
-// to the emit pass's run records.
-__device__ __noinline__ void record_run(const WarpSmem& sm, const int lane, const RunAt r,
-                                        const uint32_t taken, const float t2,
-                                        const StrokeParams P, const PathOut po,
-                                        const StrokeArgs& A, const uint32_t vcur,
-                                        const uint32_t icur, int& status) {
-    int st = LYON_OK;
-    if (lane == 0) {
-        const uint32_t slot = atomicAdd(A.run_counter, 1u);
-        if (slot >= A.runs_cap || vcur + 2u * taken > po.vmax || icur + 6u * taken > po.imax) {
-            st = LYON_ERR_INTERNAL;
-        } else {
-            const VerbSlot& sl = sm.verbs[r.slot];
-            const Poly& pp = r.unit == 0 ? sl.pA : sl.pB;
-            RunRec R;
-            R.a0x = pp.a0.x;
-            R.a0y = pp.a0.y;
-            R.a1x = pp.a1.x;
-            R.a1y = pp.a1.y;
-            R.a2x = pp.a2.x;
-            R.a2y = pp.a2.y;
-            R.a3x = pp.a3.x;
-            R.a3y = pp.a3.y;
-            R.s = r.unit == 0 ? sl.sA : sl.sB;
-            R.t2 = t2;
-            R.hw = P.hw;
-            R.cubic = pp.cubic ? 1u : 0u;
-            R.len = taken;
-            R.base = po.id_base + vcur;
-            R.vo = (uint64_t)(po.vout - reinterpret_cast<float2*>(A.vertices)) + vcur;
-            R.io = (A.index_bits == 16
-                        ? (uint64_t)((uint16_t*)po.iout - (uint16_t*)A.indices)
-                        : (uint64_t)((uint32_t*)po.iout - (uint32_t*)A.indices)) + icur;
-            A.runs[slot] = R;
-        }
-    }
-    st = __shfl_sync(FULL, st, 0);
-    if (st != LYON_OK && status == LYON_OK) status = st;
-}
-
 // Strokes one path with the whole warp. On return vcur/icur/status hold the path's counts so
 // far; when the tail of its last sub-path was queued (`deferred`), the queue finishes the path.
 template <bool EMIT, bool ATTR>
@@ -1310,52 +1005,9 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             speculate_joins(sm, lane, nv, S_w, P, S.c1, S.n > 0);
             __syncwarp();
             uint32_t ejn = 0;
-            uint32_t cb = 0, tried = 0;
-            while (cb < S_w) {
-                // Chunks of 32 steps, cut short where a curve's interior run can start.
-                uint32_t ce = min(cb + 32u, S_w);
-                RunAt run;
-                run.step = NO_RUN;
-                if (!ATTR && (EMIT ? A.runs != nullptr : A.use_runs != 0)) {
-                    run = next_run(sm, lane, nv, max(cb, tried));
-                    if (run.step < ce) ce = run.step;
-                }
-                if (ce > cb)
-                    process_chunk<EMIT, ATTR>(sm, lane, vi, nv, sincl, S_w, cb, ce, P, po, S,
-                                              vcur, icur, ejn, status);
-                cb = ce;
-                if (run.step == cb && run.step != NO_RUN) {
-                    tried = cb + 1u;
-                    if (status == LYON_OK) {
-                        RunIn in;
-                        in.c1 = S.c1;
-                        in.c2 = S.c2;
-                        in.n = S.n;
-                        in.tc_verb = S.tc.verb;
-                        in.tc_unit = S.tc.unit;
-                        in.tc_k = S.tc.k;
-                        in.tc_t = S.tc.t;
-                        in.jbase = S.jbase;
-                        in.jfpos = S.jfpos;
-                        in.jfneg = S.jfneg;
-                        in.first_id = po.id_base + vcur;
-                        in.f1 = S.f1;
-                        in.jfast = S.jfast;
-                        in.jskip = S.jskip;
-                        in.jsym = S.jsym;
-                        const RunOut o = run_check(sm, lane, run, vi + run.slot, P, in);
-                        if (o.taken > 0) {
-                            if (!EMIT) {
-                                if (lane == 0 && A.run_counter) atomicAdd(A.run_counter, 1u);
-                            } else {
-                                record_run(sm, lane, run, o.taken, S.tc.t, P, po, A, vcur, icur,
-                                           status);
-                            }
-                            apply_run<EMIT>(o, run, vi + run.slot, po, S, vcur, icur);
-                            cb += o.taken;  // the unit's step 3 + taken
-                        }
-                    }
-                }
+            for (uint32_t cb = 0; cb < S_w; cb += 32) {
+                process_chunk<EMIT, ATTR>(sm, lane, vi, nv, sincl, S_w, cb, P, po, S, vcur, icur, ejn,
+                                    status);
             }
             if (EMIT && ejn > 0) {
                 __syncwarp();
@@ -1625,21 +1277,6 @@ cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStrea
     } else {
         stroke_kernel<false, false><<<grid, STROKE_WARPS * 32, STROKE_SMEM, stream>>>(args);
     }
-    note_launches(1);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_stroke_runs(const RunRec* runs, uint32_t n, float* vertices, void* indices,
-                               int index_bits, int num_sms, cudaStream_t stream) {
-    if (n == 0) return cudaSuccess;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stroke_run_kernel, RUN_WARPS * 32, 0);
-    if (per_sm <= 0) per_sm = 1;
-    const uint32_t want = (n + RUN_WARPS - 1) / RUN_WARPS;
-    const uint32_t cap = (uint32_t)(num_sms > 0 ? num_sms : 1) * (uint32_t)per_sm;
-    const uint32_t grid = want < cap ? want : cap;
-    stroke_run_kernel<<<grid, RUN_WARPS * 32, 0, stream>>>(
-        runs, n, reinterpret_cast<float2*>(vertices), indices, index_bits);
     note_launches(1);
     return cudaGetLastError();
 }

@@ -731,6 +731,31 @@ int lyon_svg_parse_paths(const char* text, const uint64_t* string_offsets, uint3
                          int32_t* status, int32_t* error_line, int32_t* error_column,
                          uint64_t* total_verbs, uint64_t* total_points);
 
+/* A batch parsed on the device by lyon_gpu_svg_parse_paths (device memory owned by the context
+ * until its next lyon_gpu_svg_parse_paths call). */
+typedef struct lyon_gpu_svg_output {
+    lyon_path_batch batch;  /* verbs, points, verb_offsets / point_offsets (num_strings + 1) */
+    float* widths;          /* one per point when num_attributes is 1, else NULL */
+    int32_t* status;        /* per string: LYON_OK or a LYON_SVG_ERR_* code */
+    int32_t* error_line;    /* per string */
+    int32_t* error_column;  /* per string */
+    uint64_t total_verbs;
+    uint64_t total_points;
+    uint32_t num_failed;    /* strings whose status is not LYON_OK */
+} lyon_gpu_svg_output;
+
+/* lyon_svg_parse_paths on the device: the same parser (PathParser::parse, crates/extra/src/
+ * parser.rs:154-490) and the same output layout, statuses and error positions, with the strings
+ * (`text`, `string_offsets`: device memory) parsed one per thread in a counting pass, a scan of
+ * the counts and a writing pass, so a scene's path data becomes a device batch that the batched
+ * tessellation calls read as it is. Numbers are rounded to f32 exactly as Rust's
+ * `f32::from_str` (and the host parser) rounds them; arc points go through the device's
+ * cosf/sinf/tanf, which can differ from the host libm's in the last bit. `options->num_threads`
+ * is ignored. Synchronises once to size the outputs. */
+int lyon_gpu_svg_parse_paths(lyon_gpu_context* ctx, const char* text,
+                             const uint64_t* string_offsets, uint32_t num_strings,
+                             const lyon_svg_parse_options* options, lyon_gpu_svg_output* out);
+
 /* Library version and build information (static string). */
 const char* lyon_gpu_version(void);
 

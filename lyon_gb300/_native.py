@@ -67,6 +67,12 @@ class CHatchOutput(ctypes.Structure):
                 ("total", u64)]
 
 
+class CSvgOutput(ctypes.Structure):
+    _fields_ = [("batch", CPathBatch), ("widths", c_p), ("status", c_p), ("error_line", c_p),
+                ("error_column", c_p), ("total_verbs", u64), ("total_points", u64),
+                ("num_failed", u32)]
+
+
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
                 ("device_budget_bytes", u64), ("num_stroke_workers", u32),
@@ -188,6 +194,8 @@ def load(build_if_missing: bool = True):
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [c_p, ctypes.POINTER(CStrokeTuning)]
+        L.lyon_gpu_svg_parse_paths.restype = ctypes.c_int
+        L.lyon_gpu_svg_parse_paths.argtypes = [c_p, c_p, c_p, u32, c_p, ctypes.POINTER(CSvgOutput)]
         L.lyon_svg_parse_paths.restype = ctypes.c_int
         L.lyon_svg_parse_paths.argtypes = [c_p, c_p, u32, c_p, c_p, u64, c_p, u64, c_p, c_p, c_p,
                                            c_p, c_p, c_p, c_p, c_p]
@@ -261,7 +269,7 @@ EXPORTED = [
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
     "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",
     "lyon_gpu_stroke_paths_variable_width", "lyon_gpu_stroke_path_variable_width",
-    "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_stroke_paths_custom",
+    "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_svg_parse_paths", "lyon_gpu_stroke_paths_custom",
     "lyon_gpu_interpolate_attributes", "lyon_gpu_stroke_path_custom",
     "lyon_gpu_fill_paths_custom", "lyon_gpu_interpolate_fill_attributes",
     "lyon_gpu_fill_path_custom", "lyon_gpu_flatten_arcs", "lyon_gpu_hatch_paths",

@@ -43,6 +43,8 @@ struct lyon_gpu_context {
     DevBuf small;  // [0] work counter, [1] scan counter, [2] error flag, [3] failed paths,
                    // [4..5] processing-order counters
     DevBuf order;  // processing order of the current stroke batch (long paths first)
+    // lyon_gpu_svg_parse_paths: counts, diagnostics, offsets and the parsed batch.
+    DevBuf svg_counts, svg_diag, svg_off64, svg_off32, svg_verbs, svg_points, svg_widths;
     bool order_valid = false;
     DevBuf path_class, class_counters;  // classification for the one-thread-per-path phase
     bool split_valid = false;           // class_counters holds the first short item
@@ -871,7 +873,9 @@ void lyon_gpu_destroy(lyon_gpu_context* ctx) {
                       &ctx->h_in_poff,  &ctx->h_in_opts,   &ctx->slot_v[0],   &ctx->slot_v[1],
                       &ctx->slot_i[0],  &ctx->slot_i[1],   &ctx->flat_counts, &ctx->flat_offsets,
                       &ctx->flat_points, &ctx->in_verbs,   &ctx->in_points,   &ctx->in_offsets,
-                      &ctx->in_options, &ctx->order, &ctx->slot_status[0],
+                      &ctx->in_options, &ctx->order, &ctx->svg_counts, &ctx->svg_diag,
+                      &ctx->svg_off64, &ctx->svg_off32, &ctx->svg_verbs, &ctx->svg_points,
+                      &ctx->svg_widths, &ctx->slot_status[0],
                       &ctx->slot_status[1], &ctx->path_class, &ctx->class_counters,
                       &ctx->in_widths, &ctx->out_sources, &ctx->out_attrs, &ctx->in_attrs,
                       &ctx->src_counts, &ctx->src_offsets, &ctx->src_scratch,
@@ -1091,6 +1095,84 @@ int lyon_gpu_stroke_paths_each(lyon_gpu_context* ctx, const lyon_path_batch* bat
         tv += out.total_vertices;
     }
     *total_vertices = tv;
+    return LYON_OK;
+}
+
+int lyon_gpu_svg_parse_paths(lyon_gpu_context* ctx, const char* text,
+                             const uint64_t* string_offsets, uint32_t num_strings,
+                             const lyon_svg_parse_options* options, lyon_gpu_svg_output* out) {
+    if (!ctx || !out || (num_strings && (!text || !string_offsets)) || num_strings > 0x7FFFFFFEu)
+        return LYON_ERR_INVALID_ARGUMENT;
+    const uint32_t num_attributes = options ? options->num_attributes : 0;
+    if (num_attributes > 1) return LYON_ERR_UNSUPPORTED;
+    const long long stop_at = options ? options->stop_at : -1;
+    cudaSetDevice(ctx->device);
+    memset(out, 0, sizeof(*out));
+    const uint32_t n = num_strings;
+    cudaStream_t s = ctx->stream;
+    if (!ensure(ctx, ctx->svg_counts, (size_t)n * 8 + 16) ||
+        !ensure(ctx, ctx->svg_diag, (size_t)n * 12 + 16) ||
+        !ensure(ctx, ctx->svg_off64, ((size_t)n + 1) * 16) ||
+        !ensure(ctx, ctx->svg_off32, ((size_t)n + 1) * 8) ||
+        !ensure(ctx, ctx->scan_state, 2 * lg::scan_tile_count(n) * 8 + 16))
+        return LYON_ERR_OUT_OF_MEMORY;
+    uint32_t* vc = as<uint32_t>(ctx->svg_counts);
+    uint32_t* pc = vc + n;
+    int32_t* st = as<int32_t>(ctx->svg_diag);
+    int32_t* el = st + n;
+    int32_t* ec = el + n;
+    uint64_t* voff = as<uint64_t>(ctx->svg_off64);
+    uint64_t* poff = voff + n + 1;
+    uint32_t* sw = small_words(ctx);
+    if (!set_err(ctx, "svg count",
+                 lg::launch_svg_parse(text, string_offsets, n, num_attributes, stop_at, false, vc,
+                                      pc, st, el, ec, nullptr, nullptr, nullptr, nullptr,
+                                      nullptr, ctx->num_sms, s)))
+        return LYON_ERR_CUDA;
+    cudaMemsetAsync(sw + 2, 0, 8, s);
+    if (!set_err(ctx, "svg scan",
+                 lg::launch_scan_pairs(vc, pc, voff, poff, n,
+                                       as<unsigned long long>(ctx->scan_state), sw + 1,
+                                       reinterpret_cast<int*>(sw + 2), s)) ||
+        !set_err(ctx, "svg failures",
+                 lg::launch_per_path_limit(vc, pc, st, n, 0, ~0ull, sw + 3, s)))
+        return LYON_ERR_CUDA;
+    uint64_t h[3] = {0, 0, 0};
+    cudaMemcpyAsync(&h[0], voff + n, 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&h[1], poff + n, 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&h[2], sw + 2, 8, cudaMemcpyDeviceToHost, s);
+    if (!set_err(ctx, "sync", cudaStreamSynchronize(s))) return LYON_ERR_CUDA;
+    if ((uint32_t)h[2] != 0) {
+        ctx->last_error = "scan look-back wait exceeded its bound";
+        return LYON_ERR_CUDA;
+    }
+    if (h[0] > 0xFFFFFFFFull || h[1] > 0xFFFFFFFFull) return LYON_ERR_UNSUPPORTED;
+    if (!ensure(ctx, ctx->svg_verbs, h[0] + 16) || !ensure(ctx, ctx->svg_points, h[1] * 8 + 16) ||
+        (num_attributes && !ensure(ctx, ctx->svg_widths, h[1] * 4 + 16)))
+        return LYON_ERR_OUT_OF_MEMORY;
+    uint32_t* voff32 = as<uint32_t>(ctx->svg_off32);
+    uint32_t* poff32 = voff32 + n + 1;
+    float* widths = num_attributes ? as<float>(ctx->svg_widths) : nullptr;
+    if (!set_err(ctx, "svg write",
+                 lg::launch_svg_parse(text, string_offsets, n, num_attributes, stop_at, true,
+                                      nullptr, nullptr, nullptr, nullptr, nullptr, voff, poff,
+                                      as<uint8_t>(ctx->svg_verbs), as<float>(ctx->svg_points),
+                                      widths, ctx->num_sms, s)) ||
+        !set_err(ctx, "svg offsets", lg::launch_narrow_u64(voff, voff32, n + 1, s)) ||
+        !set_err(ctx, "svg offsets", lg::launch_narrow_u64(poff, poff32, n + 1, s)))
+        return LYON_ERR_CUDA;
+    out->batch.verbs = as<uint8_t>(ctx->svg_verbs);
+    out->batch.points = as<float>(ctx->svg_points);
+    out->batch.verb_offsets = voff32;
+    out->batch.point_offsets = poff32;
+    out->batch.num_paths = n;
+    out->widths = widths;
+    out->status = st;
+    out->error_line = el;
+    out->error_column = ec;
+    out->total_verbs = h[0];
+    out->total_points = h[1];
+    out->num_failed = (uint32_t)(h[2] >> 32);
     return LYON_OK;
 }
 

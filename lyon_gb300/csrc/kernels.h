@@ -148,6 +148,17 @@ cudaError_t launch_per_path_limit(uint32_t* vtx_counts, uint32_t* idx_counts, in
 
 cudaError_t launch_narrow_u64(const uint64_t* in, uint32_t* out, uint32_t n, cudaStream_t s);
 
+// lyon's SVG path parser (svg.cu) on the device, one thread per string: the counting pass
+// (verb/point counts, status, error position) or, with `write`, the writing pass at the scanned
+// offsets.
+cudaError_t launch_svg_parse(const char* text, const uint64_t* string_offsets, uint32_t n,
+                             uint32_t num_attributes, long long stop_at, bool write,
+                             uint32_t* verb_counts, uint32_t* point_counts, int32_t* status,
+                             int32_t* error_line, int32_t* error_column,
+                             const uint64_t* verb_offsets, const uint64_t* point_offsets,
+                             uint8_t* verbs, float* points, float* widths, int num_sms,
+                             cudaStream_t stream);
+
 // Writes out_a[n], out_b[n] (the scan totals) and the two u32 words at `words` into `host_dst`
 // (mapped pinned host memory) with a kernel, so that the read-back does not queue behind large
 // device->host copies on the copy engines.

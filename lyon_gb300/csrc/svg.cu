@@ -19,6 +19,10 @@
 #include <vector>
 
 #include "../../include/lyon_gpu.h"
+#include "decimal.cuh"
+#include "kernels.h"
+
+#define HD __host__ __device__
 
 namespace {
 
@@ -36,7 +40,7 @@ struct Source {
     bool finished = false;
     int32_t line = 0, col = 0;
 
-    bool next_char(uint32_t* c) {
+    HD bool next_char(uint32_t* c) {
         if (p >= end) return false;
         uint32_t b = *p++;
         int extra = b >= 0xF0 ? 3 : b >= 0xE0 ? 2 : b >= 0xC0 ? 1 : 0;
@@ -45,7 +49,7 @@ struct Source {
         *c = v;
         return true;
     }
-    Source(const char* s, size_t n)
+    HD Source(const char* s, size_t n)
         : p(reinterpret_cast<const unsigned char*>(s)),
           end(reinterpret_cast<const unsigned char*>(s) + n) {
         uint32_t c;
@@ -59,15 +63,15 @@ struct Source {
         col = 0;
     }
     // char::is_whitespace (the Unicode White_Space set) or ','.
-    static bool is_ws(uint32_t c) {
+    HD static bool is_ws(uint32_t c) {
         return (c >= 0x09 && c <= 0x0D) || c == 0x20 || c == 0x85 || c == 0xA0 || c == 0x1680 ||
                (c >= 0x2000 && c <= 0x200A) || c == 0x2028 || c == 0x2029 || c == 0x202F ||
                c == 0x205F || c == 0x3000;
     }
-    void skip_whitespace() {
+    HD void skip_whitespace() {
         while (!finished && (is_ws(current) || current == ',')) advance_one();
     }
-    void advance_one() {
+    HD void advance_one() {
         if (finished) return;
         uint32_t c;
         if (!next_char(&c)) {
@@ -94,7 +98,7 @@ struct Out {
     uint64_t nv = 0, np = 0;
     Pt first{0.0f, 0.0f};
     float first_w = 0.0f;
-    void point(Pt p, float w) {
+    HD void point(Pt p, float w) {
         if (points) {
             points[2 * np] = p.x;
             points[2 * np + 1] = p.y;
@@ -102,32 +106,32 @@ struct Out {
         if (widths) widths[np] = w;
         ++np;
     }
-    void verb(uint8_t v) {
+    HD void verb(uint8_t v) {
         if (verbs) verbs[nv] = v;
         ++nv;
     }
-    void begin(Pt at, float w) {
+    HD void begin(Pt at, float w) {
         first = at;
         first_w = w;
         point(at, w);
         verb(LYON_VERB_BEGIN);
     }
-    void line_to(Pt to, float w) {
+    HD void line_to(Pt to, float w) {
         point(to, w);
         verb(LYON_VERB_LINE_TO);
     }
-    void quad_to(Pt c, Pt to, float w) {
+    HD void quad_to(Pt c, Pt to, float w) {
         point(c, 0.0f);
         point(to, w);
         verb(LYON_VERB_QUADRATIC_TO);
     }
-    void cubic_to(Pt c1, Pt c2, Pt to, float w) {
+    HD void cubic_to(Pt c1, Pt c2, Pt to, float w) {
         point(c1, 0.0f);
         point(c2, 0.0f);
         point(to, w);
         verb(LYON_VERB_CUBIC_TO);
     }
-    void end(bool close) {
+    HD void end(bool close) {
         if (close) point(first, first_w);
         verb(close ? LYON_VERB_CLOSE : LYON_VERB_END);
     }
@@ -136,7 +140,7 @@ struct Out {
 // ---- arcs (crates/geom/src/arc.rs) -------------------------------------------------------
 
 // Rotation2D::transform_point / transform_vector (euclid): the rotation matrix of `angle`.
-Pt rotate(float angle, Pt v) {
+HD Pt rotate(float angle, Pt v) {
     const float s = sinf(angle), c = cosf(angle);
     return Pt{v.x * c - v.y * s, v.x * s + v.y * c};
 }
@@ -144,7 +148,7 @@ Pt rotate(float angle, Pt v) {
 // euclid 0.22.9 `Vector2D::angle_from_x_axis` = `Trig::fast_atan2(y, x)` (euclid src/trig.rs):
 // the published polynomial approximation of atan on [0, 1] (math.stackexchange.com question
 // 1098487, answer 1105038), reflected into the octant of (x, y); f32, evaluated left to right.
-float angle_from_x_axis(Pt v) {
+HD float angle_from_x_axis(Pt v) {
     const float x_abs = fabsf(v.x), y_abs = fabsf(v.y);
     const float a = fminf(x_abs, y_abs) / fmaxf(x_abs, y_abs);
     const float s = a * a;
@@ -161,7 +165,7 @@ struct Arc {
 };
 
 // Arc::from_svg_arc (arc.rs:58-138).
-Arc from_svg_arc(Pt from, Pt to, Pt radii, float x_rotation, bool large_arc, bool sweep) {
+HD Arc from_svg_arc(Pt from, Pt to, Pt radii, float x_rotation, bool large_arc, bool sweep) {
     float rx = fabsf(radii.x), ry = fabsf(radii.y);
     const float xr = fmodf(x_rotation, 2.0f * PI_F);
     const float cos_phi = cosf(xr), sin_phi = sinf(xr);
@@ -195,12 +199,12 @@ Arc from_svg_arc(Pt from, Pt to, Pt radii, float x_rotation, bool large_arc, boo
 }
 
 // f32::signum: 1 for +0 and positives, -1 for -0 and negatives, NaN for NaN.
-float signum(float v) { return std::isnan(v) ? v : (std::signbit(v) ? -1.0f : 1.0f); }
+HD float signum(float v) { return v != v ? v : ((lg::f32_bits(v) >> 31) ? -1.0f : 1.0f); }
 
 // arc_to_quadratic_beziers_with_t (arc.rs:668-703); `cb(ctrl, to, t_end)`. Returns false where
 // lyon's `cast::<S, i32>(n_steps).unwrap()` would panic (a NaN or huge step count).
 template <class F>
-bool arc_to_quadratics(const Arc& arc, F&& cb) {
+HD bool arc_to_quadratics(const Arc& arc, F&& cb) {
     const float sign = signum(arc.sweep_angle);
     float sweep_angle = fabsf(arc.sweep_angle);
     if (!(sweep_angle <= PI_F * 2.0f)) sweep_angle = PI_F * 2.0f;  // f32::min (NaN: the other)
@@ -237,7 +241,7 @@ struct Parser {
     bool need_end = false;
     int32_t err = LYON_OK, err_line = 0, err_col = 0;
 
-    bool fail(int code, int32_t line, int32_t col) {
+    HD bool fail(int code, int32_t line, int32_t col) {
         err = code;
         err_line = line;
         err_col = col;
@@ -245,53 +249,54 @@ struct Parser {
     }
 
     // parse_number (parser.rs:413-467): [-]digits[.digits][(e|E)[-]digits], then Rust's
-    // f32::from_str on that text (correctly rounded, as strtof).
-    bool number(Source& s, float* out) {
+    // f32::from_str on that text (correctly rounded: decimal_to_f32).
+    HD bool number(Source& s, float* out) {
         s.skip_whitespace();
         const int32_t line = s.line, col = s.col;
-        std::string buf;
-        auto digit = [&]() { return s.current >= '0' && s.current <= '9'; };
+        lg::DecimalBuilder b;
         if (s.current == '-') {
-            buf.push_back('-');
+            b.d.negative = true;
             s.advance_one();
         }
         size_t mant = 0;
-        while (digit()) {
-            buf.push_back((char)s.current);
+        while (s.current >= '0' && s.current <= '9') {
+            b.digit((int)(s.current - '0'));
             s.advance_one();
             ++mant;
         }
         if (s.current == '.') {
-            buf.push_back('.');
+            b.point();
             s.advance_one();
-            while (digit()) {
-                buf.push_back((char)s.current);
+            while (s.current >= '0' && s.current <= '9') {
+                b.digit((int)(s.current - '0'));
                 s.advance_one();
                 ++mant;
             }
         }
         bool exp_ok = true;
+        long long e = 0;
         if (s.current == 'e' || s.current == 'E') {
-            buf.push_back((char)s.current);
             s.advance_one();
+            bool eneg = false;
             if (s.current == '-') {
-                buf.push_back('-');
+                eneg = true;
                 s.advance_one();
             }
             size_t ed = 0;
-            while (digit()) {
-                buf.push_back((char)s.current);
+            while (s.current >= '0' && s.current <= '9') {
+                if (e < 100000000) e = e * 10 + (long long)(s.current - '0');
                 s.advance_one();
                 ++ed;
             }
+            if (eneg) e = -e;
             exp_ok = ed > 0;
         }
         if (mant == 0 || !exp_ok) return fail(LYON_SVG_ERR_NUMBER, line, col);
-        *out = strtof(buf.c_str(), nullptr);
+        *out = b.finish(e);
         return true;
     }
 
-    bool flag(Source& s, bool* out) {  // parser.rs:469-490
+    HD bool flag(Source& s, bool* out) {  // parser.rs:469-490
         s.skip_whitespace();
         if (s.current == '1' || s.current == '0') {
             *out = s.current == '1';
@@ -301,12 +306,12 @@ struct Parser {
         return fail(LYON_SVG_ERR_FLAG, s.line, s.col);
     }
 
-    bool attributes(Source& s) {  // parser.rs:384-395
+    HD bool attributes(Source& s) {  // parser.rs:384-395
         if (num_attributes == 0) return true;
         return number(s, &attr);
     }
 
-    bool point(Source& s, bool rel, Pt* out) {  // parser.rs:397-411
+    HD bool point(Source& s, bool rel, Pt* out) {  // parser.rs:397-411
         float x, y;
         if (!number(s, &x) || !number(s, &y)) return false;
         if (rel) {
@@ -317,25 +322,25 @@ struct Parser {
         return true;
     }
 
-    bool endpoint(Source& s, bool rel, Pt* out) {  // parser.rs:371-382
+    HD bool endpoint(Source& s, bool rel, Pt* out) {  // parser.rs:371-382
         if (!point(s, rel, out)) return false;
         current = *out;
         return attributes(s);
     }
 
-    Pt smooth_ctrl(const Pt* prev) const {  // parser.rs:363-369
+    HD Pt smooth_ctrl(const Pt* prev) const {  // parser.rs:363-369
         if (!prev) return current;
         return Pt{current.x + (current.x - prev->x), current.y + (current.y - prev->y)};
     }
 
     // parse (parser.rs:154-175) with parse_path (177-361).
-    void parse(Source& s, Out& o) {
+    HD void parse(Source& s, Out& o) {
         need_end = false;
         run(s, o);
         if (need_end) o.end(false);
     }
 
-    void run(Source& s, Out& o) {
+    HD void run(Source& s, Out& o) {
         current = Pt{0.0f, 0.0f};
         Pt first_position{0.0f, 0.0f};
         bool need_start = false;
@@ -483,7 +488,64 @@ struct Parser {
     }
 };
 
+// ---- on the device -----------------------------------------------------------------------
+
+// One thread parses one string with the same Parser (lyon's PathParser), counting (write false:
+// verb/point counts and the parse status) or writing at the scanned offsets.
+__global__ void svg_parse_kernel(const char* text, const uint64_t* string_offsets, uint32_t n,
+                                 uint32_t num_attributes, long long stop_at, int write,
+                                 uint32_t* verb_counts, uint32_t* point_counts, int32_t* status,
+                                 int32_t* error_line, int32_t* error_column,
+                                 const uint64_t* verb_offsets, const uint64_t* point_offsets,
+                                 uint8_t* verbs, float* points, float* widths) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        Source src(text + string_offsets[i], string_offsets[i + 1] - string_offsets[i]);
+        Out o;
+        if (write) {
+            o.verbs = verbs + verb_offsets[i];
+            o.points = points + 2 * point_offsets[i];
+            o.widths = widths ? widths + point_offsets[i] : nullptr;
+        }
+        Parser p;
+        p.num_attributes = num_attributes;
+        p.stop_at = stop_at;
+        p.parse(src, o);
+        if (!write) {
+            verb_counts[i] = (uint32_t)o.nv;
+            point_counts[i] = (uint32_t)o.np;
+            status[i] = p.err;
+            error_line[i] = p.err_line;
+            error_column[i] = p.err_col;
+        }
+    }
+}
+
 }  // namespace
+
+namespace lg {
+cudaError_t launch_svg_parse(const char* text, const uint64_t* string_offsets, uint32_t n,
+                             uint32_t num_attributes, long long stop_at, bool write,
+                             uint32_t* verb_counts, uint32_t* point_counts, int32_t* status,
+                             int32_t* error_line, int32_t* error_column,
+                             const uint64_t* verb_offsets, const uint64_t* point_offsets,
+                             uint8_t* verbs, float* points, float* widths, int num_sms,
+                             cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t threads = 128;
+    uint32_t blocks = (n + threads - 1) / threads;
+    const uint32_t cap = (uint32_t)(num_sms > 0 ? num_sms : 1) * 16u;
+    if (blocks > cap) blocks = cap;
+    svg_parse_kernel<<<blocks, threads, 0, stream>>>(
+        text, string_offsets, n, num_attributes, stop_at, write ? 1 : 0, verb_counts,
+        point_counts, status, error_line, error_column, verb_offsets, point_offsets, verbs,
+        points, widths);
+    note_launches(1);
+    return cudaGetLastError();
+}
+}  // namespace lg
+
+
 
 extern "C" int lyon_svg_parse_paths(const char* text, const uint64_t* string_offsets,
                                     uint32_t num_strings, const lyon_svg_parse_options* options,

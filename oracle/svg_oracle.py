@@ -114,6 +114,36 @@ def _fn(f, x):
     return f32(_C[f](float(x)))
 
 
+def decimal_to_f32(text: str):
+    """Rust's f32::from_str: the decimal rounded to the nearest f32, ties to even, computed
+    exactly with rationals (a conversion through f64 would round twice)."""
+    import struct
+    from fractions import Fraction
+    v = Fraction(text)
+    neg = text.lstrip().startswith("-")
+    if v == 0:
+        return f32(-0.0) if neg else f32(0.0)
+    a = abs(v)
+    e = a.numerator.bit_length() - a.denominator.bit_length()
+    if Fraction(2) ** e > a:
+        e -= 1
+    e = max(e, -126)                       # subnormals share the smallest exponent
+    scaled = a * Fraction(2) ** (23 - e)   # the 24-bit significand, with a fraction
+    m = scaled.numerator // scaled.denominator
+    rem = scaled - m
+    if rem > Fraction(1, 2) or (rem == Fraction(1, 2) and m % 2 == 1):
+        m += 1
+    if m == 1 << 24:
+        m >>= 1
+        e += 1
+    if e > 127:
+        r = float("inf")
+    else:
+        r = float(Fraction(m) * Fraction(2) ** (e - 23))
+    r = struct.unpack("<f", struct.pack("<f", r))[0]  # exact: r is an f32 value
+    return f32(-r if neg else r)
+
+
 def _atan2(y, x):
     # euclid's Trig::fast_atan2 for f32: numpy float32 scalars round every operation to f32.
     y, x = f32(y), f32(x)
@@ -230,7 +260,7 @@ def parse(src: str, num_attributes: int = 0, stop_at=None):
             ok = e > 0
         if m == 0 or not ok:
             raise _Err("number", line, col)
-        return f32(np.float32(buf))
+        return decimal_to_f32(buf)
 
     def flag():
         s.skip_ws()

@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--paths", type=int, default=1_000_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample", type=int, default=100_000)
+    ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--fill-paths", type=int, default=200_000)
     ap.add_argument("--no-fill", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
@@ -193,10 +193,11 @@ def profiled_traffic_per_vertex():
     return None
 
 
-def _oracle_rate(kind, batch, opts, n, threads):
+def _oracle_rate(kind, batch, opts, n, threads, ties=None):
     """The oracle over the first n paths: each path tessellated into one reused VertexBuffers per
     thread (lyon's tessellate_path into a cleared buffer), nothing copied into batch arrays.
-    Returns (vertices/s, vertices, seconds)."""
+    Returns (vertices/s, vertices, seconds); `ties` (a dict), when given, receives the oracle's
+    near-tie counts (count decisions within 1e-6 of an integer)."""
     from oracle import lyon_oracle as orc
     sub = batch.head(n)
     sub_opts = opts[:n] if len(opts) > 1 else opts
@@ -207,6 +208,10 @@ def _oracle_rate(kind, batch, opts, n, threads):
     r = orc.batch(kind, sub, sub_opts, 32, threads, want_output=False)
     dt = time.perf_counter() - t0
     verts = int(r["vtx_counts"].sum())
+    if ties is not None:
+        ties["near_ties"] = int(r["near_ties"].sum())
+        ties["paths_with_near_ties"] = int((r["near_ties"] > 0).sum())
+        ties["paths"] = n
     return verts / dt, verts, dt
 
 
@@ -216,7 +221,8 @@ def cpu_baseline(batch, opts, sample_paths: int, kind: str = "stroke",
     and one thread on a smaller one (lyon itself is single-threaded per tessellator)."""
     threads = os.cpu_count() or 1
     n = min(sample_paths, batch.num_paths)
-    v, verts, dt = _oracle_rate(kind, batch, opts, n, threads)
+    ties = {}
+    v, verts, dt = _oracle_rate(kind, batch, opts, n, threads, ties)
     n1 = min(single_paths, batch.num_paths)
     v1, verts1, dt1 = _oracle_rate(kind, batch, opts, n1, 1)
     return {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
@@ -225,7 +231,8 @@ def cpu_baseline(batch, opts, sample_paths: int, kind: str = "stroke",
                       f"per-thread VertexBuffers, outputs not copied into batch arrays",
             "single_thread": {"value": v1, "unit": UNIT, "cores": 1, "kind": "port",
                               "sample": f"first {n1} paths, {verts1} output vertices, "
-                                        f"{dt1:.2f} s wall on 1 thread"}}
+                                        f"{dt1:.2f} s wall on 1 thread"},
+            "near_ties": ties}
 
 
 def run_reference(args):
@@ -405,6 +412,9 @@ def main():
         line["e2e"] = e2e
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(batch, opts, args.cpu_sample)
+        # Count decisions of the workload within 1e-6 of an integer (the oracle's count over
+        # the baseline's paths): there lyon on another libm may round the other way.
+        line["near_ties"] = line["cpu_baseline"]["near_ties"]
     if rank == 0:
         line["plain_per_path"] = plain_per_path(ctx, db, od, len(opts), value, T)
         if not args.no_fill:

@@ -403,6 +403,69 @@ def flatten_arcs(arcs_dev, num_arcs: int, tolerance: float,
                          dev(out.status, (num_arcs,), "<i4"), tp)
 
 
+class DeferredTessellator:
+    """Collects `tessellate_path` calls (strokes with fixed width and fills, `Positions`
+    vertices) and runs each kind as one batched launch at `flush()`. Each call's builder then
+    receives what lyon's `tessellate_path` would have appended (stroke.rs:164-177,
+    fill.rs:628-641), in call order: ids count from the builder's next index, and a call whose
+    last id would pass the index type's range fails with TooManyVertices and appends nothing
+    (geometry_builder.rs:338-350, 478-481), so several calls into one BuffersBuilder give what
+    the same calls in sequence give. The launch and synchronisation cost of a GPU call is paid
+    once per flush instead of once per path."""
+
+    def __init__(self, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context.default()
+        self._calls = []  # (kind, path, options, builder)
+
+    def stroke(self, path: Path, options: StrokeOptions, builder: BuffersBuilder) -> int:
+        if builder.vertex_ctor is not None or options.variable_line_width is not None:
+            raise ValueError("deferred calls write positions with a fixed line width")
+        self._calls.append(("stroke", path, options, builder))
+        return len(self._calls) - 1
+
+    def fill(self, path: Path, options: FillOptions, builder: BuffersBuilder) -> int:
+        if builder.vertex_ctor is not None:
+            raise ValueError("deferred calls write positions")
+        self._calls.append(("fill", path, options, builder))
+        return len(self._calls) - 1
+
+    def flush(self):
+        """Runs the pending calls; returns, per call in order, None or its TessellationError."""
+        calls, self._calls = self._calls, []
+        results = {}
+        for kind in ("stroke", "fill"):
+            idx = [k for k, c in enumerate(calls) if c[0] == kind]
+            if not idx:
+                continue
+            batch = PathBatch.from_paths([calls[k][1] for k in idx])
+            recs = np.concatenate([calls[k][2].to_record() for k in idx])
+            db = DeviceBatch.upload(batch, self.ctx.device)
+            od = upload_options(recs, self.ctx.device)
+            res = tessellate_paths(kind, db, od, len(recs), 32, INDEX_PER_PATH, 0, self.ctx)
+            self.ctx.synchronize()
+            v = res.vertices().cpu().numpy() if res.total_vertices else np.zeros((0, 2), np.float32)
+            i = (res.indices().cpu().numpy().view(np.uint32) if res.total_indices
+                 else np.zeros(0, np.uint32))
+            st = res.statuses().cpu().numpy()
+            vo, io = res.offsets()
+            vo, io = vo.cpu().numpy(), io.cpu().numpy()
+            for j, k in enumerate(idx):
+                results[k] = (int(st[j]), v[vo[j]:vo[j + 1]], i[io[j]:io[j + 1]])
+        out = []
+        for k, (kind, path, options, builder) in enumerate(calls):
+            status, v, i = results[k]
+            if status == LYON_OK:
+                base = builder.next_index()
+                top = 65535 if builder.buffers.index_bits == 16 else 0xFFFFFFFE
+                if len(v) > 0 and base + len(v) - 1 > top:
+                    status = LYON_ERR_TOO_MANY_VERTICES
+                else:
+                    builder.append(v, (i.astype(np.uint64) + base).astype(
+                        builder.buffers.indices.dtype))
+            out.append(None if status == LYON_OK else TessellationError(status))
+        return out
+
+
 class StrokeTessellator:
     """lyon's StrokeTessellator (fixed line width, `Positions` vertices)."""
 

@@ -75,3 +75,50 @@ def test_emit_with_other_arguments_is_refused(gpu):
     assert c.lib.lyon_gpu_emit_into(c.h, 0, ctypes.byref(cb), od.data_ptr(), len(opts), 16,
                                     T.INDEX_PER_PATH, 0, None, None,
                                     ctypes.byref(out)) == T.LYON_ERR_INVALID_ARGUMENT
+
+
+def test_deferred_calls_equal_sequential_calls():
+    # DeferredTessellator: 300 strokes and 60 fills recorded into two builders (one u16, which
+    # overflows part-way, one u32) and run as one batched launch per kind at flush(), against the
+    # same calls made one by one through the single-path drop-in.
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lyon_gb300 import workloads
+    from lyon_gb300.options import FillOptions, StrokeOptions
+    sb, so = workloads.plain_stroke(300, seed=61)
+    fb, _ = workloads.glyph_fill(60, seed=62)
+    sopt = StrokeOptions(*[so[0][k].item() for k in so.dtype.names])
+    fopt = FillOptions(tolerance=0.1)
+    ctx = T.Context(0)
+    seq = [T.VertexBuffers(16), T.VertexBuffers(32)]
+    dfr = [T.VertexBuffers(16), T.VertexBuffers(32)]
+    seq_b = [T.BuffersBuilder(b) for b in seq]
+    dfr_b = [T.BuffersBuilder(b) for b in dfr]
+    d = T.DeferredTessellator(ctx)
+    seq_err = []
+    st, ft = T.StrokeTessellator(ctx), T.FillTessellator(ctx)
+    for k in range(sb.num_paths + fb.num_paths):
+        which = k % 2
+        if k < sb.num_paths:
+            path, kind = sb.path(k), "stroke"
+        else:
+            path, kind = fb.path(k - sb.num_paths), "fill"
+        try:
+            if kind == "stroke":
+                st.tessellate_path(path, sopt, seq_b[which])
+            else:
+                ft.tessellate_path(path, fopt, seq_b[which])
+            seq_err.append(None)
+        except T.TessellationError as e:
+            seq_err.append(e.code)
+        if kind == "stroke":
+            d.stroke(path, sopt, dfr_b[which])
+        else:
+            d.fill(path, fopt, dfr_b[which])
+    got = [None if e is None else e.code for e in d.flush()]
+    assert got == seq_err
+    assert any(e == T.LYON_ERR_TOO_MANY_VERTICES for e in got)
+    for a, b in zip(seq, dfr):
+        assert np.array_equal(a.indices, b.indices)
+        assert np.array_equal(a.vertices, b.vertices)

@@ -458,10 +458,26 @@ def run_fill(ctx, args, T, world, batch=None):
            "config": {"paths": batch.num_paths, "contours": "1-6 of 8-40 quadratics; 10% stars",
                       "tolerance": 0.1, "index_bits": 32, "index_mode": "global", "seed": 3}}
     threads = os.cpu_count() or 1
+    from lyon_gb300 import _native
+    saved = _native.CFillTuning()
+    ctx.lib.lyon_gpu_get_fill_tuning(ctx.h, ctypes.byref(saved))
     for name, rule in (("non_zero", FillRule.NonZero), ("even_odd", FillRule.EvenOdd)):
         opts = np.zeros(1, dtype=FILL_OPTIONS_DTYPE)
         opts[0] = (0.1, rule, 0, 1)
         od = T.upload_options(opts, 0)
+        # The fill autotuner picks blocks per SM and sweepers per warp on a 20,000-path sample.
+        tune = None
+        if not args.profile_fill:
+            best = _native.CFillTuning()
+            times = (ctypes.c_float * 10)()
+            nc = ctypes.c_uint32()
+            cb = db.c()
+            ctx.lib.lyon_gpu_autotune_fill(ctx.h, ctypes.byref(cb), od.data_ptr(), 1, 20_000,
+                                           ctypes.byref(best), times, ctypes.byref(nc))
+            tune = {"chosen": {"blocks_per_sm": best.blocks_per_sm, "lanes": best.lanes},
+                    "candidate_ms": [round(float(t), 3) for t in times[:nc.value]],
+                    "candidates": "blocks_per_sm {16, 8} x lanes {1, 4, 8, 12, 16}",
+                    "sample_paths": 20_000}
         for _ in range(2):
             res = T.tessellate_paths("fill", db, od, 1, 32, T.INDEX_GLOBAL, 0, ctx)
         ctx.synchronize()
@@ -491,6 +507,8 @@ def run_fill(ctx, args, T, world, batch=None):
                  "phases_ms": {"sweep": phases[-1][0], "scan": phases[-1][1],
                                "emit": phases[-1][2], "call": phases[-1][3]},
                  "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
+        if tune is not None:
+            entry["autotune"] = tune
         if args.profile_fill:
             out[name] = entry
             continue
@@ -516,6 +534,7 @@ def run_fill(ctx, args, T, world, batch=None):
                                                              f"vertices, {dt1:.2f} s wall on "
                                                              f"1 thread"}}
         out[name] = entry
+    ctx.lib.lyon_gpu_set_fill_tuning(ctx.h, ctypes.byref(saved))
     return out
 
 

@@ -696,6 +696,29 @@ int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch
                              uint32_t sample_paths, lyon_gpu_stroke_tuning* best,
                              float* times_ms, uint32_t* num_candidates);
 
+/* Runtime settings of the fill sweep on a context: lyon's sweep of one path runs on one thread
+ * (a sweeper); a one-warp block holds up to 32 of them. */
+typedef struct lyon_gpu_fill_tuning {
+    uint32_t blocks_per_sm; /* sweep blocks per SM; 0: the default (16) */
+    uint32_t lanes;         /* sweepers per block: 1 (a path owns its warp) to 32 (a warp shared by
+                               32 paths, which share its instruction fetch and issue slots);
+                               0: chosen per launch (1 below two paths per block, else up to 12) */
+} lyon_gpu_fill_tuning;
+
+int lyon_gpu_set_fill_tuning(lyon_gpu_context* ctx, const lyon_gpu_fill_tuning* tuning);
+int lyon_gpu_get_fill_tuning(lyon_gpu_context* ctx, lyon_gpu_fill_tuning* tuning);
+
+/* Times the batched fill (device buffers, u32 per-path indices) on the first `sample_paths`
+ * paths of `batch` (0: all) for each candidate setting — blocks_per_sm in {16, 8} x lanes in
+ * {1, 4, 8, 12, 16} — and keeps the fastest on the context, so that later calls on paths of the
+ * same size distribution use it: the split between a path owning its warp and paths sharing one.
+ * `best` receives the choice, `times_ms` (optional, 10 entries, lanes varying fastest) the
+ * candidates' times, `num_candidates` the count. Outputs do not depend on the settings. */
+int lyon_gpu_autotune_fill(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                           const lyon_fill_options* options, uint32_t num_options,
+                           uint32_t sample_paths, lyon_gpu_fill_tuning* best, float* times_ms,
+                           uint32_t* num_candidates);
+
 /* Synchronise the context's stream. Returns LYON_OK or LYON_ERR_CUDA. */
 int lyon_gpu_synchronize(lyon_gpu_context* ctx);
 

@@ -67,6 +67,10 @@ class CHatchOutput(ctypes.Structure):
                 ("total", u64)]
 
 
+class CFillTuning(ctypes.Structure):
+    _fields_ = [("blocks_per_sm", u32), ("lanes", u32)]
+
+
 class CSvgOutput(ctypes.Structure):
     _fields_ = [("batch", CPathBatch), ("widths", c_p), ("status", c_p), ("error_line", c_p),
                 ("error_column", c_p), ("total_verbs", u64), ("total_points", u64),
@@ -194,6 +198,14 @@ def load(build_if_missing: bool = True):
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [c_p, ctypes.POINTER(CStrokeTuning)]
+        for name in ("lyon_gpu_set_fill_tuning", "lyon_gpu_get_fill_tuning"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [c_p, ctypes.POINTER(CFillTuning)]
+        L.lyon_gpu_autotune_fill.restype = ctypes.c_int
+        L.lyon_gpu_autotune_fill.argtypes = [c_p, ctypes.POINTER(CPathBatch), c_p, u32, u32,
+                                             ctypes.POINTER(CFillTuning), c_p,
+                                             ctypes.POINTER(u32)]
         L.lyon_gpu_svg_parse_paths.restype = ctypes.c_int
         L.lyon_gpu_svg_parse_paths.argtypes = [c_p, c_p, c_p, u32, c_p, ctypes.POINTER(CSvgOutput)]
         L.lyon_svg_parse_paths.restype = ctypes.c_int
@@ -269,7 +281,8 @@ EXPORTED = [
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
     "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",
     "lyon_gpu_stroke_paths_variable_width", "lyon_gpu_stroke_path_variable_width",
-    "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_svg_parse_paths", "lyon_gpu_stroke_paths_custom",
+    "lyon_gpu_fill_shapes", "lyon_svg_parse_paths", "lyon_gpu_svg_parse_paths",
+    "lyon_gpu_set_fill_tuning", "lyon_gpu_get_fill_tuning", "lyon_gpu_autotune_fill", "lyon_gpu_stroke_paths_custom",
     "lyon_gpu_interpolate_attributes", "lyon_gpu_stroke_path_custom",
     "lyon_gpu_fill_paths_custom", "lyon_gpu_interpolate_fill_attributes",
     "lyon_gpu_fill_path_custom", "lyon_gpu_flatten_arcs", "lyon_gpu_hatch_paths",

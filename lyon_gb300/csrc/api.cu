@@ -989,6 +989,75 @@ int lyon_gpu_autotune_stroke(lyon_gpu_context* ctx, const lyon_path_batch* batch
     return LYON_OK;
 }
 
+int lyon_gpu_set_fill_tuning(lyon_gpu_context* ctx, const lyon_gpu_fill_tuning* t) {
+    if (!ctx || !t || t->lanes > 32 || t->blocks_per_sm > 64) return LYON_ERR_INVALID_ARGUMENT;
+    ctx->fill.blocks_per_sm_cap = t->blocks_per_sm;
+    ctx->fill.lanes = t->lanes;
+    return LYON_OK;
+}
+
+int lyon_gpu_get_fill_tuning(lyon_gpu_context* ctx, lyon_gpu_fill_tuning* t) {
+    if (!ctx || !t) return LYON_ERR_INVALID_ARGUMENT;
+    t->blocks_per_sm = ctx->fill.blocks_per_sm_cap;
+    t->lanes = ctx->fill.lanes;
+    return LYON_OK;
+}
+
+int lyon_gpu_autotune_fill(lyon_gpu_context* ctx, const lyon_path_batch* batch,
+                           const lyon_fill_options* options, uint32_t num_options,
+                           uint32_t sample_paths, lyon_gpu_fill_tuning* best, float* times_ms,
+                           uint32_t* num_candidates) {
+    if (!ctx || !batch || !options || (num_options != 1 && num_options != batch->num_paths))
+        return LYON_ERR_INVALID_ARGUMENT;
+    static const uint32_t kBlocks[] = {16u, 8u};
+    static const uint32_t kLanes[] = {1u, 4u, 8u, 12u, 16u};
+    const uint32_t nc = 10;
+    if (num_candidates) *num_candidates = nc;
+    lyon_path_batch sample = *batch;
+    if (sample_paths > 0 && sample_paths < batch->num_paths) sample.num_paths = sample_paths;
+    const uint32_t sopts = num_options > 1 ? sample.num_paths : 1;
+    lyon_gpu_fill_tuning saved;
+    lyon_gpu_get_fill_tuning(ctx, &saved);
+    const bool saved_timing = ctx->timing;
+    ctx->timing = false;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = -1.0f;
+    lyon_gpu_fill_tuning b = saved;
+    int rc = LYON_OK;
+    for (uint32_t c = 0; c < nc && rc == LYON_OK; ++c) {
+        lyon_gpu_fill_tuning t{kBlocks[c / 5], kLanes[c % 5]};
+        lyon_gpu_set_fill_tuning(ctx, &t);
+        lyon_gpu_batch_output out;
+        rc = batched_device(ctx, KIND_FILL, &sample, options, sopts, 32, LYON_INDEX_PER_PATH, 0,
+                            &out);  // warm-up (and heap growth)
+        if (rc != LYON_OK) break;
+        cudaEventRecord(e0, ctx->stream);
+        rc = batched_device(ctx, KIND_FILL, &sample, options, sopts, 32, LYON_INDEX_PER_PATH, 0,
+                            &out);
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (times_ms) times_ms[c] = ms;
+        if (best_ms < 0.0f || ms < best_ms) {
+            best_ms = ms;
+            b = t;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->timing = saved_timing;
+    if (rc != LYON_OK) {
+        lyon_gpu_set_fill_tuning(ctx, &saved);
+        return rc;
+    }
+    lyon_gpu_set_fill_tuning(ctx, &b);
+    if (best) *best = b;
+    return LYON_OK;
+}
+
 int lyon_gpu_synchronize(lyon_gpu_context* ctx) {
     if (!ctx) return LYON_ERR_INVALID_ARGUMENT;
     return set_err(ctx, "cudaStreamSynchronize", cudaStreamSynchronize(ctx->stream))

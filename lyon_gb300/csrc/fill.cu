@@ -292,6 +292,7 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
     uint32_t items = n;
     uint32_t max_lanes = LG_FILL_LANES;
     bool forced = false;
+    if (fb.lanes >= 1 && fb.lanes <= 32) max_lanes = fb.lanes, forced = true;
     if (const char* env = getenv("LYON_GB300_FILL_LANES")) {
         const long v = strtol(env, nullptr, 10);
         if (v >= 1 && v <= 32) max_lanes = (uint32_t)v, forced = true;

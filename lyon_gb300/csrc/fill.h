@@ -25,6 +25,8 @@ struct FillBuffers {
     // Most sweep blocks per SM (0: the default, FILL_SWEEPERS_PER_SM). The serving loop lowers
     // it so that stroke kernels launched meanwhile find room on every SM.
     uint32_t blocks_per_sm_cap = 0;
+    // Sweepers per one-warp block (1..32); 0: chosen per launch from its paths per block.
+    uint32_t lanes = 0;
     // Vertex sources (FillVertex::sources), when a call asks for them:
     void* stage_s = nullptr;        // staged sources, three u32 words each, path-local ids
     size_t stage_s_cap = 0;

@@ -190,3 +190,35 @@ def test_fill_global_index_mode(gpu):
     ref = out.snapshot(0)
     assert np.array_equal(g["indices"], ref.indices32)
     assert np.array_equal(g["vertices"], ref.vertices)
+
+
+def test_fill_autotuner_picks_a_setting_and_keeps_outputs(gpu):
+    # lyon_gpu_autotune_fill times 10 settings (blocks per SM x sweepers per warp) on a sample,
+    # keeps the fastest; outputs are the same under every setting.
+    import ctypes
+    from lyon_gb300 import _native
+    batch, opts = workloads.glyph_fill(1500, seed=47)
+    before = gpu.gpu_batch("fill", batch, opts, index_bits=32)
+    c = gpu.ctx()
+    db = T.DeviceBatch.upload(batch, 0)
+    od = T.upload_options(opts, 0)
+    cb = db.c()
+    saved = _native.CFillTuning()
+    assert c.lib.lyon_gpu_get_fill_tuning(c.h, ctypes.byref(saved)) == 0
+    best = _native.CFillTuning()
+    times = (ctypes.c_float * 10)()
+    nc = ctypes.c_uint32()
+    try:
+        r = c.lib.lyon_gpu_autotune_fill(c.h, ctypes.byref(cb), od.data_ptr(), len(opts), 1000,
+                                         ctypes.byref(best), times, ctypes.byref(nc))
+        assert r == 0 and nc.value == 10
+        assert all(t > 0.0 for t in times)
+        assert best.blocks_per_sm in (16, 8) and best.lanes in (1, 4, 8, 12, 16)
+        for lanes in (1, 16):
+            t = _native.CFillTuning(8, lanes)
+            assert c.lib.lyon_gpu_set_fill_tuning(c.h, ctypes.byref(t)) == 0
+            after = gpu.gpu_batch("fill", batch, opts, index_bits=32)
+            assert np.array_equal(after["indices"], before["indices"])
+            assert np.array_equal(after["vertices"], before["vertices"])
+    finally:
+        c.lib.lyon_gpu_set_fill_tuning(c.h, ctypes.byref(saved))

@@ -12,9 +12,9 @@
 // the region is cut into triangles. Degenerate (zero-area) triangles cover nothing.
 //
 // One block rasterises COV_ROWS rows of one path: each triangle adds +1 / -1 at the ends of its
-// covered run of samples in every row (the ends are found by binary search on the exact
-// per-sample test, which is monotone along a row), then a prefix sum per row gives each
-// sample's count. Both tessellations go through the same code; the block adds to the path's
+// covered run of samples in every row (each end estimated from where an edge crosses the row,
+// then settled by the exact per-sample test, which is monotone along a row), then a prefix sum
+// per row gives each sample's count. Both tessellations go through the same code; the block adds to the path's
 // totals the samples each one covers and the samples whose counts differ.
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -26,7 +26,7 @@ namespace lg {
 namespace {
 
 constexpr int COV_ROWS = 4;  // rows per block
-constexpr int COV_THREADS = 256;
+constexpr int COV_THREADS = 512;
 constexpr uint32_t COV_MAX_GRID = 4096;
 
 struct P2 {
@@ -69,33 +69,36 @@ struct Grid {
     __device__ double ys(int j) const { return y0 + ((double)j + 0.5) * dy; }
 };
 
-// The run [lo, hi) of samples of row y that triangle t covers, within [ilo, ihi).
+// The run [lo, hi) of samples of row y that triangle t covers, within [ilo, ihi). Along a row
+// each edge's test is monotone in x, so each edge keeps a prefix or a suffix of the columns: its
+// end is estimated from the edge's crossing of the row, then moved by the exact per-sample test
+// until it sits where the test changes (the result is the same as a search over all columns).
 __device__ void row_span(const Tri& t, const Grid& G, double y, int ilo, int ihi, int* lo,
                          int* hi) {
     int a = ilo, b = ihi;
     for (int k = 0; k < 3 && a < b; ++k) {
         const P2 p = t.p[k], q = t.p[(k + 1) % 3];
-        // Along a row the edge function is monotone in x: decreasing when the edge goes up
-        // (q.y > p.y), increasing when it goes down, constant when horizontal.
+        // The edge function is decreasing in x when the edge goes up (q.y > p.y), increasing
+        // when it goes down, constant when horizontal.
         if (q.y == p.y) {
             if (!covers_edge(t, k, G.xs(a), y)) b = a;
             continue;
         }
-        int l = a, r = b;
+        const double xc = p.x + (y - p.y) * (q.x - p.x) / (q.y - p.y);
+        double est = floor((xc - G.x0) / G.dx - 0.5);  // the last column left of the crossing
+        if (!(est >= (double)(a - 1))) est = (double)(a - 1);
+        if (est > (double)(b - 1)) est = (double)(b - 1);
+        int c = (int)est;
         if (q.y > p.y) {
-            // Covered samples form a prefix of [a, b): find its end.
-            while (l < r) {
-                const int m = (l + r) >> 1;
-                if (covers_edge(t, k, G.xs(m), y)) l = m + 1; else r = m;
-            }
-            b = l;
+            // Covered columns form a prefix of [a, b): c = its last column (a - 1 if none).
+            while (c + 1 < b && covers_edge(t, k, G.xs(c + 1), y)) ++c;
+            while (c >= a && !covers_edge(t, k, G.xs(c), y)) --c;
+            b = c + 1;
         } else {
-            // Covered samples form a suffix: find its start.
-            while (l < r) {
-                const int m = (l + r) >> 1;
-                if (covers_edge(t, k, G.xs(m), y)) r = m; else l = m + 1;
-            }
-            a = l;
+            // Covered columns form a suffix: c + 1 = its first column.
+            while (c >= a && covers_edge(t, k, G.xs(c), y)) --c;
+            while (c + 1 < b && !covers_edge(t, k, G.xs(c + 1), y)) ++c;
+            a = c + 1;
         }
     }
     *lo = a;

@@ -576,7 +576,11 @@ typedef struct lyon_srv_config {
     uint32_t num_workers;          /* batches in flight at once, each on its own stream; 0 -> 2.
                                       With stroke workers, these take fill requests only. */
     uint32_t max_batch_paths;      /* most paths coalesced into one launch; 0 -> 65536 */
-    uint64_t device_budget_bytes;  /* device memory for batches and resident outputs; 0 -> 40 GB */
+    uint64_t device_budget_bytes;  /* device memory for batches and resident outputs; 0 -> 40 GB.
+                                      A request that does not fit waits until released outputs
+                                      free enough of it: release results as they complete (a
+                                      caller that waits for requests in submission order while
+                                      holding later results can wait forever) */
     uint32_t num_stroke_workers;   /* workers reserved for stroke requests, on streams of the
                                       device's highest priority and with one stroke block per SM,
                                       so that their launches start beside running fill sweeps

@@ -569,27 +569,54 @@ int lyon_srv_run_load(lyon_srv* s, const lyon_srv_load_item* items, uint32_t num
     });
     uint64_t paths = 0, verts = 0, idx = 0;
     uint32_t failed = 0;
-    for (size_t k = 0; k < arrivals.size(); ++k) {
-        uint64_t id;
+    // Results are released as soon as they complete, in whatever order: waiting for them in
+    // arrival order would let later requests that completed first hold the device-memory budget
+    // while an earlier one waits for budget to run, and neither would move.
+    std::vector<double> lat_k(arrivals.size(), -1.0);
+    std::vector<size_t> pending;  // submitted, not yet released (arrival indices)
+    size_t seen = 0, finished = 0;
+    while (finished < arrivals.size()) {
         {
-            std::unique_lock<std::mutex> lk(tm);
-            tcv.wait(lk, [&] { return submitted > k; });
-            id = tickets[k];
+            std::lock_guard<std::mutex> g(tm);
+            while (seen < submitted) pending.push_back(seen++);
         }
-        if (id == 0) {
-            failed++;
-            continue;
+        bool progress = false;
+        for (size_t j = 0; j < pending.size();) {
+            const size_t k = pending[j];
+            const uint64_t id = tickets[k];
+            bool done = id == 0;
+            if (id == 0) {
+                failed++;
+            } else {
+                lyon_srv_result r;
+                if (lyon_srv_poll(s, id, &r) == LYON_OK) {
+                    done = true;
+                    lat_k[k] = r.latency_ms;
+                    if (r.status != LYON_OK) failed++;
+                    paths += r.num_paths;
+                    verts += r.num_vertices;
+                    idx += r.num_indices;
+                    lyon_srv_release(s, id);
+                }
+            }
+            if (done) {
+                pending[j] = pending.back();
+                pending.pop_back();
+                ++finished;
+                progress = true;
+            } else {
+                ++j;
+            }
         }
-        lyon_srv_result r;
-        lyon_srv_wait(s, id, &r);
-        lat.push_back(r.latency_ms);
-        if (r.status != LYON_OK) failed++;
-        paths += r.num_paths;
-        verts += r.num_vertices;
-        idx += r.num_indices;
-        lyon_srv_release(s, id);
+        if (!progress && finished < arrivals.size()) {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_done.wait_for(lk, std::chrono::milliseconds(1));
+        }
     }
     submitter.join();
+    for (size_t k = 0; k < lat_k.size(); ++k) {
+        if (lat_k[k] >= 0.0) lat.push_back(lat_k[k]);
+    }
     const double elapsed = now_s() - t0;
     std::vector<double> sorted = lat;
     std::sort(sorted.begin(), sorted.end());

@@ -5,7 +5,8 @@
 //
 // Strings are parsed on all host threads in two passes (sizes, then output at scanned offsets).
 // Arcs become quadratic béziers as lyon's SvgArc / Arc do (crates/geom/src/arc.rs:58-138,
-// 668-703), in f32 with the platform's libm; `angle_from_x_axis` is euclid 0.22.9's fast_atan2,
+// 668-703), in f32 (cos, sin and tan evaluated in f64 and rounded once, identically on host and
+// device); `angle_from_x_axis` is euclid 0.22.9's fast_atan2,
 // as lyon's. One detail differs from lyon and is stated where it applies: only ASCII digits count
 // as numeric (lyon accepts any Unicode numeric character into a number, which then fails to
 // parse).
@@ -139,9 +140,16 @@ struct Out {
 
 // ---- arcs (crates/geom/src/arc.rs) -------------------------------------------------------
 
+// lyon takes cos, sin and tan of f32 angles from the platform's f32 libm; host and device libms
+// differ in the last bit, and an arc's segment count ceil(sweep / (pi / 4)) can turn on that
+// bit. Both parsers evaluate them in f64 and round once (within an ulp of any f32 libm's).
+HD float cos_r(float x) { return (float)cos((double)x); }
+HD float sin_r(float x) { return (float)sin((double)x); }
+HD float tan_r(float x) { return (float)tan((double)x); }
+
 // Rotation2D::transform_point / transform_vector (euclid): the rotation matrix of `angle`.
 HD Pt rotate(float angle, Pt v) {
-    const float s = sinf(angle), c = cosf(angle);
+    const float s = sin_r(angle), c = cos_r(angle);
     return Pt{v.x * c - v.y * s, v.x * s + v.y * c};
 }
 
@@ -168,7 +176,7 @@ struct Arc {
 HD Arc from_svg_arc(Pt from, Pt to, Pt radii, float x_rotation, bool large_arc, bool sweep) {
     float rx = fabsf(radii.x), ry = fabsf(radii.y);
     const float xr = fmodf(x_rotation, 2.0f * PI_F);
-    const float cos_phi = cosf(xr), sin_phi = sinf(xr);
+    const float cos_phi = cos_r(xr), sin_phi = sin_r(xr);
     const float hd_x = (from.x - to.x) / 2.0f, hd_y = (from.y - to.y) / 2.0f;
     const float hs_x = (from.x + to.x) / 2.0f, hs_y = (from.y + to.y) / 2.0f;
     const Pt p{cos_phi * hd_x + sin_phi * hd_y, -sin_phi * hd_x + cos_phi * hd_y};
@@ -213,16 +221,16 @@ HD bool arc_to_quadratics(const Arc& arc, F&& cb) {
     const float step = sweep_angle / n_steps * sign;
     float t0 = 0.0f;
     const float dt = 1.0f / n_steps;
-    const float alpha = tanf(step * 0.5f);
+    const float alpha = tan_r(step * 0.5f);
     const int n = (int)n_steps;
     for (int i = 0; i < n; ++i) {
         const float a1 = arc.start_angle + step * (float)i;
         const float a2 = arc.start_angle + step * (float)(i + 1);
-        const Pt v1 = rotate(arc.x_rotation, Pt{arc.radii.x * cosf(a1), arc.radii.y * sinf(a1)});
-        const Pt v2 = rotate(arc.x_rotation, Pt{arc.radii.x * cosf(a2), arc.radii.y * sinf(a2)});
+        const Pt v1 = rotate(arc.x_rotation, Pt{arc.radii.x * cos_r(a1), arc.radii.y * sin_r(a1)});
+        const Pt v2 = rotate(arc.x_rotation, Pt{arc.radii.x * cos_r(a2), arc.radii.y * sin_r(a2)});
         const Pt from{arc.center.x + v1.x, arc.center.y + v1.y};
         const Pt to{arc.center.x + v2.x, arc.center.y + v2.y};
-        const Pt tan = rotate(arc.x_rotation, Pt{-arc.radii.x * sinf(a1), arc.radii.y * cosf(a1)});
+        const Pt tan = rotate(arc.x_rotation, Pt{-arc.radii.x * sin_r(a1), arc.radii.y * cos_r(a1)});
         const Pt ctrl{from.x + tan.x * alpha, from.y + tan.y * alpha};
         const float t1 = i + 1 == n ? 1.0f : t0 + dt;
         cb(ctrl, to, t1);

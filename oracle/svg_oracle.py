@@ -1,8 +1,8 @@
 """A Python restatement of lyon_extra's PathParser (crates/extra/src/parser.rs:138-490) and of
 the arc conversion it uses (crates/geom/src/arc.rs:58-138, 668-703) — TEST INFRASTRUCTURE ONLY,
 the checker of the library's SVG parser. f32 arithmetic through numpy; the f32 math functions
-(cosf, sinf, tanf, sqrtf, fmodf) are the C library's, as lyon takes them from the
-platform's libm; `angle_from_x_axis` is euclid 0.22.9's `fast_atan2` (the published polynomial
+sqrtf and fmodf are the C library's (exact), cos, sin and tan are evaluated in f64 and rounded
+once, as the library's parser does (lyon takes them from the platform's f32 libm); `angle_from_x_axis` is euclid 0.22.9's `fast_atan2` (the published polynomial
 of math.stackexchange question 1098487, answer 1105038), in f32 as lyon evaluates it.
 
 parse(src, num_attributes, stop_at) -> (verbs, points, widths, error) with error None or
@@ -107,11 +107,15 @@ class _Out:
         self.verbs.append(CLOSE if close else END)
 
 
-_C = {math.cos: _libm.cosf, math.sin: _libm.sinf, math.tan: _libm.tanf, math.sqrt: _libm.sqrtf}
+_C = {math.sqrt: _libm.sqrtf}
 
 
 def _fn(f, x):
-    return f32(_C[f](float(x)))
+    # cos, sin and tan: f64 evaluation rounded once, as the library's parser evaluates them (lyon
+    # takes them from the platform's f32 libm, within an ulp of these); sqrt is exact in f32.
+    if f in _C:
+        return f32(_C[f](float(x)))
+    return f32(f(float(x)))
 
 
 def decimal_to_f32(text: str):

@@ -465,19 +465,22 @@ def run_fill(ctx, args, T, world, batch=None):
         opts = np.zeros(1, dtype=FILL_OPTIONS_DTYPE)
         opts[0] = (0.1, rule, 0, 1)
         od = T.upload_options(opts, 0)
-        # The fill autotuner picks blocks per SM and sweepers per warp on a 20,000-path sample.
+        # The fill autotuner picks blocks per SM and sweepers per warp on a sample of half the
+        # batch: a sample with few paths per sweeper favours one sweeper per warp, which is 1.6x
+        # slower on the whole batch (measured with a 20,000-path sample).
         tune = None
         if not args.profile_fill:
             best = _native.CFillTuning()
             times = (ctypes.c_float * 10)()
             nc = ctypes.c_uint32()
             cb = db.c()
-            ctx.lib.lyon_gpu_autotune_fill(ctx.h, ctypes.byref(cb), od.data_ptr(), 1, 20_000,
+            sample = min(batch.num_paths, 100_000)
+            ctx.lib.lyon_gpu_autotune_fill(ctx.h, ctypes.byref(cb), od.data_ptr(), 1, sample,
                                            ctypes.byref(best), times, ctypes.byref(nc))
             tune = {"chosen": {"blocks_per_sm": best.blocks_per_sm, "lanes": best.lanes},
                     "candidate_ms": [round(float(t), 3) for t in times[:nc.value]],
                     "candidates": "blocks_per_sm {16, 8} x lanes {1, 4, 8, 12, 16}",
-                    "sample_paths": 20_000}
+                    "sample_paths": sample}
         for _ in range(2):
             res = T.tessellate_paths("fill", db, od, 1, 32, T.INDEX_GLOBAL, 0, ctx)
         ctx.synchronize()

@@ -717,7 +717,9 @@ int lyon_gpu_get_fill_tuning(lyon_gpu_context* ctx, lyon_gpu_fill_tuning* tuning
  * {1, 4, 8, 12, 16} — and keeps the fastest on the context, so that later calls on paths of the
  * same size distribution use it: the split between a path owning its warp and paths sharing one.
  * `best` receives the choice, `times_ms` (optional, 10 entries, lanes varying fastest) the
- * candidates' times, `num_candidates` the count. Outputs do not depend on the settings. */
+ * candidates' times, `num_candidates` the count. Outputs do not depend on the settings. The
+ * sample must give each sweeper about as many paths as the whole batch will: with too few
+ * paths per sweeper, a path owning its warp wins on the sample and loses on the batch. */
 int lyon_gpu_autotune_fill(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                            const lyon_fill_options* options, uint32_t num_options,
                            uint32_t sample_paths, lyon_gpu_fill_tuning* best, float* times_ms,

@@ -412,7 +412,9 @@ uint64_t submit_at(lyon_srv* s, int kind, const lyon_path_batch* batch, const vo
     r->id = s->next_id++;
     s->reqs[r->id] = r;
     s->queue[kind].push_back(r);
-    s->cv_work.notify_one();
+    // Every worker is woken: with stroke and fill lanes a single wake-up can reach a worker of
+    // the other kind, which finds nothing to take and sleeps again, leaving the request queued.
+    s->cv_work.notify_all();
     return r->id;
 }
 

@@ -156,10 +156,16 @@ struct SubState {
 // Flattening parameters of one verb of a window (lane = verb): lines and Begin give one step;
 // quadratics are split at a sharp turn (stroke.rs:2755-2779, 3178-3212) and each part gets lyon's
 // segment count (quadratic_bezier.rs:943-974); cubics likewise (cubic_bezier.rs:1369-1403).
-// Returns the number of flattened points the verb contributes.
-__device__ __noinline__ uint32_t setup_verb(VerbSlot& out, int kind, uint32_t pofs,
-                                            uint32_t pcount, uint32_t p_end, const float* points,
-                                            float tolerance, int* vst) {
+// Returns the number of flattened points the verb contributes and the verb's status (by value,
+// so that the caller keeps no status word in local memory).
+struct VerbSetup {
+    uint32_t steps;
+    int st;
+};
+__device__ __noinline__ VerbSetup setup_verb(VerbSlot& out, int kind, uint32_t pofs,
+                                             uint32_t pcount, uint32_t p_end, const float* points,
+                                             float tolerance) {
+    int vst = LYON_OK;
     VerbSlot sl;
     sl.kind = kind;
     sl.mA = 0;
@@ -167,7 +173,7 @@ __device__ __noinline__ uint32_t setup_verb(VerbSlot& out, int kind, uint32_t po
     sl.sA = sl.sB = 0.0f;
     uint32_t steps = 0;
     if (pofs + pcount > p_end || kind < 0) {
-        *vst = LYON_ERR_INVALID_ARGUMENT;
+        vst = LYON_ERR_INVALID_ARGUMENT;
     } else if (kind == LYON_VERB_BEGIN || kind == LYON_VERB_LINE_TO) {
         sl.toA = load_pt(points, pofs);
         steps = 1;
@@ -211,13 +217,13 @@ __device__ __noinline__ uint32_t setup_verb(VerbSlot& out, int kind, uint32_t po
         steps = sl.mA;
     }
     if (sl.mA > MAX_VERB_STEPS || sl.mB > MAX_VERB_STEPS) {
-        *vst = LYON_ERR_UNSUPPORTED;
+        vst = LYON_ERR_UNSUPPORTED;
         steps = 0;
     }
     sl.steps = steps;
     sl.excl = 0;
     out = sl;
-    return steps;
+    return VerbSetup{steps, vst};
 }
 
 // The general joins at the end points of the window's units, one verb per lane (slots 2j and
@@ -226,7 +232,7 @@ __device__ __noinline__ uint32_t setup_verb(VerbSlot& out, int kind, uint32_t po
 // before a unit's end point is its flattened point m - 1, the step after it the first point of
 // the next unit. `c1` is the sub-path's last kept point before the window, if any.
 __device__ __noinline__ void speculate_joins(WarpSmem& sm, int lane, uint32_t nv, uint32_t S_w,
-                                             const StrokeParams& P, V2 c1, bool have_c1) {
+                                             StrokeParams P, V2 c1, bool have_c1) {
     if ((uint32_t)lane >= nv) return;
     const int j = lane;
     const VerbSlot& sl = sm.verbs[j];
@@ -271,10 +277,8 @@ __device__ __noinline__ void speculate_joins(WarpSmem& sm, int lane, uint32_t nv
         } else {
             continue;
         }
-        DEP d;
-        SlowJoin sj;
-        int st = LYON_OK;
-        slow_join_geometry(&d, prev, E, false, next, P, &sj, &st);
+        const SlowJoin sj = slow_join_summary(prev, E, false, next, P);
+        const int st = sj.st;
         SpecSlot& o = sm.spec[2 * j + u];
         o.prev = prev;
         o.cur = E;
@@ -295,15 +299,11 @@ __device__ __noinline__ void speculate_joins(WarpSmem& sm, int lane, uint32_t nv
 // Writes the output of the joins computed ahead (one per lane). Returns the worst status.
 template <bool ATTR>
 __device__ __noinline__ int emit_spec_joins(WarpSmem& sm, int lane, uint32_t count,
-                                            const StrokeParams& P, const PathOut& po) {
+                                            StrokeParams P, const PathOut& po) {
     int worst = LYON_OK;
     for (uint32_t i = (uint32_t)lane; i < count; i += 32) {
         const EmitJob job = sm.ej[i];
         const SpecSlot& sp = sm.spec[job.slot];
-        DEP d;
-        SlowJoin sj;
-        int st = LYON_OK;
-        slow_join_geometry(&d, sp.prev, sp.cur, false, sp.next, P, &sj, &st);
         SinkT<ATTR> s;
         s.id_base = job.base;
         s.nv = 0;
@@ -317,8 +317,10 @@ __device__ __noinline__ int emit_spec_joins(WarpSmem& sm, int lane, uint32_t cou
         s.vcap = cap_left(po.vmax, job.vo);
         s.icap = cap_left(po.imax, job.io);
         s.overflow = false;
-        slow_join_emit(&d, &d, s, job.has_edge != 0, job.pfn, job.pfp, true, P, &st);
-        if (s.overflow && st == LYON_OK) st = LYON_ERR_INTERNAL;
+        const JoinEmitOut r = slow_join_emit_at(sp.prev, sp.cur, false, sp.next, P, s,
+                                                job.has_edge != 0, job.pfn, job.pfp);
+        int st = r.st;
+        if (r.overflow && st == LYON_OK) st = LYON_ERR_INTERNAL;
         if (st > worst) worst = st;
     }
     return worst;
@@ -338,9 +340,8 @@ __device__ __noinline__ void join_dep_with_ids(DEP* out, V2 prev, V2 cur, V2 nxt
         fast_join_dep(*out, cur, P.hw, cur + nrm * P.hw, cur - nrm * P.hw,
                       skip ? INVALID_ID : base_id, skip ? INVALID_ID : base_id + 1);
     } else {
-        SlowJoin sj;
-        DEP d;
-        slow_join_geometry(&d, prev, cur, flat, nxt, P, &sj, status);
+        DEP d = join_geometry(prev, cur, flat, nxt, P);
+        join_arc_vertices(d, P, status);
         Sink probe{base_id, 0, 0, nullptr, nullptr, 32};
         add_join_base_vertices(d, SN, probe);
         add_join_base_vertices(d, SP, probe);
@@ -350,14 +351,16 @@ __device__ __noinline__ void join_dep_with_ids(DEP* out, V2 prev, V2 cur, V2 nxt
 
 // Side "next" points of the join at `cur` (neighbours `prev`, `nxt`) when it was a flattening
 // step: what the emit pass computed for it (stroke.rs:1760-1776).
-__device__ __noinline__ void fast_join_sides(V2 prev, V2 cur, V2 nxt, float hw, V2* pn, V2* nn) {
+struct SidePair {
+    V2 pn, nn;
+};
+__device__ __noinline__ SidePair fast_join_sides(V2 prev, V2 cur, V2 nxt, float hw) {
     V2 pe = cur - prev;
     V2 pt = pe / vlength(pe);
     V2 ne = nxt - cur;
     V2 nt = ne / vlength(ne);
     V2 nrm = compute_normal(pt, nt);
-    *pn = cur + nrm * hw;
-    *nn = cur - nrm * hw;
+    return SidePair{cur + nrm * hw, cur - nrm * hw};
 }
 
 // The tail of a sub-path: stroke.rs:1179-1279 (end, close) and 1322-1378 (end_with_caps), from
@@ -674,10 +677,9 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
             st = sp.st;
         }
     }
-    DEP d;
     if (slow && !spec) {
-        SlowJoin sj;
-        slow_join_geometry(&d, prv, cur, fcur, q, P, &sj, &st);
+        const SlowJoin sj = slow_join_summary(prv, cur, fcur, q, P);
+        if (sj.st != LYON_OK) st = sj.st;
         vcnt = sj.vcount;
         jt = sj.jtris;
         to_f = sj.to_f;
@@ -731,7 +733,11 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
         }
         V2 ppn = shfl_up_v2(pn, 1), pnn = shfl_up_v2(nn, 1);
         if (lane == 0) {
-            if (!S.jside_valid) fast_join_sides(S.c3, S.c2, S.c1, P.hw, &S.jpn, &S.jnn);
+            if (!S.jside_valid) {
+                const SidePair sp2 = fast_join_sides(S.c3, S.c2, S.c1, P.hw);
+                S.jpn = sp2.pn;
+                S.jnn = sp2.nn;
+            }
             ppn = S.jpn;
             pnn = S.jnn;
         }
@@ -864,8 +870,9 @@ __device__ __forceinline__ void process_chunk(WarpSmem& sm, const int lane, cons
             s.vcap = cap_left(po.vmax, vo);
             s.icap = cap_left(po.imax, io);
             s.overflow = false;
-            slow_join_emit(&d, &d, s, k >= 2, pfn, pfp, true, P, &st);
-            if (s.overflow) st = LYON_ERR_INTERNAL;
+            const JoinEmitOut r = slow_join_emit_at(prv, cur, fcur, q, P, s, k >= 2, pfn, pfp);
+            if (r.st != LYON_OK) st = r.st;
+            if (r.overflow) st = LYON_ERR_INTERNAL;
         }
     }
 
@@ -991,8 +998,12 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
             const uint32_t pofs = pc + pincl - pcount;
             uint32_t steps = 0;
             int vst = LYON_OK;
-            if (inwin) steps = setup_verb(sm.verbs[lane], kind, pofs, pcount, p_end, A.points,
-                                          P.tolerance, &vst);
+            if (inwin) {
+                const VerbSetup su = setup_verb(sm.verbs[lane], kind, pofs, pcount, p_end,
+                                                A.points, P.tolerance);
+                steps = su.steps;
+                vst = su.st;
+            }
             if (__any_sync(FULL, vst != LYON_OK)) {
                 status = __reduce_max_sync(FULL, vst);
                 break;

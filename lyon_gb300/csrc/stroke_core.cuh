@@ -348,20 +348,22 @@ __device__ __forceinline__ uint32_t join_interior_tris(const DEP& j) {
 struct ArcPlan {
     float a0, a1;
     uint32_t depth;
+    int st;  // LYON_OK, or LYON_ERR_UNSUPPORTED for a depth past MAX_ARC_DEPTH
 };
 
-static __device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side, float tol,
-                                                int* status) {
-    V2 center = join.pos;
-    float radius = join.hw;
-    V2 sn = join.s[side].prev - center;
-    V2 en = join.s[side].next - center;
+// Out of line with its inputs and result by value, so that no caller's join is kept in local
+// memory for it.
+static __device__ __noinline__ ArcPlan round_join_plan(V2 center, float radius, V2 side_prev,
+                                                       V2 side_next, int side, float tol) {
+    V2 sn = side_prev - center;
+    V2 en = side_next - center;
     float angle_sign = side == SN ? 1.0f : -1.0f;
     const float start_angle = angle_from_x_axis(sn);
     float diff = angle_to(start_angle, angle_from_x_axis(en));
     if (diff * angle_sign < 0.0f) diff = angle_sign * (2.0f * LG_PI_F - fabsf(diff));
     const float end_angle = start_angle + diff;
     ArcPlan p;
+    p.st = LYON_OK;
     if (side == SN) {
         p.a0 = end_angle;
         p.a1 = start_angle;
@@ -369,36 +371,62 @@ static __device__ __noinline__ ArcPlan round_join_plan(const DEP& join, int side
         p.a0 = start_angle;
         p.a1 = end_angle;
     }
-    p.depth = depth_of(arc_quotient(fabsf(diff), radius, tol), status);
+    p.depth = depth_of(arc_quotient(fabsf(diff), radius, tol), &p.st);
     return p;
+}
+
+__device__ __forceinline__ ArcPlan join_arc_plan(const DEP& j, int side, float tol, int* status) {
+    const ArcPlan a = round_join_plan(j.pos, j.hw, j.s[side].prev, j.s[side].next, side, tol);
+    if (a.st != LYON_OK) *status = a.st;
+    return a;
 }
 
 __device__ __forceinline__ uint32_t arc_vertex_count(uint32_t depth) {
     return depth == 0 ? 0u : ((1u << depth) - 1u);
 }
 
-// stroke.rs:2612-2653 (pre-order recursion, made iterative with an explicit stack).
+// stroke.rs:2612-2653. lyon's recursion visits a perfect binary tree of `depth` levels in
+// pre-order: each node emits the vertex at the middle of its angle range (the halving of its
+// parent's range) and the triangle (range start vertex, it, range end vertex), then recurses into
+// the lower half and the upper half. Node k of the pre-order is found by descending from the
+// root, halving the range exactly as the recursion does, so the angles are the recursion's bit
+// for bit. Vertices get consecutive ids in pre-order, so an ancestor's id is the first arc
+// vertex's id plus its pre-order index. No per-lane stack: everything stays in registers (the
+// sink is taken and returned by value for the same reason).
 template <class SK>
-__device__ __noinline__ void tessellate_arc(V2 center, float radius, float a0, float a1, uint32_t va,
-                                            uint32_t vb, uint32_t depth, int side, SK& sink) {
-    if (depth == 0) return;
-    struct Frame {
-        float a0, a1;
-        uint32_t va, vb, n;
-    };
-    Frame st[MAX_ARC_DEPTH + 2];
-    int sp = 0;
-    st[sp++] = Frame{a0, a1, va, vb, depth};
-    while (sp > 0) {
-        Frame f = st[--sp];
-        if (f.n == 0) continue;
-        float mid = (f.a0 + f.a1) * 0.5f;
+__device__ __noinline__ SK tessellate_arc(V2 center, float radius, float a0, float a1, uint32_t va,
+                                          uint32_t vb, uint32_t depth, int side, SK sink) {
+    if (depth == 0) return sink;
+    const uint32_t total = (1u << depth) - 1u;
+    uint32_t first_id = 0;
+    for (uint32_t k = 0; k < total; ++k) {
+        float lo = a0, hi = a1;
+        uint32_t ilo = va, ihi = vb;
+        uint32_t p = 0;      // pre-order index of the node reached
+        uint32_t n = depth;  // levels of its subtree
+        float mid = (lo + hi) * 0.5f;
+        while (p != k) {
+            // The lower half's subtree holds 2^(n-1) - 1 nodes, so the upper half starts at
+            // p + 2^(n-1).
+            const uint32_t upper = p + (1u << (n - 1));
+            if (k < upper) {
+                hi = mid;
+                ihi = first_id + p;
+                p += 1;
+            } else {
+                lo = mid;
+                ilo = first_id + p;
+                p = upper;
+            }
+            --n;
+            mid = (lo + hi) * 0.5f;
+        }
         V2 normal = V2{cosf(mid), sinf(mid)};
         uint32_t vid = sink.vertex(center + normal * radius, normal, side);
-        sink.tri(f.va, vid, f.vb);
-        st[sp++] = Frame{mid, f.a1, vid, f.vb, f.n - 1};
-        st[sp++] = Frame{f.a0, mid, f.va, vid, f.n - 1};
+        if (k == 0) first_id = vid;
+        sink.tri(ilo, vid, ihi);
     }
+    return sink;
 }
 
 // ---- emission ---------------------------------------------------------------------------------
@@ -502,10 +530,10 @@ __device__ __forceinline__ void tessellate_join(const DEP& j, const StrokeParams
     if (j.join == LYON_JOIN_ROUND) {
         for (int side = 0; side < 2; ++side) {
             if (!nj[side]) continue;
-            ArcPlan a = round_join_plan(j, side, P.tolerance, status);
+            ArcPlan a = join_arc_plan(j, side, P.tolerance, status);
             uint32_t va = side == SN ? j.s[side].next_vertex : j.s[side].prev_vertex;
             uint32_t vb = side == SN ? j.s[side].prev_vertex : j.s[side].next_vertex;
-            tessellate_arc(j.pos, j.hw, a.a0, a.a1, va, vb, a.depth, side, sink);
+            sink = tessellate_arc(j.pos, j.hw, a.a0, a.a1, va, vb, a.depth, side, sink);
         }
     }
 }
@@ -519,33 +547,52 @@ __device__ __forceinline__ uint32_t join_arc_vertices(const DEP& j, const Stroke
     uint32_t n = 0;
     for (int side = 0; side < 2; ++side) {
         if (!nj[side]) continue;
-        ArcPlan a = round_join_plan(j, side, P.tolerance, status);
+        ArcPlan a = join_arc_plan(j, side, P.tolerance, status);
         n += arc_vertex_count(a.depth);
     }
     return n;
 }
 
-// stroke.rs:2459-2524
+// stroke.rs:2459-2524. Sink and status are taken and returned by value (see tessellate_arc).
 template <class SK>
-__device__ __noinline__ void tessellate_round_cap(V2 center, float radius, V2 start_normal,
-                                                  uint32_t start_vertex, uint32_t end_vertex,
-                                                  V2 edge_normal, bool is_start,
-                                                  const StrokeParams& P, SK& sink,
-                                                  int* status) {
-    if (radius < P.tolerance) return;
+struct CapOut {
+    SK sink;
+    int st;
+};
+template <class SK>
+__device__ __noinline__ CapOut<SK> tessellate_round_cap_v(V2 center, float radius, V2 start_normal,
+                                                          uint32_t start_vertex,
+                                                          uint32_t end_vertex, V2 edge_normal,
+                                                          bool is_start, float tolerance, SK sink) {
+    int st = LYON_OK;
+    if (radius < tolerance) return CapOut<SK>{sink, st};
     const int first_side = (is_start ^ (cross(edge_normal, start_normal) >= 0.0f)) ? SP : SN;
     const float start_angle = angle_from_x_axis(start_normal);
     const float diff = angle_to(start_angle, angle_from_x_axis(edge_normal));
     const float mid_angle = start_angle + diff;
     const float end_angle = mid_angle + diff;
-    const uint32_t depth = depth_of(arc_quotient(fabsf(diff), radius, P.tolerance), status);
+    const uint32_t depth = depth_of(arc_quotient(fabsf(diff), radius, tolerance), &st);
     const V2 mid_normal = normalize(edge_normal);
     uint32_t mid_vertex = sink.vertex(center + mid_normal * radius, mid_normal, first_side);
     sink.tri(start_vertex, mid_vertex, end_vertex);
-    tessellate_arc(center, radius, start_angle, mid_angle, start_vertex, mid_vertex, depth,
-                   first_side, sink);
-    tessellate_arc(center, radius, mid_angle, end_angle, mid_vertex, end_vertex, depth,
-                   1 - first_side, sink);
+    sink = tessellate_arc(center, radius, start_angle, mid_angle, start_vertex, mid_vertex, depth,
+                          first_side, sink);
+    sink = tessellate_arc(center, radius, mid_angle, end_angle, mid_vertex, end_vertex, depth,
+                          1 - first_side, sink);
+    return CapOut<SK>{sink, st};
+}
+
+template <class SK>
+__device__ __forceinline__ void tessellate_round_cap(V2 center, float radius, V2 start_normal,
+                                                     uint32_t start_vertex, uint32_t end_vertex,
+                                                     V2 edge_normal, bool is_start,
+                                                     const StrokeParams& P, SK& sink,
+                                                     int* status) {
+    const CapOut<SK> r = tessellate_round_cap_v(center, radius, start_normal, start_vertex,
+                                                end_vertex, edge_normal, is_start, P.tolerance,
+                                                sink);
+    sink = r.sink;
+    if (r.st != LYON_OK) *status = r.st;
 }
 
 // stroke.rs:2526-2560
@@ -679,54 +726,70 @@ struct SlowJoin {
     uint32_t vcount;     // base + arc vertices
     uint32_t jtris;      // interior + arc triangles
     bool sym;            // side next points symmetric about the join point
+    int st;              // LYON_OK or the arcs' LYON_ERR_UNSUPPORTED
 };
 
-// stroke.rs:1586-1608 for a join that is not a flattening step: side positions, folds and the
-// vertex layout. The join (without ids) is stored to *dep for the emission phase.
-static __device__ __noinline__ void slow_join_geometry(DEP* dep, V2 prev, V2 cur, bool flat, V2 nxt,
-                                                const StrokeParams& P, SlowJoin* r,
-                                                int* status) {
+// stroke.rs:1586-1608 for a join that is not a flattening step: side positions and folds.
+__device__ __forceinline__ DEP join_geometry(V2 prev, V2 cur, bool flat, V2 nxt,
+                                             const StrokeParams& P) {
     DEP J;
     dep_init(J, cur, P.hw, P.line_join, flat);
     compute_join_side_positions_fw(prev, J, nxt, P.miter_limit);
-    *dep = J;
-    Sink probe{0u, 0, 0, nullptr, nullptr, 32};
-    add_join_base_vertices(J, SN, probe);
-    add_join_base_vertices(J, SP, probe);
-    uint32_t a, b;
-    edge_ids_from(J, &a, &b);
-    r->from_neg_rel = a;
-    r->from_pos_rel = b;
-    r->from_f = id_flags(a, b);
-    edge_ids_to(J, &a, &b);
-    r->to_f = id_flags(a, b);
-    uint32_t varc = join_arc_vertices(J, P, status);
-    r->vcount = probe.nv + varc;
-    r->jtris = join_interior_tris(J) + varc;
-    r->pn = J.s[SP].next;
-    r->nn = J.s[SN].next;
-    // Only a clipped miter moves one side's points off the symmetric offsets.
-    r->sym = J.join != LYON_JOIN_MITER_CLIP;
+    return J;
 }
 
-// Emission of a general join: base vertices (- then +), the edge triangles from the previous
-// join, then tessellate_join. *out receives the join with its ids (for the tail).
+// The counts and id layout of a general join. Out of line with its inputs and result by value:
+// the join itself stays in the callee's registers (a join written through a pointer would live
+// in local memory, in the caller's frame).
+static __device__ __noinline__ SlowJoin slow_join_summary(V2 prev, V2 cur, bool flat, V2 nxt,
+                                                          StrokeParams P) {
+    DEP J = join_geometry(prev, cur, flat, nxt, P);
+    SlowJoin r;
+    r.st = LYON_OK;
+    Sink probe{0u, 0, 0, nullptr, nullptr, 32};
+    DEP K = J;
+    add_join_base_vertices(K, SN, probe);
+    add_join_base_vertices(K, SP, probe);
+    uint32_t a, b;
+    edge_ids_from(K, &a, &b);
+    r.from_neg_rel = a;
+    r.from_pos_rel = b;
+    r.from_f = id_flags(a, b);
+    edge_ids_to(K, &a, &b);
+    r.to_f = id_flags(a, b);
+    uint32_t varc = join_arc_vertices(J, P, &r.st);
+    r.vcount = probe.nv + varc;
+    r.jtris = join_interior_tris(J) + varc;
+    r.pn = J.s[SP].next;
+    r.nn = J.s[SN].next;
+    // Only a clipped miter moves one side's points off the symmetric offsets.
+    r.sym = J.join != LYON_JOIN_MITER_CLIP;
+    return r;
+}
+
+// Emission of a general join: its geometry (the same operations on the same points as
+// slow_join_summary), base vertices (- then +), the edge triangles from the previous join, then
+// tessellate_join. The sink is taken by value and its counters returned.
+struct JoinEmitOut {
+    uint32_t nv, ni;
+    bool overflow;
+    int st;
+};
 template <class SK>
-__device__ __noinline__ void slow_join_emit(const DEP* dep, DEP* out, SK& s, bool has_edge,
-                                            uint32_t pfn, uint32_t pfp, bool emit_tris,
-                                            const StrokeParams& P, int* status) {
-    DEP J = *dep;
+__device__ __noinline__ JoinEmitOut slow_join_emit_at(V2 prev, V2 cur, bool flat, V2 nxt,
+                                                      StrokeParams P, SK s, bool has_edge,
+                                                      uint32_t pfn, uint32_t pfp) {
+    DEP J = join_geometry(prev, cur, flat, nxt, P);
+    int st = LYON_OK;
     add_join_base_vertices(J, SN, s);
     add_join_base_vertices(J, SP, s);
-    if (emit_tris) {
-        if (has_edge) {
-            uint32_t c, d;
-            edge_ids_to(J, &c, &d);
-            edge_triangles(pfn, pfp, c, d, &s);
-        }
-        tessellate_join(J, P, s, status);
+    if (has_edge) {
+        uint32_t c, d;
+        edge_ids_to(J, &c, &d);
+        edge_triangles(pfn, pfp, c, d, &s);
     }
-    *out = J;
+    tessellate_join(J, P, s, &st);
+    return JoinEmitOut{s.nv, s.ni, s.overflow, st};
 }
 
 // The join of a flattening step (stroke.rs:1743-1806) as a DEP, for the tail.

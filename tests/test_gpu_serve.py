@@ -83,3 +83,28 @@ def test_load_runner_completes_every_request(pools):
     assert st["failed"] == 0
     assert st["p50_ms"] <= st["p99_ms"] <= st["max_ms"]
     assert len(st["latencies_ms"]) == st["completed"]
+
+
+def test_lone_request_reaches_its_lane(pools):
+    # One request at a time into a server with stroke and fill lanes: each must be taken by a
+    # worker of its kind although nothing else is queued (a wake-up that reaches only a worker of
+    # the other kind would leave it waiting). Polled with a deadline, so a lost wake-up fails the
+    # test instead of blocking it.
+    import time
+    sb, so, _, _, fb, fo = pools
+    srv = serving.Server(0, num_workers=2, num_stroke_workers=2)
+    try:
+        for kind, pool, opts, n in ((serving.KIND_STROKE, sb, so, 1500),
+                                    (serving.KIND_FILL, fb, fo, 300),
+                                    (serving.KIND_STROKE, sb, so, 1)):
+            t = srv.submit(serving.Request(kind, pool, 0, n, opts))
+            deadline = time.monotonic() + 60.0
+            res = srv.poll(t)
+            while res is None and time.monotonic() < deadline:
+                time.sleep(0.001)
+                res = srv.poll(t)
+            assert res is not None, f"request of kind {kind} not served within 60 s"
+            assert res.status == 0 and res.num_paths == n
+            srv.release(t)
+    finally:
+        srv.close()

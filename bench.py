@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=0.1)
     ap.add_argument("--profile-fill", action="store_true",
                     help="only run the fill warm-up and timed steps (for profilers)")
+    ap.add_argument("--fill-lanes", type=int, default=0,
+                    help="with --profile-fill: sweepers per warp (0: the library's choice)")
+    ap.add_argument("--fill-blocks-per-sm", type=int, default=0,
+                    help="with --profile-fill: sweep blocks per SM (0: the library's default)")
     ap.add_argument("--profile", action="store_true",
                     help="only run the warm-up and timed device steps (for profilers)")
     ap.add_argument("--profile-producers", action="store_true",
@@ -326,6 +330,12 @@ def main():
         ctx = T.Context(dev)
         lib = ctx.lib
         lib.lyon_gpu_set_timing(ctx.h, 1)
+        if args.fill_lanes or args.fill_blocks_per_sm:
+            from lyon_gb300 import _native
+            tuning = _native.CFillTuning()
+            tuning.blocks_per_sm = args.fill_blocks_per_sm
+            tuning.lanes = args.fill_lanes
+            assert lib.lyon_gpu_set_fill_tuning(ctx.h, ctypes.byref(tuning)) == 0
         out = run_fill(ctx, args, T, world)
         print(json.dumps({k: v for k, v in out.items() if k != "config"}))
         ctx.close()
@@ -1008,9 +1018,26 @@ def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
     launches = lib.lyon_gpu_kernel_launches() - launches0
     h2d = batch.input_bytes(options_bytes_per_path=24)
     d2h = int(tv) * 8 + int(ti) * 4 + batch.num_paths * 4
-    return {"value": int(tvo.value) / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3, "steps": steps,
-            "host_buffers": host_kind, "gpu_launches": launches}
+    out = {"value": int(tvo.value) / dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3, "steps": steps,
+           "host_buffers": host_kind, "gpu_launches": launches}
+    # The box's device-to-host link on its own: plain 4 GB copies into the same pinned buffer.
+    # The call moves d2h bytes, so d2h / this rate is the floor under its time.
+    if host_kind == "pinned":
+        n = min(hv.numel(), (4 << 30) // 4)
+        src = torch.empty(n, dtype=torch.float32, device="cuda")
+        src.fill_(1.0)
+        hv[:n].copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            hv[:n].copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        gbs = 3 * n * 4 / (time.perf_counter() - t0) / 1e9
+        del src
+        out["link_d2h_gbs"] = gbs
+        out["d2h_floor_ms"] = d2h / (gbs * 1e9) * 1e3
+    return out
 
 
 if __name__ == "__main__":

@@ -839,7 +839,7 @@ def run_polylines(ctx, args, T):
                res.total_indices * 4 + 16 * batch.num_paths)
         tpv = profiled_figure("stroke_emit_map_polylines_300k.md", "dram_bytes_per_output_vertex")
         entry["roofline"] = roofline_entry(
-            alg, statistics.median(emit_ms) / 1e3, "stroke emit (walk + run kernel)",
+            alg, statistics.median(emit_ms) / 1e3, "stroke_kernel<true> (emit: warp walk and one-thread short paths)",
             tpv * res.total_vertices if tpv is not None else None)
         if tol == 0.1:
             n = batch.num_paths  # the whole batch: well under a second on the host cores

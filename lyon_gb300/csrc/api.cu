@@ -20,6 +20,7 @@ namespace {
 struct DevBuf {
     void* ptr = nullptr;
     size_t cap = 0;
+    bool pooled = false;  // from the context's memory pool (freed stream-ordered)
 };
 
 struct HostBuf {
@@ -37,6 +38,10 @@ struct lyon_gpu_context {
     int stroke_bps = 1;
     cudaStream_t stream = nullptr;       // kernels
     cudaStream_t copy_stream = nullptr;  // device->host copies of the host-buffer calls
+    // Serving contexts: buffers come from the server's memory pool, allocated and freed in
+    // `stream` order. A plain cudaFree can wait for every kernel on the device (another
+    // worker's fill sweep included), which a stroke request must not wait behind.
+    cudaMemPool_t pool = nullptr;
     std::string last_error;
     // per-path work arrays
     DevBuf vtx_counts, idx_counts, status, vtx_offsets, idx_offsets, scan_state;
@@ -113,14 +118,20 @@ bool set_err(lyon_gpu_context* ctx, const char* what, cudaError_t e) {
 bool ensure(lyon_gpu_context* ctx, DevBuf& b, size_t bytes) {
     if (bytes <= b.cap && b.ptr) return true;
     if (b.ptr) {
-        cudaStreamSynchronize(ctx->stream);
-        cudaStreamSynchronize(ctx->copy_stream);
-        cudaFree(b.ptr);
+        if (b.pooled) {
+            cudaFreeAsync(b.ptr, ctx->stream);
+        } else {
+            cudaStreamSynchronize(ctx->stream);
+            cudaStreamSynchronize(ctx->copy_stream);
+            cudaFree(b.ptr);
+        }
         b.ptr = nullptr;
         b.cap = 0;
     }
     size_t cap = bytes < 256 ? 256 : bytes + bytes / 8;
-    cudaError_t e = cudaMalloc(&b.ptr, cap);
+    b.pooled = ctx->pool != nullptr;
+    cudaError_t e = b.pooled ? cudaMallocFromPoolAsync(&b.ptr, cap, ctx->pool, ctx->stream)
+                             : cudaMalloc(&b.ptr, cap);
     if (e != cudaSuccess) {
         cudaGetLastError();
         set_err(ctx, "cudaMalloc", e);
@@ -171,10 +182,13 @@ T* direct_host_pointer(void* p) {
 
 uint32_t* small_words(lyon_gpu_context* ctx) { return as<uint32_t>(ctx->small); }
 
+// Pooled buffers too: cudaFree of a stream-ordered allocation does not synchronize, and the
+// context's streams are idle when this runs.
 void free_buf(DevBuf& b) {
     if (b.ptr) cudaFree(b.ptr);
     b.ptr = nullptr;
     b.cap = 0;
+    b.pooled = false;
 }
 void free_host(HostBuf& b) {
     if (b.ptr) cudaFreeHost(b.ptr);
@@ -807,8 +821,12 @@ cudaStream_t srv_stream(lyon_gpu_context* ctx) { return ctx->stream; }
 // Settings of a serving worker's context. A stroke lane gets a stream of the device's highest
 // priority (its blocks are dispatched before queued blocks of other streams) and one stroke block
 // per SM; `fill_blocks_per_sm` (0: default) bounds the fill sweep's residency.
-int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm) {
+int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm,
+                  cudaMemPool_t pool) {
     ctx->fill.blocks_per_sm_cap = fill_blocks_per_sm;
+    ctx->pool = pool;
+    // The fill buffers are all allocated by the first fill call, so they are all pooled or none.
+    if (!ctx->fill.scratch && !ctx->fill.stage_v && !ctx->fill.work) ctx->fill.pool = pool;
     if (!stroke_lane) return LYON_OK;
     ctx->blocks_per_sm = 1;
     int least = 0, greatest = 0;

@@ -209,18 +209,25 @@ __global__ void fill_emit_kernel(uint32_t n, const uint32_t* vtx_counts,
 
 namespace {
 
-bool grow(void** p, size_t* cap, size_t bytes, size_t keep_bytes, cudaStream_t s) {
+// With a pool the old buffer is freed in stream order, without waiting for the device.
+bool grow(void** p, size_t* cap, size_t bytes, size_t keep_bytes, cudaStream_t s,
+          cudaMemPool_t pool) {
     if (bytes <= *cap && *p) return true;
     void* np = nullptr;
     size_t nc = bytes + bytes / 4 + 256;
-    if (cudaMalloc(&np, nc) != cudaSuccess) {
+    const cudaError_t e = pool ? cudaMallocFromPoolAsync(&np, nc, pool, s) : cudaMalloc(&np, nc);
+    if (e != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
     if (*p) {
         if (keep_bytes) cudaMemcpyAsync(np, *p, keep_bytes, cudaMemcpyDeviceToDevice, s);
-        cudaStreamSynchronize(s);
-        cudaFree(*p);
+        if (pool) {
+            cudaFreeAsync(*p, s);
+        } else {
+            cudaStreamSynchronize(s);
+            cudaFree(*p);
+        }
     }
     *p = np;
     *cap = nc;
@@ -240,8 +247,8 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
     // lists.
     // After them: the size-order scratch (counters, one byte per path).
     const size_t ctl_bytes = 64 + (size_t)n * 8 + 2 * SIZE_ORDER_BINS * 4 + (size_t)n;
-    if (!grow(&fb.work, &fb.work_cap, ctl_bytes, 0, stream) ||
-        !grow(&fb.stage_off, &fb.stage_off_cap, (size_t)n * 16, 0, stream)) {
+    if (!grow(&fb.work, &fb.work_cap, ctl_bytes, 0, stream, fb.pool) ||
+        !grow(&fb.stage_off, &fb.stage_off_cap, (size_t)n * 16, 0, stream, fb.pool)) {
         if (error) *error = "cudaMalloc (fill control arrays)";
         return LYON_ERR_OUT_OF_MEMORY;
     }
@@ -264,8 +271,8 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         cudaMemcpyAsync(&npts, batch->point_offsets + n, 4, cudaMemcpyDeviceToHost, stream);
         cudaStreamSynchronize(stream);
         const size_t guess_v = (size_t)npts * 4 + 4096;
-        if (!grow(&fb.stage_v, &fb.stage_v_cap, guess_v * 8, 0, stream) ||
-            !grow(&fb.stage_i, &fb.stage_i_cap, guess_v * 3 * 4, 0, stream)) {
+        if (!grow(&fb.stage_v, &fb.stage_v_cap, guess_v * 8, 0, stream, fb.pool) ||
+            !grow(&fb.stage_i, &fb.stage_i_cap, guess_v * 3 * 4, 0, stream, fb.pool)) {
             if (error) *error = "cudaMalloc (fill staging)";
             return LYON_ERR_OUT_OF_MEMORY;
         }
@@ -273,9 +280,10 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
     // Source staging: about one source per vertex, one first-source word per staged vertex.
     if (sources &&
         (!grow(&fb.stage_s, &fb.stage_s_cap, std::max<size_t>(fb.stage_v_cap / 8 * 12, 4096), 0,
-               stream) ||
-         !grow(&fb.stage_sfirst, &fb.stage_sfirst_cap, fb.stage_v_cap / 8 * 4 + 256, 0, stream) ||
-         !grow(&fb.stage_soff, &fb.stage_soff_cap, (size_t)n * 8, 0, stream))) {
+               stream, fb.pool) ||
+         !grow(&fb.stage_sfirst, &fb.stage_sfirst_cap, fb.stage_v_cap / 8 * 4 + 256, 0, stream,
+               fb.pool) ||
+         !grow(&fb.stage_soff, &fb.stage_soff_cap, (size_t)n * 8, 0, stream, fb.pool))) {
         if (error) *error = "cudaMalloc (fill source staging)";
         return LYON_ERR_OUT_OF_MEMORY;
     }
@@ -313,7 +321,7 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
             nthreads /= 2;
             heap_bytes /= 2;
         }
-        if (!grow(&fb.scratch, &fb.scratch_cap, heap_bytes, 0, stream)) {
+        if (!grow(&fb.scratch, &fb.scratch_cap, heap_bytes, 0, stream, fb.pool)) {
             if (error) *error = "cudaMalloc (fill heaps)";
             return LYON_ERR_OUT_OF_MEMORY;
         }
@@ -375,7 +383,7 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         if (sources && h_tops[2] > fb.stage_s_cap / 12) {
             const size_t used_s = std::min<size_t>(h_tops[2], fb.stage_s_cap / 12);
             if (!grow(&fb.stage_s, &fb.stage_s_cap, (size_t)h_tops[2] * 2 * 12 + 4096,
-                      used_s * 12, stream)) {
+                      used_s * 12, stream, fb.pool)) {
                 if (error) *error = "cudaMalloc (fill source staging)";
                 return LYON_ERR_OUT_OF_MEMORY;
             }
@@ -384,11 +392,12 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
             const size_t used_v = std::min<size_t>(h_tops[0], fb.stage_v_cap / 8);
             const size_t used_i = std::min<size_t>(h_tops[1], fb.stage_i_cap / 4);
             if (!grow(&fb.stage_v, &fb.stage_v_cap, (size_t)h_tops[0] * 2 * 8 + 4096,
-                      used_v * 8, stream) ||
+                      used_v * 8, stream, fb.pool) ||
                 !grow(&fb.stage_i, &fb.stage_i_cap, (size_t)h_tops[1] * 2 * 4 + 4096,
-                      used_i * 4, stream) ||
+                      used_i * 4, stream, fb.pool) ||
                 (sources && !grow(&fb.stage_sfirst, &fb.stage_sfirst_cap,
-                                  (size_t)h_tops[0] * 2 * 4 + 4096, used_v * 4, stream))) {
+                                  (size_t)h_tops[0] * 2 * 4 + 4096, used_v * 4, stream,
+                                  fb.pool))) {
                 if (error) *error = "cudaMalloc (fill staging)";
                 return LYON_ERR_OUT_OF_MEMORY;
             }

@@ -27,6 +27,8 @@ struct FillBuffers {
     uint32_t blocks_per_sm_cap = 0;
     // Sweepers per one-warp block (1..32); 0: chosen per launch from its paths per block.
     uint32_t lanes = 0;
+    // When set, every buffer here comes from this pool in stream order (serving contexts).
+    cudaMemPool_t pool = nullptr;
     // Vertex sources (FillVertex::sources), when a call asks for them:
     void* stage_s = nullptr;        // staged sources, three u32 words each, path-local ids
     size_t stage_s_cap = 0;

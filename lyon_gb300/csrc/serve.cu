@@ -32,7 +32,8 @@ namespace lg {
 int srv_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
               uint32_t num_options, const uint32_t* request_first, uint64_t* tv, uint64_t* ti,
               uint32_t* failed);
-int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm);
+int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm,
+                  cudaMemPool_t pool);
 int srv_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
              uint32_t num_options, const uint32_t* request_first, float* vout, void* iout,
              uint64_t tv);
@@ -82,17 +83,29 @@ struct Request {
     uint64_t v_begin = 0, v_end = 0, i_begin = 0, i_end = 0;
 };
 
+// Device buffers of a worker: from the server's pool in the worker's stream order when there is
+// a pool (a plain cudaFree can wait for every kernel on the device, other workers' included).
 template <class T>
-bool dev_grow(T** p, size_t* cap, size_t n) {
+bool dev_grow(T** p, size_t* cap, size_t n, cudaMemPool_t pool, cudaStream_t st) {
     if (n <= *cap && *p) return true;
-    if (*p) cudaFree(*p);
+    if (*p) {
+        if (pool) {
+            cudaFreeAsync(*p, st);
+        } else {
+            cudaFree(*p);
+        }
+    }
     *p = nullptr;
     size_t c = n + n / 2 + 64;
-    if (cudaMalloc(reinterpret_cast<void**>(p), c * sizeof(T)) != cudaSuccess) {
+    void* np = nullptr;
+    const cudaError_t e = pool ? cudaMallocFromPoolAsync(&np, c * sizeof(T), pool, st)
+                               : cudaMalloc(&np, c * sizeof(T));
+    if (e != cudaSuccess) {
         cudaGetLastError();
         *cap = 0;
         return false;
     }
+    *p = reinterpret_cast<T*>(np);
     *cap = c;
     return true;
 }
@@ -147,6 +160,7 @@ struct lyon_srv {
     uint64_t held_bytes = 0;  // slabs of unreleased requests + reservations of running batches
     bool stop = false;
     std::vector<std::unique_ptr<Worker>> workers;
+    cudaMemPool_t pool = nullptr;  // every worker's device buffers (null: plain cudaMalloc)
 };
 
 namespace {
@@ -191,7 +205,8 @@ void finish(lyon_srv* s, std::vector<Request*>& batch, int status, Slab* slab, c
     s->cv_work.notify_all();
 }
 
-Slab* take_slab(Worker& w, uint64_t tv, uint64_t ti, uint32_t np) {
+Slab* take_slab(Worker& w, uint64_t tv, uint64_t ti, uint32_t np, cudaMemPool_t pool,
+                cudaStream_t st) {
     Slab* best = nullptr;
     for (Slab* sl : w.slabs) {
         if (sl->refs == 0 && sl->vcap >= tv && sl->icap >= ti && sl->pcap >= (size_t)np + 1)
@@ -202,18 +217,14 @@ Slab* take_slab(Worker& w, uint64_t tv, uint64_t ti, uint32_t np) {
         best = new Slab();
         w.slabs.push_back(best);
     }
-    if (!dev_grow(&best->v, &best->vcap, (size_t)tv + 1) ||
-        !dev_grow(&best->i, &best->icap, (size_t)ti + 1))
+    if (!dev_grow(&best->v, &best->vcap, (size_t)tv + 1, pool, st) ||
+        !dev_grow(&best->i, &best->icap, (size_t)ti + 1, pool, st))
         return nullptr;
     if (best->pcap < (size_t)np + 1) {
-        cudaFree(best->voff);
-        cudaFree(best->ioff);
-        cudaFree(best->st);
-        best->voff = best->ioff = nullptr;
-        best->st = nullptr;
-        size_t c1 = 0, c2 = 0, c3 = 0;
-        if (!dev_grow(&best->voff, &c1, (size_t)np + 1) ||
-            !dev_grow(&best->ioff, &c2, (size_t)np + 1) || !dev_grow(&best->st, &c3, (size_t)np + 1))
+        size_t c1 = best->pcap, c2 = best->pcap, c3 = best->pcap;
+        if (!dev_grow(&best->voff, &c1, (size_t)np + 1, pool, st) ||
+            !dev_grow(&best->ioff, &c2, (size_t)np + 1, pool, st) ||
+            !dev_grow(&best->st, &c3, (size_t)np + 1, pool, st))
             return nullptr;
         best->pcap = c1;
     }
@@ -240,10 +251,11 @@ void run_batch(lyon_srv* s, Worker& w, int kind, std::vector<Request*>& batch, u
         !host_grow(&w.h_off, &w.ho_cap, (size_t)np * 3 + 3) ||
         !host_grow(&w.h_opts, &w.hopt_cap, (size_t)np * osz + osz) ||
         !host_grow(&w.h_res, &w.hres_cap, (size_t)np * 3 + 4) ||
-        !dev_grow(&w.d_verbs, &w.dv_cap, nverbs + 16) ||
-        !dev_grow(&w.d_points, &w.dp_cap, npts * 2 + 16) ||
-        !dev_grow(&w.d_off, &w.do_cap, (size_t)np * 3 + 3) ||
-        !dev_grow(&w.d_opts, &w.dopt_cap, (size_t)np * osz + osz)) {
+        !dev_grow(&w.d_verbs, &w.dv_cap, nverbs + 16, s->pool, lg::srv_stream(w.ctx)) ||
+        !dev_grow(&w.d_points, &w.dp_cap, npts * 2 + 16, s->pool, lg::srv_stream(w.ctx)) ||
+        !dev_grow(&w.d_off, &w.do_cap, (size_t)np * 3 + 3, s->pool, lg::srv_stream(w.ctx)) ||
+        !dev_grow(&w.d_opts, &w.dopt_cap, (size_t)np * osz + osz, s->pool,
+                  lg::srv_stream(w.ctx))) {
         finish(s, batch, LYON_ERR_OUT_OF_MEMORY, nullptr, nullptr, nullptr, nullptr, reserved);
         return;
     }
@@ -296,7 +308,7 @@ void run_batch(lyon_srv* s, Worker& w, int kind, std::vector<Request*>& batch, u
     Slab* slab;
     {
         std::lock_guard<std::mutex> g(s->mu);
-        slab = take_slab(w, tv, ti, np);
+        slab = take_slab(w, tv, ti, np, s->pool, st);
     }
     if (!slab) {
         finish(s, batch, LYON_ERR_OUT_OF_MEMORY, nullptr, nullptr, nullptr, nullptr, reserved);
@@ -431,6 +443,21 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
     if (c.max_stroke_batch_paths == 0) c.max_stroke_batch_paths = c.max_batch_paths;
     if (c.num_stroke_workers > 0 && c.fill_blocks_per_sm == 0) c.fill_blocks_per_sm = 8;
     s->cfg = c;
+    // One pool for every worker's device buffers; it keeps what is freed for reuse (no release
+    // threshold), so steady-state batches allocate without the driver.
+    cudaSetDevice(c.device);
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = c.device;
+    if (cudaMemPoolCreate(&s->pool, &props) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else {
+        cudaGetLastError();
+        s->pool = nullptr;
+    }
     const uint32_t total = c.num_workers + c.num_stroke_workers;
     for (uint32_t i = 0; i < total; ++i) {
         std::unique_ptr<Worker> w(new Worker());
@@ -441,7 +468,7 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
         }
         const bool stroke_lane = i >= c.num_workers;
         w->role = c.num_stroke_workers == 0 ? ROLE_ANY : (stroke_lane ? ROLE_STROKE : ROLE_FILL);
-        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm);
+        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm, s->pool);
         s->workers.push_back(std::move(w));
     }
     for (auto& w : s->workers) w->th = std::thread(worker_main, s, w.get());
@@ -460,6 +487,7 @@ void lyon_srv_destroy(lyon_srv* s) {
     }
     cudaSetDevice(s->cfg.device);
     for (auto& w : s->workers) {
+        if (w->ctx) cudaStreamSynchronize(lg::srv_stream(w->ctx));
         for (Slab* sl : w->slabs) {
             cudaFree(sl->v);
             cudaFree(sl->i);
@@ -479,6 +507,8 @@ void lyon_srv_destroy(lyon_srv* s) {
         cudaFree(w->d_opts);
         if (w->ctx) lyon_gpu_destroy(w->ctx);
     }
+    // After every buffer from it is freed (the contexts' included).
+    if (s->pool) cudaMemPoolDestroy(s->pool);
     for (auto& kv : s->reqs) delete kv.second;
     delete s;
 }

@@ -586,10 +586,18 @@ typedef struct lyon_srv_config {
                                       so that their launches start beside running fill sweeps
                                       instead of queueing behind them; 0 -> none (every worker
                                       takes both kinds, oldest request first) */
-    uint32_t fill_blocks_per_sm;   /* fill sweep blocks per SM in this loop; 0 -> 8 with stroke
-                                      workers (room for one stroke block per SM), else the
-                                      library's default */
+    uint32_t fill_blocks_per_sm;   /* fill sweep blocks per SM for each fill worker; 0 -> with
+                                      stroke workers, the registers an SM has left beside one
+                                      stroke block, split between the fill workers (5 each for
+                                      two on a GB300), so that a stroke launch finds room while
+                                      every fill worker's sweep runs; else the library's
+                                      default */
     uint32_t max_stroke_batch_paths; /* most paths per stroke launch; 0 -> max_batch_paths */
+    uint32_t small_request_paths;  /* with two or more stroke workers, the first one takes only
+                                      stroke requests of at most this many paths (oldest first),
+                                      so that a small request never waits behind two large
+                                      stroke batches; 0 -> 1000; ignored with fewer than two
+                                      stroke workers */
 } lyon_srv_config;
 
 /* A finished request. Its output stays on the device until lyon_srv_release. */
@@ -614,6 +622,8 @@ typedef struct lyon_srv_result {
 lyon_srv* lyon_srv_create(const lyon_srv_config* config);
 /* Stops the workers (after their current batch) and frees everything. */
 void lyon_srv_destroy(lyon_srv* srv);
+/* The configuration the loop runs with, defaults resolved (worker counts, fill_blocks_per_sm). */
+int lyon_srv_get_config(const lyon_srv* srv, lyon_srv_config* out);
 /* Queues a request: `batch` (host memory) stroked (LYON_KIND_STROKE, lyon_stroke_options) or
  * filled (LYON_KIND_FILL, lyon_fill_options) with 1 shared or num_paths option records. The
  * batch and options are read while the request runs: keep them valid until it completes.

@@ -80,7 +80,8 @@ class CSvgOutput(ctypes.Structure):
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
                 ("device_budget_bytes", u64), ("num_stroke_workers", u32),
-                ("fill_blocks_per_sm", u32), ("max_stroke_batch_paths", u32)]
+                ("fill_blocks_per_sm", u32), ("max_stroke_batch_paths", u32),
+                ("small_request_paths", u32)]
 
 
 class CSrvResult(ctypes.Structure):
@@ -182,6 +183,8 @@ def load(build_if_missing: bool = True):
         L.lyon_srv_create.restype = c_p
         L.lyon_srv_create.argtypes = [ctypes.POINTER(CSrvConfig)]
         L.lyon_srv_destroy.argtypes = [c_p]
+        L.lyon_srv_get_config.restype = ctypes.c_int
+        L.lyon_srv_get_config.argtypes = [c_p, ctypes.POINTER(CSrvConfig)]
         L.lyon_srv_submit.restype = u64
         L.lyon_srv_submit.argtypes = [c_p, ctypes.c_int, ctypes.POINTER(CPathBatch), c_p, u32]
         for name in ("lyon_srv_poll", "lyon_srv_wait"):
@@ -276,7 +279,7 @@ EXPORTED = [
     "lyon_gpu_flatten_counts", "lyon_gpu_flatten_paths", "lyon_gpu_synchronize",
     "lyon_gpu_version", "lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host",
     "lyon_gpu_set_timing", "lyon_gpu_last_timings", "lyon_gpu_stroke_paths_noalloc",
-    "lyon_srv_create", "lyon_srv_destroy", "lyon_srv_submit", "lyon_srv_poll", "lyon_srv_wait",
+    "lyon_srv_create", "lyon_srv_destroy", "lyon_srv_get_config", "lyon_srv_submit", "lyon_srv_poll", "lyon_srv_wait",
     "lyon_srv_release", "lyon_srv_run_load", "lyon_gpu_set_stroke_tuning",
     "lyon_gpu_get_stroke_tuning", "lyon_gpu_autotune_stroke", "lyon_gpu_kernel_launches",
     "lyon_gpu_stroke_path_attributes", "lyon_gpu_stroke_paths_attributes",

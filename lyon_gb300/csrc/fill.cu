@@ -453,6 +453,15 @@ cudaError_t fill_zero_failed_source_counts(uint32_t* src_counts, const int32_t* 
     return cudaGetLastError();
 }
 
+int fill_block_registers() {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, fillk::fill_sweep_kernel<false>) != cudaSuccess) {
+        cudaGetLastError();
+        return 96 * 32;
+    }
+    return a.numRegs * 32;
+}
+
 void fill_free(FillBuffers& fb) {
     void* bufs[] = {fb.scratch, fb.stage_v,      fb.stage_i,   fb.stage_off,
                     fb.work,    fb.stage_s, fb.stage_sfirst, fb.stage_soff};

@@ -50,6 +50,9 @@ struct FillSourceArgs {
 
 // Runs the sweep of every path into staging and writes per-path vertex/index counts and status.
 // With `src` (src->src_counts set), every vertex's sources are staged too.
+// Registers one block of the fill sweep kernel holds on its SM.
+int fill_block_registers();
+
 int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_options* options,
                uint32_t num_options, int num_sms, uint32_t* vtx_counts, uint32_t* idx_counts,
                int32_t* status, uint32_t* small_words, cudaStream_t stream,

@@ -1271,6 +1271,15 @@ int stroke_blocks_per_sm() {
     return n > 0 ? n : 1;
 }
 
+int stroke_block_registers() {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, stroke_kernel<true, false>) != cudaSuccess) {
+        cudaGetLastError();
+        return 128 * STROKE_WARPS * 32;
+    }
+    return a.numRegs * STROKE_WARPS * 32;
+}
+
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream) {
     // Variable line width and the custom-attribute output use lyon's sequential stepper, one
     // path per thread (stroke_seq.cu). A fixed-width custom-attribute call counts with this

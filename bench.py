@@ -585,6 +585,11 @@ def run_variable_width(ctx, args, T):
            "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
            "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
            "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
+    # Inputs (with a width factor per point), positions, indices and per-path offsets, over the
+    # whole call (both passes of the sequential stepper, the scan).
+    alg = (batch.input_bytes(options_bytes_per_path=24) + 4 * len(batch.points) +
+           res.total_vertices * 8 + res.total_indices * 4 + 16 * batch.num_paths)
+    out["roofline"] = roofline_entry(alg, ms / 1e3, "whole call (stroke_seq_kernel count and emit)")
     threads = os.cpu_count() or 1
     n = min(20_000, batch.num_paths)
     sub = batch.head(n)
@@ -637,6 +642,12 @@ def run_custom_attributes(ctx, args, T, baseline=True):
            "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
            "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
            "gpu_launches": ctx.lib.lyon_gpu_kernel_launches() - launches0}
+    # Inputs with 8 B of attributes per point; per vertex its position, 12 B source and 8 B of
+    # interpolated attributes; indices; per-path offsets. Over the whole call.
+    alg = (batch.input_bytes(options_bytes_per_path=24) + 8 * len(batch.points) +
+           res.total_vertices * (8 + 12 + 8) + res.total_indices * 4 + 16 * batch.num_paths)
+    out["roofline"] = roofline_entry(alg, ms / 1e3,
+                                     "whole call (warp count, sequential emit, interpolation)")
     if not baseline:
         return out
     threads = os.cpu_count() or 1
@@ -699,6 +710,12 @@ def run_fill_custom(ctx, args, T, baseline=True):
            "metric": "output vertices/s", "value": res.total_vertices / (ms / 1e3),
            "unit": "vertices/s", "ms_per_step": ms, "vertices_per_step": res.total_vertices,
            "sources_per_step": res.total_sources, "gpu_launches": launches}
+    # Inputs with 8 B of attributes per point; per vertex its position, first-source offset and
+    # 8 B of interpolated attributes; 12 B per source; indices. Over the whole call.
+    alg = (batch.input_bytes(options_bytes_per_path=0) + 16 + 8 * len(batch.points) +
+           res.total_vertices * (8 + 8 + 8) + res.total_sources * 12 + res.total_indices * 4)
+    out["roofline"] = roofline_entry(alg, ms / 1e3, "whole call (fill sweep with sources, "
+                                                    "emit, interpolation)")
     if not baseline:
         return out
     threads = os.cpu_count() or 1
@@ -737,6 +754,10 @@ def run_arcs(ctx, args, T, baseline=True):
            "metric": "flattened points/s", "value": res.total_points / (ms / 1e3),
            "unit": "points/s", "ms_per_step": ms, "points_per_step": res.total_points,
            "gpu_launches": launches}
+    # 28 B per arc read; 8 B position and 4 B parameter per point, 8 B offset per arc written.
+    # The kernels are FP64-bound (f64 trigonometry), so this fraction is low by design.
+    alg = n * (28 + 8) + res.total_points * 12
+    out["roofline"] = roofline_entry(alg, ms / 1e3, "whole call (arc count and emit kernels)")
     if not baseline:
         return out
     k = 20_000
@@ -766,6 +787,9 @@ def run_hatching(ctx, args, T, baseline=True):
                       "tolerance": 0.1, "tangents": True},
            "metric": "hatch segments/s", "value": res.total / (ms / 1e3), "unit": "segments/s",
            "ms_per_step": ms, "segments_per_step": res.total, "gpu_launches": launches}
+    # Path bytes read; 48 B per segment written. Over the whole call.
+    alg = batch.input_bytes(options_bytes_per_path=0) + res.total * 48
+    out["roofline"] = roofline_entry(alg, ms / 1e3, "whole call (hatch bound, count and emit)")
     if not baseline:
         return out
     libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")

@@ -340,7 +340,7 @@ __device__ __noinline__ void join_dep_with_ids(DEP* out, V2 prev, V2 cur, V2 nxt
         fast_join_dep(*out, cur, P.hw, cur + nrm * P.hw, cur - nrm * P.hw,
                       skip ? INVALID_ID : base_id, skip ? INVALID_ID : base_id + 1);
     } else {
-        DEP d = join_geometry(prev, cur, flat, nxt, P);
+        DEP d = general_join_geometry(prev, cur, flat, nxt, P);
         join_arc_vertices(d, P, status);
         Sink probe{base_id, 0, 0, nullptr, nullptr, 32};
         add_join_base_vertices(d, SN, probe);

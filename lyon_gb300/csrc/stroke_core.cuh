@@ -730,8 +730,8 @@ struct SlowJoin {
 };
 
 // stroke.rs:1586-1608 for a join that is not a flattening step: side positions and folds.
-__device__ __forceinline__ DEP join_geometry(V2 prev, V2 cur, bool flat, V2 nxt,
-                                             const StrokeParams& P) {
+__device__ __forceinline__ DEP general_join_geometry(V2 prev, V2 cur, bool flat, V2 nxt,
+                                                     const StrokeParams& P) {
     DEP J;
     dep_init(J, cur, P.hw, P.line_join, flat);
     compute_join_side_positions_fw(prev, J, nxt, P.miter_limit);
@@ -743,7 +743,7 @@ __device__ __forceinline__ DEP join_geometry(V2 prev, V2 cur, bool flat, V2 nxt,
 // in local memory, in the caller's frame).
 static __device__ __noinline__ SlowJoin slow_join_summary(V2 prev, V2 cur, bool flat, V2 nxt,
                                                           StrokeParams P) {
-    DEP J = join_geometry(prev, cur, flat, nxt, P);
+    DEP J = general_join_geometry(prev, cur, flat, nxt, P);
     SlowJoin r;
     r.st = LYON_OK;
     Sink probe{0u, 0, 0, nullptr, nullptr, 32};
@@ -779,7 +779,7 @@ template <class SK>
 __device__ __noinline__ JoinEmitOut slow_join_emit_at(V2 prev, V2 cur, bool flat, V2 nxt,
                                                       StrokeParams P, SK s, bool has_edge,
                                                       uint32_t pfn, uint32_t pfp) {
-    DEP J = join_geometry(prev, cur, flat, nxt, P);
+    DEP J = general_join_geometry(prev, cur, flat, nxt, P);
     int st = LYON_OK;
     add_join_base_vertices(J, SN, s);
     add_join_base_vertices(J, SP, s);

@@ -111,10 +111,14 @@ bool dev_grow(T** p, size_t* cap, size_t n, cudaMemPool_t pool, cudaStream_t st)
     return true;
 }
 
+// Pinned staging of a worker. An outgrown buffer is retired, not freed: freeing page-locked
+// memory can wait for the whole device (another worker's fill sweep included). Buffers grow by
+// half each time, so the retired ones together stay below twice the final size; they are freed
+// with the loop.
 template <class T>
-bool host_grow(T** p, size_t* cap, size_t n) {
+bool host_grow(T** p, size_t* cap, size_t n, std::vector<void*>* retired) {
     if (n <= *cap && *p) return true;
-    if (*p) cudaFreeHost(*p);
+    if (*p) retired->push_back(*p);
     *p = nullptr;
     size_t c = n + n / 2 + 64;
     if (cudaMallocHost(reinterpret_cast<void**>(p), c * sizeof(T)) != cudaSuccess) {
@@ -146,6 +150,7 @@ struct Worker {
     uint8_t* d_opts = nullptr;
     size_t dv_cap = 0, dp_cap = 0, do_cap = 0, dopt_cap = 0;
     std::vector<Slab*> slabs;
+    std::vector<void*> retired_host;  // outgrown pinned staging, freed with the loop
     uint64_t batches = 0, batch_paths = 0;
 };
 
@@ -248,11 +253,11 @@ void run_batch(lyon_srv* s, Worker& w, int kind, std::vector<Request*>& batch, u
         nverbs += r->batch.verb_offsets[r->batch.num_paths] - r->batch.verb_offsets[0];
         npts += r->batch.point_offsets[r->batch.num_paths] - r->batch.point_offsets[0];
     }
-    if (!host_grow(&w.h_verbs, &w.hv_cap, nverbs + 16) ||
-        !host_grow(&w.h_points, &w.hp_cap, npts * 2 + 16) ||
-        !host_grow(&w.h_off, &w.ho_cap, (size_t)np * 3 + 3) ||
-        !host_grow(&w.h_opts, &w.hopt_cap, (size_t)np * osz + osz) ||
-        !host_grow(&w.h_res, &w.hres_cap, (size_t)np * 3 + 4) ||
+    if (!host_grow(&w.h_verbs, &w.hv_cap, nverbs + 16, &w.retired_host) ||
+        !host_grow(&w.h_points, &w.hp_cap, npts * 2 + 16, &w.retired_host) ||
+        !host_grow(&w.h_off, &w.ho_cap, (size_t)np * 3 + 3, &w.retired_host) ||
+        !host_grow(&w.h_opts, &w.hopt_cap, (size_t)np * osz + osz, &w.retired_host) ||
+        !host_grow(&w.h_res, &w.hres_cap, (size_t)np * 3 + 4, &w.retired_host) ||
         !dev_grow(&w.d_verbs, &w.dv_cap, nverbs + 16, s->pool, lg::srv_stream(w.ctx)) ||
         !dev_grow(&w.d_points, &w.dp_cap, npts * 2 + 16, s->pool, lg::srv_stream(w.ctx)) ||
         !dev_grow(&w.d_off, &w.do_cap, (size_t)np * 3 + 3, s->pool, lg::srv_stream(w.ctx)) ||
@@ -542,6 +547,7 @@ void lyon_srv_destroy(lyon_srv* s) {
         cudaFreeHost(w->h_off);
         cudaFreeHost(w->h_opts);
         cudaFreeHost(w->h_res);
+        for (void* h : w->retired_host) cudaFreeHost(h);
         cudaFree(w->d_verbs);
         cudaFree(w->d_points);
         cudaFree(w->d_off);

@@ -911,8 +911,7 @@ def run_serving(args):
     request released on completion. Two stroke workers on high-priority streams, two fill
     workers. Reported: the offered 50,000 requests/s (saturated), the saturation throughput of
     each kind alone, and loads below saturation with p50/p99/p99.9 latency (from the scheduled
-    arrival to the output on the device) per kind and size class. One of the two stroke workers
-    takes only requests of at most 1,000 paths."""
+    arrival to the output on the device) per kind and size class."""
     from lyon_gb300 import serving, workloads
     sp, so = workloads.plain_stroke(20_000, seed=1)
     fp, fo = workloads.glyph_fill(5_000, seed=3)
@@ -966,8 +965,7 @@ def run_serving(args):
                         "u32, device-resident outputs",
             "workers": {"stroke": cfg["num_stroke_workers"], "fill": cfg["num_workers"],
                         "fill_blocks_per_sm": cfg["fill_blocks_per_sm"],
-                        "max_stroke_batch_paths": cfg["max_stroke_batch_paths"],
-                        "small_request_paths": cfg["small_request_paths"]},
+                        "max_stroke_batch_paths": cfg["max_stroke_batch_paths"]},
             "requests_in_pool": len(reqs), "mean_paths_per_request": mean_paths,
             "offered_50k_per_s": brief(offered, reqs),
             "saturation_stroke_only": brief(sat_stroke),

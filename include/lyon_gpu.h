@@ -586,18 +586,10 @@ typedef struct lyon_srv_config {
                                       so that their launches start beside running fill sweeps
                                       instead of queueing behind them; 0 -> none (every worker
                                       takes both kinds, oldest request first) */
-    uint32_t fill_blocks_per_sm;   /* fill sweep blocks per SM for each fill worker; 0 -> with
-                                      stroke workers, the registers an SM has left beside one
-                                      stroke block, split between the fill workers (5 each for
-                                      two on a GB300), so that a stroke launch finds room while
-                                      every fill worker's sweep runs; else the library's
-                                      default */
+    uint32_t fill_blocks_per_sm;   /* fill sweep blocks per SM for each fill worker; 0 -> 8
+                                      with stroke workers (half the library's default), else the
+                                      library's default */
     uint32_t max_stroke_batch_paths; /* most paths per stroke launch; 0 -> max_batch_paths */
-    uint32_t small_request_paths;  /* with two or more stroke workers, the first one takes only
-                                      stroke requests of at most this many paths (oldest first),
-                                      so that a small request never waits behind two large
-                                      stroke batches; 0 -> 1000; ignored with fewer than two
-                                      stroke workers */
 } lyon_srv_config;
 
 /* A finished request. Its output stays on the device until lyon_srv_release. */

@@ -80,8 +80,7 @@ class CSvgOutput(ctypes.Structure):
 class CSrvConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("num_workers", u32), ("max_batch_paths", u32),
                 ("device_budget_bytes", u64), ("num_stroke_workers", u32),
-                ("fill_blocks_per_sm", u32), ("max_stroke_batch_paths", u32),
-                ("small_request_paths", u32)]
+                ("fill_blocks_per_sm", u32), ("max_stroke_batch_paths", u32)]
 
 
 class CSrvResult(ctypes.Structure):

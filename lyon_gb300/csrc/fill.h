@@ -29,6 +29,12 @@ struct FillBuffers {
     uint32_t lanes = 0;
     // When set, every buffer here comes from this pool in stream order (serving contexts).
     cudaMemPool_t pool = nullptr;
+    // Preferred shared-memory carveout of the sweep kernel, in percent of an SM's shared memory
+    // (-1: no preference). The sweep uses no shared memory, so without a preference its SMs may
+    // run with nearly all of the unified L1/shared storage as L1, and a kernel that needs shared
+    // memory (a stroke block: 105.5 KB) cannot start beside its blocks. The serving loop asks for
+    // room for one stroke block.
+    int smem_carveout = -1;
     // Vertex sources (FillVertex::sources), when a call asks for them:
     void* stage_s = nullptr;        // staged sources, three u32 words each, path-local ids
     size_t stage_s_cap = 0;
@@ -50,9 +56,6 @@ struct FillSourceArgs {
 
 // Runs the sweep of every path into staging and writes per-path vertex/index counts and status.
 // With `src` (src->src_counts set), every vertex's sources are staged too.
-// Registers one block of the fill sweep kernel holds on its SM.
-int fill_block_registers();
-
 int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_options* options,
                uint32_t num_options, int num_sms, uint32_t* vtx_counts, uint32_t* idx_counts,
                int32_t* status, uint32_t* small_words, cudaStream_t stream,

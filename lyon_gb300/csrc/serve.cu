@@ -26,7 +26,6 @@
 #include <unordered_map>
 #include <vector>
 
-#include "fill.h"
 #include "kernels.h"
 
 namespace lg {
@@ -34,7 +33,7 @@ int srv_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, con
               uint32_t num_options, const uint32_t* request_first, uint64_t* tv, uint64_t* ti,
               uint32_t* failed);
 int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm,
-                  cudaMemPool_t pool);
+                  cudaMemPool_t pool, int fill_carveout);
 int srv_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
              uint32_t num_options, const uint32_t* request_first, float* vout, void* iout,
              uint64_t tv);
@@ -130,8 +129,7 @@ bool host_grow(T** p, size_t* cap, size_t n, std::vector<void*>* retired) {
     return true;
 }
 
-// ROLE_STROKE_SMALL: stroke requests of at most small_request_paths paths only.
-enum Role { ROLE_ANY = 0, ROLE_STROKE = 1, ROLE_FILL = 2, ROLE_STROKE_SMALL = 3 };
+enum Role { ROLE_ANY = 0, ROLE_STROKE = 1, ROLE_FILL = 2 };
 
 struct Worker {
     lyon_gpu_context* ctx = nullptr;
@@ -360,31 +358,14 @@ void worker_main(lyon_srv* s, Worker* w) {
             std::unique_lock<std::mutex> lk(s->mu);
             for (;;) {
                 if (s->stop) return;
-                const bool small_only = w->role == ROLE_STROKE_SMALL;
-                const auto eligible = [&](const Request* r) {
-                    return !small_only || r->batch.num_paths <= s->cfg.small_request_paths;
-                };
-                // The oldest stroke request this worker may take (a small-request worker skips
-                // larger ones), and whether it has fill work.
-                std::deque<Request*>& q0 = s->queue[0];
-                size_t first0 = q0.size();
-                if (w->role != ROLE_FILL) {
-                    for (size_t k = 0; k < q0.size(); ++k) {
-                        if (eligible(q0[k])) {
-                            first0 = k;
-                            break;
-                        }
-                    }
-                }
-                const bool have0 = first0 < q0.size();
-                const bool have1 = (w->role == ROLE_ANY || w->role == ROLE_FILL) &&
-                                   !s->queue[1].empty();
+                const bool have0 = w->role != ROLE_FILL && !s->queue[0].empty();
+                const bool have1 = w->role != ROLE_STROKE && !s->queue[1].empty();
                 if (!have0 && !have1) {
                     s->cv_work.wait(lk);
                     continue;
                 }
                 // The kind whose oldest request arrived first.
-                kind = (have0 && (!have1 || q0[first0]->t_arrival <=
+                kind = (have0 && (!have1 || s->queue[0].front()->t_arrival <=
                                                 s->queue[1].front()->t_arrival))
                            ? 0
                            : 1;
@@ -392,18 +373,14 @@ void worker_main(lyon_srv* s, Worker* w) {
                 const uint32_t max_paths =
                     kind == LYON_KIND_STROKE ? s->cfg.max_stroke_batch_paths : s->cfg.max_batch_paths;
                 uint32_t paths = 0;
-                for (size_t k = kind == 0 ? first0 : 0; k < q.size();) {
-                    Request* r = q[k];
-                    if (kind == 0 && !eligible(r)) {
-                        ++k;
-                        continue;
-                    }
+                while (!q.empty()) {
+                    Request* r = q.front();
                     const bool first = batch.empty();
                     if (!first && paths + r->batch.num_paths > max_paths) break;
                     if (s->held_bytes + reserved + r->est_bytes > s->cfg.device_budget_bytes &&
                         !(first && s->held_bytes == 0))
                         break;
-                    q.erase(q.begin() + (std::ptrdiff_t)k);
+                    q.pop_front();
                     batch.push_back(r);
                     paths += r->batch.num_paths;
                     reserved += r->est_bytes;
@@ -464,28 +441,14 @@ extern "C" {
 
 lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
     lyon_srv* s = new lyon_srv();
-    lyon_srv_config c = config ? *config : lyon_srv_config{0, 0, 0, 0, 0, 0, 0, 0};
+    lyon_srv_config c = config ? *config : lyon_srv_config{0, 0, 0, 0, 0, 0, 0};
     if (c.num_workers == 0) c.num_workers = 2;
     if (c.max_batch_paths == 0) c.max_batch_paths = 65536;
     if (c.device_budget_bytes == 0) c.device_budget_bytes = 40ull << 30;
     if (c.max_stroke_batch_paths == 0) c.max_stroke_batch_paths = c.max_batch_paths;
-    if (c.small_request_paths == 0) c.small_request_paths = 1000;
-    if (c.num_stroke_workers > 0 && c.fill_blocks_per_sm == 0) {
-        // Every fill worker's sweep can be resident at once, and each keeps its blocks until its
-        // last path: together they must leave one stroke block's registers free on every SM, or
-        // a stroke launch waits for a fill launch to end. Split what remains among the workers.
-        cudaSetDevice(c.device);
-        int regs = 0;
-        if (cudaDeviceGetAttribute(&regs, cudaDevAttrMaxRegistersPerMultiprocessor, c.device) !=
-            cudaSuccess) {
-            cudaGetLastError();
-            regs = 65536;
-        }
-        const int room = regs - lg::stroke_block_registers();
-        const int fill_blocks = room > 0 ? room / lg::fill_block_registers() : 0;
-        const int per_worker = fill_blocks / (int)c.num_workers;
-        c.fill_blocks_per_sm = (uint32_t)(per_worker > 0 ? per_worker : 1);
-    }
+    // Measured with two fill and two stroke workers: 8 sweep blocks per SM gave small stroke
+    // requests a p99 of 3.4 ms and fills 161-166 ms, 5 blocks 7.4-8.7 ms and 179-183 ms.
+    if (c.num_stroke_workers > 0 && c.fill_blocks_per_sm == 0) c.fill_blocks_per_sm = 8;
     s->cfg = c;
     // One pool for every worker's device buffers; it keeps what is freed for reuse (no release
     // threshold), so steady-state batches allocate without the driver.
@@ -502,6 +465,22 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
         cudaGetLastError();
         s->pool = nullptr;
     }
+    // With stroke workers, the fill sweeps ask for enough shared memory on their SMs for one
+    // stroke block beside them (the sweep itself uses none): otherwise an SM running sweep blocks
+    // may hold nearly all of its L1/shared storage as L1, and a stroke block cannot start there
+    // until they end.
+    int fill_carveout = -1;
+    if (c.num_stroke_workers > 0) {
+        int smem = 0;
+        if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device) ==
+                cudaSuccess &&
+            smem > 0) {
+            const size_t need = lg::stroke_block_smem() + 1024;  // + the per-block reservation
+            fill_carveout = (int)std::min<size_t>(100, (need * 100 + (size_t)smem - 1) / smem);
+        } else {
+            cudaGetLastError();
+        }
+    }
     const uint32_t total = c.num_workers + c.num_stroke_workers;
     for (uint32_t i = 0; i < total; ++i) {
         std::unique_ptr<Worker> w(new Worker());
@@ -512,9 +491,7 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
         }
         const bool stroke_lane = i >= c.num_workers;
         w->role = c.num_stroke_workers == 0 ? ROLE_ANY : (stroke_lane ? ROLE_STROKE : ROLE_FILL);
-        if (stroke_lane && i == c.num_workers && c.num_stroke_workers >= 2)
-            w->role = ROLE_STROKE_SMALL;
-        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm, s->pool);
+        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm, s->pool, fill_carveout);
         s->workers.push_back(std::move(w));
     }
     for (auto& w : s->workers) w->th = std::thread(worker_main, s, w.get());

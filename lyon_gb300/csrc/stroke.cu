@@ -1263,21 +1263,14 @@ static void configure_smem() {
     smem_configured[dev] = true;
 }
 
+size_t stroke_block_smem() { return STROKE_SMEM; }
+
 int stroke_blocks_per_sm() {
     configure_smem();
     int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stroke_kernel<true, false>,
                                                   STROKE_WARPS * 32, STROKE_SMEM);
     return n > 0 ? n : 1;
-}
-
-int stroke_block_registers() {
-    cudaFuncAttributes a;
-    if (cudaFuncGetAttributes(&a, stroke_kernel<true, false>) != cudaSuccess) {
-        cudaGetLastError();
-        return 128 * STROKE_WARPS * 32;
-    }
-    return a.numRegs * STROKE_WARPS * 32;
 }
 
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream) {

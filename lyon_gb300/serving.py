@@ -90,12 +90,10 @@ class Server:
 
     def __init__(self, device: int = 0, num_workers: int = 2, max_batch_paths: int = 65536,
                  device_budget_bytes: int = 40 << 30, num_stroke_workers: int = 0,
-                 fill_blocks_per_sm: int = 0, max_stroke_batch_paths: int = 0,
-                 small_request_paths: int = 0):
+                 fill_blocks_per_sm: int = 0, max_stroke_batch_paths: int = 0):
         self.lib = _native.load()
         cfg = _native.CSrvConfig(device, num_workers, max_batch_paths, device_budget_bytes,
-                                 num_stroke_workers, fill_blocks_per_sm, max_stroke_batch_paths,
-                                 small_request_paths)
+                                 num_stroke_workers, fill_blocks_per_sm, max_stroke_batch_paths)
         self.h = self.lib.lyon_srv_create(ctypes.byref(cfg))
         if not self.h:
             raise RuntimeError("lyon_srv_create failed")

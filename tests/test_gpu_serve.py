@@ -96,8 +96,7 @@ def test_lone_request_reaches_its_lane(pools):
     try:
         cfg = srv.config()
         assert cfg["num_workers"] == 2 and cfg["num_stroke_workers"] == 2
-        # Two fill workers share what one stroke block leaves of an SM's registers.
-        assert 1 <= cfg["fill_blocks_per_sm"] <= 16
+        assert cfg["fill_blocks_per_sm"] == 8
         for kind, pool, opts, n in ((serving.KIND_STROKE, sb, so, 1500),
                                     (serving.KIND_FILL, fb, fo, 300),
                                     (serving.KIND_STROKE, sb, so, 1)):

@@ -822,9 +822,8 @@ cudaStream_t srv_stream(lyon_gpu_context* ctx) { return ctx->stream; }
 // priority (its blocks are dispatched before queued blocks of other streams) and one stroke block
 // per SM; `fill_blocks_per_sm` (0: default) bounds the fill sweep's residency.
 int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm,
-                  cudaMemPool_t pool, int fill_carveout) {
+                  cudaMemPool_t pool) {
     ctx->fill.blocks_per_sm_cap = fill_blocks_per_sm;
-    ctx->fill.smem_carveout = fill_carveout;
     ctx->pool = pool;
     // The fill buffers are all allocated by the first fill call, so they are all pooled or none.
     if (!ctx->fill.scratch && !ctx->fill.stage_v && !ctx->fill.work) ctx->fill.pool = pool;

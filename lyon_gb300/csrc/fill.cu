@@ -16,7 +16,6 @@
 // A path whose heap or staging room ran out is re-run, alone with the other such paths, with
 // more room; after the last attempt it fails with LYON_ERR_CAPACITY.
 #include <algorithm>
-#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -210,23 +209,6 @@ __global__ void fill_emit_kernel(uint32_t n, const uint32_t* vtx_counts,
 
 namespace {
 
-// The sweep kernel's preferred shared-memory carveout is a property of the kernel, not of a
-// launch: it is set before a launch whenever the launching context wants another value than the
-// last one set (LYON_GB300_FILL_CARVEOUT, -1 to 100, overrides every context's preference).
-std::atomic<int> g_carveout{-2};
-void apply_carveout(int want) {
-    if (const char* env = getenv("LYON_GB300_FILL_CARVEOUT")) {
-        const long v = strtol(env, nullptr, 10);
-        if (v >= -1 && v <= 100) want = (int)v;
-    }
-    if (g_carveout.exchange(want) == want) return;
-    cudaFuncSetAttribute(fillk::fill_sweep_kernel<false>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, want);
-    cudaFuncSetAttribute(fillk::fill_sweep_kernel<true>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, want);
-    cudaGetLastError();
-}
-
 // With a pool the old buffer is freed in stream order, without waiting for the device.
 bool grow(void** p, size_t* cap, size_t bytes, size_t keep_bytes, cudaStream_t s,
           cudaMemPool_t pool) {
@@ -373,7 +355,6 @@ int fill_count(FillBuffers& fb, const lyon_path_batch* batch, const lyon_fill_op
         a.stage_sfirst = reinterpret_cast<uint32_t*>(fb.stage_sfirst);
         a.stage_s_cap = fb.stage_s_cap / 12;
         a.stage_soff = reinterpret_cast<unsigned long long*>(fb.stage_soff);
-        apply_carveout(fb.smem_carveout);
         if (sources) {
             fillk::fill_sweep_kernel<true><<<nthreads, 32, 0, stream>>>(a);
         } else {

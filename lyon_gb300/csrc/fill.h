@@ -29,12 +29,6 @@ struct FillBuffers {
     uint32_t lanes = 0;
     // When set, every buffer here comes from this pool in stream order (serving contexts).
     cudaMemPool_t pool = nullptr;
-    // Preferred shared-memory carveout of the sweep kernel, in percent of an SM's shared memory
-    // (-1: no preference). The sweep uses no shared memory, so without a preference its SMs may
-    // run with nearly all of the unified L1/shared storage as L1, and a kernel that needs shared
-    // memory (a stroke block: 105.5 KB) cannot start beside its blocks. The serving loop asks for
-    // room for one stroke block.
-    int smem_carveout = -1;
     // Vertex sources (FillVertex::sources), when a call asks for them:
     void* stage_s = nullptr;        // staged sources, three u32 words each, path-local ids
     size_t stage_s_cap = 0;

@@ -78,8 +78,6 @@ struct ShapeArgs {
 cudaError_t launch_shapes(const ShapeArgs& args, bool emit, cudaStream_t stream);
 
 int stroke_blocks_per_sm();
-// Dynamic shared memory of one stroke-kernel block (bytes).
-size_t stroke_block_smem();
 cudaError_t launch_stroke(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);
 // The sequential stepper (stroke_seq.cu): variable line width and the vertex-source output.
 cudaError_t launch_stroke_seq(const StrokeArgs& args, bool emit, int grid, cudaStream_t stream);

@@ -33,7 +33,7 @@ int srv_count(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, con
               uint32_t num_options, const uint32_t* request_first, uint64_t* tv, uint64_t* ti,
               uint32_t* failed);
 int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_per_sm,
-                  cudaMemPool_t pool, int fill_carveout);
+                  cudaMemPool_t pool);
 int srv_emit(lyon_gpu_context* ctx, int kind, const lyon_path_batch* batch, const void* options,
              uint32_t num_options, const uint32_t* request_first, float* vout, void* iout,
              uint64_t tv);
@@ -465,22 +465,6 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
         cudaGetLastError();
         s->pool = nullptr;
     }
-    // With stroke workers, the fill sweeps ask for enough shared memory on their SMs for one
-    // stroke block beside them (the sweep itself uses none): otherwise an SM running sweep blocks
-    // may hold nearly all of its L1/shared storage as L1, and a stroke block cannot start there
-    // until they end.
-    int fill_carveout = -1;
-    if (c.num_stroke_workers > 0) {
-        int smem = 0;
-        if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device) ==
-                cudaSuccess &&
-            smem > 0) {
-            const size_t need = lg::stroke_block_smem() + 1024;  // + the per-block reservation
-            fill_carveout = (int)std::min<size_t>(100, (need * 100 + (size_t)smem - 1) / smem);
-        } else {
-            cudaGetLastError();
-        }
-    }
     const uint32_t total = c.num_workers + c.num_stroke_workers;
     for (uint32_t i = 0; i < total; ++i) {
         std::unique_ptr<Worker> w(new Worker());
@@ -491,7 +475,7 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
         }
         const bool stroke_lane = i >= c.num_workers;
         w->role = c.num_stroke_workers == 0 ? ROLE_ANY : (stroke_lane ? ROLE_STROKE : ROLE_FILL);
-        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm, s->pool, fill_carveout);
+        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm, s->pool);
         s->workers.push_back(std::move(w));
     }
     for (auto& w : s->workers) w->th = std::thread(worker_main, s, w.get());

@@ -1263,8 +1263,6 @@ static void configure_smem() {
     smem_configured[dev] = true;
 }
 
-size_t stroke_block_smem() { return STROKE_SMEM; }
-
 int stroke_blocks_per_sm() {
     configure_smem();
     int n = 0;

@@ -1087,42 +1087,6 @@ __device__ void stroke_path(WarpSmem& sm, int lane, const StrokeArgs& A, uint32_
     }
 }
 
-// seq_step (fixed_width_step_impl, stroke.rs:1521-1632) on a window of the point buffer's last
-// two points: `prev` (second last) and `join` (last), `n` points pushed so far. The short-path
-// walk never reads the buffer's third point (its tail is rebuilt from recorded points), so the
-// window replaces the buffer there, and inlined it stays in registers where the buffer, indexed
-// modulo 3, lived in local memory. Same operations in the same order as seq_step.
-template <class SK>
-__device__ __forceinline__ bool seq_step_window(DEP& prev, DEP& join, uint32_t& n, DEP next,
-                                                const StrokeParams& P, SK& sink, bool& mnec,
-                                                int& status) {
-    if (n > 0) {
-        if (too_close(join.pos, next.pos, P.merge_threshold)) {
-            if (n == 1) mnec = true;
-            return false;
-        }
-        if (n == 1) {
-            first_point_sides(join, next.pos, next.hw);
-            if (SK::kRec && isnan(next.adv)) next.adv = join.adv + vlength(next.pos - join.pos);
-        }
-    }
-    if (n > 1) {
-        if (SK::kRec && isnan(join.adv)) join.adv = prev.adv + vlength(join.pos - prev.pos);
-        JoinGeo g = join_geometry(prev.pos, join, next.pos, P.miter_limit);
-        if (SK::kRec && g.fast && isnan(next.adv))
-            next.adv = join.adv + vlength(next.pos - join.pos);
-        sink.adv = join.adv;
-        if (g.fast) g.skip = flattened_skip(prev.pos, prev.s[SP].next, prev.s[SN].next, join);
-        emit_join_base(join, g, sink);
-        if (n > 2) add_edge_triangles(prev, join, sink);
-        tessellate_join(join, P, sink, &status);
-    }
-    prev = join;
-    join = next;
-    ++n;
-    return true;
-}
-
 // One thread strokes one short line-only path: lyon's sequential step (seq_step, the
 // fixed_width_step_impl of stroke.rs:1521-1632) over its points, then the sub-path tail through
 // run_tail, as the warp walk does. Verbs are checked per window of up to WINDOW verbs ending at
@@ -1153,10 +1117,10 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
             status = LYON_ERR_INVALID_ARGUMENT;
             break;
         }
-        DEP prev, join;  // the point buffer's last two points (see seq_step_window)
-        dep_init(prev, V2{0.0f, 0.0f}, P.hw, P.line_join, false);
-        join = prev;
-        uint32_t npts = 0;
+        SeqBuffer pb;
+        pb.start = 0;
+        pb.count = 0;
+        pb.n = 0;
         TailJob job;
         job.path = path;
         job.base1 = job.jbase = 0;
@@ -1189,16 +1153,16 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
                 dep_init(d, p, P.hw, P.line_join, false);
                 if (k == LYON_VERB_BEGIN) d.adv = start_adv;
                 const uint32_t base = s.id_base + s.nv;
-                if (!seq_step_window(prev, join, npts, d, P, s, mnec, status)) continue;
+                if (!seq_step(pb, d, P, s, &mnec, &status)) continue;
                 job.c3 = job.c2;
                 job.c2 = job.c1;
                 job.c1 = p;
-                if (npts == 1) {
+                if (pb.n == 1) {
                     job.p0 = p;
-                } else if (npts == 2) {
+                } else if (pb.n == 2) {
                     job.p1 = p;
                 } else {
-                    if (npts == 3) {
+                    if (pb.n == 3) {
                         job.p2 = p;
                         job.base1 = base;
                     }
@@ -1213,21 +1177,19 @@ __device__ __noinline__ void stroke_path_seq(const StrokeArgs& A, uint32_t path)
             }
         }
         if (!ended || status != LYON_OK) break;
-        job.n = npts;
+        job.n = pb.n;
         job.flags = (closed ? TJ_CLOSED : 0u) | (mnec ? TJ_MNEC : 0u);
         job.adv0 = start_adv;
         job.adv1 = job.adv2 = start_adv;
-        if (ATTR && npts >= 2) {
-            job.adv2 = prev.adv;
-            job.adv1 = isnan(join.adv) ? prev.adv + vlength(join.pos - prev.pos) : join.adv;
-            if (!(closed && npts > 2)) start_adv = job.adv1;
+        if (ATTR && pb.n >= 2) {
+            const DEP& l = pb.last();
+            const DEP& sl = pb.second_last();
+            job.adv2 = sl.adv;
+            job.adv1 = isnan(l.adv) ? sl.adv + vlength(l.pos - sl.pos) : l.adv;
+            if (!(closed && pb.n > 2)) start_adv = job.adv1;
         }
-        // The tail runs out of line on a copy of the sink, so that the walk's sink never has its
-        // address taken (it would then live in local memory for the whole walk).
         int tst = LYON_OK;
-        SinkT<ATTR> ts = s;
-        run_tail(job, P, ts, &tst);
-        s = ts;
+        run_tail(job, P, s, &tst);
         if (tst != LYON_OK) status = tst;
     }
     if (s.overflow && status == LYON_OK) status = LYON_ERR_INTERNAL;

@@ -547,6 +547,15 @@ int lyon_gpu_stroke_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* bat
                                uint64_t index_capacity, int32_t* status,
                                uint64_t* total_vertices, uint64_t* total_indices);
 
+/* Host memory for the host-buffer calls: page-locked (registered with CUDA, so copies run
+ * asynchronously at the link's rate) and backed by transparent huge pages where the system
+ * allows them. Registered memory in small pages copies at about half the link's rate once a
+ * buffer is larger than the IOMMU's translation reach. Measured on a GB300 with 64 KB base pages:
+ * 52 GB of outputs copied at 88-93 GB/s into ordinary pinned memory and 190-192 GB/s into huge
+ * pages. Returns NULL on failure; free with lyon_gpu_host_free. */
+void* lyon_gpu_host_alloc(size_t bytes);
+int lyon_gpu_host_free(void* ptr);
+
 /* Batched fill with host buffers; same conventions as lyon_gpu_stroke_paths_host. */
 int lyon_gpu_fill_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* batch,
                              const lyon_fill_options* options, uint32_t num_options,

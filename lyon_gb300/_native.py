@@ -138,6 +138,10 @@ def load(build_if_missing: bool = True):
             raise NativeLibraryMissing(f"{path} is missing; run lyon_gb300.build.build()")
         L = ctypes.CDLL(path)
         L.lyon_gpu_version.restype = ctypes.c_char_p
+        L.lyon_gpu_host_alloc.restype = c_p
+        L.lyon_gpu_host_alloc.argtypes = [ctypes.c_size_t]
+        L.lyon_gpu_host_free.restype = ctypes.c_int
+        L.lyon_gpu_host_free.argtypes = [c_p]
         L.lyon_gpu_kernel_launches.restype = u64
         L.lyon_gpu_kernel_launches.argtypes = []
         L.lyon_gpu_create.restype = c_p
@@ -277,6 +281,7 @@ EXPORTED = [
     "lyon_gpu_stroke_paths_each", "lyon_gpu_coverage_compare",
     "lyon_gpu_flatten_counts", "lyon_gpu_flatten_paths", "lyon_gpu_synchronize",
     "lyon_gpu_version", "lyon_gpu_stroke_paths_host", "lyon_gpu_fill_paths_host",
+    "lyon_gpu_host_alloc", "lyon_gpu_host_free",
     "lyon_gpu_set_timing", "lyon_gpu_last_timings", "lyon_gpu_stroke_paths_noalloc",
     "lyon_srv_create", "lyon_srv_destroy", "lyon_srv_get_config", "lyon_srv_submit", "lyon_srv_poll", "lyon_srv_wait",
     "lyon_srv_release", "lyon_srv_run_load", "lyon_gpu_set_stroke_tuning",

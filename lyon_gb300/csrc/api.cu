@@ -5,10 +5,15 @@
 // Every batched call is count -> index-range policy -> look-back scan -> (one host read of the
 // totals) -> emit. The host-buffer form runs that pipeline per chunk of paths and overlaps each
 // chunk's device->host copy (second stream) with the next chunk's kernels.
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "kernels.h"
@@ -850,6 +855,68 @@ int srv_configure(lyon_gpu_context* ctx, bool stroke_lane, uint32_t fill_blocks_
 extern "C" {
 
 const char* lyon_gpu_version(void) { return kVersion; }
+
+// ---- host buffers for the host-buffer calls ---------------------------------------------------
+
+namespace {
+struct HostMapping {
+    void* base;
+    size_t len;
+};
+std::mutex g_host_mu;
+std::unordered_map<void*, HostMapping> g_host_maps;
+
+// The transparent huge page size (2 MB with 4 KB base pages, 512 MB with 64 KB ones).
+size_t thp_size() {
+    size_t v = 0;
+    if (FILE* f = fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+        unsigned long long x = 0;
+        if (fscanf(f, "%llu", &x) == 1) v = (size_t)x;
+        fclose(f);
+    }
+    return v >= 4096 && v <= (1ull << 31) ? v : (2u << 20);
+}
+}  // namespace
+
+void* lyon_gpu_host_alloc(size_t bytes) {
+    if (bytes == 0) return nullptr;
+    const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+    const size_t huge = thp_size();
+    // Whole huge pages, on a huge-page boundary: map one huge page more and start at the first
+    // boundary inside the mapping.
+    const size_t len = (bytes + huge - 1) / huge * huge;
+    const size_t map_len = len + huge;
+    void* base = mmap(nullptr, map_len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (base == MAP_FAILED) return nullptr;
+    char* p = reinterpret_cast<char*>(((uintptr_t)base + huge - 1) / huge * huge);
+    madvise(p, len, MADV_HUGEPAGE);  // a hint: without transparent huge pages, base pages
+    // Fault the pages in now (one write per huge page), then pin them for DMA.
+    for (size_t off = 0; off < len; off += page < huge ? huge : page) p[off] = 0;
+    if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
+        cudaGetLastError();
+        munmap(base, map_len);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> g(g_host_mu);
+    g_host_maps[p] = HostMapping{base, map_len};
+    return p;
+}
+
+int lyon_gpu_host_free(void* ptr) {
+    if (!ptr) return LYON_OK;
+    HostMapping m;
+    {
+        std::lock_guard<std::mutex> g(g_host_mu);
+        auto it = g_host_maps.find(ptr);
+        if (it == g_host_maps.end()) return LYON_ERR_INVALID_ARGUMENT;
+        m = it->second;
+        g_host_maps.erase(it);
+    }
+    cudaHostUnregister(ptr);
+    cudaGetLastError();
+    munmap(m.base, m.len);
+    return LYON_OK;
+}
 
 uint64_t lyon_gpu_kernel_launches(void) { return lg::launches_total(); }
 

@@ -157,6 +157,38 @@ class Context:
         return int(self.lib.lyon_gpu_stream(self.h) or 0)
 
 
+class HostBuffer:
+    """Page-locked host memory backed by huge pages (lyon_gpu_host_alloc), for the host-buffer
+    calls' inputs and outputs: large outputs copy out at the link's rate into it, about twice
+    the rate into ordinary pinned memory on a GB300. `array(dtype, count)` views it as numpy."""
+
+    def __init__(self, nbytes: int):
+        self.lib = _native.load()
+        self.nbytes = int(nbytes)
+        self.ptr = self.lib.lyon_gpu_host_alloc(max(self.nbytes, 1))
+        if not self.ptr:
+            raise MemoryError(f"lyon_gpu_host_alloc({self.nbytes}) failed")
+
+    def array(self, dtype, count: Optional[int] = None) -> np.ndarray:
+        dtype = np.dtype(dtype)
+        n = self.nbytes // dtype.itemsize if count is None else int(count)
+        if n * dtype.itemsize > self.nbytes:
+            raise ValueError("view larger than the buffer")
+        raw = (ctypes.c_char * (n * dtype.itemsize)).from_address(self.ptr)
+        return np.frombuffer(raw, dtype=dtype, count=n)
+
+    def close(self) -> None:
+        if self.ptr:
+            self.lib.lyon_gpu_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
 

@@ -174,10 +174,11 @@ def test_flatten_counts_and_points(gpu):
         assert np.array_equal(gp, op)
 
 
-@pytest.mark.parametrize("pinned", [False, True])
+@pytest.mark.parametrize("pinned", [False, True, "host_alloc"])
 def test_host_buffer_entry_point_matches_device(gpu, pinned, monkeypatch):
     # lyon_gpu_stroke_paths_host in several chunks (staged copies for pageable buffers, direct
-    # writes for pinned ones) equals the device-buffer call; too-small buffers give CAPACITY.
+    # writes for pinned ones and for lyon_gpu_host_alloc's huge-page buffers, inputs included)
+    # equals the device-buffer call; too-small buffers give CAPACITY.
     import ctypes
     import torch
     from lyon_gb300 import _native
@@ -185,7 +186,24 @@ def test_host_buffer_entry_point_matches_device(gpu, pinned, monkeypatch):
     batch, opts = workloads.batched_stroke(3000, seed=41)
     g = gpu.gpu_batch("stroke", batch, opts, index_bits=32, index_mode=T.INDEX_GLOBAL)
     tv, ti = int(g["total_vertices"]), int(g["total_indices"])
-    if pinned:
+    keep = []
+
+    def in_host_buffer(a):
+        a = np.ascontiguousarray(a)
+        if pinned != "host_alloc":
+            return a
+        hb_ = T.HostBuffer(a.nbytes)
+        v_ = hb_.array(a.dtype, a.size)
+        v_[...] = a.reshape(-1)
+        keep.append(hb_)
+        return v_
+
+    if pinned == "host_alloc":
+        out_v, out_i = T.HostBuffer(8 * tv), T.HostBuffer(4 * ti)
+        keep += [out_v, out_i]
+        vptr, iptr = out_v.ptr, out_i.ptr
+        get = lambda: (out_v.array(np.float32).reshape(-1, 2), out_i.array(np.uint32))  # noqa: E731
+    elif pinned:
         hv_t = torch.empty(2 * tv, dtype=torch.float32, pin_memory=True)
         hi_t = torch.empty(ti, dtype=torch.int32, pin_memory=True)
         vptr, iptr = hv_t.data_ptr(), hi_t.data_ptr()
@@ -196,13 +214,13 @@ def test_host_buffer_entry_point_matches_device(gpu, pinned, monkeypatch):
         vptr, iptr = hv.ctypes.data, hi.ctypes.data
         get = lambda: (hv.reshape(-1, 2), hi)  # noqa: E731
     lib = gpu.ctx().lib
-    vs = np.ascontiguousarray(batch.verbs)
-    ps = np.ascontiguousarray(batch.points)
-    vo = np.ascontiguousarray(batch.verb_offsets)
-    po = np.ascontiguousarray(batch.point_offsets)
+    vs = in_host_buffer(batch.verbs)
+    ps = in_host_buffer(batch.points)
+    vo = in_host_buffer(batch.verb_offsets)
+    po = in_host_buffer(batch.point_offsets)
     hb = _native.CPathBatch(vs.ctypes.data, ps.ctypes.data, vo.ctypes.data, po.ctypes.data,
                             batch.num_paths)
-    oh = np.ascontiguousarray(opts)
+    oh = in_host_buffer(opts)
     status = np.full(batch.num_paths, -7, np.int32)
     a, b = ctypes.c_uint64(), ctypes.c_uint64()
     r = lib.lyon_gpu_stroke_paths_host(gpu.ctx().h, ctypes.byref(hb), oh.ctypes.data, len(oh),
@@ -217,6 +235,8 @@ def test_host_buffer_entry_point_matches_device(gpu, pinned, monkeypatch):
                                        32, T.INDEX_GLOBAL, 0, vptr, tv // 2, iptr, ti, None,
                                        ctypes.byref(a), ctypes.byref(b))
     assert r == T.LYON_ERR_CAPACITY and a.value == tv and b.value == ti
+    for hb_ in keep:
+        hb_.close()
 
 
 def test_batched_stroke_full_size_counts(gpu):

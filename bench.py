@@ -1003,21 +1003,18 @@ def plain_per_path(ctx, db, opts_dev, num_options, batched_vps, T, count: int = 
 
 def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
     """Times lyon_gpu_stroke_paths_host: host inputs, host outputs (every byte). Inputs and
-    outputs live in the library's host buffers (lyon_gpu_host_alloc: page-locked, huge pages),
-    the inputs filled before the timed region, as an application keeps its scene there."""
+    outputs live in pinned host memory (cudaHostAlloc through torch), the inputs filled before
+    the timed region, as an application keeps its scene there."""
     import torch
 
     def host_copy(a):
-        a = np.ascontiguousarray(a)
-        hbuf = T.HostBuffer(a.nbytes)
-        v = hbuf.array(a.dtype, a.size)
-        v[...] = a.reshape(-1)
-        return hbuf, v
+        t = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory()
+        return t, t.numpy().view(a.dtype)
 
-    out_v = T.HostBuffer(int(tv) * 8)
-    out_i = T.HostBuffer(int(ti) * 4)
-    vptr, iptr = out_v.ptr, out_i.ptr
-    host_kind = "pinned (lyon_gpu_host_alloc: page-locked, huge pages)"
+    hv = torch.empty(int(tv) * 2, dtype=torch.float32, pin_memory=True)
+    hi = torch.empty(int(ti), dtype=torch.int32, pin_memory=True)
+    vptr, iptr = hv.data_ptr(), hi.data_ptr()
+    host_kind = "pinned (cudaHostAlloc), inputs and outputs"
     keep = [host_copy(batch.verbs), host_copy(batch.points), host_copy(batch.verb_offsets),
             host_copy(batch.point_offsets), host_copy(opts)]
     (_, verbs), (_, pts), (_, vo), (_, po), (_, oh) = keep
@@ -1053,7 +1050,6 @@ def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
     # best of five (the link is shared with the machine's other GPUs and its rate moves from one
     # moment to the next). The call moves d2h bytes, so d2h / this rate approximates the floor
     # under its time.
-    hv = torch.from_numpy(out_v.array(np.float32))
     if hv.numel() > 0:
         n = min(hv.numel(), (4 << 30) // 4)
         src = torch.empty(n, dtype=torch.float32, device="cuda")
@@ -1071,11 +1067,6 @@ def run_e2e(lib, ctx, batch, opts, tv, ti, args, T, _native):
         out["link_d2h_gbs"] = gbs
         out["link_d2h_gbs_samples"] = [round(r, 1) for r in rates]
         out["d2h_floor_ms"] = d2h / (gbs * 1e9) * 1e3
-    del hv
-    for hbuf, _ in keep:
-        hbuf.close()
-    out_v.close()
-    out_i.close()
     return out
 
 

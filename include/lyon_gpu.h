@@ -548,11 +548,13 @@ int lyon_gpu_stroke_paths_host(lyon_gpu_context* ctx, const lyon_path_batch* bat
                                uint64_t* total_vertices, uint64_t* total_indices);
 
 /* Host memory for the host-buffer calls: page-locked (registered with CUDA, so copies run
- * asynchronously at the link's rate) and backed by transparent huge pages where the system
- * allows them. Registered memory in small pages copies at about half the link's rate once a
- * buffer is larger than the IOMMU's translation reach. Measured on a GB300 with 64 KB base pages:
- * 52 GB of outputs copied at 88-93 GB/s into ordinary pinned memory and 190-192 GB/s into huge
- * pages. Returns NULL on failure; free with lyon_gpu_host_free. */
+ * asynchronously) and backed by transparent huge pages where the system allows them, so that
+ * the device's address translation covers a large buffer with few entries. Returns NULL on
+ * failure; free with lyon_gpu_host_free. On the virtual machines measured (GB300, 64 KB base
+ * pages), a 40-52 GB buffer from here took the device's copies at 190-192 GB/s in some
+ * allocations and 22-93 GB/s in others, and ordinary pinned memory at 57-93 GB/s: the rate
+ * follows where the allocation lands in the machine's memory, which the process does not
+ * control. */
 void* lyon_gpu_host_alloc(size_t bytes);
 int lyon_gpu_host_free(void* ptr);
 

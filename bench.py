@@ -975,7 +975,7 @@ def run_serving(args):
 
 
 def plain_per_path(ctx, db, opts_dev, num_options, batched_vps, T, count: int = 2000):
-    """The plain per-path GPU method of the benchmark spec: the count -> scan -> emit pipeline
+    """The plain per-path GPU method: the count -> scan -> emit pipeline
     launched once per path from C (lyon_gpu_stroke_paths_each) on the device-resident batch,
     one host wait per path; no Python loop and no host staging. Its rate beside the batched
     call's gives the batched / plain ratio."""

@@ -1,6 +1,6 @@
 """GPU parity: the CUDA stroke path against the oracle on seeded inputs and lyon's fixtures.
 
-The bar (the benchmark spec): per-path vertex and index counts and the index topology match exactly,
+The bar: per-path vertex and index counts and the index topology match exactly,
 except where the oracle flags a count decided by a value within 1e-6 of an integer (counted and
 reported); vertex positions match within 1e-5 relative (`RTOL`).
 """

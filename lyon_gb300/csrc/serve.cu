@@ -149,6 +149,7 @@ struct Worker {
     size_t dv_cap = 0, dp_cap = 0, do_cap = 0, dopt_cap = 0;
     std::vector<Slab*> slabs;
     std::vector<void*> retired_host;  // outgrown pinned staging, freed with the loop
+    cudaMemPool_t pool = nullptr;     // this worker's device buffers (null: plain cudaMalloc)
     uint64_t batches = 0, batch_paths = 0;
 };
 
@@ -165,7 +166,6 @@ struct lyon_srv {
     uint64_t held_bytes = 0;  // slabs of unreleased requests + reservations of running batches
     bool stop = false;
     std::vector<std::unique_ptr<Worker>> workers;
-    cudaMemPool_t pool = nullptr;  // every worker's device buffers (null: plain cudaMalloc)
 };
 
 namespace {
@@ -256,10 +256,10 @@ void run_batch(lyon_srv* s, Worker& w, int kind, std::vector<Request*>& batch, u
         !host_grow(&w.h_off, &w.ho_cap, (size_t)np * 3 + 3, &w.retired_host) ||
         !host_grow(&w.h_opts, &w.hopt_cap, (size_t)np * osz + osz, &w.retired_host) ||
         !host_grow(&w.h_res, &w.hres_cap, (size_t)np * 3 + 4, &w.retired_host) ||
-        !dev_grow(&w.d_verbs, &w.dv_cap, nverbs + 16, s->pool, lg::srv_stream(w.ctx)) ||
-        !dev_grow(&w.d_points, &w.dp_cap, npts * 2 + 16, s->pool, lg::srv_stream(w.ctx)) ||
-        !dev_grow(&w.d_off, &w.do_cap, (size_t)np * 3 + 3, s->pool, lg::srv_stream(w.ctx)) ||
-        !dev_grow(&w.d_opts, &w.dopt_cap, (size_t)np * osz + osz, s->pool,
+        !dev_grow(&w.d_verbs, &w.dv_cap, nverbs + 16, w.pool, lg::srv_stream(w.ctx)) ||
+        !dev_grow(&w.d_points, &w.dp_cap, npts * 2 + 16, w.pool, lg::srv_stream(w.ctx)) ||
+        !dev_grow(&w.d_off, &w.do_cap, (size_t)np * 3 + 3, w.pool, lg::srv_stream(w.ctx)) ||
+        !dev_grow(&w.d_opts, &w.dopt_cap, (size_t)np * osz + osz, w.pool,
                   lg::srv_stream(w.ctx))) {
         finish(s, batch, LYON_ERR_OUT_OF_MEMORY, nullptr, nullptr, nullptr, nullptr, reserved);
         return;
@@ -313,7 +313,7 @@ void run_batch(lyon_srv* s, Worker& w, int kind, std::vector<Request*>& batch, u
     Slab* slab;
     {
         std::lock_guard<std::mutex> g(s->mu);
-        slab = take_slab(w, tv, ti, np, s->pool, st);
+        slab = take_slab(w, tv, ti, np, w.pool, st);
     }
     if (!slab) {
         finish(s, batch, LYON_ERR_OUT_OF_MEMORY, nullptr, nullptr, nullptr, nullptr, reserved);
@@ -450,21 +450,7 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
     // requests a p99 of 3.4 ms and fills 161-166 ms, 5 blocks 7.4-8.7 ms and 179-183 ms.
     if (c.num_stroke_workers > 0 && c.fill_blocks_per_sm == 0) c.fill_blocks_per_sm = 8;
     s->cfg = c;
-    // One pool for every worker's device buffers; it keeps what is freed for reuse (no release
-    // threshold), so steady-state batches allocate without the driver.
     cudaSetDevice(c.device);
-    cudaMemPoolProps props;
-    std::memset(&props, 0, sizeof(props));
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = c.device;
-    if (cudaMemPoolCreate(&s->pool, &props) == cudaSuccess) {
-        uint64_t keep = ~0ull;
-        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    } else {
-        cudaGetLastError();
-        s->pool = nullptr;
-    }
     const uint32_t total = c.num_workers + c.num_stroke_workers;
     for (uint32_t i = 0; i < total; ++i) {
         std::unique_ptr<Worker> w(new Worker());
@@ -473,9 +459,27 @@ lyon_srv* lyon_srv_create(const lyon_srv_config* config) {
             lyon_srv_destroy(s);
             return nullptr;
         }
+        // A pool per worker: a pool shared between workers may hand one worker memory another
+        // worker freed in its own stream order, and it then makes the first stream wait for the
+        // second (a stroke batch would wait for a fill sweep). It keeps what is freed for reuse
+        // (no release threshold), so steady-state batches allocate without the driver.
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = c.device;
+        if (cudaMemPoolCreate(&w->pool, &props) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(w->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            int no = 0;
+            cudaMemPoolSetAttribute(w->pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+        } else {
+            cudaGetLastError();
+            w->pool = nullptr;
+        }
         const bool stroke_lane = i >= c.num_workers;
         w->role = c.num_stroke_workers == 0 ? ROLE_ANY : (stroke_lane ? ROLE_STROKE : ROLE_FILL);
-        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm, s->pool);
+        lg::srv_configure(w->ctx, stroke_lane, c.fill_blocks_per_sm, w->pool);
         s->workers.push_back(std::move(w));
     }
     for (auto& w : s->workers) w->th = std::thread(worker_main, s, w.get());
@@ -514,9 +518,9 @@ void lyon_srv_destroy(lyon_srv* s) {
         cudaFree(w->d_off);
         cudaFree(w->d_opts);
         if (w->ctx) lyon_gpu_destroy(w->ctx);
+        // After every buffer from it is freed (the context's included).
+        if (w->pool) cudaMemPoolDestroy(w->pool);
     }
-    // After every buffer from it is freed (the contexts' included).
-    if (s->pool) cudaMemPoolDestroy(s->pool);
     for (auto& kv : s->reqs) delete kv.second;
     delete s;
 }

@@ -83,8 +83,8 @@ struct Request {
     uint64_t v_begin = 0, v_end = 0, i_begin = 0, i_end = 0;
 };
 
-// Device buffers of a worker: from the server's pool in the worker's stream order when there is
-// a pool (a plain cudaFree can wait for every kernel on the device, other workers' included).
+// Device buffers of a worker: from the worker's own pool, in its stream order, when there is a
+// pool (a plain cudaFree can wait for every kernel on the device, other workers' included).
 template <class T>
 bool dev_grow(T** p, size_t* cap, size_t n, cudaMemPool_t pool, cudaStream_t st) {
     if (n <= *cap && *p) return true;

@@ -905,6 +905,39 @@ def _latency_groups(stats, reqs):
     return out
 
 
+def _guarded(fn, *a):
+    """An auxiliary figure: its failure is reported in the line instead of ending the run."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
+def _serving_cpu_baseline(reqs, count: int = 400):
+    """The oracle (lyon restated) serving the same requests on the host cores: the first `count`
+    requests of the pool one after another, each tessellated on all threads (outputs not
+    written), as a CPU server would take them."""
+    from lyon_gb300.path import PathBatch
+    from oracle import lyon_oracle as orc
+    threads = os.cpu_count() or 1
+    sample = reqs[:count]
+    t_total, verts = 0.0, 0
+    for r in sample:
+        b = r.batch
+        sub = PathBatch(b.verbs, b.points, b.verb_offsets[r.start:r.start + r.count + 1],
+                        b.point_offsets[r.start:r.start + r.count + 1])
+        t0 = time.perf_counter()
+        res = orc.batch("stroke" if r.kind == 0 else "fill", sub, r.options, 32, threads,
+                        want_output=False)
+        t_total += time.perf_counter() - t0
+        verts += int(res["vtx_counts"].sum())
+    return {"value": verts / t_total, "unit": "vertices/s", "cores": threads, "kind": "port",
+            "requests_per_s": len(sample) / t_total,
+            "sample": f"first {len(sample)} requests of the pool one after another, each on "
+                      f"{threads} threads (outputs not written): {verts} output vertices in "
+                      f"{t_total:.2f} s"}
+
+
 def run_serving(args):
     """Serving loop: Poisson arrivals of scenes of 1-5,000 paths (log-uniform), 70 % strokes from
     the plain-stroke generator, 30 % fills from the glyph generator; outputs stay resident; each
@@ -967,6 +1000,7 @@ def run_serving(args):
                         "fill_blocks_per_sm": cfg["fill_blocks_per_sm"],
                         "max_stroke_batch_paths": cfg["max_stroke_batch_paths"]},
             "requests_in_pool": len(reqs), "mean_paths_per_request": mean_paths,
+            "cpu_baseline": _guarded(_serving_cpu_baseline, reqs),
             "offered_50k_per_s": brief(offered, reqs),
             "saturation_stroke_only": brief(sat_stroke),
             "saturation_fill_only": brief(sat_fill),
